@@ -1,0 +1,210 @@
+/*
+ * mcgpu_gb300.h -- C ABI of the GB300-native Metropolis trial-move energy
+ * path.  Plain pointers and sizes only; every call returns an mcgpu_status
+ * (0 = ok) and leaves a message for mcgpu_last_error() on failure.
+ *
+ * The plain single-chain entry points replace, one for one, the
+ * SimulationStep contract that MCGPU's Simulation::run drives
+ * (src/Metropolis/SimulationStep.h:24-94) over the SimBox rows
+ * (src/Metropolis/SimBox.h:120-149) that GPUCopy mirrors to the device
+ * (src/Metropolis/GPUCopy.cpp:97-188).  The chain, batch and serve entry
+ * points are the device-resident forms: the proposal RNG, the energy
+ * difference, the Metropolis decision and the commit or rollback all stay on
+ * the GPU.
+ *
+ * Thread safety: a context and the boxes, batches and servers made from it
+ * belong to one host thread at a time.
+ */
+#ifndef MCGPU_GB300_H
+#define MCGPU_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  MCGPU_OK = 0,
+  MCGPU_ERR_INVALID = 1,     /* bad argument (index, size, null pointer)   */
+  MCGPU_ERR_CUDA = 2,        /* a CUDA runtime call failed                 */
+  MCGPU_ERR_NOMEM = 3,       /* device or host allocation failed           */
+  MCGPU_ERR_UNSUPPORTED = 4, /* outside the supported limits (see below)   */
+  MCGPU_ERR_DEVICE = 5,      /* a kernel reported an error status word     */
+  MCGPU_ERR_CAPACITY = 6     /* server slot table or HBM budget exhausted  */
+} mcgpu_status;
+
+/* Pair arithmetic of a box. */
+typedef enum {
+  MCGPU_PREC_FP64 = 0,  /* FP64 pair terms, the reference's Real=double     */
+  MCGPU_PREC_MIXED = 1  /* FP32 pair terms, FP64 per-neighbour sums and totals */
+} mcgpu_precision;
+
+/* Rotation form of a device-drawn trial move. */
+typedef enum {
+  MCGPU_ROT_EULER = 0,  /* X->Y->Z Euler angles in degrees about the vertex atom
+                           (SimulationStep.cpp:527-555)                     */
+  MCGPU_ROT_AXIS = 1    /* angle about a uniform random axis through the vertex */
+} mcgpu_rotation;
+
+/* Limits of this build. */
+#define MCGPU_MAX_MOL_ATOMS 64   /* atoms in one molecule                      */
+#define MCGPU_MAX_MOL_PIDX 8     /* primary indexes of one molecule            */
+
+/* Host description of one box: the SimBox rows, FP64, structure of arrays.
+ * mol_pidx_* index into pidx[], and pidx[] holds absolute atom indexes, as
+ * SimBoxBuilder::addPrimaryIndexes builds them (SimBoxBuilder.cpp:282-299). */
+typedef struct {
+  int32_t n_mol, n_atom, n_pidx, pad0;
+  const double *x, *y, *z;             /* atomCoordinates rows [n_atom]     */
+  const double *sigma, *epsilon, *charge; /* atomData rows [n_atom]         */
+  const int32_t *mol_start, *mol_len;  /* moleculeData MOL_START / MOL_LEN  */
+  const int32_t *mol_pidx_start, *mol_pidx_count; /* MOL_PIDX_START/COUNT   */
+  const int32_t *pidx;                 /* primaryIndexes [n_pidx]           */
+  double size[3];                      /* box edges (cubic in practice)     */
+  double cutoff;                       /* molecular cutoff, Angstrom        */
+  double temperature;                  /* K; kT = T * 0.00198717            */
+  double max_translate, max_rotate;    /* Angstrom, degrees                 */
+} mcgpu_box_desc;
+
+/* A host-drawn trial move (the seven draws of SimCalcs::intermolecularMove,
+ * SimulationStep.cpp:527-535, in their draw order). */
+typedef struct {
+  int32_t vertex, pad0;
+  double dx, dy, dz;
+  double rx, ry, rz;   /* degrees */
+} mcgpu_move;
+
+/* Per-chain counters of a device-resident run. */
+typedef struct {
+  double energy;          /* running total: initial system energy + sum dE */
+  int64_t steps;          /* steps taken so far                            */
+  int64_t accepted;       /* accepted moves so far                         */
+  int64_t pairs;          /* atom pairs evaluated (old + new), if counted  */
+  int32_t error;          /* device error status word (0 = none)           */
+  int32_t ties;           /* decisions re-taken with FP64 pairs because the
+                             FP32 dE fell within its rounding bound of the
+                             acceptance threshold                           */
+} mcgpu_chain_stats;
+
+/* One step of a recorded device trajectory (for replay checks). */
+typedef struct {
+  int32_t mol, accepted;
+  double e_old, e_new, de, u;
+  int32_t fp64;           /* 1 if this step's energies are the FP64 re-take */
+  int32_t pad0;
+} mcgpu_trace;
+
+typedef struct mcgpu_ctx mcgpu_ctx;
+typedef struct mcgpu_box mcgpu_box;
+typedef struct mcgpu_batch mcgpu_batch;
+typedef struct mcgpu_server mcgpu_server;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Creates a context on CUDA device `device` (one GPU per context). */
+int mcgpu_ctx_create(mcgpu_ctx** out, int device);
+int mcgpu_ctx_destroy(mcgpu_ctx* ctx);
+/* Makes the context launch on the caller's CUDA stream (a cudaStream_t
+ * passed as a plain pointer; NULL restores the context's own stream).  The
+ * caller keeps the stream alive while the context uses it. */
+int mcgpu_ctx_set_stream(mcgpu_ctx* ctx, void* stream);
+/* Copies the last error message of the context (or of the process when ctx
+ * is NULL) into buf, NUL-terminated. */
+int mcgpu_last_error(const mcgpu_ctx* ctx, char* buf, size_t len);
+/* Library version string, e.g. "mcgpu_gb300 0.1 sm_103a". */
+const char* mcgpu_version(void);
+
+/* ---- plain single-chain path: the SimulationStep contract --------------- */
+
+/* Replaces GPUCopy::copyIn (GPUCopy.cpp:97-188): uploads the box to a
+ * device-resident structure of arrays.  The box keeps its own copy. */
+int mcgpu_box_upload(mcgpu_ctx* ctx, const mcgpu_box_desc* desc, int precision,
+                     mcgpu_box** out);
+int mcgpu_box_destroy(mcgpu_box* box);
+/* Replaces GPUCopy::copyOut (GPUCopy.cpp:190-222): current coordinates and
+ * box edges (size may be NULL). */
+int mcgpu_box_download(mcgpu_box* box, double* x, double* y, double* z,
+                       double* size);
+
+/* Replaces BruteForceCalcs::calcMolecularEnergyContribution
+ * (BruteForceStep.cpp:15-46): energy of molecule curr_mol with every
+ * molecule in [start_mol, n_mol) other than itself whose primary indexes
+ * come within the cutoff. */
+int mcgpu_mol_energy(mcgpu_box* box, int curr_mol, int start_mol, double* out);
+
+/* Replaces SimulationStep::changeMolecule -> SimCalcs::intermolecularMove
+ * (SimulationStep.cpp:520-566) with the draws supplied by the caller: saves
+ * the rollback copy, rotates about the vertex atom, translates, wraps. */
+int mcgpu_change_molecule(mcgpu_box* box, int mol, const mcgpu_move* mv);
+
+/* Replaces SimulationStep::rollback -> SimCalcs::rollback
+ * (SimulationStep.cpp:731-749). */
+int mcgpu_rollback(mcgpu_box* box, int mol);
+
+/* Replaces SimulationStep::calcSystemEnergy (SimulationStep.cpp:40-71) with
+ * subLJ = subCharge = 0: every in-range molecule pair counted once. */
+int mcgpu_system_energy(mcgpu_box* box, double* out);
+
+/* One whole trial move in one launch: old energy, move, new energy (the
+ * calls Simulation.cpp:244-250 makes), both energies returned. */
+int mcgpu_move_energies(mcgpu_box* box, int mol, const mcgpu_move* mv,
+                        double* e_old, double* e_new);
+
+/* ---- device-resident chain (Philox RNG, on-device accept) --------------- */
+
+/* Runs n_steps Metropolis steps of this box as chain `chain_id` with the
+ * Philox4x32-10 key `seed`, proposals drawn on the device; the running
+ * energy starts from a full system energy on the first call.  If trace is
+ * non-NULL it receives n_steps records. */
+int mcgpu_chain_run(mcgpu_box* box, uint64_t seed, uint32_t chain_id,
+                    int n_steps, int rotation, mcgpu_chain_stats* stats,
+                    mcgpu_trace* trace);
+
+/* ---- batched chains: one persistent kernel advances many chains --------- */
+
+/* Uploads n_chains independent boxes (uneven sizes and temperatures allowed)
+ * into one device pool; chain c uses Philox key seeds[c] and counter
+ * chain id c.  precision is MCGPU_PREC_MIXED in this build. */
+int mcgpu_batch_create(mcgpu_ctx* ctx, int n_chains, const mcgpu_box_desc* descs,
+                       const uint64_t* seeds, int rotation, mcgpu_batch** out);
+int mcgpu_batch_destroy(mcgpu_batch* batch);
+/* Advances every chain by n_steps steps (launches of steps_per_launch steps,
+ * replayed from a captured CUDA graph).  Asynchronous on the batch stream
+ * unless sync != 0. */
+int mcgpu_batch_run(mcgpu_batch* batch, int n_steps, int sync);
+/* Chooses steps_per_launch, chains per CTA and threads per molecule by timing
+ * candidate tiles on this batch (state is saved and restored). */
+int mcgpu_batch_autotune(mcgpu_batch* batch, int trial_steps);
+/* Sets the tile explicitly: threads per CTA (64..512), chains per CTA
+ * (1, 2, 4), steps per launch (>= 1). */
+int mcgpu_batch_set_tile(mcgpu_batch* batch, int threads, int chains_per_cta,
+                         int steps_per_launch);
+int mcgpu_batch_get_tile(mcgpu_batch* batch, int* threads, int* chains_per_cta,
+                         int* steps_per_launch);
+/* Like mcgpu_batch_run (synchronous, no graph) and records every step:
+ * out[c * n_steps + s] is step s of chain c. */
+int mcgpu_batch_run_traced(mcgpu_batch* batch, int n_steps, mcgpu_trace* out);
+int mcgpu_batch_sync(mcgpu_batch* batch);
+int mcgpu_batch_stats(mcgpu_batch* batch, mcgpu_chain_stats* stats);
+/* Coordinates of chain c (arrays sized like its descriptor). */
+int mcgpu_batch_download(mcgpu_batch* batch, int chain, double* x, double* y,
+                         double* z);
+/* Recomputes every chain's total energy from scratch (FP64 accumulate) into
+ * out[n_chains]; the running totals are not changed. */
+int mcgpu_batch_system_energy(mcgpu_batch* batch, double* out);
+
+/* ---- initial configuration (host only, no GPU) -------------------------- */
+
+/* Places n points uniformly in [0, L)^3 with minimum-image separation >= dmin
+ * by random sequential addition (every rejected candidate redrawn), seeded;
+ * out[3*i + d].  The reference builds its initial boxes on the host as an
+ * FCC lattice (FileUtilities.cpp:550-642); this is the random-start builder
+ * of the synthetic workloads.  Returns 0, 1 (bad argument) or 2 (no room). */
+int mcgpu_build_centres(int n, double L, double dmin, uint64_t seed, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,129 @@
+"""ctypes binding of the C ABI in ``include/mcgpu_gb300.h``.
+
+The shared library is built in-tree (``mcgpu_gb300/libmcgpu_gb300.so``) by
+``mcgpu_gb300/build.py``.  There is no fallback: if the library is missing or
+fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libmcgpu_gb300.so"
+
+MCGPU_OK = 0
+STATUS_NAMES = {
+    0: "MCGPU_OK", 1: "MCGPU_ERR_INVALID", 2: "MCGPU_ERR_CUDA", 3: "MCGPU_ERR_NOMEM",
+    4: "MCGPU_ERR_UNSUPPORTED", 5: "MCGPU_ERR_DEVICE", 6: "MCGPU_ERR_CAPACITY",
+}
+PREC_FP64 = 0
+PREC_MIXED = 1
+ROT_EULER = 0
+ROT_AXIS = 1
+MAX_MOL_ATOMS = 64
+MAX_MOL_PIDX = 8
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+class BoxDesc(C.Structure):
+    _fields_ = [
+        ("n_mol", C.c_int32), ("n_atom", C.c_int32), ("n_pidx", C.c_int32), ("pad0", C.c_int32),
+        ("x", _dp), ("y", _dp), ("z", _dp),
+        ("sigma", _dp), ("epsilon", _dp), ("charge", _dp),
+        ("mol_start", _ip), ("mol_len", _ip),
+        ("mol_pidx_start", _ip), ("mol_pidx_count", _ip),
+        ("pidx", _ip),
+        ("size", C.c_double * 3),
+        ("cutoff", C.c_double), ("temperature", C.c_double),
+        ("max_translate", C.c_double), ("max_rotate", C.c_double),
+    ]
+
+
+class Move(C.Structure):
+    _fields_ = [("vertex", C.c_int32), ("pad0", C.c_int32),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("rx", C.c_double), ("ry", C.c_double), ("rz", C.c_double)]
+
+
+class ChainStats(C.Structure):
+    _fields_ = [("energy", C.c_double), ("steps", C.c_int64), ("accepted", C.c_int64),
+                ("pairs", C.c_int64), ("error", C.c_int32), ("ties", C.c_int32)]
+
+
+class Trace(C.Structure):
+    _fields_ = [("mol", C.c_int32), ("accepted", C.c_int32), ("e_old", C.c_double),
+                ("e_new", C.c_double), ("de", C.c_double), ("u", C.c_double),
+                ("fp64", C.c_int32), ("pad0", C.c_int32)]
+
+
+_vp = C.c_void_p
+_PROTOS = {
+    "mcgpu_version": (C.c_char_p, []),
+    "mcgpu_ctx_create": (C.c_int, [C.POINTER(_vp), C.c_int]),
+    "mcgpu_ctx_destroy": (C.c_int, [_vp]),
+    "mcgpu_ctx_set_stream": (C.c_int, [_vp, _vp]),
+    "mcgpu_last_error": (C.c_int, [_vp, C.c_char_p, C.c_size_t]),
+    "mcgpu_box_upload": (C.c_int, [_vp, C.POINTER(BoxDesc), C.c_int, C.POINTER(_vp)]),
+    "mcgpu_box_destroy": (C.c_int, [_vp]),
+    "mcgpu_box_download": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "mcgpu_mol_energy": (C.c_int, [_vp, C.c_int, C.c_int, _dp]),
+    "mcgpu_change_molecule": (C.c_int, [_vp, C.c_int, C.POINTER(Move)]),
+    "mcgpu_rollback": (C.c_int, [_vp, C.c_int]),
+    "mcgpu_system_energy": (C.c_int, [_vp, _dp]),
+    "mcgpu_move_energies": (C.c_int, [_vp, C.c_int, C.POINTER(Move), _dp, _dp]),
+    "mcgpu_chain_run": (C.c_int, [_vp, C.c_uint64, C.c_uint32, C.c_int, C.c_int,
+                                  C.POINTER(ChainStats), C.POINTER(Trace)]),
+    "mcgpu_batch_create": (C.c_int, [_vp, C.c_int, C.POINTER(BoxDesc), C.POINTER(C.c_uint64),
+                                     C.c_int, C.POINTER(_vp)]),
+    "mcgpu_batch_destroy": (C.c_int, [_vp]),
+    "mcgpu_batch_run": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "mcgpu_batch_autotune": (C.c_int, [_vp, C.c_int]),
+    "mcgpu_batch_set_tile": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
+    "mcgpu_batch_get_tile": (C.c_int, [_vp, _ip, _ip, _ip]),
+    "mcgpu_batch_sync": (C.c_int, [_vp]),
+    "mcgpu_batch_run_traced": (C.c_int, [_vp, C.c_int, C.POINTER(Trace)]),
+    "mcgpu_batch_stats": (C.c_int, [_vp, C.POINTER(ChainStats)]),
+    "mcgpu_batch_download": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
+    "mcgpu_batch_system_energy": (C.c_int, [_vp, _dp]),
+    "mcgpu_build_centres": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint64, _dp]),
+}
+
+_lib = None
+
+
+class MCGPUError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def lib() -> C.CDLL:
+    """Loads the in-tree CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python mcgpu_gb300/build.py` "
+                "(there is no CPU fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in _PROTOS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_PROTOS)
+
+
+def check(status: int, ctx=None) -> None:
+    if status != MCGPU_OK:
+        buf = C.create_string_buffer(512)
+        lib().mcgpu_last_error(ctx, buf, 512)
+        raise MCGPUError(status, buf.value.decode(errors="replace"))

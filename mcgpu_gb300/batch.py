@@ -1,0 +1,87 @@
+"""Batched device-resident chains: many independent Metropolis chains of
+uneven size and temperature advanced by one persistent kernel, replayed as a
+captured CUDA graph, with autotuned tiles (mcgpu_batch_* in the C ABI)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from .step import Context
+from .workloads import BoxData
+
+
+class ChainBatch:
+    def __init__(self, ctx: Context, boxes: list[BoxData], seeds, rotation: int = _abi.ROT_AXIS):
+        self.ctx = ctx
+        self.boxes = [b.copy().normalise() for b in boxes]
+        n = len(self.boxes)
+        self._descs = (_abi.BoxDesc * n)()
+        for i, b in enumerate(self.boxes):
+            self._descs[i] = b.desc()
+        self._seeds = (C.c_uint64 * n)(*[int(s) & (2 ** 64 - 1) for s in seeds])
+        self._h = C.c_void_p()
+        _abi.check(_abi.lib().mcgpu_batch_create(ctx.handle, n, self._descs, self._seeds,
+                                                 int(rotation), C.byref(self._h)), ctx.handle)
+        self.n_chains = n
+
+    def _check(self, st: int) -> None:
+        _abi.check(st, self.ctx.handle)
+
+    def close(self) -> None:
+        if self._h:
+            _abi.lib().mcgpu_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, n_steps: int, sync: bool = True) -> None:
+        self._check(_abi.lib().mcgpu_batch_run(self._h, int(n_steps), 1 if sync else 0))
+
+    def run_traced(self, n_steps: int) -> list[list]:
+        """Runs n_steps and returns, per chain, the list of step records."""
+        arr = (_abi.Trace * (n_steps * self.n_chains))()
+        self._check(_abi.lib().mcgpu_batch_run_traced(self._h, int(n_steps), arr))
+        flat = list(arr)
+        return [flat[c * n_steps:(c + 1) * n_steps] for c in range(self.n_chains)]
+
+    def sync(self) -> None:
+        self._check(_abi.lib().mcgpu_batch_sync(self._h))
+
+    def autotune(self, trial_steps: int = 64) -> tuple[int, int, int]:
+        self._check(_abi.lib().mcgpu_batch_autotune(self._h, int(trial_steps)))
+        return self.tile
+
+    def set_tile(self, threads: int, chains_per_cta: int, steps_per_launch: int) -> None:
+        self._check(_abi.lib().mcgpu_batch_set_tile(self._h, threads, chains_per_cta,
+                                                    steps_per_launch))
+
+    @property
+    def tile(self) -> tuple[int, int, int]:
+        t, c, s = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(_abi.lib().mcgpu_batch_get_tile(self._h, C.byref(t), C.byref(c), C.byref(s)))
+        return t.value, c.value, s.value
+
+    def stats(self) -> list[_abi.ChainStats]:
+        arr = (_abi.ChainStats * self.n_chains)()
+        self._check(_abi.lib().mcgpu_batch_stats(self._h, arr))
+        return list(arr)
+
+    def download(self, chain: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n = self.boxes[chain].n_atom
+        x, y, z = np.empty(n), np.empty(n), np.empty(n)
+        dp = C.POINTER(C.c_double)
+        self._check(_abi.lib().mcgpu_batch_download(self._h, int(chain), x.ctypes.data_as(dp),
+                                                    y.ctypes.data_as(dp), z.ctypes.data_as(dp)))
+        return x, y, z
+
+    def system_energies(self) -> np.ndarray:
+        out = np.empty(self.n_chains)
+        self._check(_abi.lib().mcgpu_batch_system_energy(
+            self._h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out

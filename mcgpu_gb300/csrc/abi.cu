@@ -1,0 +1,979 @@
+// abi.cu -- host side of the C ABI declared in include/mcgpu_gb300.h.
+//
+// A box (plain single chain) and a batch (many chains) are both a device
+// "pool": one allocation per row, chains concatenated, per-chain headers.
+// Kernels live in kernels.cu; this file validates inputs, lays out the pool,
+// launches, and turns CUDA failures into status codes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "device.cuh"
+
+namespace mcgpu {
+__global__ void k_refresh_mirrors(Pool P, const int* mol_chain, int n_mol_total);
+__global__ void k_change_molecule(Pool P, int chain, int mol, Proposal prop, SmemShape shape);
+__global__ void k_rollback(Pool P, int chain, int mol);
+__global__ void k_chain_sums(Pool P, const double* emol, double* out);
+__global__ void k_set_energy(Pool P, const double* e);
+__global__ void k_chain_steps(Pool P, int n_steps, unsigned* queue, const int* order, int n_tasks,
+                              int gwarps, SmemShape shape, mcgpu_trace* trace, int trace_off,
+                              int trace_stride);
+cudaError_t launch_mol_energy(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
+                              Pool P, int chain, int curr, int start, double* partials,
+                              unsigned* counter, double* out);
+cudaError_t launch_move_energies(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
+                                 Pool P, int chain, int mol, Proposal prop, double* partials,
+                                 unsigned* counter, double* out);
+cudaError_t launch_mol_pair_sums(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
+                                 Pool P, const int* mol_chain, int m_begin, double* emol,
+                                 long long* pairs);
+}  // namespace mcgpu
+
+using namespace mcgpu;
+
+// ---- errors ------------------------------------------------------------------
+
+static thread_local std::string g_err;
+
+struct mcgpu_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;   // stream every launch goes to
+  cudaStream_t own = nullptr;      // the context's own stream
+  std::string err;
+};
+
+static int set_err(mcgpu_ctx* ctx, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  if (ctx) ctx->err = buf;
+  return code;
+}
+
+#define CK(ctx, call)                                                                  \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return set_err((ctx), MCGPU_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+// ---- pool ----------------------------------------------------------------------
+
+namespace {
+
+template <class T>
+T* dalloc(size_t n, cudaError_t* e) {
+  T* p = nullptr;
+  cudaError_t r = cudaMalloc((void**)&p, sizeof(T) * std::max<size_t>(n, 1));
+  if (r != cudaSuccess && *e == cudaSuccess) *e = r;
+  return p;
+}
+
+struct HostPool {
+  std::vector<double> x, y, z, sig, eps, q;
+  std::vector<float4> aoff;
+  std::vector<float2> aeq;
+  std::vector<int> mstart, mlen, pidx, mol_chain;
+  std::vector<int2> mpi;
+  std::vector<float> mrad;
+  std::vector<ChainHdr> hdr;
+  int max_len = 0;
+};
+
+// Validates one descriptor and appends it as chain `c` of the host pool.
+int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
+                 unsigned long long seed, int rot_mode) {
+  if (!d) return set_err(ctx, MCGPU_ERR_INVALID, "null box descriptor");
+  if (d->n_mol <= 0 || d->n_atom <= 0 || d->n_pidx <= 0)
+    return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: empty box (n_mol=%d n_atom=%d n_pidx=%d)", c,
+                   d->n_mol, d->n_atom, d->n_pidx);
+  if (!d->x || !d->y || !d->z || !d->sigma || !d->epsilon || !d->charge || !d->mol_start ||
+      !d->mol_len || !d->mol_pidx_start || !d->mol_pidx_count || !d->pidx)
+    return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: null row pointer", c);
+  for (int k = 0; k < 3; k++)
+    if (!(d->size[k] > 0) || !std::isfinite(d->size[k]))
+      return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: box edge %d is %g", c, k, d->size[k]);
+  if (!(d->cutoff > 0) || !(d->temperature > 0))
+    return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: cutoff %g / temperature %g must be > 0", c,
+                   d->cutoff, d->temperature);
+  const int atom0 = (int)hp.x.size(), mol0 = (int)hp.mstart.size(), pidx0 = (int)hp.pidx.size();
+  const long long tot_atoms = (long long)atom0 + d->n_atom;
+  if (tot_atoms > (1LL << 30) || (long long)mol0 + d->n_mol > (1LL << 26))
+    return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "pool too large");
+  for (int a = 0; a < d->n_atom; a++) {
+    hp.x.push_back(d->x[a]);
+    hp.y.push_back(d->y[a]);
+    hp.z.push_back(d->z[a]);
+    hp.sig.push_back(d->sigma[a]);
+    hp.eps.push_back(d->epsilon[a]);
+    hp.q.push_back(d->charge[a]);
+    if (!std::isfinite(d->x[a]) || !std::isfinite(d->y[a]) || !std::isfinite(d->z[a]))
+      return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: non-finite coordinate at atom %d", c, a);
+    const bool active = d->sigma[a] >= 0 && d->epsilon[a] >= 0;  // BruteForceStep.cpp:64-65
+    hp.aoff.push_back(make_float4(0.f, 0.f, 0.f, active ? (float)d->sigma[a] : 0.f));
+    hp.aeq.push_back(active ? make_float2((float)(2.0 * std::sqrt(std::fabs(d->epsilon[a]))),
+                                          (float)(d->charge[a] * std::sqrt(kCoulomb)))
+                            : make_float2(0.f, 0.f));
+  }
+  int max_len = 0;
+  double max_rad = 0;
+  for (int m = 0; m < d->n_mol; m++) {
+    const int s = d->mol_start[m], len = d->mol_len[m];
+    const int ps = d->mol_pidx_start[m], pc = d->mol_pidx_count[m];
+    if (len < 1 || len > kMaxA)
+      return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "chain %d molecule %d: %d atoms (limit %d)", c, m,
+                     len, kMaxA);
+    if (s < 0 || s + len > d->n_atom)
+      return set_err(ctx, MCGPU_ERR_INVALID, "chain %d molecule %d: atoms [%d,%d) outside [0,%d)",
+                     c, m, s, s + len, d->n_atom);
+    if (pc < 1 || pc > kMaxP)
+      return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "chain %d molecule %d: %d primary indexes (1..%d)",
+                     c, m, pc, kMaxP);
+    if (ps < 0 || ps + pc > d->n_pidx)
+      return set_err(ctx, MCGPU_ERR_INVALID, "chain %d molecule %d: primary range outside pidx", c,
+                     m);
+    int act = 0;
+    for (int a = s; a < s + len; a++) act += (d->sigma[a] >= 0 && d->epsilon[a] >= 0);
+    for (int k = ps; k < ps + pc; k++) {
+      const int p = d->pidx[k];
+      if (p < s || p >= s + len)
+        return set_err(ctx, MCGPU_ERR_INVALID,
+                       "chain %d molecule %d: primary index %d outside its atoms", c, m, p);
+    }
+    const int an = d->pidx[ps];
+    double rad = 0;
+    for (int a = s; a < s + len; a++) {
+      const double dx = d->x[a] - d->x[an], dy = d->y[a] - d->y[an], dz = d->z[a] - d->z[an];
+      rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    max_rad = std::max(max_rad, rad);
+    max_len = std::max(max_len, len);
+    hp.mstart.push_back(atom0 + s);
+    hp.mlen.push_back(len | (act << 8));
+    hp.mpi.push_back(make_int2(pidx0 + ps, pc));
+    hp.mrad.push_back((float)(rad * (1 + 1e-6) + 1e-4));
+    hp.mol_chain.push_back(c);
+  }
+  const double Lmin = std::min(d->size[0], std::min(d->size[1], d->size[2]));
+  if (max_rad >= 0.25 * Lmin)
+    return set_err(ctx, MCGPU_ERR_UNSUPPORTED,
+                   "chain %d: molecule radius %.3f A reaches a quarter of the box edge %.3f A", c,
+                   max_rad, Lmin);
+  for (int k = 0; k < d->n_pidx; k++) hp.pidx.push_back(atom0 + d->pidx[k]);
+
+  ChainHdr h;
+  std::memset(&h, 0, sizeof(h));
+  h.atom0 = atom0;
+  h.mol0 = mol0;
+  h.pidx0 = pidx0;
+  h.n_mol = d->n_mol;
+  h.n_atom = d->n_atom;
+  h.n_pidx = d->n_pidx;
+  h.max_len = max_len;
+  int T = 1;
+  while (T < max_len && T < 32) T <<= 1;
+  h.tpm = T;
+  h.rot_mode = rot_mode;
+  h.chain_id = (int)c;
+  const double rc = d->cutoff;
+  double ulpL = std::ldexp(1.0, (int)std::floor(std::log2(std::max(
+                                    d->size[0], std::max(d->size[1], d->size[2])))) - 23);
+  double band = 4.0 * (2.0 * std::sqrt(3.0) * rc * 1.5 * ulpL + 4.0 * std::ldexp(rc * rc, -24)) + 1e-6;
+  h.cut2_lo = (float)(rc * rc - band);
+  h.cut2_hi = (float)(rc * rc + band);
+  for (int k = 0; k < 3; k++) {
+    h.L[k] = d->size[k];
+    h.Lf[k] = (float)d->size[k];
+    h.fxinv[k] = 4294967296.0 / d->size[k];
+    h.fxs[k] = (float)(d->size[k] / 4294967296.0);
+  }
+  h.cutoff = rc;
+  h.kT = d->temperature * kBoltz;  // SimBoxBuilder.cpp:29
+  h.max_t = d->max_translate;
+  h.max_r = d->max_rotate;
+  h.seed = seed;
+  hp.hdr.push_back(h);
+  hp.max_len = std::max(hp.max_len, max_len);
+  return MCGPU_OK;
+}
+
+struct DevPool {
+  Pool P{};
+  int n_chains = 0, n_mol = 0, n_atom = 0, n_pidx = 0, max_len = 0;
+  int* mol_chain = nullptr;
+  double* emol = nullptr;
+  long long* pairs = nullptr;
+  double* esum = nullptr;
+  std::vector<ChainHdr> hdr;  // host copy of the headers at upload
+  std::vector<int> mstart, mlen;  // host copies (pool-absolute)
+
+  void release() {
+    void* ptrs[] = {P.x, P.y, P.z, P.sig, P.eps, P.q, P.aoff, P.aeq, P.mstart, P.mlen, P.mpi,
+                    P.mfix, P.mrad, P.pidx, P.ppos, P.hdr, P.rb, P.trace, mol_chain, emol, pairs,
+                    esum};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    P = Pool{};
+    mol_chain = nullptr;
+    emol = nullptr;
+    pairs = nullptr;
+    esum = nullptr;
+  }
+};
+
+int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
+  cudaError_t e = cudaSuccess;
+  const size_t na = hp.x.size(), nm = hp.mstart.size(), np = hp.pidx.size(), nc = hp.hdr.size();
+  dp.n_chains = (int)nc;
+  dp.n_atom = (int)na;
+  dp.n_mol = (int)nm;
+  dp.n_pidx = (int)np;
+  dp.max_len = hp.max_len;
+  Pool& P = dp.P;
+  P.x = dalloc<double>(na, &e); P.y = dalloc<double>(na, &e); P.z = dalloc<double>(na, &e);
+  P.sig = dalloc<double>(na, &e); P.eps = dalloc<double>(na, &e); P.q = dalloc<double>(na, &e);
+  P.aoff = dalloc<float4>(na, &e); P.aeq = dalloc<float2>(na, &e);
+  P.mstart = dalloc<int>(nm, &e); P.mlen = dalloc<int>(nm, &e); P.mpi = dalloc<int2>(nm, &e);
+  P.mfix = dalloc<uint4>(nm, &e); P.mrad = dalloc<float>(nm, &e);
+  P.pidx = dalloc<int>(np, &e); P.ppos = dalloc<float4>(np, &e);
+  P.hdr = dalloc<ChainHdr>(nc, &e);
+  P.rb = dalloc<double>(nc * 3 * (size_t)hp.max_len, &e);
+  P.trace = nullptr;
+  P.n_chains = (int)nc;
+  dp.mol_chain = dalloc<int>(nm, &e);
+  dp.emol = dalloc<double>(nm, &e);
+  dp.pairs = dalloc<long long>(nm, &e);
+  dp.esum = dalloc<double>(nc, &e);
+  if (e != cudaSuccess) {
+    dp.release();
+    return set_err(ctx, MCGPU_ERR_NOMEM, "device allocation failed: %s", cudaGetErrorString(e));
+  }
+  cudaStream_t st = ctx->stream;
+#define UP(dst, src) CK(ctx, cudaMemcpyAsync(dst, src.data(), sizeof(src[0]) * src.size(), cudaMemcpyHostToDevice, st))
+  UP(P.x, hp.x); UP(P.y, hp.y); UP(P.z, hp.z);
+  UP(P.sig, hp.sig); UP(P.eps, hp.eps); UP(P.q, hp.q);
+  UP(P.aoff, hp.aoff); UP(P.aeq, hp.aeq);
+  UP(P.mstart, hp.mstart); UP(P.mlen, hp.mlen); UP(P.mpi, hp.mpi); UP(P.mrad, hp.mrad);
+  UP(P.pidx, hp.pidx); UP(P.hdr, hp.hdr); UP(dp.mol_chain, hp.mol_chain);
+#undef UP
+  const int wpb = 8;
+  k_refresh_mirrors<<<(int)((nm + wpb - 1) / wpb), wpb * 32, 0, st>>>(P, dp.mol_chain, (int)nm);
+  CK(ctx, cudaGetLastError());
+  CK(ctx, cudaStreamSynchronize(st));
+  dp.hdr = hp.hdr;
+  dp.mstart = hp.mstart;
+  dp.mlen = hp.mlen;
+  return MCGPU_OK;
+}
+
+SmemShape shape_for(int max_len, int nwarps) {
+  SmemShape s;
+  s.maxA = std::max(max_len, 1);
+  s.nwarps = nwarps;
+  return s;
+}
+
+// Full system energy of every chain of the pool into dp.esum (device).
+int pool_system_energy(mcgpu_ctx* ctx, DevPool& dp, bool f64, cudaStream_t st) {
+  const int nw = 4;
+  SmemShape sh = shape_for(dp.max_len, nw);
+  const int bytes = sh.bytes();
+  // split the grid to keep launches moderate
+  const int chunk = 1 << 20;
+  for (int m0 = 0; m0 < dp.n_mol; m0 += chunk) {
+    int n = std::min(chunk, dp.n_mol - m0);
+    (void)bytes;
+    CK(ctx, launch_mol_pair_sums(f64, n, nw * 32, sh, st, dp.P, dp.mol_chain, m0, dp.emol, dp.pairs));
+  }
+  k_chain_sums<<<dp.n_chains, 256, 0, st>>>(dp.P, dp.emol, dp.esum);
+  CK(ctx, cudaGetLastError());
+  return MCGPU_OK;
+}
+
+}  // namespace
+
+// ---- context ---------------------------------------------------------------------
+
+extern "C" const char* mcgpu_version(void) { return "mcgpu_gb300 0.1 sm_103a"; }
+
+extern "C" int mcgpu_ctx_create(mcgpu_ctx** out, int device) {
+  if (!out) return set_err(nullptr, MCGPU_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return set_err(nullptr, MCGPU_ERR_CUDA, "no CUDA device: %s",
+                   e != cudaSuccess ? cudaGetErrorString(e) : "0 devices");
+  if (device < 0 || device >= n)
+    return set_err(nullptr, MCGPU_ERR_INVALID, "device %d out of range [0,%d)", device, n);
+  CK(nullptr, cudaSetDevice(device));
+  cudaDeviceProp prop;
+  CK(nullptr, cudaGetDeviceProperties(&prop, device));
+  if (prop.major != 10)
+    return set_err(nullptr, MCGPU_ERR_UNSUPPORTED,
+                   "device %d is sm_%d%d; this library is built for sm_103a (GB300)", device,
+                   prop.major, prop.minor);
+  mcgpu_ctx* c = new mcgpu_ctx();
+  c->device = device;
+  c->sm_count = prop.multiProcessorCount;
+  if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return set_err(nullptr, MCGPU_ERR_CUDA, "stream creation failed");
+  }
+  c->stream = c->own;
+  *out = c;
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_ctx_destroy(mcgpu_ctx* ctx) {
+  if (!ctx) return MCGPU_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->own) cudaStreamDestroy(ctx->own);
+  delete ctx;
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_ctx_set_stream(mcgpu_ctx* ctx, void* stream) {
+  if (!ctx) return set_err(nullptr, MCGPU_ERR_INVALID, "null context");
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_last_error(const mcgpu_ctx* ctx, char* buf, size_t len) {
+  if (!buf || len == 0) return MCGPU_ERR_INVALID;
+  const std::string& s = ctx ? ctx->err : g_err;
+  std::snprintf(buf, len, "%s", s.c_str());
+  return MCGPU_OK;
+}
+
+// ---- box (plain single chain) -------------------------------------------------------
+
+struct mcgpu_box {
+  mcgpu_ctx* ctx = nullptr;
+  DevPool pool;
+  int precision = MCGPU_PREC_FP64;
+  int max_grid = 1;
+  double* partials = nullptr;
+  unsigned* counter = nullptr;
+  double* dout = nullptr;
+  double* hout = nullptr;  // pinned
+  bool energy_ready = false;
+  mcgpu_trace* dtrace = nullptr;
+  int trace_cap = 0;
+  unsigned* queue = nullptr;
+  int* order = nullptr;
+};
+
+static int box_grid(const mcgpu_box* b, int n_cand) {
+  int g = (n_cand + 127) / 128;
+  return std::max(1, std::min(g, b->max_grid));
+}
+
+static Proposal host_proposal(const mcgpu_move* mv) {
+  Proposal p;
+  std::memset(&p, 0, sizeof(p));
+  p.vertex = mv->vertex;
+  p.mode = MCGPU_ROT_EULER;
+  p.dx = mv->dx; p.dy = mv->dy; p.dz = mv->dz;
+  p.r0 = mv->rx; p.r1 = mv->ry; p.r2 = mv->rz;
+  return p;
+}
+
+extern "C" int mcgpu_box_upload(mcgpu_ctx* ctx, const mcgpu_box_desc* desc, int precision,
+                                mcgpu_box** out) {
+  if (!ctx || !desc || !out) return set_err(ctx, MCGPU_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (precision != MCGPU_PREC_FP64 && precision != MCGPU_PREC_MIXED)
+    return set_err(ctx, MCGPU_ERR_INVALID, "unknown precision %d", precision);
+  CK(ctx, cudaSetDevice(ctx->device));
+  HostPool hp;
+  int rc = append_chain(ctx, hp, desc, 0, 0ull, MCGPU_ROT_EULER);
+  if (rc) return rc;
+  mcgpu_box* b = new mcgpu_box();
+  b->ctx = ctx;
+  b->precision = precision;
+  rc = upload_pool(ctx, hp, b->pool);
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  b->max_grid = 4 * ctx->sm_count;
+  cudaError_t e = cudaSuccess;
+  b->partials = dalloc<double>(2 * (size_t)b->max_grid, &e);
+  b->counter = dalloc<unsigned>(2, &e);
+  b->dout = dalloc<double>(4, &e);
+  b->queue = dalloc<unsigned>(1, &e);
+  b->order = dalloc<int>(1, &e);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&b->hout, 4 * sizeof(double));
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->counter, 0, 2 * sizeof(unsigned), ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->order, 0, sizeof(int), ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    mcgpu_box_destroy(b);
+    return set_err(ctx, MCGPU_ERR_NOMEM, "box scratch allocation failed: %s", cudaGetErrorString(e));
+  }
+  *out = b;
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_box_destroy(mcgpu_box* b) {
+  if (!b) return MCGPU_OK;
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(b->ctx->stream);
+  b->pool.release();
+  if (b->partials) cudaFree(b->partials);
+  if (b->counter) cudaFree(b->counter);
+  if (b->dout) cudaFree(b->dout);
+  if (b->hout) cudaFreeHost(b->hout);
+  if (b->dtrace) cudaFree(b->dtrace);
+  if (b->queue) cudaFree(b->queue);
+  if (b->order) cudaFree(b->order);
+  delete b;
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_box_download(mcgpu_box* b, double* x, double* y, double* z, double* size) {
+  if (!b || !x || !y || !z) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = b->ctx;
+  const size_t n = (size_t)b->pool.n_atom;
+  CK(ctx, cudaMemcpyAsync(x, b->pool.P.x, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(y, b->pool.P.y, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(z, b->pool.P.z, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (size)
+    for (int k = 0; k < 3; k++) size[k] = b->pool.hdr[0].L[k];
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_mol_energy(mcgpu_box* b, int curr, int start, double* out) {
+  if (!b || !out) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = b->ctx;
+  const int n = b->pool.n_mol;
+  if (curr < 0 || curr >= n) return set_err(ctx, MCGPU_ERR_INVALID, "molecule %d out of [0,%d)", curr, n);
+  if (start < 0 || start > n) return set_err(ctx, MCGPU_ERR_INVALID, "start %d out of [0,%d]", start, n);
+  if (start == n) {
+    *out = 0.0;
+    return MCGPU_OK;
+  }
+  const int nw = 4;
+  SmemShape sh = shape_for(b->pool.max_len, nw);
+  const int grid = box_grid(b, n - start);
+  CK(ctx, launch_mol_energy(b->precision == MCGPU_PREC_FP64, grid, nw * 32, sh, ctx->stream,
+                            b->pool.P, 0, curr, start, b->partials, b->counter, b->dout));
+  CK(ctx, cudaMemcpyAsync(b->hout, b->dout, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = b->hout[0];
+  return MCGPU_OK;
+}
+
+static int check_move(mcgpu_box* b, int mol, const mcgpu_move* mv) {
+  mcgpu_ctx* ctx = b->ctx;
+  if (!mv) return set_err(ctx, MCGPU_ERR_INVALID, "null move");
+  if (mol < 0 || mol >= b->pool.n_mol)
+    return set_err(ctx, MCGPU_ERR_INVALID, "molecule %d out of [0,%d)", mol, b->pool.n_mol);
+  const int len = b->pool.mlen[mol] & 255;
+  if (mv->vertex < 0 || mv->vertex >= len)
+    return set_err(ctx, MCGPU_ERR_INVALID, "vertex %d out of [0,%d) for molecule %d", mv->vertex,
+                   len, mol);
+  if (!std::isfinite(mv->dx) || !std::isfinite(mv->dy) || !std::isfinite(mv->dz) ||
+      !std::isfinite(mv->rx) || !std::isfinite(mv->ry) || !std::isfinite(mv->rz))
+    return set_err(ctx, MCGPU_ERR_INVALID, "non-finite move");
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_change_molecule(mcgpu_box* b, int mol, const mcgpu_move* mv) {
+  if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  int rc = check_move(b, mol, mv);
+  if (rc) return rc;
+  mcgpu_ctx* ctx = b->ctx;
+  SmemShape sh = shape_for(b->pool.max_len, 1);
+  k_change_molecule<<<1, 32, sh.bytes(), ctx->stream>>>(b->pool.P, 0, mol, host_proposal(mv), sh);
+  CK(ctx, cudaGetLastError());
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_rollback(mcgpu_box* b, int mol) {
+  if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  mcgpu_ctx* ctx = b->ctx;
+  if (mol < 0 || mol >= b->pool.n_mol)
+    return set_err(ctx, MCGPU_ERR_INVALID, "molecule %d out of [0,%d)", mol, b->pool.n_mol);
+  k_rollback<<<1, 32, 0, ctx->stream>>>(b->pool.P, 0, mol);
+  CK(ctx, cudaGetLastError());
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_move_energies(mcgpu_box* b, int mol, const mcgpu_move* mv, double* e_old,
+                                   double* e_new) {
+  if (!b || !e_old || !e_new) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  int rc = check_move(b, mol, mv);
+  if (rc) return rc;
+  mcgpu_ctx* ctx = b->ctx;
+  const int nw = 4;
+  SmemShape sh = shape_for(b->pool.max_len, nw);
+  const int grid = box_grid(b, b->pool.n_mol);
+  CK(ctx, launch_move_energies(b->precision == MCGPU_PREC_FP64, grid, nw * 32, sh, ctx->stream,
+                               b->pool.P, 0, mol, host_proposal(mv), b->partials, b->counter,
+                               b->dout));
+  CK(ctx, cudaMemcpyAsync(b->hout, b->dout, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  *e_old = b->hout[0];
+  *e_new = b->hout[1];
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_system_energy(mcgpu_box* b, double* out) {
+  if (!b || !out) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = b->ctx;
+  int rc = pool_system_energy(ctx, b->pool, b->precision == MCGPU_PREC_FP64, ctx->stream);
+  if (rc) return rc;
+  CK(ctx, cudaMemcpyAsync(b->hout, b->pool.esum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = b->hout[0];
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, int n_steps,
+                               int rotation, mcgpu_chain_stats* stats, mcgpu_trace* trace) {
+  if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  mcgpu_ctx* ctx = b->ctx;
+  if (n_steps < 0) return set_err(ctx, MCGPU_ERR_INVALID, "negative step count");
+  if (rotation != MCGPU_ROT_EULER && rotation != MCGPU_ROT_AXIS)
+    return set_err(ctx, MCGPU_ERR_INVALID, "unknown rotation form %d", rotation);
+  cudaStream_t st = ctx->stream;
+  DevPool& dp = b->pool;
+  ChainHdr* dh = dp.P.hdr;
+  // key, counter chain id and rotation form of this run
+  CK(ctx, cudaMemcpyAsync(&dh->seed, &seed, 8, cudaMemcpyHostToDevice, st));
+  int cid = (int)chain_id;
+  CK(ctx, cudaMemcpyAsync(&dh->chain_id, &cid, 4, cudaMemcpyHostToDevice, st));
+  CK(ctx, cudaMemcpyAsync(&dh->rot_mode, &rotation, 4, cudaMemcpyHostToDevice, st));
+  if (!b->energy_ready) {
+    int rc = pool_system_energy(ctx, dp, true, st);
+    if (rc) return rc;
+    k_set_energy<<<1, 32, 0, st>>>(dp.P, dp.esum);
+    CK(ctx, cudaGetLastError());
+    b->energy_ready = true;
+  }
+  if (trace && n_steps > b->trace_cap) {
+    if (b->dtrace) cudaFree(b->dtrace);
+    b->dtrace = nullptr;
+    CK(ctx, cudaMalloc((void**)&b->dtrace, sizeof(mcgpu_trace) * (size_t)n_steps));
+    b->trace_cap = n_steps;
+  }
+  const int nw = std::max(1, std::min(16, dp.n_mol / 256));
+  SmemShape sh = shape_for(dp.max_len, nw);
+  const int seg = 1024;
+  for (int done = 0; done < n_steps; done += seg) {
+    const int k = std::min(seg, n_steps - done);
+    CK(ctx, cudaMemsetAsync(b->queue, 0, sizeof(unsigned), st));
+    Pool P = dp.P;
+    P.trace = nullptr;
+    k_chain_steps<<<1, nw * 32, sh.bytes(), st>>>(P, k, b->queue, b->order, 1, nw, sh,
+                                                  trace ? b->dtrace : nullptr, done, 0);
+    CK(ctx, cudaGetLastError());
+  }
+  if (trace && n_steps > 0)
+    CK(ctx, cudaMemcpyAsync(trace, b->dtrace, sizeof(mcgpu_trace) * (size_t)n_steps,
+                            cudaMemcpyDeviceToHost, st));
+  if (stats) {
+    ChainHdr h;
+    CK(ctx, cudaMemcpyAsync(&h, dh, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CK(ctx, cudaStreamSynchronize(st));
+    stats->energy = h.energy;
+    stats->steps = (int64_t)h.step;
+    stats->accepted = h.accepted;
+    stats->pairs = h.pairs;
+    stats->error = h.error;
+    stats->ties = h.ties;
+  }
+  CK(ctx, cudaStreamSynchronize(st));
+  return MCGPU_OK;
+}
+
+// ---- batch ---------------------------------------------------------------------------
+
+struct mcgpu_batch {
+  mcgpu_ctx* ctx = nullptr;
+  DevPool pool;
+  unsigned* queue = nullptr;   // one counter per launch slot of a graph
+  int* order = nullptr;
+  int threads = 128, cpc = 1, spl = 16;  // CTA threads, chains per CTA, steps per launch
+  int max_slots = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_launches = 0, graph_spl = 0, graph_threads = 0, graph_cpc = 0;
+  // snapshot for the autotuner
+  std::vector<void*> snap;
+};
+
+static int batch_gwarps(const mcgpu_batch* bt) { return (bt->threads / 32) / bt->cpc; }
+
+static int batch_grid(mcgpu_batch* bt, int* smem_out) {
+  const int gw = batch_gwarps(bt);
+  SmemShape sh = shape_for(bt->pool.max_len, gw);
+  const int smem = sh.bytes() * bt->cpc;
+  *smem_out = smem;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chain_steps, bt->threads, smem);
+  per_sm = std::max(per_sm, 1);
+  const int need = (bt->pool.n_chains + bt->cpc - 1) / bt->cpc;
+  return std::max(1, std::min(need, per_sm * bt->ctx->sm_count));
+}
+
+static int batch_launch(mcgpu_batch* bt, int steps, unsigned* q, cudaStream_t st,
+                        mcgpu_trace* trace = nullptr, int trace_off = 0, int trace_stride = 0) {
+  mcgpu_ctx* ctx = bt->ctx;
+  int smem = 0;
+  const int grid = batch_grid(bt, &smem);
+  const int gw = batch_gwarps(bt);
+  SmemShape sh = shape_for(bt->pool.max_len, gw);
+  CK(ctx, cudaMemsetAsync(q, 0, sizeof(unsigned), st));
+  k_chain_steps<<<grid, bt->threads, smem, st>>>(bt->pool.P, steps, q, bt->order,
+                                                 bt->pool.n_chains, gw, sh, trace, trace_off,
+                                                 trace_stride);
+  CK(ctx, cudaGetLastError());
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_create(mcgpu_ctx* ctx, int n_chains, const mcgpu_box_desc* descs,
+                                  const uint64_t* seeds, int rotation, mcgpu_batch** out) {
+  if (!ctx || !descs || !seeds || !out) return set_err(ctx, MCGPU_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (n_chains <= 0) return set_err(ctx, MCGPU_ERR_INVALID, "n_chains %d must be > 0", n_chains);
+  if (rotation != MCGPU_ROT_EULER && rotation != MCGPU_ROT_AXIS)
+    return set_err(ctx, MCGPU_ERR_INVALID, "unknown rotation form %d", rotation);
+  CK(ctx, cudaSetDevice(ctx->device));
+  HostPool hp;
+  for (int c = 0; c < n_chains; c++) {
+    int rc = append_chain(ctx, hp, &descs[c], c, seeds[c], rotation);
+    if (rc) return rc;
+  }
+  mcgpu_batch* bt = new mcgpu_batch();
+  bt->ctx = ctx;
+  int rc = upload_pool(ctx, hp, bt->pool);
+  if (rc) {
+    delete bt;
+    return rc;
+  }
+  // Cost-descending task order (largest chains first): screen ~ n_mol,
+  // pairs ~ max_len^2.
+  std::vector<int> order(n_chains);
+  for (int c = 0; c < n_chains; c++) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b2) {
+    const ChainHdr &ha = hp.hdr[a], &hb = hp.hdr[b2];
+    return (double)ha.n_mol * (1 + ha.max_len) > (double)hb.n_mol * (1 + hb.max_len);
+  });
+  bt->max_slots = 64;
+  cudaError_t e = cudaSuccess;
+  bt->queue = dalloc<unsigned>(bt->max_slots, &e);
+  bt->order = dalloc<int>(n_chains, &e);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(bt->order, order.data(), sizeof(int) * n_chains, cudaMemcpyHostToDevice,
+                        ctx->stream);
+  if (e != cudaSuccess) {
+    mcgpu_batch_destroy(bt);
+    return set_err(ctx, MCGPU_ERR_NOMEM, "batch allocation failed: %s", cudaGetErrorString(e));
+  }
+  // initial running energies: full FP64 system energy of every chain
+  rc = pool_system_energy(ctx, bt->pool, true, ctx->stream);
+  if (rc) {
+    mcgpu_batch_destroy(bt);
+    return rc;
+  }
+  k_set_energy<<<(n_chains + 127) / 128, 128, 0, ctx->stream>>>(bt->pool.P, bt->pool.esum);
+  CK(ctx, cudaGetLastError());
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = bt;
+  return MCGPU_OK;
+}
+
+static void batch_drop_graph(mcgpu_batch* bt) {
+  if (bt->graph) cudaGraphExecDestroy(bt->graph);
+  bt->graph = nullptr;
+}
+
+extern "C" int mcgpu_batch_destroy(mcgpu_batch* bt) {
+  if (!bt) return MCGPU_OK;
+  cudaSetDevice(bt->ctx->device);
+  cudaStreamSynchronize(bt->ctx->stream);
+  batch_drop_graph(bt);
+  bt->pool.release();
+  if (bt->queue) cudaFree(bt->queue);
+  if (bt->order) cudaFree(bt->order);
+  for (void* p : bt->snap)
+    if (p) cudaFree(p);
+  delete bt;
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_set_tile(mcgpu_batch* bt, int threads, int cpc, int spl) {
+  if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
+  mcgpu_ctx* ctx = bt->ctx;
+  if (threads < 32 || threads > 512 || threads % 32)
+    return set_err(ctx, MCGPU_ERR_INVALID, "threads %d must be a multiple of 32 in [32,512]", threads);
+  if (cpc < 1 || (threads / 32) % cpc || (threads / 32) / cpc < 1)
+    return set_err(ctx, MCGPU_ERR_INVALID, "chains per CTA %d must divide the CTA's %d warps", cpc,
+                   threads / 32);
+  if ((threads / 32) / cpc > 1 && cpc > 15)
+    return set_err(ctx, MCGPU_ERR_INVALID, "at most 15 multi-warp groups per CTA");
+  if (spl < 1) return set_err(ctx, MCGPU_ERR_INVALID, "steps per launch %d must be >= 1", spl);
+  int smem = shape_for(bt->pool.max_len, (threads / 32) / cpc).bytes() * cpc;
+  if (smem > 200 * 1024) return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "tile needs %d B shared memory", smem);
+  if (smem > 48 * 1024)
+    CK(ctx, cudaFuncSetAttribute(k_chain_steps, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  bt->threads = threads;
+  bt->cpc = cpc;
+  bt->spl = spl;
+  batch_drop_graph(bt);
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_get_tile(mcgpu_batch* bt, int* threads, int* cpc, int* spl) {
+  if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
+  if (threads) *threads = bt->threads;
+  if (cpc) *cpc = bt->cpc;
+  if (spl) *spl = bt->spl;
+  return MCGPU_OK;
+}
+
+// Captures `launches` launches of spl steps each into a graph (one queue
+// counter per launch, reset by a memset node).
+static int batch_build_graph(mcgpu_batch* bt, int launches) {
+  mcgpu_ctx* ctx = bt->ctx;
+  batch_drop_graph(bt);
+  cudaStream_t st = ctx->stream;
+  cudaGraph_t g = nullptr;
+  CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  int rc = MCGPU_OK;
+  for (int l = 0; l < launches && rc == MCGPU_OK; l++) rc = batch_launch(bt, bt->spl, bt->queue + l, st);
+  cudaError_t e = cudaStreamEndCapture(st, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return set_err(ctx, MCGPU_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&bt->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return set_err(ctx, MCGPU_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+  bt->graph_launches = launches;
+  bt->graph_spl = bt->spl;
+  bt->graph_threads = bt->threads;
+  bt->graph_cpc = bt->cpc;
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_run(mcgpu_batch* bt, int n_steps, int sync) {
+  if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
+  mcgpu_ctx* ctx = bt->ctx;
+  if (n_steps < 0) return set_err(ctx, MCGPU_ERR_INVALID, "negative step count");
+  const int spl = bt->spl;
+  const int full = n_steps / spl, rem = n_steps % spl;
+  const int per_graph = std::min(bt->max_slots, 32);
+  if (full >= per_graph) {
+    if (!bt->graph || bt->graph_spl != spl || bt->graph_launches != per_graph ||
+        bt->graph_threads != bt->threads || bt->graph_cpc != bt->cpc) {
+      int rc = batch_build_graph(bt, per_graph);
+      if (rc) return rc;
+    }
+  }
+  int done = 0;
+  while (full - done >= per_graph && bt->graph) {
+    CK(ctx, cudaGraphLaunch(bt->graph, ctx->stream));
+    done += per_graph;
+  }
+  for (; done < full; done++) {
+    int rc = batch_launch(bt, spl, bt->queue + (done % bt->max_slots), ctx->stream);
+    if (rc) return rc;
+  }
+  if (rem) {
+    int rc = batch_launch(bt, rem, bt->queue, ctx->stream);
+    if (rc) return rc;
+  }
+  if (sync) CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_run_traced(mcgpu_batch* bt, int n_steps, mcgpu_trace* out) {
+  if (!bt || !out) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = bt->ctx;
+  if (n_steps <= 0) return set_err(ctx, MCGPU_ERR_INVALID, "step count %d must be > 0", n_steps);
+  const size_t n = (size_t)n_steps * bt->pool.n_chains;
+  mcgpu_trace* d = nullptr;
+  CK(ctx, cudaMalloc((void**)&d, sizeof(mcgpu_trace) * n));
+  int rc = MCGPU_OK;
+  for (int done = 0; done < n_steps && rc == MCGPU_OK; done += bt->spl) {
+    const int k = std::min(bt->spl, n_steps - done);
+    rc = batch_launch(bt, k, bt->queue, ctx->stream, d, done, n_steps);
+  }
+  cudaError_t e = cudaSuccess;
+  if (rc == MCGPU_OK)
+    e = cudaMemcpyAsync(out, d, sizeof(mcgpu_trace) * n, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  if (rc) return rc;
+  if (e != cudaSuccess) return set_err(ctx, MCGPU_ERR_CUDA, "traced run failed: %s", cudaGetErrorString(e));
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_sync(mcgpu_batch* bt) {
+  if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
+  CK(bt->ctx, cudaStreamSynchronize(bt->ctx->stream));
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_stats(mcgpu_batch* bt, mcgpu_chain_stats* stats) {
+  if (!bt || !stats) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = bt->ctx;
+  std::vector<ChainHdr> h(bt->pool.n_chains);
+  CK(ctx, cudaMemcpyAsync(h.data(), bt->pool.P.hdr, sizeof(ChainHdr) * h.size(),
+                          cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  int err = 0;
+  for (size_t c = 0; c < h.size(); c++) {
+    stats[c].energy = h[c].energy;
+    stats[c].steps = (int64_t)h[c].step;
+    stats[c].accepted = h[c].accepted;
+    stats[c].pairs = h[c].pairs;
+    stats[c].error = h[c].error;
+    stats[c].ties = h[c].ties;
+    err |= h[c].error;
+  }
+  if (err) return set_err(ctx, MCGPU_ERR_DEVICE, "a chain reported device error status %d", err);
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_download(mcgpu_batch* bt, int chain, double* x, double* y, double* z) {
+  if (!bt || !x || !y || !z) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = bt->ctx;
+  if (chain < 0 || chain >= bt->pool.n_chains)
+    return set_err(ctx, MCGPU_ERR_INVALID, "chain %d out of [0,%d)", chain, bt->pool.n_chains);
+  const ChainHdr& h = bt->pool.hdr[chain];
+  const size_t n = (size_t)h.n_atom;
+  CK(ctx, cudaMemcpyAsync(x, bt->pool.P.x + h.atom0, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(y, bt->pool.P.y + h.atom0, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(z, bt->pool.P.z + h.atom0, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_system_energy(mcgpu_batch* bt, double* out) {
+  if (!bt || !out) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = bt->ctx;
+  int rc = pool_system_energy(ctx, bt->pool, true, ctx->stream);
+  if (rc) return rc;
+  CK(ctx, cudaMemcpyAsync(out, bt->pool.esum, sizeof(double) * bt->pool.n_chains,
+                          cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MCGPU_OK;
+}
+
+// ---- autotuner ---------------------------------------------------------------------
+
+// Device state a run changes: coordinates and mirrors of all atoms, the
+// molecule anchors, the screen positions and the chain headers.
+static int batch_snapshot(mcgpu_batch* bt, bool restore) {
+  mcgpu_ctx* ctx = bt->ctx;
+  DevPool& dp = bt->pool;
+  struct Row { void* p; size_t bytes; } rows[] = {
+      {dp.P.x, 8ull * dp.n_atom}, {dp.P.y, 8ull * dp.n_atom}, {dp.P.z, 8ull * dp.n_atom},
+      {dp.P.aoff, 16ull * dp.n_atom}, {dp.P.mfix, 16ull * dp.n_mol}, {dp.P.ppos, 16ull * dp.n_pidx},
+      {dp.P.hdr, sizeof(ChainHdr) * (size_t)dp.n_chains}};
+  const int nr = (int)(sizeof(rows) / sizeof(rows[0]));
+  if (bt->snap.empty()) {
+    bt->snap.assign(nr, nullptr);
+    for (int r = 0; r < nr; r++) CK(ctx, cudaMalloc(&bt->snap[r], rows[r].bytes));
+  }
+  for (int r = 0; r < nr; r++) {
+    if (restore)
+      CK(ctx, cudaMemcpyAsync(rows[r].p, bt->snap[r], rows[r].bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    else
+      CK(ctx, cudaMemcpyAsync(bt->snap[r], rows[r].p, rows[r].bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
+  if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
+  mcgpu_ctx* ctx = bt->ctx;
+  if (trial_steps < 1) trial_steps = 64;
+  int rc = batch_snapshot(bt, false);
+  if (rc) return rc;
+  struct Tile { int threads, cpc, spl; };
+  std::vector<Tile> cands;
+  const int tw[] = {64, 128, 256};
+  for (int t : tw)
+    for (int gw = 1; gw <= t / 32; gw *= 2) {
+      const int cpc = (t / 32) / gw;
+      if (gw > 1 && cpc > 15) continue;
+      cands.push_back({t, cpc, 16});
+    }
+  cudaEvent_t e0, e1;
+  CK(ctx, cudaEventCreate(&e0));
+  CK(ctx, cudaEventCreate(&e1));
+  float best = 1e30f;
+  Tile bestT = {bt->threads, bt->cpc, bt->spl};
+  for (const Tile& T : cands) {
+    if (mcgpu_batch_set_tile(bt, T.threads, T.cpc, T.spl) != MCGPU_OK) continue;
+    rc = batch_snapshot(bt, true);
+    if (rc) break;
+    rc = mcgpu_batch_run(bt, T.spl, 0);  // warm-up
+    if (rc) break;
+    CK(ctx, cudaEventRecord(e0, ctx->stream));
+    rc = mcgpu_batch_run(bt, trial_steps, 0);
+    if (rc) break;
+    CK(ctx, cudaEventRecord(e1, ctx->stream));
+    CK(ctx, cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      bestT = T;
+    }
+  }
+  // steps per launch for the best shape
+  const int spls[] = {4, 16, 64};
+  for (int spl : spls) {
+    if (rc) break;
+    if (mcgpu_batch_set_tile(bt, bestT.threads, bestT.cpc, spl) != MCGPU_OK) continue;
+    rc = batch_snapshot(bt, true);
+    if (rc) break;
+    rc = mcgpu_batch_run(bt, spl, 0);
+    if (rc) break;
+    CK(ctx, cudaEventRecord(e0, ctx->stream));
+    rc = mcgpu_batch_run(bt, std::max(trial_steps, 2 * spl), 0);
+    if (rc) break;
+    CK(ctx, cudaEventRecord(e1, ctx->stream));
+    CK(ctx, cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms *= (float)trial_steps / (float)std::max(trial_steps, 2 * spl);
+    if (ms <= best) {
+      best = ms;
+      bestT.spl = spl;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  rc = mcgpu_batch_set_tile(bt, bestT.threads, bestT.cpc, bestT.spl);
+  if (rc) return rc;
+  rc = batch_snapshot(bt, true);
+  if (rc) return rc;
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MCGPU_OK;
+}

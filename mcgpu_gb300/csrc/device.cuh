@@ -1,0 +1,348 @@
+// device.cuh -- device-side layout and building blocks of the GB300 trial-move
+// energy path.
+//
+// HBM layout (one "pool" holds one box or many chains, all rows
+// pool-absolute):
+//   atoms      x,y,z,sig,eps,q   FP64 master rows (the SimBox rows,
+//                                SimBox.h:120-149) -- moves and the FP64
+//                                path read these
+//              aoff  float4      (x,y,z) - anchor, FP32, w = sigma (0 for a
+//                                dummy site); anchor = first primary atom
+//              aeq   float2      (2*sqrt|eps|, q*sqrt(332.06)), 0 for dummies
+//   molecules  mstart,mlen       MOL_START / MOL_LEN
+//              mpi   int2        (MOL_PIDX_START, MOL_PIDX_COUNT)
+//              mfix  uint4       anchor position in 32-bit fixed point of the
+//                                box edge: differences wrap to the minimum
+//                                image for free and convert with one I2F
+//              mrad  float       max |atom - anchor| (rigid: move-invariant)
+//              mlen packs (atoms | non-dummy atoms << 8)
+//   primaries  pidx              primaryIndexes, absolute
+//              ppos  float4      primary position wrapped into [0, L), FP32,
+//                                for the cutoff screen
+//   chains     hdr   ChainHdr    per-chain offsets, box, RNG key, counters
+//
+// The cutoff decision is the reference's FP64 test (SimulationStep.cpp:
+// 317-330): the FP32 screen decides outright only outside a guard band
+// around rc^2 and re-tests in FP64 from the master rows inside it.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/mcgpu_gb300.h"
+
+namespace mcgpu {
+
+constexpr int kMaxA = MCGPU_MAX_MOL_ATOMS;
+constexpr int kMaxP = MCGPU_MAX_MOL_PIDX;
+constexpr double kBoltz = 0.00198717;        // SimBox.h:16
+constexpr double kCoulomb = 332.06;          // SimulationStep.cpp:364
+// Bound on the FP32-pair rounding error of a molecule energy, relative to
+// the sum of the magnitudes of its FP32 terms (observed worst case ~1e-8;
+// the bound keeps a 100x margin).
+constexpr double kTieRel = 1e-6;
+
+// Device error status words (ChainHdr::error, Pool::error).
+enum : int {
+  kErrNone = 0,
+  kErrListOverflow = 1,
+  kErrBadIndex = 2,
+  kErrNonFinite = 3,
+};
+
+// Per-chain header: 256 bytes, one per chain (a single box is chain 0).
+struct __align__(16) ChainHdr {
+  int atom0, mol0, pidx0, n_mol;      // pool offsets and molecule count
+  int n_atom, n_pidx, max_len, tpm;   // tpm: lanes per neighbour molecule
+  int rot_mode, chain_id, pad0, pad1b;
+  float Lf[3], cut2_lo;               // FP32 box and guard band
+  float fxs[3], cut2_hi;              // fixed point -> Angstrom scale
+  double L[3], cutoff;
+  double fxinv[3], kT;                // Angstrom -> fixed point scale
+  double max_t, max_r, energy, pad1;
+  unsigned long long seed, step;
+  long long accepted, pairs;
+  int error, ties, pad3, pad4;   // ties: decisions re-taken with FP64 pairs
+};
+static_assert(sizeof(ChainHdr) % 16 == 0, "ChainHdr alignment");
+
+struct Pool {
+  double *x, *y, *z, *sig, *eps, *q;
+  float4* aoff;
+  float2* aeq;
+  int *mstart, *mlen;
+  int2* mpi;
+  uint4* mfix;
+  float* mrad;
+  int* pidx;
+  float4* ppos;
+  ChainHdr* hdr;
+  double* rb;          // rollback rows, 3 * max_len per chain
+  mcgpu_trace* trace;  // optional step records
+  int n_chains;
+};
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), from the published
+// description: ten rounds, two 32x32->64 multiplies per round, Weyl key bumps.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    unsigned hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    unsigned hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += 0x9E3779B9u;
+    k.y += 0xBB67AE85u;
+  }
+  return c;
+}
+__device__ __forceinline__ double u01(unsigned r) {
+  return ((double)r + 0.5) * 2.3283064365386963e-10;
+}
+__device__ __forceinline__ int uidx(unsigned r, int n) {
+  return (int)(((unsigned long long)r * (unsigned long long)n) >> 32);
+}
+
+// A trial move: vertex, translation, rotation (Euler degrees or axis+angle).
+struct Proposal {
+  int mol, vertex, mode, pad;
+  double dx, dy, dz, r0, r1, r2, r3, u;
+};
+
+// Draws the proposal of (seed, chain, step): the counter layout and the
+// uniform/index mappings are fixed so a CPU replay gets the same values.
+__device__ inline Proposal draw_proposal(unsigned long long seed, unsigned chain,
+                                         unsigned long long step, int n_mol,
+                                         const int* mlen_chain, double max_t,
+                                         double max_r, int mode) {
+  uint2 key = make_uint2((unsigned)seed, (unsigned)(seed >> 32));
+  uint4 a = philox4x32_10(make_uint4((unsigned)step, (unsigned)(step >> 32), chain, 0u), key);
+  uint4 c = philox4x32_10(make_uint4((unsigned)step, (unsigned)(step >> 32), chain, 1u), key);
+  uint4 d = philox4x32_10(make_uint4((unsigned)step, (unsigned)(step >> 32), chain, 2u), key);
+  Proposal p;
+  p.mol = uidx(a.x, n_mol);
+  p.vertex = uidx(a.y, mlen_chain[p.mol] & 255);
+  p.mode = mode;
+  p.pad = 0;
+  p.dx = __dadd_rn(__dmul_rn(2.0 * max_t, u01(a.z)), -max_t);
+  p.dy = __dadd_rn(__dmul_rn(2.0 * max_t, u01(a.w)), -max_t);
+  p.dz = __dadd_rn(__dmul_rn(2.0 * max_t, u01(c.x)), -max_t);
+  if (mode == MCGPU_ROT_EULER) {
+    p.r0 = __dadd_rn(__dmul_rn(2.0 * max_r, u01(c.y)), -max_r);
+    p.r1 = __dadd_rn(__dmul_rn(2.0 * max_r, u01(c.z)), -max_r);
+    p.r2 = __dadd_rn(__dmul_rn(2.0 * max_r, u01(c.w)), -max_r);
+    p.r3 = 0.0;
+  } else {
+    double zc = __dadd_rn(__dmul_rn(2.0, u01(c.y)), -1.0);
+    double phi = __dmul_rn(6.283185307179586, u01(c.z));
+    double s = sqrt(__dadd_rn(1.0, -__dmul_rn(zc, zc)));
+    double sp, cp;
+    sincos(phi, &sp, &cp);
+    p.r0 = __dmul_rn(s, cp);
+    p.r1 = __dmul_rn(s, sp);
+    p.r2 = zc;
+    p.r3 = __dadd_rn(__dmul_rn(2.0 * max_r, u01(c.w)), -max_r);
+  }
+  p.u = u01(d.x);
+  return p;
+}
+
+// Rotation matrix of a proposal, applied to v = atom - pivot:
+// Euler: rotateX, then rotateY, then rotateZ (SimulationStep.cpp:400-422),
+// composed as separate rounded steps exactly like the reference.
+struct Rot {
+  double cx, sx, cy, sy, cz, sz;   // Euler; axis form: cx=cos, sx=sin, cy=1-cos
+  double kx, ky, kz;               // axis form: unit axis
+  int mode;
+};
+
+__device__ inline Rot make_rot(const Proposal& p) {
+  Rot R;
+  R.mode = p.mode;
+  if (p.mode == MCGPU_ROT_EULER) {
+    sincos(__dmul_rn(p.r0, 3.14159265358979) / 180.0, &R.sx, &R.cx);
+    sincos(__dmul_rn(p.r1, 3.14159265358979) / 180.0, &R.sy, &R.cy);
+    sincos(__dmul_rn(p.r2, 3.14159265358979) / 180.0, &R.sz, &R.cz);
+  } else {
+    sincos(__dmul_rn(p.r3, 3.14159265358979) / 180.0, &R.sx, &R.cx);
+    R.cy = __dadd_rn(1.0, -R.cx);
+    R.kx = p.r0; R.ky = p.r1; R.kz = p.r2;
+  }
+  return R;
+}
+
+// Applies the rotation to v (in place).
+__device__ __forceinline__ void rot_apply(const Rot& R, double& vx, double& vy, double& vz) {
+  if (R.mode == MCGPU_ROT_EULER) {
+    double oy = vy, oz = vz;   // rotateX
+    vy = __dadd_rn(__dmul_rn(oy, R.cx), __dmul_rn(oz, R.sx));
+    vz = __dadd_rn(__dmul_rn(oz, R.cx), -__dmul_rn(oy, R.sx));
+    oz = vz;
+    double ox = vx;            // rotateY
+    vz = __dadd_rn(__dmul_rn(oz, R.cy), __dmul_rn(ox, R.sy));
+    vx = __dadd_rn(__dmul_rn(ox, R.cy), -__dmul_rn(oz, R.sy));
+    ox = vx;
+    oy = vy;                   // rotateZ
+    vx = __dadd_rn(__dmul_rn(ox, R.cz), __dmul_rn(oy, R.sz));
+    vy = __dadd_rn(__dmul_rn(oy, R.cz), -__dmul_rn(ox, R.sz));
+  } else {
+    // Rodrigues: v' = v c + (k x v) s + k (k.v)(1-c)
+    double kv = R.kx * vx + R.ky * vy + R.kz * vz;
+    double qx = R.ky * vz - R.kz * vy, qy = R.kz * vx - R.kx * vz, qz = R.kx * vy - R.ky * vx;
+    double x = vx * R.cx + qx * R.sx + R.kx * kv * R.cy;
+    double y = vy * R.cx + qy * R.sx + R.ky * kv * R.cy;
+    double z = vz * R.cx + qz * R.sx + R.kz * kv * R.cy;
+    vx = x; vy = y; vz = z;
+  }
+}
+
+// SimCalcs::makePeriodic (SimulationStep.cpp:377-385), FP64.
+__device__ __forceinline__ double make_periodic(double x, double L) {
+  if (x < -0.5 * L) x = __dadd_rn(x, L);
+  if (x > 0.5 * L) x = __dadd_rn(x, -L);
+  return x;
+}
+
+// ---- groups: the warps that advance one chain --------------------------
+struct Group {
+  int tid, nthreads, bar;
+  __device__ __forceinline__ int warp() const { return tid >> 5; }
+  __device__ __forceinline__ int nwarps() const { return nthreads >> 5; }
+  __device__ __forceinline__ void sync() const {
+    if (nthreads == 32) {
+      __syncwarp();
+    } else {
+      asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(nthreads) : "memory");
+    }
+  }
+};
+
+// Shared-memory state of one group; carved from dynamic shared memory with
+// sizes fixed per launch (max molecule length, warps per group).  Each warp
+// owns a 64-entry ring of neighbour-list entries: the warp screens 32
+// candidates per round, appends the in-range ones, and evaluates full
+// batches of 32 entries, so the screen -> list -> pair pipeline needs no
+// group barrier.
+constexpr int kRing = 64;
+
+struct GroupSmem {
+  // moved molecule
+  double* ox; double* oy; double* oz;   // old FP64 coords [maxA]
+  double* nx; double* ny; double* nz;   // new FP64 coords [maxA]
+  double* sd; double* ed; double* qd;   // FP64 sigma, epsilon, charge [maxA]
+  float4* o_old; float4* o_new;         // FP32 offsets from the anchor, w=sigma [maxA]
+  float4* eq;                           // FP32 (2sqrt|eps|, q sqrt(332.06), |o_old|^2, |o_new|^2) [maxA]
+  float4* p_old; float4* p_new;         // wrapped FP32 primaries [kMaxP]
+  int* pa;                              // primary atom slots in the molecule [kMaxP]
+  // per-warp neighbour rings [nwarps * kRing]
+  int* lj;                              // (j << 4) | flags
+  float4* lA;                           // (Dold.xyz, Dnew.x)
+  float2* lB;                           // (Dnew.y, Dnew.z)
+  double* red;                          // [3 * nwarps] reduction scratch
+  long long* redl;                      // [nwarps]
+  int* misc;                            // [32] broadcast ints
+  double* miscd;                        // [32] broadcast doubles
+};
+
+struct SmemShape {
+  int maxA, nwarps;
+  __host__ __device__ static int align16(int v) { return (v + 15) & ~15; }
+  __host__ __device__ int bytes() const {
+    int b = 0;
+    b += align16(9 * maxA * 8);
+    b += align16(2 * maxA * 16);
+    b += align16(maxA * 16);
+    b += align16(2 * kMaxP * 16);
+    b += align16(kMaxP * 4);
+    b += align16(nwarps * kRing * 4);
+    b += align16(nwarps * kRing * 16);
+    b += align16(nwarps * kRing * 8);
+    b += align16(3 * nwarps * 8);
+    b += align16(nwarps * 8);
+    b += align16(32 * 4);
+    b += align16(32 * 8);
+    return b;
+  }
+  __device__ GroupSmem carve(char* base) const {
+    GroupSmem s;
+    char* p = base;
+    s.ox = (double*)p; s.oy = s.ox + maxA; s.oz = s.oy + maxA;
+    s.nx = s.oz + maxA; s.ny = s.nx + maxA; s.nz = s.ny + maxA;
+    s.sd = s.nz + maxA; s.ed = s.sd + maxA; s.qd = s.ed + maxA;
+    p += align16(9 * maxA * 8);
+    s.o_old = (float4*)p; s.o_new = s.o_old + maxA; p += align16(2 * maxA * 16);
+    s.eq = (float4*)p; p += align16(maxA * 16);
+    s.p_old = (float4*)p; s.p_new = s.p_old + kMaxP; p += align16(2 * kMaxP * 16);
+    s.pa = (int*)p; p += align16(kMaxP * 4);
+    s.lj = (int*)p; p += align16(nwarps * kRing * 4);
+    s.lA = (float4*)p; p += align16(nwarps * kRing * 16);
+    s.lB = (float2*)p; p += align16(nwarps * kRing * 8);
+    s.red = (double*)p; p += align16(3 * nwarps * 8);
+    s.redl = (long long*)p; p += align16(nwarps * 8);
+    s.misc = (int*)p; p += align16(32 * 4);
+    s.miscd = (double*)p;
+    return s;
+  }
+};
+
+// Flags of a neighbour-list entry.
+enum : int { kInOld = 1, kInNew = 2, kWrapOld = 4, kWrapNew = 8 };
+
+// Moved-molecule scalars, identical in every thread of a group after
+// staging.  states: bit 0 = evaluate the current ("old") placement, bit 1 =
+// evaluate the proposed ("new") placement.
+struct MovedInfo {
+  int mol, atom0, len, npidx, act, states, vertex, pad;
+  uint4 fx_old, fx_new;
+  float rad, qm;  // qm: net FP32 charge factor sum_a q_a sqrt(332.06)
+};
+
+__device__ __forceinline__ float wrapf(float d, float L) {
+  float a = fabsf(d);
+  return fminf(a, L - a);
+}
+
+// Reciprocal square root, hardware estimate refined by one Newton-Raphson
+// step y' = y + (y/2)(1 - r2 y^2): the estimate is good to about 2^-23
+// relative, the refined value to about one ulp.
+__device__ __forceinline__ float rsqrt_nr(float r2) {
+  float ir = rsqrtf(r2);
+  const float t0 = r2 * ir;
+  const float h = fmaf(-t0, ir, 1.0f);
+  return fmaf(0.5f * ir, h, ir);
+}
+
+// Hardware reciprocal estimate (rcp.approx, ~1 ulp); used only on a factor
+// of an already small term, where its relative error is harmless.
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// LJ part of a pair term from per-atom factors (sigma, 2sqrt|eps|) and the
+// refined 1/r: 4 eps (s^12 - s^6), s = sigma_ab^2 / r^2 with geometric
+// blending (SimulationStep.cpp:344-358, :369-375).
+__device__ __forceinline__ float lj32(float ir, float sa, float sb, float ea, float eb) {
+  const float ir2 = ir * ir;
+  const float t = (sa * sb) * ir2;
+  const float t3 = t * t * t;
+  return (ea * eb) * fmaf(t3, t3, -t3);
+}
+
+// FP64 pair term restating SimulationStep.cpp:344-375 and
+// BruteForceStep.cpp:64-73 for a non-dummy pair at squared distance r2.
+__device__ __forceinline__ double pair64(double r2, double sa, double sb, double ea,
+                                         double eb, double qa, double qb) {
+  if (r2 == 0.0) return 0.0;
+  double ss = sa * sb, ee = ea * eb;
+  double sigma = sqrt(ss >= 0 ? ss : -ss);
+  double eps = sqrt(ee >= 0 ? ee : -ee);
+  double s2r2 = (sigma * sigma) / r2;
+  double s6r6 = s2r2 * s2r2 * s2r2;
+  double s12r12 = s6r6 * s6r6;
+  double lj = 4.0 * eps * (s12r12 - s6r6);
+  double r = sqrt(r2);
+  return lj + (qa * qb * kCoulomb) / r;
+}
+
+}  // namespace mcgpu

@@ -1,0 +1,536 @@
+// kernels.cuh -- the group-level pieces shared by every kernel: staging of
+// the moved molecule, the cutoff screen, the per-warp neighbour rings, the
+// pair batches (FP32 pair terms with FP64 per-neighbour sums, or FP64 pair
+// terms), reductions and the commit.
+#pragma once
+
+#include "device.cuh"
+
+namespace mcgpu {
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Primary position wrapped into [0, L) (FP32), for the screen.
+__device__ __forceinline__ float4 wrap_pos(double x, double y, double z, const ChainHdr& H) {
+  double wx = x - H.L[0] * floor(x / H.L[0]);
+  double wy = y - H.L[1] * floor(y / H.L[1]);
+  double wz = z - H.L[2] * floor(z / H.L[2]);
+  return make_float4((float)wx, (float)wy, (float)wz, 0.f);
+}
+
+// Anchor position in 32-bit fixed point of the box edge (wraps mod 2^32).
+__device__ __forceinline__ uint4 fixpos(double x, double y, double z, const ChainHdr& H) {
+  return make_uint4((unsigned)(unsigned long long)__double2ll_rn(x * H.fxinv[0]),
+                    (unsigned)(unsigned long long)__double2ll_rn(y * H.fxinv[1]),
+                    (unsigned)(unsigned long long)__double2ll_rn(z * H.fxinv[2]), 0u);
+}
+
+// Minimum-image anchor difference b - a in Angstrom (FP32).
+__device__ __forceinline__ float3 fixdiff(uint4 b, uint4 a, const ChainHdr& H) {
+  return make_float3((float)(int)(b.x - a.x) * H.fxs[0], (float)(int)(b.y - a.y) * H.fxs[1],
+                     (float)(int)(b.z - a.z) * H.fxs[2]);
+}
+
+// True when an atom pair of these two molecules may need its own periodic
+// image (|D| + radii reaches half a box edge in some dimension).
+__device__ __forceinline__ bool needs_wrap(float3 D, float rr, const ChainHdr& H) {
+  return fabsf(D.x) + rr > 0.5f * H.Lf[0] - 1e-3f || fabsf(D.y) + rr > 0.5f * H.Lf[1] - 1e-3f ||
+         fabsf(D.z) + rr > 0.5f * H.Lf[2] - 1e-3f;
+}
+
+// The reference's cutoff test for one primary pair, FP64, same rounding
+// (SimulationStep.cpp:325-326 with :332-342 and :377-385).
+__device__ __forceinline__ bool in_range64(double x1, double y1, double z1, int p2,
+                                           const Pool& P, const ChainHdr& H) {
+  double dx = make_periodic(P.x[p2] - x1, H.L[0]);
+  double dy = make_periodic(P.y[p2] - y1, H.L[1]);
+  double dz = make_periodic(P.z[p2] - z1, H.L[2]);
+  double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+  return r2 <= __dmul_rn(H.cutoff, H.cutoff);
+}
+
+__device__ __forceinline__ float r2_screen(float4 a, float4 b, const ChainHdr& H) {
+  float dx = wrapf(b.x - a.x, H.Lf[0]);
+  float dy = wrapf(b.y - a.y, H.Lf[1]);
+  float dz = wrapf(b.z - a.z, H.Lf[2]);
+  return fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+}
+
+// ---- staging ------------------------------------------------------------
+
+// Lanes of ONE warp stage molecule m: its current placement ("old") and, if
+// p is non-null, the proposed placement ("new") computed as
+// SimCalcs::intermolecularMove does (SimulationStep.cpp:544-565): every
+// non-vertex atom rotated about the vertex and translated, the vertex
+// translated, then the molecule wrapped by its first primary atom
+// (keepMoleculeInBox, :710-729).  Results go to shared memory; scalars to
+// misc/miscd.  The caller synchronises the group afterwards.
+__device__ void stage(const Pool& P, const ChainHdr& H, int m, const Proposal* p,
+                      const GroupSmem& s, int lane) {
+  const int a0 = P.mstart[m];
+  const int lw = P.mlen[m];
+  const int len = lw & 255;
+  const int2 pi = P.mpi[m];
+  for (int i = lane; i < len; i += 32) {
+    int a = a0 + i;
+    s.ox[i] = P.x[a]; s.oy[i] = P.y[a]; s.oz[i] = P.z[a];
+    s.sd[i] = P.sig[a]; s.ed[i] = P.eps[a]; s.qd[i] = P.q[a];
+    const float4 o = P.aoff[a];
+    const float2 q = P.aeq[a];
+    s.o_old[i] = o;
+    s.eq[i] = make_float4(q.x, q.y, fmaf(o.x, o.x, fmaf(o.y, o.y, o.z * o.z)), 0.f);
+  }
+  // net FP32 charge factor of the molecule (sum over lanes, fixed order)
+  float qsum = 0.f;
+  for (int i = lane; i < len; i += 32) qsum += P.aeq[a0 + i].y;
+  for (int off = 16; off > 0; off >>= 1) qsum += __shfl_xor_sync(~0u, qsum, off);
+  for (int k = lane; k < pi.y; k += 32) {
+    s.p_old[k] = P.ppos[pi.x + k];
+    s.pa[k] = P.pidx[pi.x + k] - a0;
+  }
+  uint4 fo = P.mfix[m];
+  if (lane == 0) {
+    s.misc[0] = m; s.misc[1] = a0; s.misc[2] = len; s.misc[3] = pi.y;
+    s.misc[4] = lw >> 8; s.misc[5] = p ? 3 : 1; s.misc[6] = p ? p->vertex : -1;
+    s.misc[8] = (int)fo.x; s.misc[9] = (int)fo.y; s.misc[10] = (int)fo.z;
+    s.miscd[0] = (double)P.mrad[m];
+    s.miscd[1] = (double)qsum;
+  }
+  if (!p) return;
+  Rot R;
+  if (lane == 0) R = make_rot(*p);
+  R.mode = p->mode;
+  R.cx = __shfl_sync(~0u, R.cx, 0); R.sx = __shfl_sync(~0u, R.sx, 0);
+  R.cy = __shfl_sync(~0u, R.cy, 0); R.sy = __shfl_sync(~0u, R.sy, 0);
+  R.cz = __shfl_sync(~0u, R.cz, 0); R.sz = __shfl_sync(~0u, R.sz, 0);
+  R.kx = __shfl_sync(~0u, R.kx, 0); R.ky = __shfl_sync(~0u, R.ky, 0);
+  R.kz = __shfl_sync(~0u, R.kz, 0);
+  __syncwarp();
+  const int v = p->vertex;
+  const double px = s.ox[v], py = s.oy[v], pz = s.oz[v];
+  for (int i = lane; i < len; i += 32) {
+    double x, y, z;
+    if (i == v) {
+      x = __dadd_rn(px, p->dx); y = __dadd_rn(py, p->dy); z = __dadd_rn(pz, p->dz);
+    } else {
+      double vx = __dadd_rn(s.ox[i], -px), vy = __dadd_rn(s.oy[i], -py), vz = __dadd_rn(s.oz[i], -pz);
+      rot_apply(R, vx, vy, vz);
+      x = __dadd_rn(__dadd_rn(vx, px), p->dx);
+      y = __dadd_rn(__dadd_rn(vy, py), p->dy);
+      z = __dadd_rn(__dadd_rn(vz, pz), p->dz);
+    }
+    s.nx[i] = x; s.ny[i] = y; s.nz[i] = z;
+  }
+  __syncwarp();
+  const int an = s.pa[0];
+  double ax = s.nx[an], ay = s.ny[an], az = s.nz[an];
+  double shx = 0, shy = 0, shz = 0;
+  if (ax < 0) shx = H.L[0]; else if (ax > H.L[0]) shx = -H.L[0];
+  if (ay < 0) shy = H.L[1]; else if (ay > H.L[1]) shy = -H.L[1];
+  if (az < 0) shz = H.L[2]; else if (az > H.L[2]) shz = -H.L[2];
+  if (shx != 0) ax = __dadd_rn(ax, shx);
+  if (shy != 0) ay = __dadd_rn(ay, shy);
+  if (shz != 0) az = __dadd_rn(az, shz);
+  __syncwarp();
+  for (int i = lane; i < len; i += 32) {
+    double x = s.nx[i], y = s.ny[i], z = s.nz[i];
+    if (shx != 0) x = __dadd_rn(x, shx);
+    if (shy != 0) y = __dadd_rn(y, shy);
+    if (shz != 0) z = __dadd_rn(z, shz);
+    s.nx[i] = x; s.ny[i] = y; s.nz[i] = z;
+    const float4 o = make_float4((float)(x - ax), (float)(y - ay), (float)(z - az), s.o_old[i].w);
+    s.o_new[i] = o;
+    s.eq[i].w = fmaf(o.x, o.x, fmaf(o.y, o.y, o.z * o.z));
+  }
+  __syncwarp();
+  for (int k = lane; k < pi.y; k += 32) {
+    int q = s.pa[k];
+    s.p_new[k] = wrap_pos(s.nx[q], s.ny[q], s.nz[q], H);
+  }
+  if (lane == 0) {
+    uint4 fn = fixpos(ax, ay, az, H);
+    s.misc[12] = (int)fn.x; s.misc[13] = (int)fn.y; s.misc[14] = (int)fn.z;
+  }
+}
+
+__device__ __forceinline__ MovedInfo load_moved(const GroupSmem& s) {
+  MovedInfo mi;
+  mi.mol = s.misc[0]; mi.atom0 = s.misc[1]; mi.len = s.misc[2]; mi.npidx = s.misc[3];
+  mi.act = s.misc[4]; mi.states = s.misc[5]; mi.vertex = s.misc[6]; mi.pad = 0;
+  mi.fx_old = make_uint4((unsigned)s.misc[8], (unsigned)s.misc[9], (unsigned)s.misc[10], 0u);
+  mi.fx_new = make_uint4((unsigned)s.misc[12], (unsigned)s.misc[13], (unsigned)s.misc[14], 0u);
+  mi.rad = (float)s.miscd[0];
+  mi.qm = (float)s.miscd[1];
+  return mi;
+}
+
+// ---- screen ---------------------------------------------------------------
+
+// FP32 screen with FP64 re-test inside the guard band; fills the entry's
+// minimum-image anchor differences for the FP32 pair path.
+__device__ __forceinline__ int screen_mixed(const Pool& P, const ChainHdr& H, const GroupSmem& s,
+                                            const MovedInfo& mi, int j, float4& A, float2& B) {
+  const int2 pj = P.mpi[j];
+  int f = 0;
+  for (int k2 = 0; k2 < pj.y; k2++) {
+    const float4 q = P.ppos[pj.x + k2];
+    for (int k1 = 0; k1 < mi.npidx; k1++) {
+      if ((mi.states & 1) && !(f & kInOld)) {
+        float r2 = r2_screen(s.p_old[k1], q, H);
+        if (r2 <= H.cut2_lo) {
+          f |= kInOld;
+        } else if (r2 <= H.cut2_hi) {
+          int pa = s.pa[k1];
+          if (in_range64(s.ox[pa], s.oy[pa], s.oz[pa], P.pidx[pj.x + k2], P, H)) f |= kInOld;
+        }
+      }
+      if ((mi.states & 2) && !(f & kInNew)) {
+        float r2 = r2_screen(s.p_new[k1], q, H);
+        if (r2 <= H.cut2_lo) {
+          f |= kInNew;
+        } else if (r2 <= H.cut2_hi) {
+          int pa = s.pa[k1];
+          if (in_range64(s.nx[pa], s.ny[pa], s.nz[pa], P.pidx[pj.x + k2], P, H)) f |= kInNew;
+        }
+      }
+    }
+  }
+  if (f) {
+    const uint4 fj = P.mfix[j];
+    const float rr = mi.rad + P.mrad[j];
+    float3 Do = make_float3(0.f, 0.f, 0.f), Dn = Do;
+    if (f & kInOld) {
+      Do = fixdiff(fj, mi.fx_old, H);
+      if (needs_wrap(Do, rr, H)) f |= kWrapOld;
+    }
+    if (f & kInNew) {
+      Dn = fixdiff(fj, mi.fx_new, H);
+      if (needs_wrap(Dn, rr, H)) f |= kWrapNew;
+    }
+    A = make_float4(Do.x, Do.y, Do.z, Dn.x);
+    B = make_float2(Dn.y, Dn.z);
+  }
+  return f;
+}
+
+// FP64 screen: the reference's test for every primary pair.
+__device__ __forceinline__ int screen_f64(const Pool& P, const ChainHdr& H, const GroupSmem& s,
+                                          const MovedInfo& mi, int j) {
+  const int2 pj = P.mpi[j];
+  int f = 0;
+  for (int k2 = 0; k2 < pj.y; k2++) {
+    const int p2 = P.pidx[pj.x + k2];
+    for (int k1 = 0; k1 < mi.npidx; k1++) {
+      const int pa = s.pa[k1];
+      if ((mi.states & 1) && !(f & kInOld) && in_range64(s.ox[pa], s.oy[pa], s.oz[pa], p2, P, H))
+        f |= kInOld;
+      if ((mi.states & 2) && !(f & kInNew) && in_range64(s.nx[pa], s.ny[pa], s.nz[pa], p2, P, H))
+        f |= kInNew;
+    }
+  }
+  return f;
+}
+
+// ---- pair batches -----------------------------------------------------------
+
+// Sum over the moved molecule's atoms a of the FP32 pair terms with one
+// neighbour atom b at anchor-relative position (bx, by, bz), per-pair
+// periodic image (entries whose atom pairs may straddle half a box edge).
+// abs accumulates |LJ| + |Coulomb| (the scale of the rounding error).
+__device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4* eq, int len,
+                                                  float bx, float by, float bz, float sb,
+                                                  float2 qb, const ChainHdr& H, float& abs) {
+  float acc = 0.f;
+  for (int i = 0; i < len; i++) {
+    const float4 a = o[i];
+    const float4 ea = eq[i];
+    const float dx = wrapf(bx - a.x, H.Lf[0]);
+    const float dy = wrapf(by - a.y, H.Lf[1]);
+    const float dz = wrapf(bz - a.z, H.Lf[2]);
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float ir = rsqrt_nr(r2);
+    const float lj = lj32(ir, a.w, sb, ea.x, qb.x);
+    const float cl = (ea.y * qb.y) * ir;
+    const bool ok = r2 > 0.f;
+    acc += ok ? lj + cl : 0.f;
+    abs += ok ? fabsf(lj) + fabsf(cl) : 0.f;
+  }
+  return acc;
+}
+
+// The same sum for an entry whose pairs all use the anchors' image, with
+// the Coulomb part written for neutral molecules: with R = |b - anchor_m|,
+//   sum_a q_a / r_ab = sum_a q_a (1/r_ab - 1/R) + Q_m / R,
+//   1/r - 1/R = (R^2 - r^2) / (r R (r + R)),  R^2 - r^2 = 2 b.o_a - |o_a|^2,
+// so every Coulomb term is O(|o_a| / R) smaller than q_a q_b / r and carries
+// proportionally less FP32 rounding.  A coincident pair (r = 0) is skipped
+// as the reference skips it (BruteForceStep.cpp:68-69).  oo selects the
+// |o_a|^2 of the placement (eq.z old, eq.w new).
+__device__ __forceinline__ float sum_moved32_cf(const float4* o, const float4* eq, int len,
+                                                bool use_new, float bx, float by, float bz,
+                                                float sb, float2 qb, float qm, float& abs) {
+  const float R2 = fmaf(bx, bx, fmaf(by, by, bz * bz));
+  const float iR = rsqrt_nr(R2);
+  const float R = R2 * iR;
+  const float tx = bx + bx, ty = by + by, tz = bz + bz;
+  float lj_acc = 0.f, phi = 0.f, lj_abs = 0.f, c_abs = 0.f;
+  for (int i = 0; i < len; i++) {
+    const float4 a = o[i];
+    const float4 ea = eq[i];
+    const float dx = bx - a.x, dy = by - a.y, dz = bz - a.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float ir = rsqrt_nr(r2);
+    const float lj = lj32(ir, a.w, sb, ea.x, qb.x);
+    const float num = fmaf(tx, a.x, fmaf(ty, a.y, fmaf(tz, a.z, -(use_new ? ea.w : ea.z))));
+    const float w = ir * rcp_approx(fmaf(r2, ir, R));
+    const bool ok = r2 > 0.f;
+    const float c = ok ? (ea.y * num) * w : -ea.y;
+    lj_acc += ok ? lj : 0.f;
+    lj_abs += ok ? fabsf(lj) : 0.f;
+    phi += c;
+    c_abs += fabsf(c);
+  }
+  const float f = qb.y * iR;
+  abs += lj_abs + fabsf(f) * (c_abs + fabsf(qm));
+  return fmaf(f, phi + qm, lj_acc);
+}
+
+// Evaluates `count` ring entries from `head` with teams of T lanes (T a
+// power of two <= 32): lane tl of a team takes neighbour atoms tl, tl+T, ...
+// of the entry's molecule against every atom of the moved molecule.  The
+// team's FP32 partial of each entry is added to the FP64 sums eo / en (and
+// its magnitude to ab) of the team's first lane.
+__device__ __forceinline__ void batch_mixed(const Pool& P, const ChainHdr& H, const GroupSmem& s,
+                                            const MovedInfo& mi, const int* rj, const float4* rA,
+                                            const float2* rB, int head, int count, int lane, int T,
+                                            double& eo, double& en, double& ab, long long& np) {
+  const int tm = lane / T, tl = lane - tm * T, nteams = 32 / T;
+  for (int e0 = 0; e0 < count; e0 += nteams) {
+    const int e = e0 + tm;
+    int f = 0, b0 = 0, lenj = 0, actj = 0;
+    float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 B = make_float2(0.f, 0.f);
+    if (e < count) {
+      const int idx = (head + e) & (kRing - 1);
+      const int jf = rj[idx];
+      A = rA[idx];
+      B = rB[idx];
+      const int j = jf >> 4;
+      f = jf & 15;
+      b0 = P.mstart[j];
+      const int lw = P.mlen[j];
+      lenj = lw & 255;
+      actj = lw >> 8;
+    }
+    float so = 0.f, sn = 0.f, sa = 0.f;
+    for (int b = b0 + tl; b < b0 + lenj; b += T) {
+      const float4 ob = P.aoff[b];
+      const float2 qb = P.aeq[b];
+      if (f & kInOld) {
+        const float bx = A.x + ob.x, by = A.y + ob.y, bz = A.z + ob.z;
+        so += (f & kWrapOld) ? sum_moved32_wrap(s.o_old, s.eq, mi.len, bx, by, bz, ob.w, qb, H, sa)
+                             : sum_moved32_cf(s.o_old, s.eq, mi.len, false, bx, by, bz, ob.w, qb,
+                                              mi.qm, sa);
+      }
+      if (f & kInNew) {
+        const float bx = A.w + ob.x, by = B.x + ob.y, bz = B.y + ob.z;
+        sn += (f & kWrapNew) ? sum_moved32_wrap(s.o_new, s.eq, mi.len, bx, by, bz, ob.w, qb, H, sa)
+                             : sum_moved32_cf(s.o_new, s.eq, mi.len, true, bx, by, bz, ob.w, qb,
+                                              mi.qm, sa);
+      }
+    }
+    for (int off = T >> 1; off > 0; off >>= 1) {
+      so += __shfl_xor_sync(~0u, so, off);
+      sn += __shfl_xor_sync(~0u, sn, off);
+      sa += __shfl_xor_sync(~0u, sa, off);
+    }
+    if (tl == 0 && f) {
+      if (f & kInOld) { eo += (double)so; np += (long long)mi.act * actj; }
+      if (f & kInNew) { en += (double)sn; np += (long long)mi.act * actj; }
+      ab += (double)sa;
+    }
+  }
+}
+
+// FP64 pair terms from the master rows, the reference's per-pair minimum
+// image and dummy-site rule (BruteForceStep.cpp:61-76).
+__device__ __forceinline__ double sum_moved64(const GroupSmem& s, bool use_new, int len, double xb,
+                                              double yb, double zb, double sb, double eb, double qb,
+                                              const ChainHdr& H) {
+  const double* xs = use_new ? s.nx : s.ox;
+  const double* ys = use_new ? s.ny : s.oy;
+  const double* zs = use_new ? s.nz : s.oz;
+  double acc = 0.0;
+  for (int i = 0; i < len; i++) {
+    const double sa = s.sd[i], ea = s.ed[i];
+    if (!(sa >= 0 && sb >= 0 && ea >= 0 && eb >= 0)) continue;
+    const double dx = make_periodic(xb - xs[i], H.L[0]);
+    const double dy = make_periodic(yb - ys[i], H.L[1]);
+    const double dz = make_periodic(zb - zs[i], H.L[2]);
+    const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    acc += pair64(r2, sa, sb, ea, eb, s.qd[i], qb);
+  }
+  return acc;
+}
+
+__device__ __forceinline__ void batch_f64(const Pool& P, const ChainHdr& H, const GroupSmem& s,
+                                          const MovedInfo& mi, const int* rj, int head, int count,
+                                          int lane, int T, double& eo, double& en, double& ab,
+                                          long long& np) {
+  const int tm = lane / T, tl = lane - tm * T, nteams = 32 / T;
+  for (int e0 = 0; e0 < count; e0 += nteams) {
+    const int e = e0 + tm;
+    int f = 0, b0 = 0, lenj = 0, actj = 0;
+    if (e < count) {
+      const int jf = rj[(head + e) & (kRing - 1)];
+      const int j = jf >> 4;
+      f = jf & 15;
+      b0 = P.mstart[j];
+      const int lw = P.mlen[j];
+      lenj = lw & 255;
+      actj = lw >> 8;
+    }
+    double so = 0.0, sn = 0.0;
+    for (int b = b0 + tl; b < b0 + lenj; b += T) {
+      const double xb = P.x[b], yb = P.y[b], zb = P.z[b];
+      const double sb = P.sig[b], eb = P.eps[b], qb = P.q[b];
+      if (f & kInOld) so += sum_moved64(s, false, mi.len, xb, yb, zb, sb, eb, qb, H);
+      if (f & kInNew) sn += sum_moved64(s, true, mi.len, xb, yb, zb, sb, eb, qb, H);
+    }
+    for (int off = T >> 1; off > 0; off >>= 1) {
+      so += __shfl_xor_sync(~0u, so, off);
+      sn += __shfl_xor_sync(~0u, sn, off);
+    }
+    if (tl == 0 && f) {
+      if (f & kInOld) { eo += so; np += (long long)mi.act * actj; }
+      if (f & kInNew) { en += sn; np += (long long)mi.act * actj; }
+      ab += fabs(so) + fabs(sn);
+    }
+  }
+}
+
+// One warp screens candidates [c_begin, c_end) in warp-strided rounds of 32
+// (round r of warp w covers c_begin + (r*nw + w)*32 + lane), appends hits to
+// its ring and evaluates them in batches of 32.
+template <bool F64>
+__device__ void warp_eval(const Pool& P, const ChainHdr& H, const GroupSmem& s, const MovedInfo& mi,
+                          int c_begin, int c_end, int w, int nw, int lane, int T, double& eo,
+                          double& en, double& ab, long long& np) {
+  int* rj = s.lj + w * kRing;
+  float4* rA = s.lA + w * kRing;
+  float2* rB = s.lB + w * kRing;
+  int head = 0, tail = 0;
+  const unsigned lt = lanemask_lt();
+  for (int base = c_begin + w * 32; base < c_end; base += nw * 32) {
+    const int j = base + lane;
+    int f = 0;
+    float4 A;
+    float2 B;
+    if (j < c_end && j != mi.mol) {
+      if (F64)
+        f = screen_f64(P, H, s, mi, j);
+      else
+        f = screen_mixed(P, H, s, mi, j, A, B);
+    }
+    const unsigned bal = __ballot_sync(~0u, f != 0);
+    if (f) {
+      const int pos = (tail + __popc(bal & lt)) & (kRing - 1);
+      rj[pos] = (j << 4) | f;
+      if (!F64) {
+        rA[pos] = A;
+        rB[pos] = B;
+      }
+    }
+    tail += __popc(bal);
+    if (tail - head >= 32) {
+      __syncwarp();
+      if (F64)
+        batch_f64(P, H, s, mi, rj, head, 32, lane, T, eo, en, ab, np);
+      else
+        batch_mixed(P, H, s, mi, rj, rA, rB, head, 32, lane, T, eo, en, ab, np);
+      head += 32;
+      __syncwarp();
+    }
+  }
+  __syncwarp();
+  if (tail > head) {
+    if (F64)
+      batch_f64(P, H, s, mi, rj, head, tail - head, lane, T, eo, en, ab, np);
+    else
+      batch_mixed(P, H, s, mi, rj, rA, rB, head, tail - head, lane, T, eo, en, ab, np);
+  }
+  __syncwarp();
+}
+
+// Group-wide deterministic sum of (a, b, d, c): warp shuffles, then every
+// thread adds the per-warp values in warp order.  Two calls must be
+// separated by a group barrier (the scratch is reused).
+__device__ __forceinline__ void group_reduce(const Group& g, const GroupSmem& s, double& a,
+                                             double& b, double& d, long long& c) {
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_xor_sync(~0u, a, off);
+    b += __shfl_xor_sync(~0u, b, off);
+    d += __shfl_xor_sync(~0u, d, off);
+    c += __shfl_xor_sync(~0u, c, off);
+  }
+  const int nw = g.nwarps();
+  if ((g.tid & 31) == 0) {
+    s.red[g.warp()] = a;
+    s.red[nw + g.warp()] = b;
+    s.red[2 * nw + g.warp()] = d;
+    s.redl[g.warp()] = c;
+  }
+  g.sync();
+  a = 0.0;
+  b = 0.0;
+  d = 0.0;
+  c = 0;
+  for (int w = 0; w < nw; w++) {
+    a += s.red[w];
+    b += s.red[nw + w];
+    d += s.red[2 * nw + w];
+    c += s.redl[w];
+  }
+}
+
+// Writes the staged new placement of the moved molecule to the pool
+// (master rows and mirrors); lanes of one warp.
+__device__ __forceinline__ void commit(const Pool& P, const GroupSmem& s, const MovedInfo& mi,
+                                       int lane) {
+  for (int i = lane; i < mi.len; i += 32) {
+    const int a = mi.atom0 + i;
+    P.x[a] = s.nx[i];
+    P.y[a] = s.ny[i];
+    P.z[a] = s.nz[i];
+    P.aoff[a] = s.o_new[i];
+  }
+  const int2 pi = P.mpi[mi.mol];
+  for (int k = lane; k < mi.npidx; k += 32) P.ppos[pi.x + k] = s.p_new[k];
+  if (lane == 0) P.mfix[mi.mol] = mi.fx_new;
+}
+
+// Recomputes molecule m's mirrors (offsets, screen positions, fixed-point
+// anchor) from its master rows; lanes [lane, nl).
+__device__ __forceinline__ void refresh_molecule(const Pool& P, const ChainHdr& H, int m, int lane,
+                                                 int nl) {
+  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
+  const int2 pi = P.mpi[m];
+  const int an = P.pidx[pi.x];
+  const double ax = P.x[an], ay = P.y[an], az = P.z[an];
+  for (int i = lane; i < len; i += nl) {
+    const int a = a0 + i;
+    const float w = P.aoff[a].w;
+    P.aoff[a] = make_float4((float)(P.x[a] - ax), (float)(P.y[a] - ay), (float)(P.z[a] - az), w);
+  }
+  for (int k = lane; k < pi.y; k += nl) {
+    const int q = P.pidx[pi.x + k];
+    P.ppos[pi.x + k] = wrap_pos(P.x[q], P.y[q], P.z[q], H);
+  }
+  if (lane == 0) P.mfix[m] = fixpos(ax, ay, az, H);
+}
+
+}  // namespace mcgpu

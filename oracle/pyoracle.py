@@ -1,0 +1,257 @@
+"""ctypes wrapper of the oracle (TEST INFRASTRUCTURE ONLY).
+
+* ``OracleBox``   the C restatement (oracle/mcgpu_oracle.c, built into
+                  oracle/_build/liboracle.so) over a BoxData's rows.
+* ``RefHarness``  the reference's own compiled CPU path plus the white-box
+                  harness (oracle/_ref/libmcgpu_ref.so); present only where
+                  the reference sources were available to compile.
+
+Only tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+this module, and only as the checker or the timed CPU baseline.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "_build" / "liboracle.so"
+REF_SO = HERE / "_ref" / "libmcgpu_ref.so"
+REF_BIN = HERE / "_ref" / "metrosim"
+REFERENCE_SRC = Path(os.environ.get("MCGPU_REFERENCE", "/root/reference"))
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+class OrcBox(C.Structure):
+    _fields_ = [
+        ("n_mol", C.c_int), ("n_atom", C.c_int), ("n_pidx", C.c_int), ("largest_mol", C.c_int),
+        ("x", _dp), ("y", _dp), ("z", _dp),
+        ("sigma", _dp), ("epsilon", _dp), ("charge", _dp),
+        ("mol_start", _ip), ("mol_len", _ip), ("mol_pidx_start", _ip), ("mol_pidx_count", _ip),
+        ("pidx", _ip),
+        ("rb_x", _dp), ("rb_y", _dp), ("rb_z", _dp),
+        ("size", C.c_double * 3),
+        ("cutoff", C.c_double), ("kT", C.c_double), ("max_translate", C.c_double),
+        ("max_rotate", C.c_double),
+    ]
+
+
+class OrcMove(C.Structure):
+    _fields_ = [("mol", C.c_int), ("vertex", C.c_int), ("mode", C.c_int), ("pad", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("r0", C.c_double), ("r1", C.c_double), ("r2", C.c_double), ("r3", C.c_double),
+                ("u", C.c_double)]
+
+
+class OrcTrace(C.Structure):
+    _fields_ = [("mol", C.c_int), ("accepted", C.c_int), ("e_old", C.c_double),
+                ("e_new", C.c_double), ("de", C.c_double), ("u", C.c_double)]
+
+
+def build(reference: bool = True) -> None:
+    """Compiles the restatement and, where the reference sources exist, the
+    reference harness."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "all"], check=True)
+    if reference and REFERENCE_SRC.is_dir():
+        subprocess.run(["make", "-s", "-j8", "-C", str(HERE), "ref", f"REF={REFERENCE_SRC}"],
+                       check=True)
+
+
+_orc = None
+
+
+def orc_lib() -> C.CDLL:
+    global _orc
+    if _orc is None:
+        if not ORACLE_SO.exists():
+            build(reference=False)
+        L = C.CDLL(str(ORACLE_SO))
+        P = C.POINTER(OrcBox)
+        protos = {
+            "orc_mol_energy": (C.c_double, [P, C.c_int, C.c_int]),
+            "orc_system_energy": (C.c_double, [P]),
+            "orc_mol_energy_abs": (C.c_double, [P, C.c_int, C.c_int]),
+            "orc_mol_pair_energy": (C.c_double, [P, C.c_int, C.c_int]),
+            "orc_count_pairs": (C.c_int, [P, C.c_int, C.POINTER(C.c_longlong),
+                                          C.POINTER(C.c_longlong)]),
+            "orc_apply_move": (None, [P, C.POINTER(OrcMove)]),
+            "orc_rollback": (None, [P, C.c_int]),
+            "orc_keep_in_box": (None, [P, C.c_int]),
+            "orc_wrap_all": (None, [P]),
+            "orc_accept": (C.c_int, [C.c_double, C.c_double, C.c_double]),
+            "orc_random_real": (C.c_double, [C.c_double, C.c_double, C.c_int]),
+            "orc_make_periodic": (C.c_double, [C.c_double, C.c_double]),
+            "orc_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                         C.POINTER(C.c_uint32)]),
+            "orc_philox_move": (None, [C.c_uint64, C.c_uint32, C.c_uint64, C.c_int, _ip,
+                                       C.c_double, C.c_double, C.c_int, C.POINTER(OrcMove)]),
+            "orc_chain_run": (C.c_double, [P, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int, C.c_int,
+                                           C.c_double, C.POINTER(OrcTrace),
+                                           C.POINTER(C.c_longlong)]),
+            "orc_chains_run_mt": (C.c_double, [P, C.c_int, C.POINTER(C.c_uint64), C.c_uint64,
+                                               C.c_int, C.c_int, C.c_int,
+                                               C.POINTER(C.c_longlong)]),
+            "orc_resize_box_centres": (None, [P, C.c_double]),
+            "orc_accept_volume": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double,
+                                            C.c_int, C.c_double, C.c_double]),
+        }
+        for name, (res, args) in protos.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _orc = L
+    return _orc
+
+
+KBOLTZ = 0.00198717
+
+
+class OracleBox:
+    """An FP64 box the restatement mutates in place (numpy rows)."""
+
+    def __init__(self, box):
+        b = box.copy().normalise()
+        self.data = b
+        self.largest = int(b.mol_len.max())
+        self.rb = [np.zeros(self.largest) for _ in range(3)]
+        s = OrcBox()
+        s.n_mol, s.n_atom, s.n_pidx, s.largest_mol = b.n_mol, b.n_atom, b.n_pidx, self.largest
+        for k in ("x", "y", "z", "sigma", "epsilon", "charge"):
+            setattr(s, k, getattr(b, k).ctypes.data_as(_dp))
+        for k in ("mol_start", "mol_len", "mol_pidx_start", "mol_pidx_count", "pidx"):
+            setattr(s, k, getattr(b, k).ctypes.data_as(_ip))
+        s.rb_x, s.rb_y, s.rb_z = (r.ctypes.data_as(_dp) for r in self.rb)
+        for i in range(3):
+            s.size[i] = float(b.size[i])
+        s.cutoff = b.cutoff
+        s.kT = b.temperature * KBOLTZ
+        s.max_translate = b.max_translate
+        s.max_rotate = b.max_rotate
+        self.s = s
+
+    @property
+    def ref(self):
+        return C.byref(self.s)
+
+    def mol_energy(self, curr: int, start: int = 0) -> float:
+        return orc_lib().orc_mol_energy(self.ref, curr, start)
+
+    def system_energy(self) -> float:
+        return orc_lib().orc_system_energy(self.ref)
+
+    def mol_energy_abs(self, curr: int, start: int = 0) -> float:
+        return orc_lib().orc_mol_energy_abs(self.ref, curr, start)
+
+    def count_pairs(self, curr: int) -> tuple[int, int]:
+        a, b = C.c_longlong(), C.c_longlong()
+        orc_lib().orc_count_pairs(self.ref, curr, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def apply_move(self, mol, vertex, dx, dy, dz, r0, r1, r2, r3=0.0, mode=0) -> None:
+        mv = OrcMove(int(mol), int(vertex), int(mode), 0, dx, dy, dz, r0, r1, r2, r3, 0.0)
+        orc_lib().orc_apply_move(self.ref, C.byref(mv))
+
+    def rollback(self, mol: int) -> None:
+        orc_lib().orc_rollback(self.ref, int(mol))
+
+    def coords(self) -> np.ndarray:
+        return np.stack([self.data.x, self.data.y, self.data.z], axis=1).copy()
+
+    def philox_move(self, seed: int, chain: int, step: int, mode: int) -> OrcMove:
+        mv = OrcMove()
+        b = self.data
+        orc_lib().orc_philox_move(int(seed) & (2 ** 64 - 1), int(chain), int(step), b.n_mol,
+                                  b.mol_len.ctypes.data_as(_ip), b.max_translate, b.max_rotate,
+                                  int(mode), C.byref(mv))
+        return mv
+
+    def chain_run(self, seed: int, chain: int, n_steps: int, mode: int, e0: float = 0.0,
+                  step0: int = 0):
+        tr = (OrcTrace * max(1, n_steps))()
+        acc = C.c_longlong()
+        e = orc_lib().orc_chain_run(self.ref, int(seed) & (2 ** 64 - 1), int(chain), int(step0),
+                                    int(n_steps), int(mode), float(e0), tr, C.byref(acc))
+        return e, acc.value, list(tr)[:n_steps]
+
+
+def philox(ctr, key) -> list[int]:
+    c = (C.c_uint32 * 4)(*[int(v) & 0xFFFFFFFF for v in ctr])
+    k = (C.c_uint32 * 2)(*[int(v) & 0xFFFFFFFF for v in key])
+    o = (C.c_uint32 * 4)()
+    orc_lib().orc_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def chains_run_mt(boxes: list[OracleBox], seeds, n_steps: int, mode: int, threads: int,
+                  step0: int = 0) -> int:
+    """Advances every chain by n_steps (steps step0 .. step0 + n_steps - 1 of
+    its Philox stream) on `threads` host threads; returns the moves made."""
+    n = len(boxes)
+    arr = (OrcBox * n)(*[b.s for b in boxes])
+    sd = (C.c_uint64 * n)(*[int(s) & (2 ** 64 - 1) for s in seeds])
+    moves = C.c_longlong()
+    orc_lib().orc_chains_run_mt(arr, n, sd, int(step0), int(n_steps), int(mode), int(threads),
+                                C.byref(moves))
+    return moves.value
+
+
+class RefHarness:
+    """The reference's own CPU path (compiled from its sources) behind the
+    white-box harness.  One global SimBox per process (the reference keeps
+    its state in globals: SimCalcs::sb, GPUCopy's row tables, rand())."""
+
+    def __init__(self):
+        if not REF_SO.exists():
+            raise FileNotFoundError(f"{REF_SO} not built (needs the reference sources)")
+        L = C.CDLL(str(REF_SO))
+        protos = {
+            "ref_box_create": (C.c_int, [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp,
+                                         _ip, _ip, _ip, _ip, _ip, _dp, C.c_double, C.c_double,
+                                         C.c_double, C.c_double]),
+            "ref_mol_energy": (C.c_double, [C.c_int, C.c_int]),
+            "ref_system_energy": (C.c_double, []),
+            "ref_apply_move": (None, [C.c_int, C.c_int] + [C.c_double] * 6),
+            "ref_intermolecular_move": (None, [C.c_int]),
+            "ref_rollback": (None, [C.c_int]),
+            "ref_accept": (C.c_int, [C.c_double]),
+            "ref_choose_molecule": (C.c_int, []),
+            "ref_seed": (None, [C.c_int]),
+            "ref_rand": (C.c_int, []),
+            "ref_wrap_all": (None, []),
+            "ref_get_coords": (None, [_dp, _dp, _dp]),
+            "ref_run_plain": (C.c_double, [C.c_int, C.c_double, C.POINTER(C.c_int)]),
+        }
+        for name, (res, args) in protos.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        self.L = L
+        self.n_atom = 0
+
+    def load(self, box) -> None:
+        b = box.copy().normalise()
+        self._keep = b
+        size = np.ascontiguousarray(b.size, dtype=np.float64)
+        self._size = size
+        self.L.ref_box_create(b.n_mol, b.n_atom, b.n_pidx, *(getattr(b, k).ctypes.data_as(_dp)
+                              for k in ("x", "y", "z", "sigma", "epsilon", "charge")),
+                              *(getattr(b, k).ctypes.data_as(_ip) for k in
+                                ("mol_start", "mol_len", "mol_pidx_start", "mol_pidx_count",
+                                 "pidx")),
+                              size.ctypes.data_as(_dp), b.cutoff, b.temperature,
+                              b.max_translate, b.max_rotate)
+        self.n_atom = b.n_atom
+
+    def coords(self) -> np.ndarray:
+        x, y, z = np.empty(self.n_atom), np.empty(self.n_atom), np.empty(self.n_atom)
+        self.L.ref_get_coords(x.ctypes.data_as(_dp), y.ctypes.data_as(_dp), z.ctypes.data_as(_dp))
+        return np.stack([x, y, z], axis=1)
+
+    def __getattr__(self, name):
+        return getattr(self.L, "ref_" + name)

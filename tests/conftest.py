@@ -1,0 +1,15 @@
+"""Test configuration: the ``gpu`` marker and import paths.
+
+``-m "not gpu"`` runs on any host (oracle vs golden vectors, host logic, the
+C ABI's load and exports); ``-m gpu`` needs a GB300 and calls through the
+C ABI of the CUDA library."""
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")

@@ -1,0 +1,74 @@
+"""The C-ABI library loads and exports every entry point its header
+declares; calls that need no GPU behave (no compute runs here)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from mcgpu_gb300 import _abi
+
+HEADERS = sorted((Path(__file__).resolve().parents[1] / "include").glob("*.h"))
+
+
+def declared():
+    names = set()
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names |= set(re.findall(r"^\s*(?:const\s+)?\w[\w\s\*]*?\b(mcgpu_\w+)\s*\(", text, re.M))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared()
+    assert "mcgpu_mol_energy" in names and "mcgpu_batch_run" in names
+    assert len(names) >= 20
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _abi.lib()
+    missing = [n for n in declared() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header():
+    assert set(declared()) <= set(_abi.exported_symbols())
+
+
+def test_version_string():
+    assert b"sm_103a" in _abi.lib().mcgpu_version()
+
+
+def test_errors_are_status_codes_without_gpu():
+    lib = _abi.lib()
+    h = C.c_void_p()
+    st = lib.mcgpu_ctx_create(C.byref(h), 0)
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    assert st in (2, 4)
+    buf = C.create_string_buffer(256)
+    assert lib.mcgpu_last_error(None, buf, 256) == 0
+    assert buf.value
+
+
+def test_null_arguments_rejected():
+    lib = _abi.lib()
+    assert lib.mcgpu_ctx_create(None, 0) == 1
+    assert lib.mcgpu_box_upload(None, None, 0, None) == 1
+    assert lib.mcgpu_mol_energy(None, 0, 0, None) == 1
+    assert lib.mcgpu_batch_run(None, 1, 1) == 1
+
+
+def test_build_centres_min_distance():
+    out = np.empty((500, 3))
+    rc = _abi.lib().mcgpu_build_centres(500, 25.0, 2.5, 123, out.ctypes.data_as(
+        C.POINTER(C.c_double)))
+    assert rc == 0
+    assert out.min() >= 0 and out.max() < 25.0
+    d = out[:, None] - out[None]
+    d -= 25.0 * np.rint(d / 25.0)
+    r = np.sqrt((d ** 2).sum(-1))
+    np.fill_diagonal(r, 99)
+    assert r.min() >= 2.5

@@ -1,0 +1,52 @@
+"""Synthetic boxes have the configured shape (sizes, density, geometry)."""
+import numpy as np
+
+from mcgpu_gb300 import workloads as W
+
+
+def test_water_box_c0_shape():
+    b = W.water_box(256, L=19.71)
+    assert b.n_mol == 256 and b.n_atom == 768 and b.n_pidx == 256
+    assert np.allclose(b.size, 19.71)
+    o = np.stack([b.x[b.pidx], b.y[b.pidx], b.z[b.pidx]], 1)
+    assert o.min() >= 0 and o.max() <= 19.71
+    d = o[:, None] - o[None]
+    d -= 19.71 * np.rint(d / 19.71)
+    r = np.sqrt((d ** 2).sum(-1))
+    np.fill_diagonal(r, 99)
+    assert r.min() >= 2.5
+    # rigid geometry: r_OH and the HOH angle
+    h1 = np.stack([b.x[1::3], b.y[1::3], b.z[1::3]], 1) - o
+    h2 = np.stack([b.x[2::3], b.y[2::3], b.z[2::3]], 1) - o
+    assert np.allclose(np.linalg.norm(h1, axis=1), 0.9572)
+    ang = np.degrees(np.arccos((h1 * h2).sum(1) / 0.9572 ** 2))
+    assert np.allclose(ang, 104.52)
+
+
+def test_bicyclic_template():
+    xyz, sig, eps, q, prim = W.bicyclic_template()
+    assert xyz.shape == (16, 3) and abs(q.sum()) < 1e-12
+    # drawn in [-0.3, 0.3], then shifted by the mean to make the molecule neutral
+    assert (np.abs(q) <= 0.6).all() and np.ptp(q) <= 0.6
+    assert sig[prim] == 3.25 and eps[prim] == 0.17
+    heavy = xyz[:9]
+    d = np.linalg.norm(heavy[:, None] - heavy[None], axis=-1)
+    bonds = np.sort(d[np.triu_indices(9, 1)])[:10]   # 6 + 5 - 1 ring bonds
+    assert np.allclose(bonds, 1.40, atol=1e-9)
+    assert np.allclose(xyz[:, 2], 0.0)                # planar
+
+
+def test_water_chains_distribution():
+    boxes, seeds = W.water_chains(16, seed=3)
+    assert len(boxes) == 16 and len(set(int(s) for s in seeds)) == 16
+    for b in boxes:
+        assert 64 <= b.n_mol <= 2048
+        assert abs(b.n_mol / b.size[0] ** 3 - W.WATER_DENSITY) < 1e-9
+        assert b.cutoff <= 9.0 and b.cutoff <= b.size[0] / 2 + 1e-12
+        assert 280 <= b.temperature <= 360
+
+
+def test_generators_are_seeded():
+    a, b = W.water_box(100, seed=5), W.water_box(100, seed=5)
+    assert np.array_equal(a.x, b.x)
+    assert not np.array_equal(a.x, W.water_box(100, seed=6).x)
