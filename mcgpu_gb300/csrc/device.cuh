@@ -319,11 +319,19 @@ __device__ __forceinline__ float rcp_approx(float x) {
   return y;
 }
 
-// LJ part of a pair term from per-atom factors (sigma, 2sqrt|eps|) and the
-// refined 1/r: 4 eps (s^12 - s^6), s = sigma_ab^2 / r^2 with geometric
-// blending (SimulationStep.cpp:344-358, :369-375).
-__device__ __forceinline__ float lj32(float ir, float sa, float sb, float ea, float eb) {
-  const float ir2 = ir * ir;
+// 1/r2 to about one ulp: hardware reciprocal estimate refined by one
+// Newton-Raphson step y' = y (2 - r2 y).
+__device__ __forceinline__ float rcp_nr(float r2) {
+  const float y = rcp_approx(r2);
+  return y * fmaf(-r2, y, 2.0f);
+}
+
+// LJ part of a pair term from per-atom factors (sigma, 2sqrt|eps|) and
+// 1/r2: 4 eps (s^12 - s^6), s = sigma_ab^2 / r^2 with geometric blending
+// (SimulationStep.cpp:344-358, :369-375).  The r^-12 term amplifies the
+// relative error of s twelvefold, so s is formed from a refined 1/r2 (one
+// rounding) rather than from (1/r)^2.
+__device__ __forceinline__ float lj32(float ir2, float sa, float sb, float ea, float eb) {
   const float t = (sa * sb) * ir2;
   const float t3 = t * t * t;
   return (ea * eb) * fmaf(t3, t3, -t3);

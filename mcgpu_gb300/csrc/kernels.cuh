@@ -253,7 +253,7 @@ __device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4*
     const float dz = wrapf(bz - a.z, H.Lf[2]);
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float ir = rsqrt_nr(r2);
-    const float lj = lj32(ir, a.w, sb, ea.x, qb.x);
+    const float lj = lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x);
     const float cl = (ea.y * qb.y) * ir;
     const bool ok = r2 > 0.f;
     acc += ok ? lj + cl : 0.f;
@@ -284,7 +284,7 @@ __device__ __forceinline__ float sum_moved32_cf(const float4* o, const float4* e
     const float dx = bx - a.x, dy = by - a.y, dz = bz - a.z;
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float ir = rsqrt_nr(r2);
-    const float lj = lj32(ir, a.w, sb, ea.x, qb.x);
+    const float lj = lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x);
     const float num = fmaf(tx, a.x, fmaf(ty, a.y, fmaf(tz, a.z, -(use_new ? ea.w : ea.z))));
     const float w = ir * rcp_approx(fmaf(r2, ir, R));
     const bool ok = r2 > 0.f;

@@ -119,9 +119,10 @@ double orc_mol_energy(const orc_box* b, int curr, int start) {
   return total;
 }
 
-/* Sum of |LJ| + |Coulomb| over the pair terms orc_mol_energy adds: the
- * scale of the cancellation in a molecule energy, used to set the
- * tolerance of FP32-pair results (|err| <= 1e-5 * max(|E|, 1e-3 * this)). */
+/* Sum of the magnitudes of the terms orc_mol_energy adds (per atom pair:
+ * 4 eps s^12, 4 eps s^6 and |Coulomb|): the scale of the cancellation in a
+ * molecule energy, used to set the tolerance of FP32-pair results
+ * (|err| <= 1e-5 * max(|E|, 1e-3 * this)). */
 double orc_mol_energy_abs(const orc_box* b, int curr, int start) {
   double total = 0;
   const int p1s = b->mol_pidx_start[curr];
@@ -139,7 +140,11 @@ double orc_mol_energy_abs(const orc_box* b, int curr, int start) {
           continue;
         const double r2 = orc_atom_dist2(b, i, j);
         if (r2 == 0.0) continue;
-        total += fabs(orc_lj(b, i, j, r2)) + fabs(orc_charge(b, i, j, sqrt(r2)));
+        /* the three terms of the pair energy: 4 eps s^12, -4 eps s^6, Coulomb */
+        const double sig = orc_blend(b->sigma[i], b->sigma[j]);
+        const double eps = orc_blend(b->epsilon[i], b->epsilon[j]);
+        const double s6 = pow(pow(sig, 2) / r2, 3);
+        total += 4.0 * eps * s6 * s6 + 4.0 * eps * s6 + fabs(orc_charge(b, i, j, sqrt(r2)));
       }
   }
   return total;
