@@ -26,6 +26,8 @@ __global__ void k_set_energy(Pool P, const double* e);
 __global__ void k_chain_steps(Pool P, int n_steps, unsigned* queue, const int* order, int n_tasks,
                               int gwarps, SmemShape shape, mcgpu_trace* trace, int trace_off,
                               int trace_stride);
+__global__ void k_chain_init(Pool P, const int* mol_chain, int n_mol_total);
+__global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol, int n_atom);
 cudaError_t launch_mol_energy(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
                               Pool P, int chain, int curr, int start, double* partials,
                               unsigned* counter, double* out);
@@ -85,7 +87,7 @@ struct HostPool {
   std::vector<double> x, y, z, sig, eps, q;
   std::vector<float4> aoff;
   std::vector<float2> aeq;
-  std::vector<int> mstart, mlen, pidx, mol_chain;
+  std::vector<int> mstart, mlen, pidx, mol_chain, atom_mol;
   std::vector<int2> mpi;
   std::vector<float> mrad;
   std::vector<ChainHdr> hdr;
@@ -129,6 +131,7 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
   }
   int max_len = 0;
   double max_rad = 0;
+  bool simple = d->n_pidx == d->n_mol;
   for (int m = 0; m < d->n_mol; m++) {
     const int s = d->mol_start[m], len = d->mol_len[m];
     const int ps = d->mol_pidx_start[m], pc = d->mol_pidx_count[m];
@@ -165,7 +168,15 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
     hp.mpi.push_back(make_int2(pidx0 + ps, pc));
     hp.mrad.push_back((float)(rad * (1 + 1e-6) + 1e-4));
     hp.mol_chain.push_back(c);
+    if (ps != m || pc != 1) simple = false;
   }
+  hp.atom_mol.resize(hp.x.size(), -1);
+  for (int m = 0; m < d->n_mol; m++)
+    for (int a = d->mol_start[m]; a < d->mol_start[m] + d->mol_len[m]; a++)
+      hp.atom_mol[atom0 + a] = mol0 + m;
+  for (int a = 0; a < d->n_atom; a++)
+    if (hp.atom_mol[atom0 + a] < 0)
+      return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: atom %d belongs to no molecule", c, a);
   const double Lmin = std::min(d->size[0], std::min(d->size[1], d->size[2]));
   if (max_rad >= 0.25 * Lmin)
     return set_err(ctx, MCGPU_ERR_UNSUPPORTED,
@@ -187,6 +198,7 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
   h.tpm = T;
   h.rot_mode = rot_mode;
   h.chain_id = (int)c;
+  h.simple_prim = simple ? 1 : 0;
   const double rc = d->cutoff;
   double ulpL = std::ldexp(1.0, (int)std::floor(std::log2(std::max(
                                     d->size[0], std::max(d->size[1], d->size[2])))) - 23);
@@ -198,7 +210,9 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
     h.Lf[k] = (float)d->size[k];
     h.fxinv[k] = 4294967296.0 / d->size[k];
     h.fxs[k] = (float)(d->size[k] / 4294967296.0);
+    h.fxinvf[k] = (float)(4294967296.0 / d->size[k]);
   }
+  h.kTinvf = (float)(1.0 / (d->temperature * kBoltz));
   h.cutoff = rc;
   h.kT = d->temperature * kBoltz;  // SimBoxBuilder.cpp:29
   h.max_t = d->max_translate;
@@ -213,6 +227,7 @@ struct DevPool {
   Pool P{};
   int n_chains = 0, n_mol = 0, n_atom = 0, n_pidx = 0, max_len = 0;
   int* mol_chain = nullptr;
+  int* atom_mol = nullptr;
   double* emol = nullptr;
   long long* pairs = nullptr;
   double* esum = nullptr;
@@ -221,12 +236,13 @@ struct DevPool {
 
   void release() {
     void* ptrs[] = {P.x, P.y, P.z, P.sig, P.eps, P.q, P.aoff, P.aeq, P.mstart, P.mlen, P.mpi,
-                    P.mfix, P.mrad, P.pidx, P.ppos, P.hdr, P.rb, P.trace, mol_chain, emol, pairs,
-                    esum};
+                    P.mfix, P.mrad, P.mq, P.atpl, P.pidx, P.ppos, P.hdr, P.rb, P.trace,
+                    mol_chain, atom_mol, emol, pairs, esum};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     P = Pool{};
     mol_chain = nullptr;
+    atom_mol = nullptr;
     emol = nullptr;
     pairs = nullptr;
     esum = nullptr;
@@ -247,12 +263,14 @@ int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
   P.aoff = dalloc<float4>(na, &e); P.aeq = dalloc<float2>(na, &e);
   P.mstart = dalloc<int>(nm, &e); P.mlen = dalloc<int>(nm, &e); P.mpi = dalloc<int2>(nm, &e);
   P.mfix = dalloc<uint4>(nm, &e); P.mrad = dalloc<float>(nm, &e);
+  P.mq = dalloc<float4>(nm, &e); P.atpl = dalloc<float4>(na, &e);
   P.pidx = dalloc<int>(np, &e); P.ppos = dalloc<float4>(np, &e);
   P.hdr = dalloc<ChainHdr>(nc, &e);
   P.rb = dalloc<double>(nc * 3 * (size_t)hp.max_len, &e);
   P.trace = nullptr;
   P.n_chains = (int)nc;
   dp.mol_chain = dalloc<int>(nm, &e);
+  dp.atom_mol = dalloc<int>(na, &e);
   dp.emol = dalloc<double>(nm, &e);
   dp.pairs = dalloc<long long>(nm, &e);
   dp.esum = dalloc<double>(nc, &e);
@@ -267,6 +285,7 @@ int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
   UP(P.aoff, hp.aoff); UP(P.aeq, hp.aeq);
   UP(P.mstart, hp.mstart); UP(P.mlen, hp.mlen); UP(P.mpi, hp.mpi); UP(P.mrad, hp.mrad);
   UP(P.pidx, hp.pidx); UP(P.hdr, hp.hdr); UP(dp.mol_chain, hp.mol_chain);
+  UP(dp.atom_mol, hp.atom_mol);
 #undef UP
   const int wpb = 8;
   k_refresh_mirrors<<<(int)((nm + wpb - 1) / wpb), wpb * 32, 0, st>>>(P, dp.mol_chain, (int)nm);
@@ -278,11 +297,41 @@ int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
   return MCGPU_OK;
 }
 
-SmemShape shape_for(int max_len, int nwarps) {
+SmemShape shape_for(int max_len, int nwarps, int cache_n = 0) {
   SmemShape s;
   s.maxA = std::max(max_len, 1);
   s.nwarps = nwarps;
+  s.cache_n = cache_n;
   return s;
+}
+
+// Largest chain whose primary screen positions a group caches in shared
+// memory (16 bytes per molecule).
+constexpr int kCacheMax = 4096;
+
+int pool_cache_n(const DevPool& dp) {
+  int n = 0;
+  for (const ChainHdr& h : dp.hdr) {
+    if (!h.simple_prim) return 0;
+    n = std::max(n, h.n_mol);
+  }
+  return n <= kCacheMax ? n : 0;
+}
+
+// Chain state from the FP64 rows (snaps the rows to it).
+int pool_chain_init(mcgpu_ctx* ctx, DevPool& dp, cudaStream_t st) {
+  const int wpb = 8;
+  k_chain_init<<<(dp.n_mol + wpb - 1) / wpb, wpb * 32, 0, st>>>(dp.P, dp.mol_chain, dp.n_mol);
+  CK(ctx, cudaGetLastError());
+  return MCGPU_OK;
+}
+
+// FP64 rows from the chain state.
+int pool_chain_export(mcgpu_ctx* ctx, DevPool& dp, cudaStream_t st) {
+  k_chain_export<<<(dp.n_atom + 255) / 256, 256, 0, st>>>(dp.P, dp.mol_chain, dp.atom_mol,
+                                                         dp.n_atom);
+  CK(ctx, cudaGetLastError());
+  return MCGPU_OK;
 }
 
 // Full system energy of every chain of the pool into dp.esum (device).
@@ -333,6 +382,12 @@ extern "C" int mcgpu_ctx_create(mcgpu_ctx** out, int device) {
     return set_err(nullptr, MCGPU_ERR_CUDA, "stream creation failed");
   }
   c->stream = c->own;
+  if (cudaFuncSetAttribute(k_chain_steps, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           200 * 1024) != cudaSuccess) {
+    cudaStreamDestroy(c->own);
+    delete c;
+    return set_err(nullptr, MCGPU_ERR_CUDA, "cannot enable large shared memory for the chain kernel");
+  }
   *out = c;
   return MCGPU_OK;
 }
@@ -376,7 +431,25 @@ struct mcgpu_box {
   int trace_cap = 0;
   unsigned* queue = nullptr;
   int* order = nullptr;
+  bool chain_state = false;  // pool holds a valid device-resident chain state
+  bool rows_stale = false;   // FP64 rows lag the chain state (export before use)
 };
+
+// FP64 rows current before a plain entry point reads them.
+static int box_rows(mcgpu_box* b) {
+  if (!b->rows_stale) return MCGPU_OK;
+  int rc = pool_chain_export(b->ctx, b->pool, b->ctx->stream);
+  if (rc) return rc;
+  b->rows_stale = false;
+  return MCGPU_OK;
+}
+
+// A plain entry point changed coordinates: the chain state and the running
+// energy must be rebuilt before the next device-resident run.
+static void box_plain_moved(mcgpu_box* b) {
+  b->chain_state = false;
+  b->energy_ready = false;
+}
 
 static int box_grid(const mcgpu_box* b, int n_cand) {
   int g = (n_cand + 127) / 128;
@@ -449,6 +522,8 @@ extern "C" int mcgpu_box_destroy(mcgpu_box* b) {
 extern "C" int mcgpu_box_download(mcgpu_box* b, double* x, double* y, double* z, double* size) {
   if (!b || !x || !y || !z) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
   mcgpu_ctx* ctx = b->ctx;
+  int rc = box_rows(b);
+  if (rc) return rc;
   const size_t n = (size_t)b->pool.n_atom;
   CK(ctx, cudaMemcpyAsync(x, b->pool.P.x, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaMemcpyAsync(y, b->pool.P.y, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
@@ -469,6 +544,8 @@ extern "C" int mcgpu_mol_energy(mcgpu_box* b, int curr, int start, double* out) 
     *out = 0.0;
     return MCGPU_OK;
   }
+  int rc = box_rows(b);
+  if (rc) return rc;
   const int nw = 4;
   SmemShape sh = shape_for(b->pool.max_len, nw);
   const int grid = box_grid(b, n - start);
@@ -499,6 +576,9 @@ extern "C" int mcgpu_change_molecule(mcgpu_box* b, int mol, const mcgpu_move* mv
   if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
   int rc = check_move(b, mol, mv);
   if (rc) return rc;
+  rc = box_rows(b);
+  if (rc) return rc;
+  box_plain_moved(b);
   mcgpu_ctx* ctx = b->ctx;
   SmemShape sh = shape_for(b->pool.max_len, 1);
   k_change_molecule<<<1, 32, sh.bytes(), ctx->stream>>>(b->pool.P, 0, mol, host_proposal(mv), sh);
@@ -512,6 +592,9 @@ extern "C" int mcgpu_rollback(mcgpu_box* b, int mol) {
   mcgpu_ctx* ctx = b->ctx;
   if (mol < 0 || mol >= b->pool.n_mol)
     return set_err(ctx, MCGPU_ERR_INVALID, "molecule %d out of [0,%d)", mol, b->pool.n_mol);
+  int rc = box_rows(b);
+  if (rc) return rc;
+  box_plain_moved(b);
   k_rollback<<<1, 32, 0, ctx->stream>>>(b->pool.P, 0, mol);
   CK(ctx, cudaGetLastError());
   CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -523,6 +606,9 @@ extern "C" int mcgpu_move_energies(mcgpu_box* b, int mol, const mcgpu_move* mv, 
   if (!b || !e_old || !e_new) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
   int rc = check_move(b, mol, mv);
   if (rc) return rc;
+  rc = box_rows(b);
+  if (rc) return rc;
+  box_plain_moved(b);
   mcgpu_ctx* ctx = b->ctx;
   const int nw = 4;
   SmemShape sh = shape_for(b->pool.max_len, nw);
@@ -540,7 +626,9 @@ extern "C" int mcgpu_move_energies(mcgpu_box* b, int mol, const mcgpu_move* mv, 
 extern "C" int mcgpu_system_energy(mcgpu_box* b, double* out) {
   if (!b || !out) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
   mcgpu_ctx* ctx = b->ctx;
-  int rc = pool_system_energy(ctx, b->pool, b->precision == MCGPU_PREC_FP64, ctx->stream);
+  int rc = box_rows(b);
+  if (rc) return rc;
+  rc = pool_system_energy(ctx, b->pool, b->precision == MCGPU_PREC_FP64, ctx->stream);
   if (rc) return rc;
   CK(ctx, cudaMemcpyAsync(b->hout, b->pool.esum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -563,8 +651,18 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
   int cid = (int)chain_id;
   CK(ctx, cudaMemcpyAsync(&dh->chain_id, &cid, 4, cudaMemcpyHostToDevice, st));
   CK(ctx, cudaMemcpyAsync(&dh->rot_mode, &rotation, 4, cudaMemcpyHostToDevice, st));
+  if (!b->chain_state) {
+    int rc = box_rows(b);
+    if (rc) return rc;
+    rc = pool_chain_init(ctx, dp, st);
+    if (rc) return rc;
+    b->chain_state = true;
+    b->energy_ready = false;
+  }
   if (!b->energy_ready) {
-    int rc = pool_system_energy(ctx, dp, true, st);
+    int rc = box_rows(b);
+    if (rc) return rc;
+    rc = pool_system_energy(ctx, dp, true, st);
     if (rc) return rc;
     k_set_energy<<<1, 32, 0, st>>>(dp.P, dp.esum);
     CK(ctx, cudaGetLastError());
@@ -576,8 +674,8 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
     CK(ctx, cudaMalloc((void**)&b->dtrace, sizeof(mcgpu_trace) * (size_t)n_steps));
     b->trace_cap = n_steps;
   }
-  const int nw = std::max(1, std::min(16, dp.n_mol / 256));
-  SmemShape sh = shape_for(dp.max_len, nw);
+  const int nw = std::max(1, std::min(8, dp.n_mol / 256));
+  SmemShape sh = shape_for(dp.max_len, nw, pool_cache_n(dp));
   const int seg = 1024;
   for (int done = 0; done < n_steps; done += seg) {
     const int k = std::min(seg, n_steps - done);
@@ -587,6 +685,7 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
     k_chain_steps<<<1, nw * 32, sh.bytes(), st>>>(P, k, b->queue, b->order, 1, nw, sh,
                                                   trace ? b->dtrace : nullptr, done, 0);
     CK(ctx, cudaGetLastError());
+    b->rows_stale = true;
   }
   if (trace && n_steps > 0)
     CK(ctx, cudaMemcpyAsync(trace, b->dtrace, sizeof(mcgpu_trace) * (size_t)n_steps,
@@ -614,6 +713,8 @@ struct mcgpu_batch {
   unsigned* queue = nullptr;   // one counter per launch slot of a graph
   int* order = nullptr;
   int threads = 128, cpc = 1, spl = 16;  // CTA threads, chains per CTA, steps per launch
+  int cache_n = 0;                        // shared-memory screen cache per group
+  bool rows_stale = false;                // FP64 rows lag the chain state
   int max_slots = 0;
   cudaGraphExec_t graph = nullptr;
   int graph_launches = 0, graph_spl = 0, graph_threads = 0, graph_cpc = 0;
@@ -625,7 +726,7 @@ static int batch_gwarps(const mcgpu_batch* bt) { return (bt->threads / 32) / bt-
 
 static int batch_grid(mcgpu_batch* bt, int* smem_out) {
   const int gw = batch_gwarps(bt);
-  SmemShape sh = shape_for(bt->pool.max_len, gw);
+  SmemShape sh = shape_for(bt->pool.max_len, gw, bt->cache_n);
   const int smem = sh.bytes() * bt->cpc;
   *smem_out = smem;
   int per_sm = 0;
@@ -641,7 +742,8 @@ static int batch_launch(mcgpu_batch* bt, int steps, unsigned* q, cudaStream_t st
   int smem = 0;
   const int grid = batch_grid(bt, &smem);
   const int gw = batch_gwarps(bt);
-  SmemShape sh = shape_for(bt->pool.max_len, gw);
+  SmemShape sh = shape_for(bt->pool.max_len, gw, bt->cache_n);
+  bt->rows_stale = true;
   CK(ctx, cudaMemsetAsync(q, 0, sizeof(unsigned), st));
   k_chain_steps<<<grid, bt->threads, smem, st>>>(bt->pool.P, steps, q, bt->order,
                                                  bt->pool.n_chains, gw, sh, trace, trace_off,
@@ -689,7 +791,14 @@ extern "C" int mcgpu_batch_create(mcgpu_ctx* ctx, int n_chains, const mcgpu_box_
     mcgpu_batch_destroy(bt);
     return set_err(ctx, MCGPU_ERR_NOMEM, "batch allocation failed: %s", cudaGetErrorString(e));
   }
-  // initial running energies: full FP64 system energy of every chain
+  bt->cache_n = pool_cache_n(bt->pool);
+  // device-resident chain state (rows snapped to it), then the initial
+  // running energies: full FP64 system energy of every chain
+  rc = pool_chain_init(ctx, bt->pool, ctx->stream);
+  if (rc) {
+    mcgpu_batch_destroy(bt);
+    return rc;
+  }
   rc = pool_system_energy(ctx, bt->pool, true, ctx->stream);
   if (rc) {
     mcgpu_batch_destroy(bt);
@@ -732,10 +841,8 @@ extern "C" int mcgpu_batch_set_tile(mcgpu_batch* bt, int threads, int cpc, int s
   if ((threads / 32) / cpc > 1 && cpc > 15)
     return set_err(ctx, MCGPU_ERR_INVALID, "at most 15 multi-warp groups per CTA");
   if (spl < 1) return set_err(ctx, MCGPU_ERR_INVALID, "steps per launch %d must be >= 1", spl);
-  int smem = shape_for(bt->pool.max_len, (threads / 32) / cpc).bytes() * cpc;
+  int smem = shape_for(bt->pool.max_len, (threads / 32) / cpc, bt->cache_n).bytes() * cpc;
   if (smem > 200 * 1024) return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "tile needs %d B shared memory", smem);
-  if (smem > 48 * 1024)
-    CK(ctx, cudaFuncSetAttribute(k_chain_steps, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
   bt->threads = threads;
   bt->cpc = cpc;
   bt->spl = spl;
@@ -862,6 +969,11 @@ extern "C" int mcgpu_batch_download(mcgpu_batch* bt, int chain, double* x, doubl
   mcgpu_ctx* ctx = bt->ctx;
   if (chain < 0 || chain >= bt->pool.n_chains)
     return set_err(ctx, MCGPU_ERR_INVALID, "chain %d out of [0,%d)", chain, bt->pool.n_chains);
+  if (bt->rows_stale) {
+    int rc = pool_chain_export(ctx, bt->pool, ctx->stream);
+    if (rc) return rc;
+    bt->rows_stale = false;
+  }
   const ChainHdr& h = bt->pool.hdr[chain];
   const size_t n = (size_t)h.n_atom;
   CK(ctx, cudaMemcpyAsync(x, bt->pool.P.x + h.atom0, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
@@ -874,6 +986,11 @@ extern "C" int mcgpu_batch_download(mcgpu_batch* bt, int chain, double* x, doubl
 extern "C" int mcgpu_batch_system_energy(mcgpu_batch* bt, double* out) {
   if (!bt || !out) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
   mcgpu_ctx* ctx = bt->ctx;
+  if (bt->rows_stale) {
+    int rc = pool_chain_export(ctx, bt->pool, ctx->stream);
+    if (rc) return rc;
+    bt->rows_stale = false;
+  }
   int rc = pool_system_energy(ctx, bt->pool, true, ctx->stream);
   if (rc) return rc;
   CK(ctx, cudaMemcpyAsync(out, bt->pool.esum, sizeof(double) * bt->pool.n_chains,
@@ -892,6 +1009,7 @@ static int batch_snapshot(mcgpu_batch* bt, bool restore) {
   struct Row { void* p; size_t bytes; } rows[] = {
       {dp.P.x, 8ull * dp.n_atom}, {dp.P.y, 8ull * dp.n_atom}, {dp.P.z, 8ull * dp.n_atom},
       {dp.P.aoff, 16ull * dp.n_atom}, {dp.P.mfix, 16ull * dp.n_mol}, {dp.P.ppos, 16ull * dp.n_pidx},
+      {dp.P.mq, 16ull * dp.n_mol},
       {dp.P.hdr, sizeof(ChainHdr) * (size_t)dp.n_chains}};
   const int nr = (int)(sizeof(rows) / sizeof(rows[0]));
   if (bt->snap.empty()) {

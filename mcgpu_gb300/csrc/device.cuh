@@ -50,19 +50,20 @@ enum : int {
   kErrNonFinite = 3,
 };
 
-// Per-chain header: 256 bytes, one per chain (a single box is chain 0).
+// Per-chain header, one per chain (a single box is chain 0).
 struct __align__(16) ChainHdr {
   int atom0, mol0, pidx0, n_mol;      // pool offsets and molecule count
   int n_atom, n_pidx, max_len, tpm;   // tpm: lanes per neighbour molecule
-  int rot_mode, chain_id, pad0, pad1b;
+  int rot_mode, chain_id, simple_prim, pad0;  // simple_prim: one primary per molecule
   float Lf[3], cut2_lo;               // FP32 box and guard band
   float fxs[3], cut2_hi;              // fixed point -> Angstrom scale
+  float fxinvf[3], kTinvf;            // Angstrom -> fixed point (FP32); 1/kT (FP32)
   double L[3], cutoff;
   double fxinv[3], kT;                // Angstrom -> fixed point scale
   double max_t, max_r, energy, pad1;
   unsigned long long seed, step;
   long long accepted, pairs;
-  int error, ties, pad3, pad4;   // ties: decisions re-taken with FP64 pairs
+  int error, ties, pad3, pad4;        // ties: decisions re-taken with FP64 pairs
 };
 static_assert(sizeof(ChainHdr) % 16 == 0, "ChainHdr alignment");
 
@@ -74,6 +75,8 @@ struct Pool {
   int2* mpi;
   uint4* mfix;
   float* mrad;
+  float4* mq;          // device-resident chains: unit quaternion (w, x, y, z)
+  float4* atpl;        // device-resident chains: template offsets R(q)^-1 o
   int* pidx;
   float4* ppos;
   ChainHdr* hdr;
@@ -241,10 +244,11 @@ struct GroupSmem {
   long long* redl;                      // [nwarps]
   int* misc;                            // [32] broadcast ints
   double* miscd;                        // [32] broadcast doubles
+  float4* pc;                           // [cache_n] screen positions of the chain (or null)
 };
 
 struct SmemShape {
-  int maxA, nwarps;
+  int maxA, nwarps, cache_n;
   __host__ __device__ static int align16(int v) { return (v + 15) & ~15; }
   __host__ __device__ int bytes() const {
     int b = 0;
@@ -260,6 +264,7 @@ struct SmemShape {
     b += align16(nwarps * 8);
     b += align16(32 * 4);
     b += align16(32 * 8);
+    b += align16(cache_n * 16);
     return b;
   }
   __device__ GroupSmem carve(char* base) const {
@@ -279,7 +284,8 @@ struct SmemShape {
     s.red = (double*)p; p += align16(3 * nwarps * 8);
     s.redl = (long long*)p; p += align16(nwarps * 8);
     s.misc = (int*)p; p += align16(32 * 4);
-    s.miscd = (double*)p;
+    s.miscd = (double*)p; p += align16(32 * 8);
+    s.pc = cache_n > 0 ? (float4*)p : nullptr;
     return s;
   }
 };

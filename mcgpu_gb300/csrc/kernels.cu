@@ -11,7 +11,7 @@
 //   k_chain_steps          persistent Metropolis steps of many chains:
 //                          Philox proposal, staging, screen, pairs, FP64
 //                          dE, decision and commit without leaving the GPU
-#include "kernels.cuh"
+#include "chain.cuh"
 
 namespace mcgpu {
 
@@ -207,15 +207,74 @@ __global__ void k_set_energy(Pool P, const double* e) {
 
 // ---- device-resident Metropolis -------------------------------------------
 
+// Puts every molecule of the pool in the device-resident chain state:
+// anchor = its first primary atom in fixed point, offsets = FP32 (atom -
+// anchor), template = offsets, quaternion = identity; then snaps the FP64
+// rows to that state (x = anchor + offset, each moved by < 1e-7 A) so both
+// descriptions agree exactly.  One warp per molecule.
+__global__ void k_chain_init(Pool P, const int* mol_chain, int n_mol_total) {
+  const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (m >= n_mol_total) return;
+  const ChainHdr& H = P.hdr[mol_chain[m]];
+  const int lane = threadIdx.x & 31;
+  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
+  const int2 pi = P.mpi[m];
+  const int an = P.pidx[pi.x];
+  const double ax = P.x[an], ay = P.y[an], az = P.z[an];
+  const uint4 A = fixpos(ax, ay, az, H);
+  __syncwarp();
+  for (int i = lane; i < len; i += 32) {
+    const int a = a0 + i;
+    const float w = P.aoff[a].w;
+    const float4 o = make_float4((float)(P.x[a] - ax), (float)(P.y[a] - ay), (float)(P.z[a] - az), w);
+    P.aoff[a] = o;
+    P.atpl[a] = make_float4(o.x, o.y, o.z, 0.f);
+  }
+  __syncwarp();
+  for (int i = lane; i < len; i += 32) {
+    const int a = a0 + i;
+    const double3 x = chain_pos3(A, P.aoff[a], H);
+    P.x[a] = x.x;
+    P.y[a] = x.y;
+    P.z[a] = x.z;
+  }
+  __syncwarp();
+  for (int k = lane; k < pi.y; k += 32) {
+    const int q = P.pidx[pi.x + k];
+    P.ppos[pi.x + k] = wrap_pos(P.x[q], P.y[q], P.z[q], H);
+  }
+  if (lane == 0) {
+    P.mfix[m] = A;
+    P.mq[m] = make_float4(1.f, 0.f, 0.f, 0.f);
+  }
+}
+
+// FP64 rows of every atom from the chain state (for downloads, FP64
+// recomputes and the plain entry points).  One thread per atom.
+__global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol, int n_atom) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n_atom) return;
+  const int m = atom_mol[a];
+  const ChainHdr& H = P.hdr[mol_chain[m]];
+  const double3 x = chain_pos3(P.mfix[m], P.aoff[a], H);
+  P.x[a] = x.x;
+  P.y[a] = x.y;
+  P.z[a] = x.z;
+}
+
 // Persistent kernel: groups of `gwarps` warps pull chain tasks from `queue`
-// (task k runs chain order[k]) and advance each by n_steps steps.  A step:
-// warp 0 draws the Philox proposal and stages the molecule (one group
-// barrier), every warp screens and evaluates its share of candidates into
-// FP64 sums, a group reduction (one barrier) gives E_old, E_new; warp 0
-// decides (dE < 0, else exp(-dE/kT) >= u, SimulationStep.cpp:794-803) and
-// commits.  If trace != nullptr, step st of chain c is recorded at
-// trace[c * trace_stride + trace_off + st].
-__global__ void __launch_bounds__(512) k_chain_steps(Pool P, int n_steps, unsigned* queue,
+// (task k runs chain order[k]) and advance each by n_steps steps on the
+// chain state.  A step: warp 0 draws the Philox move and stages it in FP32
+// (one group barrier); every warp screens its share of the candidates and
+// evaluates the in-range ones (FP32 pair terms, double-float sums); one
+// group reduction gives E_old, E_new.  Outside a guard band around the
+// acceptance threshold the decision (dE < 0, else exp(-dE/kT) >= u,
+// SimulationStep.cpp:794-803) is taken in FP32; inside it the group
+// re-evaluates both placements with FP64 pairs and decides on that.  Warp
+// 0 commits.  With cache_n > 0 each group keeps its chain's primary screen
+// positions in shared memory.  If trace != nullptr, step st of chain c is
+// recorded at trace[c * trace_stride + trace_off + st].
+__global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsigned* queue,
                                                      const int* order, int n_tasks, int gwarps,
                                                      SmemShape shape, mcgpu_trace* trace,
                                                      int trace_off, int trace_stride) {
@@ -233,80 +292,88 @@ __global__ void __launch_bounds__(512) k_chain_steps(Pool P, int n_steps, unsign
     const int c = order[task];
     ChainHdr* Hp = P.hdr + c;
     const ChainHdr& H = *Hp;
+    float4* pcache = (s.pc && H.simple_prim && H.n_mol <= shape.cache_n) ? s.pc : nullptr;
+    if (pcache)
+      for (int i = g.tid; i < H.n_mol; i += gsize) pcache[i] = P.ppos[H.pidx0 + i];
+    g.sync();
     double energy = H.energy;
-    long long acc = 0, npairs = 0;
+    long long acc_n = 0, npairs = 0;
     int ties = 0;
     const unsigned long long step0 = H.step;
     for (int st = 0; st < n_steps; st++) {
-      Proposal p;
       if (w == 0) {
+        MoveF mv;
         if (lane == 0)
-          p = draw_proposal(H.seed, H.chain_id, step0 + st, H.n_mol, P.mlen + H.mol0, H.max_t,
-                            H.max_r, H.rot_mode);
-        p.mol = __shfl_sync(~0u, p.mol, 0);
-        p.vertex = __shfl_sync(~0u, p.vertex, 0);
-        p.mode = H.rot_mode;
-        p.dx = __shfl_sync(~0u, p.dx, 0);
-        p.dy = __shfl_sync(~0u, p.dy, 0);
-        p.dz = __shfl_sync(~0u, p.dz, 0);
-        p.r0 = __shfl_sync(~0u, p.r0, 0);
-        p.r1 = __shfl_sync(~0u, p.r1, 0);
-        p.r2 = __shfl_sync(~0u, p.r2, 0);
-        p.r3 = __shfl_sync(~0u, p.r3, 0);
-        stage(P, H, H.mol0 + p.mol, &p, s, lane);
-        if (lane == 0) s.miscd[2] = p.u;
+          mv = draw_move_f32(H.seed, H.chain_id, step0 + st, H.n_mol, P.mlen + H.mol0,
+                             (float)H.max_t, (float)H.max_r, H.rot_mode);
+        mv.mol = __shfl_sync(~0u, mv.mol, 0);
+        mv.vertex = __shfl_sync(~0u, mv.vertex, 0);
+        mv.dx = __shfl_sync(~0u, mv.dx, 0);
+        mv.dy = __shfl_sync(~0u, mv.dy, 0);
+        mv.dz = __shfl_sync(~0u, mv.dz, 0);
+        mv.qd.w = __shfl_sync(~0u, mv.qd.w, 0);
+        mv.qd.x = __shfl_sync(~0u, mv.qd.x, 0);
+        mv.qd.y = __shfl_sync(~0u, mv.qd.y, 0);
+        mv.qd.z = __shfl_sync(~0u, mv.qd.z, 0);
+        mv.u = __shfl_sync(~0u, mv.u, 0);
+        stage_chain(P, H, mv, s, pcache, lane);
       }
       g.sync();
       const MovedInfo mi = load_moved(s);
-      double eo = 0.0, en = 0.0, ab = 0.0;
-      long long np = 0;
-      warp_eval<false>(P, H, s, mi, H.mol0, H.mol0 + H.n_mol, w, nw, lane, H.tpm, eo, en, ab, np);
-      group_reduce(g, s, eo, en, ab, np);
-      // Decision guard band: when exp(-dE/kT) lies within the FP32 rounding
-      // bound of u, the group re-evaluates both placements with FP64 pairs
-      // (the reference's arithmetic) and decides on that dE, so decisions
-      // match the FP64 path outside |-dE/kT - ln u| < ~1e-12.
-      int tie = 0;
-      {
-        const float u = (float)s.miscd[2];
-        const double bound = kTieRel * ab + 1e-9;
-        const double de32 = en - eo;
-        if (de32 >= -bound) {
-          const float pf = expf(-(float)(fmax(de32, 0.0) / H.kT));
-          tie = fabsf(pf - u) <= pf * (float)(1.5 * bound / H.kT) + 4e-6f;
-        }
-      }
+      // read before the reduction barrier: warp 0 restages the slot after it
+      const float u = __int_as_float(s.misc[kMiscU]);
+      AccFF acc = {0.f, 0.f, 0.f, 0.f, 0.f, 0};
+      warp_eval_chain(P, H, s, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, H.tpm, acc);
+      group_reduce_ff(g, s, acc);
+      // FP32 decision unless the FP32 dE is within its rounding bound of the
+      // threshold; the bound covers the pair terms' rounding (kTieRel of the
+      // sum of magnitudes) and the FP32 difference of the two totals.
+      const float de_f = __fadd_rn(__fsub_rn(acc.nh, acc.oh), __fsub_rn(acc.nl, acc.ol));
+      const float bound = (float)kTieRel * acc.ab + 2.4e-7f * (fabsf(acc.nh) + fabsf(acc.oh)) + 1e-9f;
+      const float pf = expf(-fmaxf(de_f, 0.f) * H.kTinvf);
+      const int tie = (de_f >= -bound) && (fabsf(pf - u) <= pf * (1.5f * bound * H.kTinvf) + 1e-6f);
+      double e_old, e_new;
       if (tie) {
+        if (w == 0) stage_chain_f64(H, s, mi, lane);
         g.sync();
-        eo = 0.0;
-        en = 0.0;
-        double ab2 = 0.0;
+        double eo = 0.0, en = 0.0, ab2 = 0.0;
         long long np2 = 0;
-        warp_eval<true>(P, H, s, mi, H.mol0, H.mol0 + H.n_mol, w, nw, lane, H.tpm, eo, en, ab2,
-                        np2);
+        warp_eval_chain64(P, H, s, mi, H.mol0, H.mol0 + H.n_mol, w, nw, lane, H.tpm, eo, en);
         group_reduce(g, s, eo, en, ab2, np2);
+        e_old = eo;
+        e_new = en;
       }
       if (w == 0) {
-        const double de = en - eo;
         int ok = 0;
-        if (lane == 0) ok = (de < 0) || (exp(-(de) / H.kT) >= p.u);
+        double de = 0.0;
+        if (lane == 0) {
+          if (!tie) {
+            e_old = (double)acc.oh + (double)acc.ol;
+            e_new = (double)acc.nh + (double)acc.nl;
+            ok = (de_f < 0.f) || (pf >= u);
+          } else {
+            const double d64 = e_new - e_old;
+            ok = (d64 < 0) || (exp(-d64 / H.kT) >= (double)u);
+          }
+          de = e_new - e_old;
+        }
         ok = __shfl_sync(~0u, ok, 0);
-        if (ok) commit(P, s, mi, lane);
+        if (ok) commit_chain(P, H, s, mi, pcache, lane);
         if (lane == 0) {
           if (ok) {
             energy += de;
-            acc++;
+            acc_n++;
           }
-          npairs += np;
+          npairs += acc.np;
           ties += tie;
           if (trace) {
             mcgpu_trace t;
             t.mol = mi.mol - H.mol0;
             t.accepted = ok;
-            t.e_old = eo;
-            t.e_new = en;
+            t.e_old = e_old;
+            t.e_new = e_new;
             t.de = de;
-            t.u = p.u;
+            t.u = (double)u;
             t.fp64 = tie;
             t.pad0 = 0;
             trace[(size_t)c * trace_stride + trace_off + st] = t;
@@ -318,7 +385,7 @@ __global__ void __launch_bounds__(512) k_chain_steps(Pool P, int n_steps, unsign
     if (g.tid == 0) {
       Hp->energy = energy;
       Hp->step = step0 + n_steps;
-      Hp->accepted += acc;
+      Hp->accepted += acc_n;
       Hp->pairs += npairs;
       Hp->ties += ties;
     }

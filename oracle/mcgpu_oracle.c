@@ -505,3 +505,227 @@ int orc_accept_volume(double de, double p_kcal_per_a3, double v_old, double v_ne
   if (arg >= 0) return 1;
   return exp(arg) >= u;
 }
+
+/* ---- device-resident chain form ----------------------------------------
+ * Restated from the definition of the FP32 move (an independent CPU
+ * implementation of the same arithmetic: every operation rounded once,
+ * fused multiply-adds only where written as fmaf). */
+
+static float u01f(uint32_t r) {
+  return fmaf((float)(r >> 8), 5.9604644775390625e-08f, 2.98023223876953125e-08f);
+}
+
+/* sin/cos: Cody-Waite reduction by pi/2 in three parts, Taylor polynomials
+ * of sin (to r^11) and cos (to r^12) by Horner's rule. */
+void orc_sincos_f32(float x, float* sp, float* cp) {
+  const float k = rintf(x * 0.636619772367581343f);
+  float r = fmaf(-k, 1.5703125f, x);
+  r = fmaf(-k, 4.83751296997070312e-04f, r);
+  r = fmaf(-k, 7.54978995489188216e-08f, r);
+  const float r2 = r * r;
+  float s = fmaf(r2, -2.50521083854417188e-08f, 2.75573192239858907e-06f);
+  s = fmaf(r2, s, -1.98412698412698413e-04f);
+  s = fmaf(r2, s, 8.33333333333333333e-03f);
+  s = fmaf(r2, s, -1.66666666666666667e-01f);
+  s = fmaf(r2 * r, s, r);
+  float c = fmaf(r2, 2.08767569878680990e-09f, -2.75573192239858907e-07f);
+  c = fmaf(r2, c, 2.48015873015873016e-05f);
+  c = fmaf(r2, c, -1.38888888888888889e-03f);
+  c = fmaf(r2, c, 4.16666666666666667e-02f);
+  c = fmaf(r2, c, -0.5f);
+  c = fmaf(r2, c, 1.0f);
+  const int q = ((int)k) & 3;
+  *sp = (q == 0) ? s : (q == 1) ? c : (q == 2) ? -s : -c;
+  *cp = (q == 0) ? c : (q == 1) ? -s : (q == 2) ? -c : s;
+}
+
+typedef struct { float w, x, y, z; } qf;
+
+static qf q_mul(qf a, qf b) {
+  qf r;
+  r.w = ((a.w * b.w - a.x * b.x) - a.y * b.y) - a.z * b.z;
+  r.x = ((a.w * b.x + a.x * b.w) + a.y * b.z) - a.z * b.y;
+  r.y = ((a.w * b.y - a.x * b.z) + a.y * b.w) + a.z * b.x;
+  r.z = ((a.w * b.z + a.x * b.y) - a.y * b.x) + a.z * b.w;
+  return r;
+}
+
+static qf q_norm(qf a) {
+  const float n = sqrtf(((a.w * a.w + a.x * a.x) + a.y * a.y) + a.z * a.z);
+  qf r = {a.w / n, a.x / n, a.y / n, a.z / n};
+  return r;
+}
+
+static void q_matrix(qf q, float* m) {
+  const float xx = q.x * q.x, yy = q.y * q.y, zz = q.z * q.z;
+  const float xy = q.x * q.y, xz = q.x * q.z, yz = q.y * q.z;
+  const float wx = q.w * q.x, wy = q.w * q.y, wz = q.w * q.z;
+  m[0] = 1.0f - 2.0f * (yy + zz);
+  m[1] = 2.0f * (xy - wz);
+  m[2] = 2.0f * (xz + wy);
+  m[3] = 2.0f * (xy + wz);
+  m[4] = 1.0f - 2.0f * (xx + zz);
+  m[5] = 2.0f * (yz - wx);
+  m[6] = 2.0f * (xz - wy);
+  m[7] = 2.0f * (yz + wx);
+  m[8] = 1.0f - 2.0f * (xx + yy);
+}
+
+static void m_vec(const float* m, const float* v, float* out) {
+  out[0] = (m[0] * v[0] + m[1] * v[1]) + m[2] * v[2];
+  out[1] = (m[3] * v[0] + m[4] * v[1]) + m[5] * v[2];
+  out[2] = (m[6] * v[0] + m[7] * v[1]) + m[8] * v[2];
+}
+
+static qf q_axis(float kx, float ky, float kz, float a) {
+  float s, c;
+  orc_sincos_f32(0.5f * a, &s, &c);
+  qf q = {c, s * kx, s * ky, s * kz};
+  return q;
+}
+
+static int fix_step(float dx, float inv_s) { return (int)rintf(dx * inv_s); }
+
+static double chain_coord(uint32_t A, float o, double L) {
+  return (double)A * (L * 2.3283064365386963e-10) + (double)o;
+}
+
+static void chain_rows(orc_chain* c, int m) {
+  orc_box* b = c->b;
+  const int s = b->mol_start[m], n = b->mol_len[m];
+  for (int a = s; a < s + n; a++) {
+    b->x[a] = chain_coord(c->A[3 * m + 0], c->off[3 * a + 0], b->size[0]);
+    b->y[a] = chain_coord(c->A[3 * m + 1], c->off[3 * a + 1], b->size[1]);
+    b->z[a] = chain_coord(c->A[3 * m + 2], c->off[3 * a + 2], b->size[2]);
+  }
+}
+
+void orc_fchain_init(orc_chain* c) {
+  orc_box* b = c->b;
+  for (int m = 0; m < b->n_mol; m++) {
+    const int an = b->pidx[b->mol_pidx_start[m]];
+    const double ax = b->x[an], ay = b->y[an], az = b->z[an];
+    c->A[3 * m + 0] = (uint32_t)(uint64_t)llrint(ax * (4294967296.0 / b->size[0]));
+    c->A[3 * m + 1] = (uint32_t)(uint64_t)llrint(ay * (4294967296.0 / b->size[1]));
+    c->A[3 * m + 2] = (uint32_t)(uint64_t)llrint(az * (4294967296.0 / b->size[2]));
+    c->q[4 * m + 0] = 1.0f;
+    c->q[4 * m + 1] = c->q[4 * m + 2] = c->q[4 * m + 3] = 0.0f;
+    const int s = b->mol_start[m], n = b->mol_len[m];
+    for (int a = s; a < s + n; a++) {
+      c->off[3 * a + 0] = c->tpl[3 * a + 0] = (float)(b->x[a] - ax);
+      c->off[3 * a + 1] = c->tpl[3 * a + 1] = (float)(b->y[a] - ay);
+      c->off[3 * a + 2] = c->tpl[3 * a + 2] = (float)(b->z[a] - az);
+    }
+    chain_rows(c, m);
+  }
+}
+
+void orc_fchain_draw(const orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step,
+                    orc_movef* mv) {
+  const orc_box* b = c->b;
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t ctr[4] = {(uint32_t)step, (uint32_t)(step >> 32), chain, 0u};
+  uint32_t a[4], cc[4], d[4];
+  orc_philox4x32_10(ctr, key, a);
+  ctr[3] = 1u;
+  orc_philox4x32_10(ctr, key, cc);
+  ctr[3] = 2u;
+  orc_philox4x32_10(ctr, key, d);
+  mv->mol = uidx(a[0], b->n_mol);
+  mv->vertex = uidx(a[1], b->mol_len[mv->mol]);
+  const float max_t = (float)b->max_translate, max_r = (float)b->max_rotate;
+  const float t2 = 2.0f * max_t;
+  mv->dx = t2 * u01f(a[2]) - max_t;
+  mv->dy = t2 * u01f(a[3]) - max_t;
+  mv->dz = t2 * u01f(cc[0]) - max_t;
+  const float r2 = 2.0f * max_r;
+  const float deg = 0.0174532925199432958f;
+  qf qd;
+  if (c->rot_mode == 0) {
+    const float ax = (r2 * u01f(cc[1]) - max_r) * deg;
+    const float ay = (r2 * u01f(cc[2]) - max_r) * deg;
+    const float az = (r2 * u01f(cc[3]) - max_r) * deg;
+    const qf qx = q_axis(-1.0f, 0.0f, 0.0f, ax);
+    const qf qy = q_axis(0.0f, -1.0f, 0.0f, ay);
+    const qf qz = q_axis(0.0f, 0.0f, -1.0f, az);
+    qd = q_mul(qz, q_mul(qy, qx));
+  } else {
+    const float zc = 2.0f * u01f(cc[1]) - 1.0f;
+    const float phi = 6.28318530717958648f * u01f(cc[2]);
+    const float sr = sqrtf(1.0f - zc * zc);
+    float sp, cp;
+    orc_sincos_f32(phi, &sp, &cp);
+    const float ang = (r2 * u01f(cc[3]) - max_r) * deg;
+    qd = q_axis(sr * cp, sr * sp, zc, ang);
+  }
+  mv->qw = qd.w; mv->qx = qd.x; mv->qy = qd.y; mv->qz = qd.z;
+  mv->u = u01f(d[0]);
+}
+
+/* The chain's Metropolis loop: draw, FP64 old energy, FP32 move of the
+ * state, FP64 new energy, the reference's decision on the FP64 dE
+ * (SimulationStep.cpp:794-803), commit or restore. */
+double orc_fchain_run(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step0,
+                     int n_steps, double e0, orc_trace* trace, long long* n_accepted) {
+  orc_box* b = c->b;
+  double e = e0;
+  long long acc = 0;
+  int big = 0;
+  for (int m = 0; m < b->n_mol; m++)
+    if (b->mol_len[m] > big) big = b->mol_len[m];
+  float* save_off = (float*)malloc(sizeof(float) * 3 * (size_t)big);
+  for (int st = 0; st < n_steps; st++) {
+    orc_movef mv;
+    orc_fchain_draw(c, seed, chain, step0 + (uint64_t)st, &mv);
+    const int m = mv.mol, a0 = b->mol_start[m], len = b->mol_len[m];
+    const double e_old = orc_mol_energy(b, m, 0);
+    /* move */
+    qf q = {c->q[4 * m], c->q[4 * m + 1], c->q[4 * m + 2], c->q[4 * m + 3]};
+    qf qd = {mv.qw, mv.qx, mv.qy, mv.qz};
+    const qf qn = q_norm(q_mul(qd, q));
+    float R[9];
+    q_matrix(qn, R);
+    const int v = a0 + mv.vertex;
+    float onv[3];
+    m_vec(R, &c->tpl[3 * v], onv);
+    const float dl[3] = {(c->off[3 * v] - onv[0]) + mv.dx, (c->off[3 * v + 1] - onv[1]) + mv.dy,
+                         (c->off[3 * v + 2] - onv[2]) + mv.dz};
+    const float inv[3] = {(float)(4294967296.0 / b->size[0]), (float)(4294967296.0 / b->size[1]),
+                          (float)(4294967296.0 / b->size[2])};
+    uint32_t Aold[3], qsave[4];
+    (void)qsave;
+    for (int k = 0; k < 3; k++) {
+      Aold[k] = c->A[3 * m + k];
+      c->A[3 * m + k] = Aold[k] + (uint32_t)fix_step(dl[k], inv[k]);
+    }
+    for (int i = 0; i < len; i++) {
+      for (int k = 0; k < 3; k++) save_off[3 * i + k] = c->off[3 * (a0 + i) + k];
+      m_vec(R, &c->tpl[3 * (a0 + i)], &c->off[3 * (a0 + i)]);
+    }
+    chain_rows(c, m);
+    const double e_new = orc_mol_energy(b, m, 0);
+    const double de = e_new - e_old;
+    const int ok = (de < 0) || (exp(-de / b->kT) >= (double)mv.u);
+    if (ok) {
+      e += de;
+      acc++;
+      c->q[4 * m] = qn.w; c->q[4 * m + 1] = qn.x; c->q[4 * m + 2] = qn.y; c->q[4 * m + 3] = qn.z;
+    } else {
+      for (int k = 0; k < 3; k++) c->A[3 * m + k] = Aold[k];
+      for (int i = 0; i < len; i++)
+        for (int k = 0; k < 3; k++) c->off[3 * (a0 + i) + k] = save_off[3 * i + k];
+      chain_rows(c, m);
+    }
+    if (trace) {
+      trace[st].mol = m;
+      trace[st].accepted = ok;
+      trace[st].e_old = e_old;
+      trace[st].e_new = e_new;
+      trace[st].de = de;
+      trace[st].u = (double)mv.u;
+    }
+  }
+  free(save_off);
+  if (n_accepted) *n_accepted = acc;
+  return e;
+}

@@ -85,3 +85,38 @@ int orc_accept_volume(double de, double p_kcal_per_a3, double v_old, double v_ne
 }
 #endif
 #endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- device-resident chain form (FP32 moves on a fixed-point + FP32
+ * offset state), mirrored from its definition so the CPU state equals the
+ * device state bit for bit; energies are the reference's FP64 arithmetic on
+ * the FP64 rows x = anchor * L / 2^32 + offset. */
+typedef struct {
+  orc_box* b;          /* FP64 rows, kept equal to the state            */
+  uint32_t* A;         /* [3 * n_mol] anchors, fixed point of the edge  */
+  float* q;            /* [4 * n_mol] unit quaternions (w, x, y, z)     */
+  float* tpl;          /* [3 * n_atom] template offsets                 */
+  float* off;          /* [3 * n_atom] current offsets                  */
+  int rot_mode;
+} orc_chain;
+
+typedef struct {
+  int mol, vertex;
+  float dx, dy, dz;
+  float qw, qx, qy, qz;
+  float u;
+} orc_movef;
+
+void orc_fchain_init(orc_chain* c);
+void orc_fchain_draw(const orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step,
+                    orc_movef* mv);
+double orc_fchain_run(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step0,
+                     int n_steps, double e0, orc_trace* trace, long long* n_accepted);
+void orc_sincos_f32(float x, float* s, float* c);
+
+#ifdef __cplusplus
+}
+#endif

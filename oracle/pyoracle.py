@@ -49,6 +49,18 @@ class OrcMove(C.Structure):
                 ("u", C.c_double)]
 
 
+class OrcChainS(C.Structure):
+    _fields_ = [("b", C.POINTER(OrcBox)), ("A", C.POINTER(C.c_uint32)),
+                ("q", C.POINTER(C.c_float)), ("tpl", C.POINTER(C.c_float)),
+                ("off", C.POINTER(C.c_float)), ("rot_mode", C.c_int)]
+
+
+class OrcMoveF(C.Structure):
+    _fields_ = [("mol", C.c_int), ("vertex", C.c_int), ("dx", C.c_float), ("dy", C.c_float),
+                ("dz", C.c_float), ("qw", C.c_float), ("qx", C.c_float), ("qy", C.c_float),
+                ("qz", C.c_float), ("u", C.c_float)]
+
+
 class OrcTrace(C.Structure):
     _fields_ = [("mol", C.c_int), ("accepted", C.c_int), ("e_old", C.c_double),
                 ("e_new", C.c_double), ("de", C.c_double), ("u", C.c_double)]
@@ -98,6 +110,13 @@ def orc_lib() -> C.CDLL:
                                                C.c_int, C.c_int, C.c_int,
                                                C.POINTER(C.c_longlong)]),
             "orc_resize_box_centres": (None, [P, C.c_double]),
+            "orc_fchain_init": (None, [C.POINTER(OrcChainS)]),
+            "orc_fchain_draw": (None, [C.POINTER(OrcChainS), C.c_uint64, C.c_uint32, C.c_uint64,
+                                       C.POINTER(OrcMoveF)]),
+            "orc_fchain_run": (C.c_double, [C.POINTER(OrcChainS), C.c_uint64, C.c_uint32,
+                                            C.c_uint64, C.c_int, C.c_double, C.POINTER(OrcTrace),
+                                            C.POINTER(C.c_longlong)]),
+            "orc_sincos_f32": (None, [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
             "orc_accept_volume": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double,
                                             C.c_int, C.c_double, C.c_double]),
         }
@@ -178,6 +197,50 @@ class OracleBox:
         e = orc_lib().orc_chain_run(self.ref, int(seed) & (2 ** 64 - 1), int(chain), int(step0),
                                     int(n_steps), int(mode), float(e0), tr, C.byref(acc))
         return e, acc.value, list(tr)[:n_steps]
+
+
+class OracleChain:
+    """The device-resident chain form on the CPU: the same FP32 moves of the
+    same fixed-point + FP32-offset state (bit for bit), FP64 energies with
+    the reference's arithmetic on the state's FP64 rows."""
+
+    def __init__(self, box, rot_mode: int):
+        self.ob = OracleBox(box)
+        b = self.ob.data
+        self.A = np.zeros(3 * b.n_mol, dtype=np.uint32)
+        self.q = np.zeros(4 * b.n_mol, dtype=np.float32)
+        self.tpl = np.zeros(3 * b.n_atom, dtype=np.float32)
+        self.off = np.zeros(3 * b.n_atom, dtype=np.float32)
+        fp = C.POINTER(C.c_float)
+        self.s = OrcChainS(C.pointer(self.ob.s), self.A.ctypes.data_as(C.POINTER(C.c_uint32)),
+                           self.q.ctypes.data_as(fp), self.tpl.ctypes.data_as(fp),
+                           self.off.ctypes.data_as(fp), int(rot_mode))
+        orc_lib().orc_fchain_init(C.byref(self.s))
+
+    def draw(self, seed: int, chain: int, step: int) -> OrcMoveF:
+        mv = OrcMoveF()
+        orc_lib().orc_fchain_draw(C.byref(self.s), int(seed) & (2 ** 64 - 1), int(chain),
+                                  int(step), C.byref(mv))
+        return mv
+
+    def run(self, seed: int, chain: int, n_steps: int, e0: float, step0: int = 0):
+        tr = (OrcTrace * max(1, n_steps))()
+        acc = C.c_longlong()
+        e = orc_lib().orc_fchain_run(C.byref(self.s), int(seed) & (2 ** 64 - 1), int(chain),
+                                     int(step0), int(n_steps), float(e0), tr, C.byref(acc))
+        return e, acc.value, list(tr)[:n_steps]
+
+    def system_energy(self) -> float:
+        return self.ob.system_energy()
+
+    def coords(self) -> np.ndarray:
+        return self.ob.coords()
+
+
+def sincos_f32(x: float) -> tuple[float, float]:
+    s, c = C.c_float(), C.c_float()
+    orc_lib().orc_sincos_f32(float(x), C.byref(s), C.byref(c))
+    return s.value, c.value
 
 
 def philox(ctr, key) -> list[int]:
