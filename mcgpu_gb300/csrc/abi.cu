@@ -199,6 +199,7 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
   h.rot_mode = rot_mode;
   h.chain_id = (int)c;
   h.simple_prim = simple ? 1 : 0;
+  h.precise = max_len >= 8 ? 1 : 0;
   const double rc = d->cutoff;
   double ulpL = std::ldexp(1.0, (int)std::floor(std::log2(std::max(
                                     d->size[0], std::max(d->size[1], d->size[2])))) - 23);
@@ -211,6 +212,7 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
     h.fxinv[k] = 4294967296.0 / d->size[k];
     h.fxs[k] = (float)(d->size[k] / 4294967296.0);
     h.fxinvf[k] = (float)(4294967296.0 / d->size[k]);
+    h.fxs_lo[k] = (float)(d->size[k] / 4294967296.0 - (double)h.fxs[k]);
   }
   h.kTinvf = (float)(1.0 / (d->temperature * kBoltz));
   h.cutoff = rc;
@@ -235,7 +237,7 @@ struct DevPool {
   std::vector<int> mstart, mlen;  // host copies (pool-absolute)
 
   void release() {
-    void* ptrs[] = {P.x, P.y, P.z, P.sig, P.eps, P.q, P.aoff, P.aeq, P.mstart, P.mlen, P.mpi,
+    void* ptrs[] = {P.x, P.y, P.z, P.sig, P.eps, P.q, P.aoff, P.aofl, P.aeq, P.mstart, P.mlen, P.mpi,
                     P.mfix, P.mrad, P.mq, P.atpl, P.pidx, P.ppos, P.hdr, P.rb, P.trace,
                     mol_chain, atom_mol, emol, pairs, esum};
     for (void* p : ptrs)
@@ -261,6 +263,7 @@ int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
   P.x = dalloc<double>(na, &e); P.y = dalloc<double>(na, &e); P.z = dalloc<double>(na, &e);
   P.sig = dalloc<double>(na, &e); P.eps = dalloc<double>(na, &e); P.q = dalloc<double>(na, &e);
   P.aoff = dalloc<float4>(na, &e); P.aeq = dalloc<float2>(na, &e);
+  P.aofl = dalloc<float4>(na, &e);
   P.mstart = dalloc<int>(nm, &e); P.mlen = dalloc<int>(nm, &e); P.mpi = dalloc<int2>(nm, &e);
   P.mfix = dalloc<uint4>(nm, &e); P.mrad = dalloc<float>(nm, &e);
   P.mq = dalloc<float4>(nm, &e); P.atpl = dalloc<float4>(na, &e);

@@ -82,6 +82,8 @@ __device__ void stage_chain(const Pool& P, const ChainHdr& H, const MoveF& mv, c
     const float3 on = mvec(R, t.x, t.y, t.z);
     s.o_old[i] = o;
     s.o_new[i] = make_float4(on.x, on.y, on.z, o.w);
+    s.l_old[i] = make_float4(0.f, 0.f, 0.f, 0.f);  // the chain state's offsets are exact
+    s.l_new[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     s.eq[i] = make_float4(qe.x, qe.y, fmaf(o.x, o.x, fmaf(o.y, o.y, o.z * o.z)),
                           fmaf(on.x, on.x, fmaf(on.y, on.y, on.z * on.z)));
     s.sd[i] = P.sig[a];
@@ -112,10 +114,11 @@ __device__ void stage_chain(const Pool& P, const ChainHdr& H, const MoveF& mv, c
 
 // Screen of candidate j against the staged molecule (both placements):
 // FP32 distance of the screen positions, decided outright outside the
-// guard band around rc^2 and by the reference's FP64 test inside it.
+// guard band around rc^2 and by the reference's FP64 test inside it.  No
+// global load outside the guard band (the positions come from the shared-
+// memory cache); the entry's anchor differences are formed in the batch.
 __device__ __forceinline__ int screen_chain(const Pool& P, const ChainHdr& H, const GroupSmem& s,
-                                            const MovedInfo& mi, int j, float4 q0, float4& A,
-                                            float2& B) {
+                                            const MovedInfo& mi, int j, float4 q0) {
   const int2 pj = H.simple_prim ? make_int2(H.pidx0 + (j - H.mol0), 1) : P.mpi[j];
   int f = 0;
   for (int k2 = 0; k2 < pj.y; k2++) {
@@ -145,88 +148,7 @@ __device__ __forceinline__ int screen_chain(const Pool& P, const ChainHdr& H, co
       }
     }
   }
-  if (f) {
-    const uint4 fj = P.mfix[j];
-    const float rr = mi.rad + P.mrad[j];
-    float3 Do = make_float3(0.f, 0.f, 0.f), Dn = Do;
-    if (f & kInOld) {
-      Do = fixdiff(fj, mi.fx_old, H);
-      if (needs_wrap(Do, rr, H)) f |= kWrapOld;
-    }
-    if (f & kInNew) {
-      Dn = fixdiff(fj, mi.fx_new, H);
-      if (needs_wrap(Dn, rr, H)) f |= kWrapNew;
-    }
-    A = make_float4(Do.x, Do.y, Do.z, Dn.x);
-    B = make_float2(Dn.y, Dn.z);
-  }
   return f;
-}
-
-// Per-thread double-float accumulators of a step.
-struct AccFF {
-  float oh, ol, nh, nl, ab;
-  long long np;
-};
-
-// Pair batch of ring entries, FP32 pair terms, per-entry team sums added in
-// double-float to the team leader's accumulators.
-__device__ __forceinline__ void batch_chain(const Pool& P, const ChainHdr& H, const GroupSmem& s,
-                                            const MovedInfo& mi, const int* rj, const float4* rA,
-                                            const float2* rB, int head, int count, int lane, int T,
-                                            AccFF& acc) {
-  const int tm = lane / T, tl = lane - tm * T, nteams = 32 / T;
-  for (int e0 = 0; e0 < count; e0 += nteams) {
-    const int e = e0 + tm;
-    int f = 0, b0 = 0, lenj = 0, actj = 0;
-    float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
-    float2 B = make_float2(0.f, 0.f);
-    if (e < count) {
-      const int idx = (head + e) & (kRing - 1);
-      const int jf = rj[idx];
-      A = rA[idx];
-      B = rB[idx];
-      const int j = jf >> 4;
-      f = jf & 15;
-      b0 = P.mstart[j];
-      const int lw = P.mlen[j];
-      lenj = lw & 255;
-      actj = lw >> 8;
-    }
-    float so = 0.f, sn = 0.f, sa = 0.f;
-    for (int b = b0 + tl; b < b0 + lenj; b += T) {
-      const float4 ob = P.aoff[b];
-      const float2 qb = P.aeq[b];
-      if (f & kInOld) {
-        const float bx = A.x + ob.x, by = A.y + ob.y, bz = A.z + ob.z;
-        so += (f & kWrapOld) ? sum_moved32_wrap(s.o_old, s.eq, mi.len, bx, by, bz, ob.w, qb, H, sa)
-                             : sum_moved32_cf(s.o_old, s.eq, mi.len, false, bx, by, bz, ob.w, qb,
-                                              mi.qm, sa);
-      }
-      if (f & kInNew) {
-        const float bx = A.w + ob.x, by = B.x + ob.y, bz = B.y + ob.z;
-        sn += (f & kWrapNew) ? sum_moved32_wrap(s.o_new, s.eq, mi.len, bx, by, bz, ob.w, qb, H, sa)
-                             : sum_moved32_cf(s.o_new, s.eq, mi.len, true, bx, by, bz, ob.w, qb,
-                                              mi.qm, sa);
-      }
-    }
-    for (int off = T >> 1; off > 0; off >>= 1) {
-      so += __shfl_xor_sync(~0u, so, off);
-      sn += __shfl_xor_sync(~0u, sn, off);
-      sa += __shfl_xor_sync(~0u, sa, off);
-    }
-    if (tl == 0 && f) {
-      if (f & kInOld) {
-        ff_add(acc.oh, acc.ol, so);
-        acc.np += (long long)mi.act * actj;
-      }
-      if (f & kInNew) {
-        ff_add(acc.nh, acc.nl, sn);
-        acc.np += (long long)mi.act * actj;
-      }
-      acc.ab += sa;
-    }
-  }
 }
 
 // One warp screens chain candidates [c_begin, c_end) in warp-strided
@@ -236,15 +158,11 @@ __device__ void warp_eval_chain(const Pool& P, const ChainHdr& H, const GroupSme
                                 const MovedInfo& mi, const float4* pcache, int c_begin, int c_end,
                                 int w, int nw, int lane, int T, AccFF& acc) {
   int* rj = s.lj + w * kRing;
-  float4* rA = s.lA + w * kRing;
-  float2* rB = s.lB + w * kRing;
   int head = 0, tail = 0;
   const unsigned lt = lanemask_lt();
   for (int base = c_begin + w * 32; base < c_end; base += nw * 32) {
     const int j = base + lane;
     int f = 0;
-    float4 A;
-    float2 B;
     if (j < c_end && j != mi.mol) {
       float4 q0;
       if (pcache)
@@ -253,25 +171,28 @@ __device__ void warp_eval_chain(const Pool& P, const ChainHdr& H, const GroupSme
         q0 = P.ppos[H.pidx0 + (j - H.mol0)];
       else
         q0 = P.ppos[P.mpi[j].x];
-      f = screen_chain(P, H, s, mi, j, q0, A, B);
+      f = screen_chain(P, H, s, mi, j, q0);
     }
     const unsigned bal = __ballot_sync(~0u, f != 0);
-    if (f) {
-      const int pos = (tail + __popc(bal & lt)) & (kRing - 1);
-      rj[pos] = (j << 4) | f;
-      rA[pos] = A;
-      rB[pos] = B;
-    }
+    if (f) rj[(tail + __popc(bal & lt)) & (kRing - 1)] = (j << 4) | f;
     tail += __popc(bal);
     if (tail - head >= 32) {
       __syncwarp();
-      batch_chain(P, H, s, mi, rj, rA, rB, head, 32, lane, T, acc);
+      if (H.precise)
+        batch_ff<true, false>(P, H, s, mi, rj, head, 32, lane, T, acc);
+      else
+        batch_ff<false, false>(P, H, s, mi, rj, head, 32, lane, T, acc);
       head += 32;
       __syncwarp();
     }
   }
   __syncwarp();
-  if (tail > head) batch_chain(P, H, s, mi, rj, rA, rB, head, tail - head, lane, T, acc);
+  if (tail > head) {
+    if (H.precise)
+      batch_ff<true, false>(P, H, s, mi, rj, head, tail - head, lane, T, acc);
+    else
+      batch_ff<false, false>(P, H, s, mi, rj, head, tail - head, lane, T, acc);
+  }
   __syncwarp();
 }
 

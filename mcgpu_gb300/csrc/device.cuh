@@ -54,10 +54,12 @@ enum : int {
 struct __align__(16) ChainHdr {
   int atom0, mol0, pidx0, n_mol;      // pool offsets and molecule count
   int n_atom, n_pidx, max_len, tpm;   // tpm: lanes per neighbour molecule
-  int rot_mode, chain_id, simple_prim, pad0;  // simple_prim: one primary per molecule
+  int rot_mode, chain_id, simple_prim, precise;  // simple_prim: one primary per molecule;
+                                                  // precise: compensated displacements
   float Lf[3], cut2_lo;               // FP32 box and guard band
   float fxs[3], cut2_hi;              // fixed point -> Angstrom scale
   float fxinvf[3], kTinvf;            // Angstrom -> fixed point (FP32); 1/kT (FP32)
+  float fxs_lo[3], pad5;              // fxs + fxs_lo = L / 2^32 to ~48 bits
   double L[3], cutoff;
   double fxinv[3], kT;                // Angstrom -> fixed point scale
   double max_t, max_r, energy, pad1;
@@ -70,6 +72,7 @@ static_assert(sizeof(ChainHdr) % 16 == 0, "ChainHdr alignment");
 struct Pool {
   double *x, *y, *z, *sig, *eps, *q;
   float4* aoff;
+  float4* aofl;        // plain path: low part of the offsets (FP64 offset - aoff)
   float2* aeq;
   int *mstart, *mlen;
   int2* mpi;
@@ -205,6 +208,22 @@ __device__ __forceinline__ double make_periodic(double x, double L) {
   return x;
 }
 
+// Double-float accumulation: (hi, lo) += v with Knuth's two-sum, so sums of
+// FP32 terms keep ~48 significant bits without FP64 instructions.
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float v) {
+  const float s = __fadd_rn(hi, v);
+  const float bb = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+
+// (hi, lo) += (h2, l2).
+__device__ __forceinline__ void ff_add2(float& hi, float& lo, float h2, float l2) {
+  ff_add(hi, lo, h2);
+  lo = __fadd_rn(lo, l2);
+}
+
 // ---- groups: the warps that advance one chain --------------------------
 struct Group {
   int tid, nthreads, bar;
@@ -233,6 +252,7 @@ struct GroupSmem {
   double* nx; double* ny; double* nz;   // new FP64 coords [maxA]
   double* sd; double* ed; double* qd;   // FP64 sigma, epsilon, charge [maxA]
   float4* o_old; float4* o_new;         // FP32 offsets from the anchor, w=sigma [maxA]
+  float4* l_old; float4* l_new;         // their low parts (plain path; zero for chains) [maxA]
   float4* eq;                           // FP32 (2sqrt|eps|, q sqrt(332.06), |o_old|^2, |o_new|^2) [maxA]
   float4* p_old; float4* p_new;         // wrapped FP32 primaries [kMaxP]
   int* pa;                              // primary atom slots in the molecule [kMaxP]
@@ -253,7 +273,7 @@ struct SmemShape {
   __host__ __device__ int bytes() const {
     int b = 0;
     b += align16(9 * maxA * 8);
-    b += align16(2 * maxA * 16);
+    b += align16(4 * maxA * 16);
     b += align16(maxA * 16);
     b += align16(2 * kMaxP * 16);
     b += align16(kMaxP * 4);
@@ -274,7 +294,8 @@ struct SmemShape {
     s.nx = s.oz + maxA; s.ny = s.nx + maxA; s.nz = s.ny + maxA;
     s.sd = s.nz + maxA; s.ed = s.sd + maxA; s.qd = s.ed + maxA;
     p += align16(9 * maxA * 8);
-    s.o_old = (float4*)p; s.o_new = s.o_old + maxA; p += align16(2 * maxA * 16);
+    s.o_old = (float4*)p; s.o_new = s.o_old + maxA;
+    s.l_old = s.o_new + maxA; s.l_new = s.l_old + maxA; p += align16(4 * maxA * 16);
     s.eq = (float4*)p; p += align16(maxA * 16);
     s.p_old = (float4*)p; s.p_new = s.p_old + kMaxP; p += align16(2 * kMaxP * 16);
     s.pa = (int*)p; p += align16(kMaxP * 4);

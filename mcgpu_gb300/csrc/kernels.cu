@@ -228,6 +228,7 @@ __global__ void k_chain_init(Pool P, const int* mol_chain, int n_mol_total) {
     const float w = P.aoff[a].w;
     const float4 o = make_float4((float)(P.x[a] - ax), (float)(P.y[a] - ay), (float)(P.z[a] - az), w);
     P.aoff[a] = o;
+    P.aofl[a] = make_float4(0.f, 0.f, 0.f, 0.f);
     P.atpl[a] = make_float4(o.x, o.y, o.z, 0.f);
   }
   __syncwarp();

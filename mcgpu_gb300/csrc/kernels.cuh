@@ -35,6 +35,28 @@ __device__ __forceinline__ float3 fixdiff(uint4 b, uint4 a, const ChainHdr& H) {
                      (float)(int)(b.z - a.z) * H.fxs[2]);
 }
 
+// The same difference as a double-float (hi + lo), exact to ~1e-14 A: the
+// fixed-point difference is split into a high part with its low 8 bits
+// cleared (exact in FP32) and the rest, each scaled by L/2^32 held as
+// fxs + fxs_lo, with the rounding of the main product recovered by an FMA.
+__device__ __forceinline__ void fixdiff_ff(uint4 b, uint4 a, const ChainHdr& H, float3& hi,
+                                           float3& lo) {
+  const int d[3] = {(int)(b.x - a.x), (int)(b.y - a.y), (int)(b.z - a.z)};
+  float h[3], l[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int dh = d[k] & ~0xFF;
+    const float fh = (float)dh, fl = (float)(d[k] - dh);
+    const float p = fh * H.fxs[k];
+    const float e = fmaf(fh, H.fxs[k], -p);
+    const float t = fmaf(fh, H.fxs_lo[k], fmaf(fl, H.fxs[k], e));
+    h[k] = p + t;
+    l[k] = t - (h[k] - p);
+  }
+  hi = make_float3(h[0], h[1], h[2]);
+  lo = make_float3(l[0], l[1], l[2]);
+}
+
 // True when an atom pair of these two molecules may need its own periodic
 // image (|D| + radii reaches half a box edge in some dimension).
 __device__ __forceinline__ bool needs_wrap(float3 D, float rr, const ChainHdr& H) {
@@ -82,6 +104,7 @@ __device__ void stage(const Pool& P, const ChainHdr& H, int m, const Proposal* p
     const float4 o = P.aoff[a];
     const float2 q = P.aeq[a];
     s.o_old[i] = o;
+    s.l_old[i] = P.aofl[a];
     s.eq[i] = make_float4(q.x, q.y, fmaf(o.x, o.x, fmaf(o.y, o.y, o.z * o.z)), 0.f);
   }
   // net FP32 charge factor of the molecule (sum over lanes, fixed order)
@@ -142,8 +165,11 @@ __device__ void stage(const Pool& P, const ChainHdr& H, int m, const Proposal* p
     if (shy != 0) y = __dadd_rn(y, shy);
     if (shz != 0) z = __dadd_rn(z, shz);
     s.nx[i] = x; s.ny[i] = y; s.nz[i] = z;
-    const float4 o = make_float4((float)(x - ax), (float)(y - ay), (float)(z - az), s.o_old[i].w);
+    const double vx = x - ax, vy = y - ay, vz = z - az;
+    const float4 o = make_float4((float)vx, (float)vy, (float)vz, s.o_old[i].w);
     s.o_new[i] = o;
+    s.l_new[i] = make_float4((float)(vx - (double)o.x), (float)(vy - (double)o.y),
+                             (float)(vz - (double)o.z), 0.f);
     s.eq[i].w = fmaf(o.x, o.x, fmaf(o.y, o.y, o.z * o.z));
   }
   __syncwarp();
@@ -170,10 +196,10 @@ __device__ __forceinline__ MovedInfo load_moved(const GroupSmem& s) {
 
 // ---- screen ---------------------------------------------------------------
 
-// FP32 screen with FP64 re-test inside the guard band; fills the entry's
-// minimum-image anchor differences for the FP32 pair path.
+// FP32 screen with FP64 re-test inside the guard band (plain path: FP64
+// positions from the master rows).
 __device__ __forceinline__ int screen_mixed(const Pool& P, const ChainHdr& H, const GroupSmem& s,
-                                            const MovedInfo& mi, int j, float4& A, float2& B) {
+                                            const MovedInfo& mi, int j) {
   const int2 pj = P.mpi[j];
   int f = 0;
   for (int k2 = 0; k2 < pj.y; k2++) {
@@ -199,21 +225,6 @@ __device__ __forceinline__ int screen_mixed(const Pool& P, const ChainHdr& H, co
       }
     }
   }
-  if (f) {
-    const uint4 fj = P.mfix[j];
-    const float rr = mi.rad + P.mrad[j];
-    float3 Do = make_float3(0.f, 0.f, 0.f), Dn = Do;
-    if (f & kInOld) {
-      Do = fixdiff(fj, mi.fx_old, H);
-      if (needs_wrap(Do, rr, H)) f |= kWrapOld;
-    }
-    if (f & kInNew) {
-      Dn = fixdiff(fj, mi.fx_new, H);
-      if (needs_wrap(Dn, rr, H)) f |= kWrapNew;
-    }
-    A = make_float4(Do.x, Do.y, Do.z, Dn.x);
-    B = make_float2(Dn.y, Dn.z);
-  }
   return f;
 }
 
@@ -237,20 +248,40 @@ __device__ __forceinline__ int screen_f64(const Pool& P, const ChainHdr& H, cons
 
 // ---- pair batches -----------------------------------------------------------
 
+// Per-thread double-float accumulators of one evaluation.
+struct AccFF {
+  float oh, ol, nh, nl, ab;
+  long long np;
+};
+
+// Displacement of a pair, atom b of the neighbour minus atom a of the moved
+// molecule, both anchor-relative to the moved molecule's anchor.  PRECISE
+// adds the low parts (bl: of b = D + o_b; la: of a's offset) so the only
+// rounding left is the final one at the displacement's own magnitude.
+template <bool PRECISE>
+__device__ __forceinline__ float3 pair_disp(float3 bh, float3 bl, float4 a, float4 la) {
+  if (PRECISE)
+    return make_float3((bh.x - a.x) + (bl.x - la.x), (bh.y - a.y) + (bl.y - la.y),
+                       (bh.z - a.z) + (bl.z - la.z));
+  return make_float3(bh.x - a.x, bh.y - a.y, bh.z - a.z);
+}
+
 // Sum over the moved molecule's atoms a of the FP32 pair terms with one
-// neighbour atom b at anchor-relative position (bx, by, bz), per-pair
-// periodic image (entries whose atom pairs may straddle half a box edge).
-// abs accumulates |LJ| + |Coulomb| (the scale of the rounding error).
-__device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4* eq, int len,
-                                                  float bx, float by, float bz, float sb,
-                                                  float2 qb, const ChainHdr& H, float& abs) {
+// neighbour atom b, per-pair periodic image (entries whose atom pairs may
+// straddle half a box edge).  abs accumulates |LJ| + |Coulomb|.
+template <bool PRECISE>
+__device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4* lo,
+                                                  const float4* eq, int len, float3 bh, float3 bl,
+                                                  float sb, float2 qb, const ChainHdr& H,
+                                                  float& abs) {
   float acc = 0.f;
   for (int i = 0; i < len; i++) {
-    const float4 a = o[i];
     const float4 ea = eq[i];
-    const float dx = wrapf(bx - a.x, H.Lf[0]);
-    const float dy = wrapf(by - a.y, H.Lf[1]);
-    const float dz = wrapf(bz - a.z, H.Lf[2]);
+    const float4 a = o[i];
+    const float3 d = pair_disp<PRECISE>(bh, bl, a, PRECISE ? lo[i] : a);
+    const float dx = wrapf(d.x, H.Lf[0]);
+    const float dy = wrapf(d.y, H.Lf[1]);
+    const float dz = wrapf(d.z, H.Lf[2]);
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float ir = rsqrt_nr(r2);
     const float lj = lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x);
@@ -268,21 +299,23 @@ __device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4*
 //   1/r - 1/R = (R^2 - r^2) / (r R (r + R)),  R^2 - r^2 = 2 b.o_a - |o_a|^2,
 // so every Coulomb term is O(|o_a| / R) smaller than q_a q_b / r and carries
 // proportionally less FP32 rounding.  A coincident pair (r = 0) is skipped
-// as the reference skips it (BruteForceStep.cpp:68-69).  oo selects the
+// as the reference skips it (BruteForceStep.cpp:68-69).  use_new selects the
 // |o_a|^2 of the placement (eq.z old, eq.w new).
-__device__ __forceinline__ float sum_moved32_cf(const float4* o, const float4* eq, int len,
-                                                bool use_new, float bx, float by, float bz,
-                                                float sb, float2 qb, float qm, float& abs) {
-  const float R2 = fmaf(bx, bx, fmaf(by, by, bz * bz));
+template <bool PRECISE>
+__device__ __forceinline__ float sum_moved32_cf(const float4* o, const float4* lo,
+                                                const float4* eq, int len, bool use_new,
+                                                float3 bh, float3 bl, float sb, float2 qb,
+                                                float qm, float& abs) {
+  const float R2 = fmaf(bh.x, bh.x, fmaf(bh.y, bh.y, bh.z * bh.z));
   const float iR = rsqrt_nr(R2);
   const float R = R2 * iR;
-  const float tx = bx + bx, ty = by + by, tz = bz + bz;
+  const float tx = bh.x + bh.x, ty = bh.y + bh.y, tz = bh.z + bh.z;
   float lj_acc = 0.f, phi = 0.f, lj_abs = 0.f, c_abs = 0.f;
   for (int i = 0; i < len; i++) {
     const float4 a = o[i];
     const float4 ea = eq[i];
-    const float dx = bx - a.x, dy = by - a.y, dz = bz - a.z;
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float3 d = pair_disp<PRECISE>(bh, bl, a, PRECISE ? lo[i] : a);
+    const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
     const float ir = rsqrt_nr(r2);
     const float lj = lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x);
     const float num = fmaf(tx, a.x, fmaf(ty, a.y, fmaf(tz, a.z, -(use_new ? ea.w : ea.z))));
@@ -299,48 +332,73 @@ __device__ __forceinline__ float sum_moved32_cf(const float4* o, const float4* e
   return fmaf(f, phi + qm, lj_acc);
 }
 
-// Evaluates `count` ring entries from `head` with teams of T lanes (T a
-// power of two <= 32): lane tl of a team takes neighbour atoms tl, tl+T, ...
-// of the entry's molecule against every atom of the moved molecule.  The
-// team's FP32 partial of each entry is added to the FP64 sums eo / en (and
-// its magnitude to ab) of the team's first lane.
-__device__ __forceinline__ void batch_mixed(const Pool& P, const ChainHdr& H, const GroupSmem& s,
-                                            const MovedInfo& mi, const int* rj, const float4* rA,
-                                            const float2* rB, int head, int count, int lane, int T,
-                                            double& eo, double& en, double& ab, long long& np) {
+// Pair batch of `count` ring entries from `head`, teams of T lanes (T a
+// power of two <= 32): the team forms the entry's anchor differences
+// (fixed point -> FP32, or double-float when PRECISE) and image flags, lane
+// tl takes neighbour atoms tl, tl+T, ... against every atom of the moved
+// molecule, and the team's FP32 partial of the entry is added in
+// double-float to the team leader's accumulators.  LO: the plain path, whose
+// FP32 offsets carry low parts (aofl, l_old/l_new).
+template <bool PRECISE, bool LO>
+__device__ __forceinline__ void batch_ff(const Pool& P, const ChainHdr& H, const GroupSmem& s,
+                                         const MovedInfo& mi, const int* rj, int head, int count,
+                                         int lane, int T, AccFF& acc) {
   const int tm = lane / T, tl = lane - tm * T, nteams = 32 / T;
   for (int e0 = 0; e0 < count; e0 += nteams) {
     const int e = e0 + tm;
     int f = 0, b0 = 0, lenj = 0, actj = 0;
-    float4 A = make_float4(0.f, 0.f, 0.f, 0.f);
-    float2 B = make_float2(0.f, 0.f);
+    float3 Do = make_float3(0.f, 0.f, 0.f), Dn = Do, Dol = Do, Dnl = Do;
     if (e < count) {
-      const int idx = (head + e) & (kRing - 1);
-      const int jf = rj[idx];
-      A = rA[idx];
-      B = rB[idx];
+      const int jf = rj[(head + e) & (kRing - 1)];
       const int j = jf >> 4;
       f = jf & 15;
       b0 = P.mstart[j];
       const int lw = P.mlen[j];
+      const uint4 fj = P.mfix[j];
+      const float rr = mi.rad + P.mrad[j];
       lenj = lw & 255;
       actj = lw >> 8;
+      if (f & kInOld) {
+        if (PRECISE) fixdiff_ff(fj, mi.fx_old, H, Do, Dol); else Do = fixdiff(fj, mi.fx_old, H);
+        if (needs_wrap(Do, rr, H)) f |= kWrapOld;
+      }
+      if (f & kInNew) {
+        if (PRECISE) fixdiff_ff(fj, mi.fx_new, H, Dn, Dnl); else Dn = fixdiff(fj, mi.fx_new, H);
+        if (needs_wrap(Dn, rr, H)) f |= kWrapNew;
+      }
     }
     float so = 0.f, sn = 0.f, sa = 0.f;
     for (int b = b0 + tl; b < b0 + lenj; b += T) {
       const float4 ob = P.aoff[b];
       const float2 qb = P.aeq[b];
+      float4 obl = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (LO && PRECISE) obl = P.aofl[b];
       if (f & kInOld) {
-        const float bx = A.x + ob.x, by = A.y + ob.y, bz = A.z + ob.z;
-        so += (f & kWrapOld) ? sum_moved32_wrap(s.o_old, s.eq, mi.len, bx, by, bz, ob.w, qb, H, sa)
-                             : sum_moved32_cf(s.o_old, s.eq, mi.len, false, bx, by, bz, ob.w, qb,
-                                              mi.qm, sa);
+        float3 bh = make_float3(Do.x + ob.x, Do.y + ob.y, Do.z + ob.z), bl = Dol;
+        if (PRECISE) {
+          // two-sum of D + o_b per axis, then the low parts
+          const float ex = (Do.x - (bh.x - (bh.x - Do.x))) + (ob.x - (bh.x - Do.x));
+          const float ey = (Do.y - (bh.y - (bh.y - Do.y))) + (ob.y - (bh.y - Do.y));
+          const float ez = (Do.z - (bh.z - (bh.z - Do.z))) + (ob.z - (bh.z - Do.z));
+          bl = make_float3(ex + (Dol.x + obl.x), ey + (Dol.y + obl.y), ez + (Dol.z + obl.z));
+        }
+        so += (f & kWrapOld)
+                  ? sum_moved32_wrap<PRECISE>(s.o_old, s.l_old, s.eq, mi.len, bh, bl, ob.w, qb, H, sa)
+                  : sum_moved32_cf<PRECISE>(s.o_old, s.l_old, s.eq, mi.len, false, bh, bl, ob.w, qb,
+                                            mi.qm, sa);
       }
       if (f & kInNew) {
-        const float bx = A.w + ob.x, by = B.x + ob.y, bz = B.y + ob.z;
-        sn += (f & kWrapNew) ? sum_moved32_wrap(s.o_new, s.eq, mi.len, bx, by, bz, ob.w, qb, H, sa)
-                             : sum_moved32_cf(s.o_new, s.eq, mi.len, true, bx, by, bz, ob.w, qb,
-                                              mi.qm, sa);
+        float3 bh = make_float3(Dn.x + ob.x, Dn.y + ob.y, Dn.z + ob.z), bl = Dnl;
+        if (PRECISE) {
+          const float ex = (Dn.x - (bh.x - (bh.x - Dn.x))) + (ob.x - (bh.x - Dn.x));
+          const float ey = (Dn.y - (bh.y - (bh.y - Dn.y))) + (ob.y - (bh.y - Dn.y));
+          const float ez = (Dn.z - (bh.z - (bh.z - Dn.z))) + (ob.z - (bh.z - Dn.z));
+          bl = make_float3(ex + (Dnl.x + obl.x), ey + (Dnl.y + obl.y), ez + (Dnl.z + obl.z));
+        }
+        sn += (f & kWrapNew)
+                  ? sum_moved32_wrap<PRECISE>(s.o_new, s.l_new, s.eq, mi.len, bh, bl, ob.w, qb, H, sa)
+                  : sum_moved32_cf<PRECISE>(s.o_new, s.l_new, s.eq, mi.len, true, bh, bl, ob.w, qb,
+                                            mi.qm, sa);
       }
     }
     for (int off = T >> 1; off > 0; off >>= 1) {
@@ -349,9 +407,15 @@ __device__ __forceinline__ void batch_mixed(const Pool& P, const ChainHdr& H, co
       sa += __shfl_xor_sync(~0u, sa, off);
     }
     if (tl == 0 && f) {
-      if (f & kInOld) { eo += (double)so; np += (long long)mi.act * actj; }
-      if (f & kInNew) { en += (double)sn; np += (long long)mi.act * actj; }
-      ab += (double)sa;
+      if (f & kInOld) {
+        ff_add(acc.oh, acc.ol, so);
+        acc.np += (long long)mi.act * actj;
+      }
+      if (f & kInNew) {
+        ff_add(acc.nh, acc.nl, sn);
+        acc.np += (long long)mi.act * actj;
+      }
+      acc.ab += sa;
     }
   }
 }
@@ -415,43 +479,31 @@ __device__ __forceinline__ void batch_f64(const Pool& P, const ChainHdr& H, cons
 
 // One warp screens candidates [c_begin, c_end) in warp-strided rounds of 32
 // (round r of warp w covers c_begin + (r*nw + w)*32 + lane), appends hits to
-// its ring and evaluates them in batches of 32.
+// its ring and evaluates them in batches of 32.  FP32 pairs accumulate in
+// double-float and are added to the FP64 sums at the end.
 template <bool F64>
 __device__ void warp_eval(const Pool& P, const ChainHdr& H, const GroupSmem& s, const MovedInfo& mi,
                           int c_begin, int c_end, int w, int nw, int lane, int T, double& eo,
                           double& en, double& ab, long long& np) {
   int* rj = s.lj + w * kRing;
-  float4* rA = s.lA + w * kRing;
-  float2* rB = s.lB + w * kRing;
   int head = 0, tail = 0;
   const unsigned lt = lanemask_lt();
+  AccFF acc = {0.f, 0.f, 0.f, 0.f, 0.f, 0};
   for (int base = c_begin + w * 32; base < c_end; base += nw * 32) {
     const int j = base + lane;
     int f = 0;
-    float4 A;
-    float2 B;
-    if (j < c_end && j != mi.mol) {
-      if (F64)
-        f = screen_f64(P, H, s, mi, j);
-      else
-        f = screen_mixed(P, H, s, mi, j, A, B);
-    }
+    if (j < c_end && j != mi.mol) f = F64 ? screen_f64(P, H, s, mi, j) : screen_mixed(P, H, s, mi, j);
     const unsigned bal = __ballot_sync(~0u, f != 0);
-    if (f) {
-      const int pos = (tail + __popc(bal & lt)) & (kRing - 1);
-      rj[pos] = (j << 4) | f;
-      if (!F64) {
-        rA[pos] = A;
-        rB[pos] = B;
-      }
-    }
+    if (f) rj[(tail + __popc(bal & lt)) & (kRing - 1)] = (j << 4) | f;
     tail += __popc(bal);
     if (tail - head >= 32) {
       __syncwarp();
       if (F64)
         batch_f64(P, H, s, mi, rj, head, 32, lane, T, eo, en, ab, np);
+      else if (H.precise)
+        batch_ff<true, true>(P, H, s, mi, rj, head, 32, lane, T, acc);
       else
-        batch_mixed(P, H, s, mi, rj, rA, rB, head, 32, lane, T, eo, en, ab, np);
+        batch_ff<false, true>(P, H, s, mi, rj, head, 32, lane, T, acc);
       head += 32;
       __syncwarp();
     }
@@ -460,10 +512,18 @@ __device__ void warp_eval(const Pool& P, const ChainHdr& H, const GroupSmem& s, 
   if (tail > head) {
     if (F64)
       batch_f64(P, H, s, mi, rj, head, tail - head, lane, T, eo, en, ab, np);
+    else if (H.precise)
+      batch_ff<true, true>(P, H, s, mi, rj, head, tail - head, lane, T, acc);
     else
-      batch_mixed(P, H, s, mi, rj, rA, rB, head, tail - head, lane, T, eo, en, ab, np);
+      batch_ff<false, true>(P, H, s, mi, rj, head, tail - head, lane, T, acc);
   }
   __syncwarp();
+  if (!F64) {
+    eo += (double)acc.oh + (double)acc.ol;
+    en += (double)acc.nh + (double)acc.nl;
+    ab += (double)acc.ab;
+    np += acc.np;
+  }
 }
 
 // Group-wide deterministic sum of (a, b, d, c): warp shuffles, then every
@@ -507,6 +567,7 @@ __device__ __forceinline__ void commit(const Pool& P, const GroupSmem& s, const 
     P.y[a] = s.ny[i];
     P.z[a] = s.nz[i];
     P.aoff[a] = s.o_new[i];
+    P.aofl[a] = s.l_new[i];
   }
   const int2 pi = P.mpi[mi.mol];
   for (int k = lane; k < mi.npidx; k += 32) P.ppos[pi.x + k] = s.p_new[k];
@@ -524,7 +585,11 @@ __device__ __forceinline__ void refresh_molecule(const Pool& P, const ChainHdr& 
   for (int i = lane; i < len; i += nl) {
     const int a = a0 + i;
     const float w = P.aoff[a].w;
-    P.aoff[a] = make_float4((float)(P.x[a] - ax), (float)(P.y[a] - ay), (float)(P.z[a] - az), w);
+    const double vx = P.x[a] - ax, vy = P.y[a] - ay, vz = P.z[a] - az;
+    const float4 o = make_float4((float)vx, (float)vy, (float)vz, w);
+    P.aoff[a] = o;
+    P.aofl[a] = make_float4((float)(vx - (double)o.x), (float)(vy - (double)o.y),
+                            (float)(vz - (double)o.z), 0.f);
   }
   for (int k = lane; k < pi.y; k += nl) {
     const int q = P.pidx[pi.x + k];

@@ -177,20 +177,4 @@ __device__ __forceinline__ int fixstep(float dx, float inv_s) {
   return __float2int_rn(__fmul_rn(dx, inv_s));
 }
 
-// Double-float accumulation: (hi, lo) += v with Knuth's two-sum, so sums of
-// FP32 terms keep ~48 significant bits without FP64 instructions.
-__device__ __forceinline__ void ff_add(float& hi, float& lo, float v) {
-  const float s = __fadd_rn(hi, v);
-  const float bb = __fsub_rn(s, hi);
-  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb));
-  hi = s;
-  lo = __fadd_rn(lo, err);
-}
-
-// (hi, lo) += (h2, l2).
-__device__ __forceinline__ void ff_add2(float& hi, float& lo, float h2, float l2) {
-  ff_add(hi, lo, h2);
-  lo = __fadd_rn(lo, l2);
-}
-
 }  // namespace mcgpu

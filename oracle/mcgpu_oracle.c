@@ -150,6 +150,38 @@ double orc_mol_energy_abs(const orc_box* b, int curr, int start) {
   return total;
 }
 
+/* Like orc_mol_energy_abs with each term weighted by its condition number
+ * with respect to the pair distance, |d ln t / d ln r|: 12 for 4 eps s^12,
+ * 6 for 4 eps s^6, 1 for Coulomb.  A term evaluated from positions with
+ * relative error d carries an error of about (weight * |t| * d), so this
+ * sum sets the rounding scale of FP32 pair terms at close contacts. */
+double orc_mol_energy_absk(const orc_box* b, int curr, int start) {
+  double total = 0;
+  const int p1s = b->mol_pidx_start[curr];
+  const int p1e = b->mol_pidx_count[curr] + p1s;
+  for (int other = start; other < b->n_mol; other++) {
+    if (other == curr) continue;
+    int p2s = b->mol_pidx_start[other];
+    int p2e = b->mol_pidx_count[other] + p2s;
+    if (!orc_molecules_in_range(b, p1s, p1e, p2s, p2e)) continue;
+    const int s1 = b->mol_start[curr], e1 = s1 + b->mol_len[curr];
+    const int s2 = b->mol_start[other], e2 = s2 + b->mol_len[other];
+    for (int i = s1; i < e1; i++)
+      for (int j = s2; j < e2; j++) {
+        if (!(b->sigma[i] >= 0 && b->sigma[j] >= 0 && b->epsilon[i] >= 0 && b->epsilon[j] >= 0))
+          continue;
+        const double r2 = orc_atom_dist2(b, i, j);
+        if (r2 == 0.0) continue;
+        const double sig = orc_blend(b->sigma[i], b->sigma[j]);
+        const double eps = orc_blend(b->epsilon[i], b->epsilon[j]);
+        const double s6 = pow(pow(sig, 2) / r2, 3);
+        total += 12.0 * 4.0 * eps * s6 * s6 + 6.0 * 4.0 * eps * s6 +
+                 fabs(orc_charge(b, i, j, sqrt(r2)));
+      }
+  }
+  return total;
+}
+
 /* SimulationStep::calcSystemEnergy, src/Metropolis/SimulationStep.cpp:40-71
  * with subLJ = subCharge = 0 and the intramolecular term disabled
  * (ENABLE_INTRA false, SimulationStep.h:15): sum over mol of

@@ -57,6 +57,7 @@ double orc_mol_pair_energy(const orc_box* b, int m1, int m2);
 double orc_mol_energy(const orc_box* b, int curr, int start);
 double orc_system_energy(const orc_box* b);
 double orc_mol_energy_abs(const orc_box* b, int curr, int start);
+double orc_mol_energy_absk(const orc_box* b, int curr, int start);
 int orc_count_pairs(const orc_box* b, int curr, long long* mol_pairs, long long* atom_pairs);
 
 void orc_keep_in_box(orc_box* b, int mol);

@@ -89,6 +89,7 @@ def orc_lib() -> C.CDLL:
             "orc_mol_energy": (C.c_double, [P, C.c_int, C.c_int]),
             "orc_system_energy": (C.c_double, [P]),
             "orc_mol_energy_abs": (C.c_double, [P, C.c_int, C.c_int]),
+            "orc_mol_energy_absk": (C.c_double, [P, C.c_int, C.c_int]),
             "orc_mol_pair_energy": (C.c_double, [P, C.c_int, C.c_int]),
             "orc_count_pairs": (C.c_int, [P, C.c_int, C.POINTER(C.c_longlong),
                                           C.POINTER(C.c_longlong)]),
@@ -165,7 +166,10 @@ class OracleBox:
         return orc_lib().orc_system_energy(self.ref)
 
     def mol_energy_abs(self, curr: int, start: int = 0) -> float:
-        return orc_lib().orc_mol_energy_abs(self.ref, curr, start)
+        """Scale of an FP32-pair result's rounding: the sum over the pair
+        terms of |term| times its condition number with respect to distance
+        (12 for 4 eps s^12, 6 for 4 eps s^6, 1 for Coulomb)."""
+        return orc_lib().orc_mol_energy_absk(self.ref, curr, start)
 
     def count_pairs(self, curr: int) -> tuple[int, int]:
         a, b = C.c_longlong(), C.c_longlong()

@@ -10,7 +10,12 @@ from mcgpu_gb300.workloads import BoxData
 GOLDEN = Path(__file__).resolve().parent / "golden"
 GOLDEN_NAMES = ["water256", "t3p64", "bicyclic100", "mixed", "water48_halfbox"]
 
-# FP32 pair terms: |err| <= REL * max(|E|, FLOOR * sum|pair terms|)
+# FP32 pair terms: |err| <= REL * max(|E|, FLOOR * sum_t k_t |t|), the sum over
+# the pair terms of each term's magnitude times its condition number with
+# respect to the pair distance (k = 12 for 4 eps s^12, 6 for 4 eps s^6, 1 for
+# Coulomb; OracleBox.mol_energy_abs): FP32 positions carry a relative error of
+# order 1e-7 that each term amplifies by k, so at close LJ contacts the plain
+# sum of |terms| under-states the rounding scale twelvefold.
 REL = 1e-5
 FLOOR = 1e-3
 # FP64 pair terms, different summation order only
