@@ -195,6 +195,34 @@ int mcgpu_batch_download(mcgpu_batch* batch, int chain, double* x, double* y,
  * out[n_chains]; the running totals are not changed. */
 int mcgpu_batch_system_energy(mcgpu_batch* batch, double* out);
 
+/* ---- no-allocation system energy ---------------------------------------- */
+
+/* No counterpart in the reference: an extra entry point for callers that may
+ * not allocate device memory through this library -- an OpenACC/OpenMP
+ * offload program whose SimBox rows already live in its own device data
+ * region, or an application whose device memory belongs to another
+ * allocator (a caching allocator, a fixed arena) that forbids allocations by
+ * third-party code.  It computes what mcgpu_system_energy computes with FP64
+ * pairs (SimulationStep::calcSystemEnergy, SimulationStep.cpp:40-71, with
+ * subLJ = subCharge = 0) without any context, box or allocation:
+ *   rows   -- a descriptor whose row pointers are DEVICE pointers of the
+ *             current CUDA device (only n_*, the rows, size and cutoff are
+ *             read);
+ *   out    -- a DEVICE pointer to one double, written by the call;
+ *   stream -- a cudaStream_t as a plain pointer (NULL = default stream).
+ * The call is asynchronous: *out is ready when the stream reaches it.
+ * Its per-molecule partials go to a fixed array in device memory that the
+ * library reserves on every GPU it is loaded on (256 KiB), so n_mol is at
+ * most 32768; larger boxes return MCGPU_ERR_UNSUPPORTED.  Nothing has to be
+ * zeroed first: every partial a call reads, it has written.  Calls share the
+ * array, so two calls that can run at the same time on one device (two
+ * streams without ordering, two host threads) race and give wrong sums.  The
+ * first call on each device looks up the array's address with that device
+ * current; make that first call before any stream capture.  Rows that index
+ * out of range give NaN instead of being read.  Errors: MCGPU_ERR_INVALID,
+ * MCGPU_ERR_UNSUPPORTED, MCGPU_ERR_CUDA; text via mcgpu_last_error(NULL). */
+int mcgpu_system_energy_static(const mcgpu_box_desc* rows, double* out, void* stream);
+
 /* ---- initial configuration (host only, no GPU) -------------------------- */
 
 /* Places n points uniformly in [0, L)^3 with minimum-image separation >= dmin

@@ -88,6 +88,7 @@ _PROTOS = {
     "mcgpu_batch_download": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
     "mcgpu_batch_system_energy": (C.c_int, [_vp, _dp]),
     "mcgpu_build_centres": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint64, _dp]),
+    "mcgpu_system_energy_static": (C.c_int, [C.POINTER(BoxDesc), _vp, _vp]),
 }
 
 _lib = None

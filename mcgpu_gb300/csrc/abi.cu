@@ -64,6 +64,11 @@ static int set_err(mcgpu_ctx* ctx, int code, const char* fmt, ...) {
   return code;
 }
 
+namespace mcgpu {
+// Error text of context-free entry points, read by mcgpu_last_error(NULL, ...).
+void note_process_error(const char* msg) { g_err = msg; }
+}  // namespace mcgpu
+
 #define CK(ctx, call)                                                                  \
   do {                                                                                 \
     cudaError_t e_ = (call);                                                           \

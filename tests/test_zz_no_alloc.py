@@ -1,0 +1,108 @@
+"""mcgpu_system_energy_static, the system energy that allocates nothing,
+against mcgpu_system_energy (FP64 pairs) through the C ABI.
+
+The caller owns every device buffer (here torch tensors stand in for an
+offload program's own device rows); the entry point gets device pointers and
+writes one device double.  Same FP64 pair terms, different summation order:
+agreement within REL64.  The file is named to be collected last so that it
+also runs after every other GPU test in the same process."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from helpers import load_golden, tol64
+from mcgpu_gb300 import PREC_FP64, Context, GpuBox, _abi
+from mcgpu_gb300.workloads import water_box
+
+pytestmark = pytest.mark.gpu
+
+MAX_MOL = 32768
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = Context(0)
+    yield c
+    c.close()
+
+
+class DeviceRows:
+    """SimBox rows in caller-owned device memory and a descriptor over them."""
+
+    def __init__(self, box):
+        import torch
+        dev = torch.device("cuda:0")
+        f64 = lambda a: torch.tensor(np.ascontiguousarray(a, np.float64), device=dev)
+        i32 = lambda a: torch.tensor(np.ascontiguousarray(a, np.int32), device=dev)
+        self.t = [f64(box.x), f64(box.y), f64(box.z), f64(box.sigma), f64(box.epsilon),
+                  f64(box.charge), i32(box.mol_start), i32(box.mol_len),
+                  i32(box.mol_pidx_start), i32(box.mol_pidx_count), i32(box.pidx)]
+        self.out = torch.full((1,), float("nan"), dtype=torch.float64, device=dev)
+        d = _abi.BoxDesc()
+        d.n_mol, d.n_atom, d.n_pidx = box.n_mol, box.n_atom, len(box.pidx)
+        names = ["x", "y", "z", "sigma", "epsilon", "charge", "mol_start", "mol_len",
+                 "mol_pidx_start", "mol_pidx_count", "pidx"]
+        for n, t in zip(names, self.t):
+            ptype = _abi._dp if t.dtype == torch.float64 else _abi._ip
+            setattr(d, n, C.cast(C.c_void_p(t.data_ptr()), ptype))
+        for k in range(3):
+            d.size[k] = float(box.size[k])
+        d.cutoff = float(box.cutoff)
+        self.desc = d
+
+    def energy(self) -> float:
+        import torch
+        stream = torch.cuda.current_stream().cuda_stream
+        st = _abi.lib().mcgpu_system_energy_static(C.byref(self.desc),
+                                                   C.c_void_p(self.out.data_ptr()),
+                                                   C.c_void_p(stream))
+        _abi.check(st)
+        torch.cuda.synchronize()
+        return float(self.out.item())
+
+
+def reference_energy(ctx, box) -> float:
+    g = GpuBox(ctx, box, PREC_FP64)
+    e = g.system_energy()
+    g.close()
+    return e
+
+
+def test_static_energy_two_calls_in_a_row(ctx):
+    """Two boxes of different sizes back to back, then the first again: the
+    scratch left by one call does not leak into the next."""
+    boxes = [load_golden("water256")[0], load_golden("t3p64")[0], load_golden("bicyclic100")[0]]
+    refs = [reference_energy(ctx, b) for b in boxes]
+    rows = [DeviceRows(b) for b in boxes]
+    for i in (0, 1, 0, 2, 1):
+        e = rows[i].energy()
+        assert abs(e - refs[i]) <= tol64(refs[i]), (boxes[i].name, e, refs[i])
+    e1, e2 = rows[0].energy(), rows[0].energy()
+    assert e1 == e2
+
+
+def test_static_energy_allocates_nothing_after_setup(ctx):
+    import torch
+    box = water_box(1000, seed=5)
+    ref = reference_energy(ctx, box)
+    rows = DeviceRows(box)
+    assert abs(rows.energy() - ref) <= tol64(ref)      # first call: address lookup
+    free0 = torch.cuda.mem_get_info(0)[0]
+    for _ in range(2):
+        assert abs(rows.energy() - ref) <= tol64(ref)
+    assert torch.cuda.mem_get_info(0)[0] == free0
+
+
+def test_static_energy_rejects_oversized_box():
+    import torch
+    d = _abi.BoxDesc()
+    d.n_mol, d.n_atom, d.n_pidx = MAX_MOL + 1, 3 * (MAX_MOL + 1), MAX_MOL + 1
+    buf_out = torch.zeros(1, dtype=torch.float64, device="cuda:0")
+    out = C.c_void_p(buf_out.data_ptr())
+    st = _abi.lib().mcgpu_system_energy_static(C.byref(d), out, None)
+    assert st == 4   # MCGPU_ERR_UNSUPPORTED, before any device access
+    buf = C.create_string_buffer(256)
+    _abi.lib().mcgpu_last_error(None, buf, 256)
+    assert b"32768" in buf.value
+    assert _abi.lib().mcgpu_system_energy_static(None, out, None) == 1
