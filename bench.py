@@ -233,6 +233,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tile", default=None,
+                    help="threads,chains_per_cta,steps_per_launch,lanes (skips the autotuner)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_info()
@@ -249,8 +251,12 @@ def main():
 
     boxes, seeds = M.water_chains(N_CHAINS, seed=2024 + 7919 * rank)
     bt = M.ChainBatch(ctx, boxes, seeds, rotation=M.ROT_AXIS)
-    tile = bt.autotune(64) if not args.no_autotune else bt.tile
-    threads, cpc, spl = tile
+    if args.tile:
+        bt.set_tile(*[int(v) for v in args.tile.split(",")])
+        tile = bt.tile
+    else:
+        tile = bt.autotune(64) if not args.no_autotune else bt.tile
+    threads, cpc, spl, lanes = tile
     launches_per_step = math.ceil(STEPS_PER_BENCH / spl)
 
     # The library launches on a torch stream, so CUDA events recorded on that
@@ -306,7 +312,7 @@ def main():
         d2h = sum(b.n_atom * 24 for b in boxes) + N_CHAINS * 40
         t0 = time.perf_counter()
         b2 = M.ChainBatch(ctx, boxes, seeds, rotation=M.ROT_AXIS)
-        b2.set_tile(threads, cpc, spl)
+        b2.set_tile(threads, cpc, spl, lanes)
         b2.run(STEPS_PER_BENCH * args.steps, sync=True)
         st_e2e = b2.stats()
         for c in range(N_CHAINS):
@@ -336,7 +342,8 @@ def main():
         "config": {"workload": WORKLOAD, "chains": N_CHAINS,
                    "molecules": sum(b.n_mol for b in boxes),
                    "steps_per_bench_step": STEPS_PER_BENCH,
-                   "tile": {"threads": threads, "chains_per_cta": cpc, "steps_per_launch": spl},
+                   "tile": {"threads": threads, "chains_per_cta": cpc, "steps_per_launch": spl,
+                            "lanes_per_molecule": lanes},
                    "precision": "FP32 pair terms, FP64 per-neighbour sums, dE and totals",
                    "l2": "flushed between timed steps (256 MiB write); the chains' state "
                          "(~14 MB) is re-read from HBM at each step start",

@@ -86,7 +86,22 @@ typedef struct {
   int32_t ties;           /* decisions re-taken with FP64 pairs because the
                              FP32 dE fell within its rounding bound of the
                              acceptance threshold                           */
+  double box[3];          /* current box edges (they change under NPT)     */
+  int32_t vol_tried;      /* volume moves attempted                        */
+  int32_t vol_accepted;   /* volume moves accepted                         */
 } mcgpu_chain_stats;
+
+/* One volume move of an NPT chain (for replay checks). */
+typedef struct {
+  int64_t step;           /* chain step count when the move was made       */
+  int32_t accepted;
+  int32_t evaluated;      /* 0 if rejected outright (the new edge would be
+                             at most four times the largest molecule
+                             radius)                                        */
+  double e_old, e_new;    /* FP64 system energies at V and V'              */
+  double dlnv, u;         /* the ln V step and the acceptance uniform      */
+  double edge;            /* box edge x after the decision                 */
+} mcgpu_vol_trace;
 
 /* One step of a recorded device trajectory (for replay checks). */
 typedef struct {
@@ -177,15 +192,36 @@ int mcgpu_batch_run(mcgpu_batch* batch, int n_steps, int sync);
 /* Chooses steps_per_launch, chains per CTA and threads per molecule by timing
  * candidate tiles on this batch (state is saved and restored). */
 int mcgpu_batch_autotune(mcgpu_batch* batch, int trial_steps);
-/* Sets the tile explicitly: threads per CTA (64..512), chains per CTA
- * (1, 2, 4), steps per launch (>= 1). */
+/* Sets the tile explicitly: threads per CTA (32..512, a multiple of 32),
+ * chains per CTA (dividing its warps), steps per launch (>= 1), and lanes
+ * per neighbour molecule (a power of two <= 32 capping every chain's
+ * default, the power of two at or above its largest molecule; 0 keeps the
+ * defaults).  Results do not depend on the first three; the lanes change the
+ * FP32 summation order and so the last bits of the energies. */
 int mcgpu_batch_set_tile(mcgpu_batch* batch, int threads, int chains_per_cta,
-                         int steps_per_launch);
+                         int steps_per_launch, int lanes_per_molecule);
 int mcgpu_batch_get_tile(mcgpu_batch* batch, int* threads, int* chains_per_cta,
-                         int* steps_per_launch);
+                         int* steps_per_launch, int* lanes_per_molecule);
 /* Like mcgpu_batch_run (synchronous, no graph) and records every step:
- * out[c * n_steps + s] is step s of chain c. */
-int mcgpu_batch_run_traced(mcgpu_batch* batch, int n_steps, mcgpu_trace* out);
+ * out[c * n_steps + s] is step s of chain c.  If vol_out is non-NULL it
+ * receives the volume moves of an NPT batch: vol_out[c * (n_steps /
+ * interval + 1) + k] is the k-th volume move of chain c in this call. */
+int mcgpu_batch_run_traced(mcgpu_batch* batch, int n_steps, mcgpu_trace* out,
+                           mcgpu_vol_trace* vol_out);
+/* Makes the batch isobaric (NPT): after every `interval` steps of a chain
+ * (its step count a multiple of interval) it attempts one volume move,
+ * ln V' = ln V + U(-max_dlnv[c], max_dlnv[c]) with every edge scaled by
+ * exp(dlnv / 3) and the molecules' centres (first primary atoms) scaled
+ * with it, accepted by the isobaric criterion
+ *   exp(-(U(V') - U(V) + P (V' - V)) / kT + (N + 1) dlnv) >= u
+ * at pressure_atm[c] atmospheres (1 atm = 1.4584e-5 kcal/mol/A^3), with
+ * U(V) and U(V') full FP64 system energies; the chain's running energy then
+ * restarts from the FP64 energy of the volume it keeps.  The reference's
+ * NPTEnsemble (Ensemble.cpp:9-23, SimulationStep.cpp:476-518) is the
+ * counterpart; its fixed factor 1.1 and unitless P dV are not reproduced.
+ * interval 0 makes the batch NVT again.  max_dlnv in (0, 0.1]. */
+int mcgpu_batch_set_npt(mcgpu_batch* batch, int interval, const double* pressure_atm,
+                        const double* max_dlnv);
 int mcgpu_batch_sync(mcgpu_batch* batch);
 int mcgpu_batch_stats(mcgpu_batch* batch, mcgpu_chain_stats* stats);
 /* Coordinates of chain c (arrays sized like its descriptor). */

@@ -49,7 +49,14 @@ class Move(C.Structure):
 
 class ChainStats(C.Structure):
     _fields_ = [("energy", C.c_double), ("steps", C.c_int64), ("accepted", C.c_int64),
-                ("pairs", C.c_int64), ("error", C.c_int32), ("ties", C.c_int32)]
+                ("pairs", C.c_int64), ("error", C.c_int32), ("ties", C.c_int32),
+                ("box", C.c_double * 3), ("vol_tried", C.c_int32), ("vol_accepted", C.c_int32)]
+
+
+class VolTrace(C.Structure):
+    _fields_ = [("step", C.c_int64), ("accepted", C.c_int32), ("evaluated", C.c_int32),
+                ("e_old", C.c_double), ("e_new", C.c_double), ("dlnv", C.c_double),
+                ("u", C.c_double), ("edge", C.c_double)]
 
 
 class Trace(C.Structure):
@@ -80,10 +87,11 @@ _PROTOS = {
     "mcgpu_batch_destroy": (C.c_int, [_vp]),
     "mcgpu_batch_run": (C.c_int, [_vp, C.c_int, C.c_int]),
     "mcgpu_batch_autotune": (C.c_int, [_vp, C.c_int]),
-    "mcgpu_batch_set_tile": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int]),
-    "mcgpu_batch_get_tile": (C.c_int, [_vp, _ip, _ip, _ip]),
+    "mcgpu_batch_set_tile": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "mcgpu_batch_get_tile": (C.c_int, [_vp, _ip, _ip, _ip, _ip]),
     "mcgpu_batch_sync": (C.c_int, [_vp]),
-    "mcgpu_batch_run_traced": (C.c_int, [_vp, C.c_int, C.POINTER(Trace)]),
+    "mcgpu_batch_run_traced": (C.c_int, [_vp, C.c_int, C.POINTER(Trace), C.POINTER(VolTrace)]),
+    "mcgpu_batch_set_npt": (C.c_int, [_vp, C.c_int, _dp, _dp]),
     "mcgpu_batch_stats": (C.c_int, [_vp, C.POINTER(ChainStats)]),
     "mcgpu_batch_download": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
     "mcgpu_batch_system_energy": (C.c_int, [_vp, _dp]),

@@ -43,29 +43,56 @@ class ChainBatch:
     def run(self, n_steps: int, sync: bool = True) -> None:
         self._check(_abi.lib().mcgpu_batch_run(self._h, int(n_steps), 1 if sync else 0))
 
-    def run_traced(self, n_steps: int) -> list[list]:
-        """Runs n_steps and returns, per chain, the list of step records."""
+    def run_traced(self, n_steps: int, volume: bool = False):
+        """Runs n_steps and returns, per chain, the list of step records;
+        with volume=True also, per chain, the volume-move records of an NPT
+        batch (as a second list)."""
         arr = (_abi.Trace * (n_steps * self.n_chains))()
-        self._check(_abi.lib().mcgpu_batch_run_traced(self._h, int(n_steps), arr))
+        vs = n_steps // self.vol_interval + 1 if (volume and self.vol_interval > 0) else 0
+        varr = (_abi.VolTrace * max(1, vs * self.n_chains))() if vs else None
+        self._check(_abi.lib().mcgpu_batch_run_traced(self._h, int(n_steps), arr, varr))
         flat = list(arr)
-        return [flat[c * n_steps:(c + 1) * n_steps] for c in range(self.n_chains)]
+        steps = [flat[c * n_steps:(c + 1) * n_steps] for c in range(self.n_chains)]
+        if not volume:
+            return steps
+        vols = []
+        for c in range(self.n_chains):
+            recs = list(varr[c * vs:(c + 1) * vs]) if vs else []
+            vols.append([r for r in recs if r.step > 0])
+        return steps, vols
+
+    vol_interval = 0
+
+    def set_npt(self, interval: int, pressure_atm, max_dlnv) -> None:
+        """Isobaric volume moves every `interval` steps (0 = NVT again);
+        pressure_atm and max_dlnv are scalars or one value per chain."""
+        n = self.n_chains
+        p = np.broadcast_to(np.asarray(pressure_atm, np.float64), (n,)).copy()
+        d = np.broadcast_to(np.asarray(max_dlnv, np.float64), (n,)).copy()
+        dp = C.POINTER(C.c_double)
+        self._check(_abi.lib().mcgpu_batch_set_npt(self._h, int(interval), p.ctypes.data_as(dp),
+                                                   d.ctypes.data_as(dp)))
+        self.vol_interval = int(interval)
 
     def sync(self) -> None:
         self._check(_abi.lib().mcgpu_batch_sync(self._h))
 
-    def autotune(self, trial_steps: int = 64) -> tuple[int, int, int]:
+    def autotune(self, trial_steps: int = 64) -> tuple[int, int, int, int]:
         self._check(_abi.lib().mcgpu_batch_autotune(self._h, int(trial_steps)))
         return self.tile
 
-    def set_tile(self, threads: int, chains_per_cta: int, steps_per_launch: int) -> None:
+    def set_tile(self, threads: int, chains_per_cta: int, steps_per_launch: int,
+                 lanes_per_molecule: int = 0) -> None:
         self._check(_abi.lib().mcgpu_batch_set_tile(self._h, threads, chains_per_cta,
-                                                    steps_per_launch))
+                                                    steps_per_launch, lanes_per_molecule))
 
     @property
-    def tile(self) -> tuple[int, int, int]:
-        t, c, s = C.c_int32(), C.c_int32(), C.c_int32()
-        self._check(_abi.lib().mcgpu_batch_get_tile(self._h, C.byref(t), C.byref(c), C.byref(s)))
-        return t.value, c.value, s.value
+    def tile(self) -> tuple[int, int, int, int]:
+        """(threads per CTA, chains per CTA, steps per launch, lanes cap)."""
+        t, c, s, l = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(_abi.lib().mcgpu_batch_get_tile(self._h, C.byref(t), C.byref(c), C.byref(s),
+                                                    C.byref(l)))
+        return t.value, c.value, s.value, l.value
 
     def stats(self) -> list[_abi.ChainStats]:
         arr = (_abi.ChainStats * self.n_chains)()

@@ -25,7 +25,7 @@ __global__ void k_chain_sums(Pool P, const double* emol, double* out);
 __global__ void k_set_energy(Pool P, const double* e);
 __global__ void k_chain_steps(Pool P, int n_steps, unsigned* queue, const int* order, int n_tasks,
                               int gwarps, SmemShape shape, mcgpu_trace* trace, int trace_off,
-                              int trace_stride);
+                              int trace_stride, int lanes_cap);
 __global__ void k_chain_init(Pool P, const int* mol_chain, int n_mol_total);
 __global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol, int n_atom);
 cudaError_t launch_mol_energy(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
@@ -37,6 +37,9 @@ cudaError_t launch_move_energies(bool f64, int grid, int threads, SmemShape sh, 
 cudaError_t launch_mol_pair_sums(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
                                  Pool P, const int* mol_chain, int m_begin, double* emol,
                                  long long* pairs);
+cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
+                                double2* emol2, double2* esum, mcgpu_vol_trace* trace,
+                                int trace_slot, int trace_stride, cudaStream_t st);
 }  // namespace mcgpu
 
 using namespace mcgpu;
@@ -206,21 +209,10 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
   h.simple_prim = simple ? 1 : 0;
   h.precise = max_len >= 8 ? 1 : 0;
   const double rc = d->cutoff;
-  double ulpL = std::ldexp(1.0, (int)std::floor(std::log2(std::max(
-                                    d->size[0], std::max(d->size[1], d->size[2])))) - 23);
-  double band = 4.0 * (2.0 * std::sqrt(3.0) * rc * 1.5 * ulpL + 4.0 * std::ldexp(rc * rc, -24)) + 1e-6;
-  h.cut2_lo = (float)(rc * rc - band);
-  h.cut2_hi = (float)(rc * rc + band);
-  for (int k = 0; k < 3; k++) {
-    h.L[k] = d->size[k];
-    h.Lf[k] = (float)d->size[k];
-    h.fxinv[k] = 4294967296.0 / d->size[k];
-    h.fxs[k] = (float)(d->size[k] / 4294967296.0);
-    h.fxinvf[k] = (float)(4294967296.0 / d->size[k]);
-    h.fxs_lo[k] = (float)(d->size[k] / 4294967296.0 - (double)h.fxs[k]);
-  }
-  h.kTinvf = (float)(1.0 / (d->temperature * kBoltz));
   h.cutoff = rc;
+  hdr_set_box(h, d->size);
+  h.kTinvf = (float)(1.0 / (d->temperature * kBoltz));
+  h.rad_max = (float)max_rad;
   h.kT = d->temperature * kBoltz;  // SimBoxBuilder.cpp:29
   h.max_t = d->max_translate;
   h.max_r = d->max_rotate;
@@ -691,7 +683,7 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
     Pool P = dp.P;
     P.trace = nullptr;
     k_chain_steps<<<1, nw * 32, sh.bytes(), st>>>(P, k, b->queue, b->order, 1, nw, sh,
-                                                  trace ? b->dtrace : nullptr, done, 0);
+                                                  trace ? b->dtrace : nullptr, done, 0, 0);
     CK(ctx, cudaGetLastError());
     b->rows_stale = true;
   }
@@ -721,11 +713,20 @@ struct mcgpu_batch {
   unsigned* queue = nullptr;   // one counter per launch slot of a graph
   int* order = nullptr;
   int threads = 128, cpc = 1, spl = 16;  // CTA threads, chains per CTA, steps per launch
+  int lanes = 0;                          // lanes per neighbour molecule cap (0 = per chain)
   int cache_n = 0;                        // shared-memory screen cache per group
   bool rows_stale = false;                // FP64 rows lag the chain state
   int max_slots = 0;
   cudaGraphExec_t graph = nullptr;
-  int graph_launches = 0, graph_spl = 0, graph_threads = 0, graph_cpc = 0;
+  int graph_launches = 0, graph_spl = 0, graph_threads = 0, graph_cpc = 0, graph_lanes = 0;
+  int graph_interval = 0;                 // NPT interval the graph covers (0 = NVT graph)
+  // NPT: steps every chain has taken (all chains advance together), the
+  // volume interval, and the volume phase's device buffers
+  long long steps_done = 0;
+  int vol_interval = 0;
+  VolMove* vm = nullptr;
+  double2* emol2 = nullptr;
+  double2* vsum = nullptr;
   // snapshot for the autotuner
   std::vector<void*> snap;
 };
@@ -755,7 +756,7 @@ static int batch_launch(mcgpu_batch* bt, int steps, unsigned* q, cudaStream_t st
   CK(ctx, cudaMemsetAsync(q, 0, sizeof(unsigned), st));
   k_chain_steps<<<grid, bt->threads, smem, st>>>(bt->pool.P, steps, q, bt->order,
                                                  bt->pool.n_chains, gw, sh, trace, trace_off,
-                                                 trace_stride);
+                                                 trace_stride, bt->lanes);
   CK(ctx, cudaGetLastError());
   return MCGPU_OK;
 }
@@ -832,13 +833,16 @@ extern "C" int mcgpu_batch_destroy(mcgpu_batch* bt) {
   bt->pool.release();
   if (bt->queue) cudaFree(bt->queue);
   if (bt->order) cudaFree(bt->order);
+  if (bt->vm) cudaFree(bt->vm);
+  if (bt->emol2) cudaFree(bt->emol2);
+  if (bt->vsum) cudaFree(bt->vsum);
   for (void* p : bt->snap)
     if (p) cudaFree(p);
   delete bt;
   return MCGPU_OK;
 }
 
-extern "C" int mcgpu_batch_set_tile(mcgpu_batch* bt, int threads, int cpc, int spl) {
+extern "C" int mcgpu_batch_set_tile(mcgpu_batch* bt, int threads, int cpc, int spl, int lanes) {
   if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
   mcgpu_ctx* ctx = bt->ctx;
   if (threads < 32 || threads > 512 || threads % 32)
@@ -849,33 +853,54 @@ extern "C" int mcgpu_batch_set_tile(mcgpu_batch* bt, int threads, int cpc, int s
   if ((threads / 32) / cpc > 1 && cpc > 15)
     return set_err(ctx, MCGPU_ERR_INVALID, "at most 15 multi-warp groups per CTA");
   if (spl < 1) return set_err(ctx, MCGPU_ERR_INVALID, "steps per launch %d must be >= 1", spl);
+  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 16 && lanes != 32)
+    return set_err(ctx, MCGPU_ERR_INVALID, "lanes per molecule %d must be 0 or a power of two <= 32",
+                   lanes);
   int smem = shape_for(bt->pool.max_len, (threads / 32) / cpc, bt->cache_n).bytes() * cpc;
   if (smem > 200 * 1024) return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "tile needs %d B shared memory", smem);
   bt->threads = threads;
   bt->cpc = cpc;
   bt->spl = spl;
+  bt->lanes = lanes;
   batch_drop_graph(bt);
   return MCGPU_OK;
 }
 
-extern "C" int mcgpu_batch_get_tile(mcgpu_batch* bt, int* threads, int* cpc, int* spl) {
+extern "C" int mcgpu_batch_get_tile(mcgpu_batch* bt, int* threads, int* cpc, int* spl, int* lanes) {
   if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
   if (threads) *threads = bt->threads;
   if (cpc) *cpc = bt->cpc;
   if (spl) *spl = bt->spl;
+  if (lanes) *lanes = bt->lanes;
   return MCGPU_OK;
 }
 
 // Captures `launches` launches of spl steps each into a graph (one queue
-// counter per launch, reset by a memset node).
-static int batch_build_graph(mcgpu_batch* bt, int launches) {
+// counter per launch, reset by a memset node).  With interval > 0 the graph
+// is one NPT interval instead: launches covering `interval` steps, then the
+// volume phase.
+static int batch_build_graph(mcgpu_batch* bt, int launches, int interval) {
   mcgpu_ctx* ctx = bt->ctx;
   batch_drop_graph(bt);
   cudaStream_t st = ctx->stream;
   cudaGraph_t g = nullptr;
   CK(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   int rc = MCGPU_OK;
-  for (int l = 0; l < launches && rc == MCGPU_OK; l++) rc = batch_launch(bt, bt->spl, bt->queue + l, st);
+  if (interval > 0) {
+    int done = 0;
+    for (int l = 0; done < interval && rc == MCGPU_OK; l++) {
+      const int k = std::min(bt->spl, interval - done);
+      rc = batch_launch(bt, k, bt->queue + l, st);
+      done += k;
+    }
+    if (rc == MCGPU_OK) {
+      cudaError_t e = launch_volume_phase(bt->pool.P, bt->pool.mol_chain, bt->pool.n_mol, bt->vm,
+                                          bt->emol2, bt->vsum, nullptr, 0, 0, st);
+      if (e != cudaSuccess) rc = set_err(ctx, MCGPU_ERR_CUDA, "volume phase launch: %s", cudaGetErrorString(e));
+    }
+  } else {
+    for (int l = 0; l < launches && rc == MCGPU_OK; l++) rc = batch_launch(bt, bt->spl, bt->queue + l, st);
+  }
   cudaError_t e = cudaStreamEndCapture(st, &g);
   if (rc) {
     if (g) cudaGraphDestroy(g);
@@ -889,6 +914,84 @@ static int batch_build_graph(mcgpu_batch* bt, int launches) {
   bt->graph_spl = bt->spl;
   bt->graph_threads = bt->threads;
   bt->graph_cpc = bt->cpc;
+  bt->graph_lanes = bt->lanes;
+  bt->graph_interval = interval;
+  return MCGPU_OK;
+}
+
+static bool batch_graph_matches(const mcgpu_batch* bt, int launches, int interval) {
+  return bt->graph && bt->graph_spl == bt->spl && bt->graph_launches == launches &&
+         bt->graph_threads == bt->threads && bt->graph_cpc == bt->cpc &&
+         bt->graph_lanes == bt->lanes && bt->graph_interval == interval;
+}
+
+// Steps n_steps with direct launches of at most spl steps (recording steps
+// at trace[c * trace_stride + trace_off + s] when trace is non-null).
+static int batch_steps_direct(mcgpu_batch* bt, int n_steps, mcgpu_trace* trace, int trace_off,
+                              int trace_stride) {
+  for (int done = 0; done < n_steps;) {
+    const int k = std::min(bt->spl, n_steps - done);
+    int rc = batch_launch(bt, k, bt->queue + ((done / bt->spl) % bt->max_slots), bt->ctx->stream,
+                          trace, trace_off + done, trace_stride);
+    if (rc) return rc;
+    done += k;
+  }
+  return MCGPU_OK;
+}
+
+// Advances every chain by n_steps: NVT in graph replays of 32 launches
+// where possible; NPT interval by interval, each followed by the volume
+// phase (one graph per interval when no trace is recorded).
+static int batch_advance(mcgpu_batch* bt, int n_steps, mcgpu_trace* trace, int trace_stride,
+                         mcgpu_vol_trace* vtrace, int vstride) {
+  mcgpu_ctx* ctx = bt->ctx;
+  const int spl = bt->spl;
+  const int iv = bt->vol_interval;
+  if (iv <= 0) {
+    const int full = n_steps / spl;
+    const int per_graph = std::min(bt->max_slots, 32);
+    int done = 0;
+    if (!trace && full >= per_graph) {
+      if (!batch_graph_matches(bt, per_graph, 0)) {
+        int rc = batch_build_graph(bt, per_graph, 0);
+        if (rc) return rc;
+      }
+      while (full - done >= per_graph) {
+        CK(ctx, cudaGraphLaunch(bt->graph, ctx->stream));
+        done += per_graph;
+      }
+    }
+    int rc = batch_steps_direct(bt, n_steps - done * spl, trace, done * spl, trace_stride);
+    if (rc) return rc;
+    bt->steps_done += n_steps;
+    return MCGPU_OK;
+  }
+  const int launches_per_interval = (iv + spl - 1) / spl;
+  const bool graphable = !trace && !vtrace && launches_per_interval <= bt->max_slots;
+  int done = 0, vk = 0;
+  while (done < n_steps) {
+    const int phase = (int)(bt->steps_done % iv);
+    if (phase == 0 && n_steps - done >= iv && graphable) {
+      if (!batch_graph_matches(bt, launches_per_interval, iv)) {
+        int rc = batch_build_graph(bt, launches_per_interval, iv);
+        if (rc) return rc;
+      }
+      CK(ctx, cudaGraphLaunch(bt->graph, ctx->stream));
+      done += iv;
+      bt->steps_done += iv;
+      continue;
+    }
+    const int seg = std::min(n_steps - done, iv - phase);
+    int rc = batch_steps_direct(bt, seg, trace, done, trace_stride);
+    if (rc) return rc;
+    done += seg;
+    bt->steps_done += seg;
+    if (bt->steps_done % iv == 0) {
+      CK(ctx, launch_volume_phase(bt->pool.P, bt->pool.mol_chain, bt->pool.n_mol, bt->vm, bt->emol2,
+                                  bt->vsum, vtrace, vk, vstride, ctx->stream));
+      vk++;
+    }
+  }
   return MCGPU_OK;
 }
 
@@ -896,52 +999,78 @@ extern "C" int mcgpu_batch_run(mcgpu_batch* bt, int n_steps, int sync) {
   if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
   mcgpu_ctx* ctx = bt->ctx;
   if (n_steps < 0) return set_err(ctx, MCGPU_ERR_INVALID, "negative step count");
-  const int spl = bt->spl;
-  const int full = n_steps / spl, rem = n_steps % spl;
-  const int per_graph = std::min(bt->max_slots, 32);
-  if (full >= per_graph) {
-    if (!bt->graph || bt->graph_spl != spl || bt->graph_launches != per_graph ||
-        bt->graph_threads != bt->threads || bt->graph_cpc != bt->cpc) {
-      int rc = batch_build_graph(bt, per_graph);
-      if (rc) return rc;
-    }
-  }
-  int done = 0;
-  while (full - done >= per_graph && bt->graph) {
-    CK(ctx, cudaGraphLaunch(bt->graph, ctx->stream));
-    done += per_graph;
-  }
-  for (; done < full; done++) {
-    int rc = batch_launch(bt, spl, bt->queue + (done % bt->max_slots), ctx->stream);
-    if (rc) return rc;
-  }
-  if (rem) {
-    int rc = batch_launch(bt, rem, bt->queue, ctx->stream);
-    if (rc) return rc;
-  }
+  int rc = batch_advance(bt, n_steps, nullptr, 0, nullptr, 0);
+  if (rc) return rc;
   if (sync) CK(ctx, cudaStreamSynchronize(ctx->stream));
   return MCGPU_OK;
 }
 
-extern "C" int mcgpu_batch_run_traced(mcgpu_batch* bt, int n_steps, mcgpu_trace* out) {
+extern "C" int mcgpu_batch_run_traced(mcgpu_batch* bt, int n_steps, mcgpu_trace* out,
+                                      mcgpu_vol_trace* vol_out) {
   if (!bt || !out) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
   mcgpu_ctx* ctx = bt->ctx;
   if (n_steps <= 0) return set_err(ctx, MCGPU_ERR_INVALID, "step count %d must be > 0", n_steps);
   const size_t n = (size_t)n_steps * bt->pool.n_chains;
+  const int vstride = bt->vol_interval > 0 ? n_steps / bt->vol_interval + 1 : 0;
+  const size_t nv = (size_t)vstride * bt->pool.n_chains;
   mcgpu_trace* d = nullptr;
+  mcgpu_vol_trace* dv = nullptr;
   CK(ctx, cudaMalloc((void**)&d, sizeof(mcgpu_trace) * n));
-  int rc = MCGPU_OK;
-  for (int done = 0; done < n_steps && rc == MCGPU_OK; done += bt->spl) {
-    const int k = std::min(bt->spl, n_steps - done);
-    rc = batch_launch(bt, k, bt->queue, ctx->stream, d, done, n_steps);
-  }
   cudaError_t e = cudaSuccess;
-  if (rc == MCGPU_OK)
+  if (vol_out && nv > 0) {
+    e = cudaMalloc((void**)&dv, sizeof(mcgpu_vol_trace) * nv);
+    if (e == cudaSuccess) e = cudaMemsetAsync(dv, 0, sizeof(mcgpu_vol_trace) * nv, ctx->stream);
+  }
+  int rc = MCGPU_OK;
+  if (e == cudaSuccess) rc = batch_advance(bt, n_steps, d, n_steps, dv, vstride);
+  if (rc == MCGPU_OK && e == cudaSuccess)
     e = cudaMemcpyAsync(out, d, sizeof(mcgpu_trace) * n, cudaMemcpyDeviceToHost, ctx->stream);
+  if (rc == MCGPU_OK && e == cudaSuccess && dv)
+    e = cudaMemcpyAsync(vol_out, dv, sizeof(mcgpu_vol_trace) * nv, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   cudaFree(d);
+  if (dv) cudaFree(dv);
   if (rc) return rc;
   if (e != cudaSuccess) return set_err(ctx, MCGPU_ERR_CUDA, "traced run failed: %s", cudaGetErrorString(e));
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_set_npt(mcgpu_batch* bt, int interval, const double* pressure_atm,
+                                   const double* max_dlnv) {
+  if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
+  mcgpu_ctx* ctx = bt->ctx;
+  const int nc = bt->pool.n_chains;
+  if (interval < 0) return set_err(ctx, MCGPU_ERR_INVALID, "volume interval %d must be >= 0", interval);
+  std::vector<double> p(nc, 0.0), dl(nc, 0.0);
+  std::vector<int> iv(nc, interval);
+  if (interval > 0) {
+    if (!pressure_atm || !max_dlnv) return set_err(ctx, MCGPU_ERR_INVALID, "null NPT parameters");
+    for (int c = 0; c < nc; c++) {
+      if (!std::isfinite(pressure_atm[c]) || pressure_atm[c] < 0)
+        return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: pressure %g atm", c, pressure_atm[c]);
+      if (!(max_dlnv[c] > 0 && max_dlnv[c] <= 0.1))
+        return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: max ln V step %g outside (0, 0.1]", c,
+                       max_dlnv[c]);
+      p[c] = pressure_atm[c] * kAtmKcal;
+      dl[c] = max_dlnv[c];
+    }
+    cudaError_t e = cudaSuccess;
+    if (!bt->vm) bt->vm = dalloc<VolMove>(nc, &e);
+    if (!bt->emol2) bt->emol2 = dalloc<double2>(bt->pool.n_mol, &e);
+    if (!bt->vsum) bt->vsum = dalloc<double2>(nc, &e);
+    if (e != cudaSuccess) return set_err(ctx, MCGPU_ERR_NOMEM, "NPT buffers: %s", cudaGetErrorString(e));
+  }
+  cudaStream_t st = ctx->stream;
+  ChainHdr* h = bt->pool.P.hdr;
+  CK(ctx, cudaMemcpy2DAsync(&h->pressure, sizeof(ChainHdr), p.data(), sizeof(double), sizeof(double),
+                            nc, cudaMemcpyHostToDevice, st));
+  CK(ctx, cudaMemcpy2DAsync(&h->max_dlnv, sizeof(ChainHdr), dl.data(), sizeof(double), sizeof(double),
+                            nc, cudaMemcpyHostToDevice, st));
+  CK(ctx, cudaMemcpy2DAsync(&h->vol_interval, sizeof(ChainHdr), iv.data(), sizeof(int), sizeof(int),
+                            nc, cudaMemcpyHostToDevice, st));
+  CK(ctx, cudaStreamSynchronize(st));
+  bt->vol_interval = interval;
+  batch_drop_graph(bt);
   return MCGPU_OK;
 }
 
@@ -966,6 +1095,9 @@ extern "C" int mcgpu_batch_stats(mcgpu_batch* bt, mcgpu_chain_stats* stats) {
     stats[c].pairs = h[c].pairs;
     stats[c].error = h[c].error;
     stats[c].ties = h[c].ties;
+    for (int k = 0; k < 3; k++) stats[c].box[k] = h[c].L[k];
+    stats[c].vol_tried = h[c].vol_tried;
+    stats[c].vol_accepted = h[c].vol_accepted;
     err |= h[c].error;
   }
   if (err) return set_err(ctx, MCGPU_ERR_DEVICE, "a chain reported device error status %d", err);
@@ -1039,24 +1171,26 @@ extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
   if (trial_steps < 1) trial_steps = 64;
   int rc = batch_snapshot(bt, false);
   if (rc) return rc;
-  struct Tile { int threads, cpc, spl; };
+  const long long steps0 = bt->steps_done;
+  struct Tile { int threads, cpc, spl, lanes; };
   std::vector<Tile> cands;
   const int tw[] = {64, 128, 256};
   for (int t : tw)
     for (int gw = 1; gw <= t / 32; gw *= 2) {
       const int cpc = (t / 32) / gw;
       if (gw > 1 && cpc > 15) continue;
-      cands.push_back({t, cpc, 16});
+      cands.push_back({t, cpc, 16, 0});
     }
   cudaEvent_t e0, e1;
   CK(ctx, cudaEventCreate(&e0));
   CK(ctx, cudaEventCreate(&e1));
   float best = 1e30f;
-  Tile bestT = {bt->threads, bt->cpc, bt->spl};
+  Tile bestT = {bt->threads, bt->cpc, bt->spl, bt->lanes};
   for (const Tile& T : cands) {
-    if (mcgpu_batch_set_tile(bt, T.threads, T.cpc, T.spl) != MCGPU_OK) continue;
+    if (mcgpu_batch_set_tile(bt, T.threads, T.cpc, T.spl, T.lanes) != MCGPU_OK) continue;
     rc = batch_snapshot(bt, true);
     if (rc) break;
+    bt->steps_done = steps0;
     rc = mcgpu_batch_run(bt, T.spl, 0);  // warm-up
     if (rc) break;
     CK(ctx, cudaEventRecord(e0, ctx->stream));
@@ -1071,13 +1205,36 @@ extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
       bestT = T;
     }
   }
+  // lanes per neighbour molecule for the best shape
+  int max_tpm = 1;
+  for (const ChainHdr& h : bt->pool.hdr) max_tpm = std::max(max_tpm, h.tpm);
+  for (int lanes = 1; lanes < max_tpm && rc == MCGPU_OK; lanes <<= 1) {
+    if (mcgpu_batch_set_tile(bt, bestT.threads, bestT.cpc, bestT.spl, lanes) != MCGPU_OK) continue;
+    rc = batch_snapshot(bt, true);
+    if (rc) break;
+    bt->steps_done = steps0;
+    rc = mcgpu_batch_run(bt, bestT.spl, 0);
+    if (rc) break;
+    CK(ctx, cudaEventRecord(e0, ctx->stream));
+    rc = mcgpu_batch_run(bt, trial_steps, 0);
+    if (rc) break;
+    CK(ctx, cudaEventRecord(e1, ctx->stream));
+    CK(ctx, cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      bestT.lanes = lanes;
+    }
+  }
   // steps per launch for the best shape
   const int spls[] = {4, 16, 64};
   for (int spl : spls) {
     if (rc) break;
-    if (mcgpu_batch_set_tile(bt, bestT.threads, bestT.cpc, spl) != MCGPU_OK) continue;
+    if (mcgpu_batch_set_tile(bt, bestT.threads, bestT.cpc, spl, bestT.lanes) != MCGPU_OK) continue;
     rc = batch_snapshot(bt, true);
     if (rc) break;
+    bt->steps_done = steps0;
     rc = mcgpu_batch_run(bt, spl, 0);
     if (rc) break;
     CK(ctx, cudaEventRecord(e0, ctx->stream));
@@ -1096,10 +1253,11 @@ extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
-  rc = mcgpu_batch_set_tile(bt, bestT.threads, bestT.cpc, bestT.spl);
+  rc = mcgpu_batch_set_tile(bt, bestT.threads, bestT.cpc, bestT.spl, bestT.lanes);
   if (rc) return rc;
   rc = batch_snapshot(bt, true);
   if (rc) return rc;
+  bt->steps_done = steps0;
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   return MCGPU_OK;
 }

@@ -47,7 +47,7 @@ enum : int { kMiscQn = 16, kMiscU = 20 };
 // new offsets (o_old, o_new), pair factors and |o|^2 (eq), screen
 // positions of the primaries (p_old, p_new), old and new fixed-point
 // anchors, the new quaternion.  No FP64.
-__device__ void stage_chain(const Pool& P, const ChainHdr& H, const MoveF& mv, const GroupSmem& s,
+__device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF& mv, const GroupSmem& s,
                             const float4* pcache, int lane) {
   const int m = H.mol0 + mv.mol;
   const int a0 = P.mstart[m];
@@ -154,7 +154,7 @@ __device__ __forceinline__ int screen_chain(const Pool& P, const ChainHdr& H, co
 // One warp screens chain candidates [c_begin, c_end) in warp-strided
 // rounds of 32 (screen positions from the shared-memory cache when given)
 // and evaluates the in-range ones in batches of 32.
-__device__ void warp_eval_chain(const Pool& P, const ChainHdr& H, const GroupSmem& s,
+__device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const GroupSmem& s,
                                 const MovedInfo& mi, const float4* pcache, int c_begin, int c_end,
                                 int w, int nw, int lane, int T, AccFF& acc) {
   int* rj = s.lj + w * kRing;
@@ -232,7 +232,7 @@ __device__ __forceinline__ void group_reduce_ff(const Group& g, const GroupSmem&
 // arithmetic (BruteForceStep.cpp:48-79) on the FP64 positions of the chain
 // state (anchor + offset).  Warp 0 first writes the moved molecule's old
 // and new FP64 coordinates to shared memory; the caller synchronises.
-__device__ void stage_chain_f64(const ChainHdr& H, const GroupSmem& s, const MovedInfo& mi,
+__device__ inline void stage_chain_f64(const ChainHdr& H, const GroupSmem& s, const MovedInfo& mi,
                                 int lane) {
   for (int i = lane; i < mi.len; i += 32) {
     const double3 a = chain_pos3(mi.fx_old, s.o_old[i], H);
@@ -278,7 +278,7 @@ __device__ __forceinline__ void batch_chain64(const Pool& P, const ChainHdr& H, 
 
 // The FP64 re-take's screen: the reference's test for every primary pair
 // on the chain state's FP64 positions.
-__device__ void warp_eval_chain64(const Pool& P, const ChainHdr& H, const GroupSmem& s,
+__device__ inline void warp_eval_chain64(const Pool& P, const ChainHdr& H, const GroupSmem& s,
                                   const MovedInfo& mi, int c_begin, int c_end, int w, int nw,
                                   int lane, int T, double& eo, double& en) {
   int* rj = s.lj + w * kRing;

@@ -37,6 +37,8 @@ constexpr int kMaxA = MCGPU_MAX_MOL_ATOMS;
 constexpr int kMaxP = MCGPU_MAX_MOL_PIDX;
 constexpr double kBoltz = 0.00198717;        // SimBox.h:16
 constexpr double kCoulomb = 332.06;          // SimulationStep.cpp:364
+// 1 atm in kcal/mol/A^3: 101325 Pa * 1e-30 m^3/A^3 * N_A / 4184 J/kcal.
+constexpr double kAtmKcal = 1.4583972574259083e-05;
 // Bound on the FP32-pair rounding error of a molecule energy, relative to
 // the sum of the magnitudes of its FP32 terms (observed worst case ~1e-8;
 // the bound keeps a 100x margin).
@@ -59,15 +61,54 @@ struct __align__(16) ChainHdr {
   float Lf[3], cut2_lo;               // FP32 box and guard band
   float fxs[3], cut2_hi;              // fixed point -> Angstrom scale
   float fxinvf[3], kTinvf;            // Angstrom -> fixed point (FP32); 1/kT (FP32)
-  float fxs_lo[3], pad5;              // fxs + fxs_lo = L / 2^32 to ~48 bits
+  float fxs_lo[3], rad_max;           // fxs + fxs_lo = L / 2^32 to ~48 bits;
+                                      // rad_max: largest molecule radius
   double L[3], cutoff;
   double fxinv[3], kT;                // Angstrom -> fixed point scale
   double max_t, max_r, energy, pad1;
   unsigned long long seed, step;
   long long accepted, pairs;
   int error, ties, pad3, pad4;        // ties: decisions re-taken with FP64 pairs
+  // isobaric (NPT) volume moves: every vol_interval steps (0 = NVT), ln V
+  // step uniform in +-max_dlnv, pressure in kcal/mol/A^3
+  double pressure, max_dlnv;
+  int vol_interval, vol_tried, vol_accepted, pad6;
 };
 static_assert(sizeof(ChainHdr) % 16 == 0, "ChainHdr alignment");
+
+// Guard band of the FP32 cutoff screen around rc^2 for box edges up to
+// Lmax: FP32 positions carry ~1.5 ulp(Lmax) each, r2 adds its own rounding.
+__host__ __device__ inline double screen_band(double rc, double Lmax) {
+  int ex = 0;
+  frexp(Lmax, &ex);                         // Lmax in [2^(ex-1), 2^ex)
+  const double ulpL = ldexp(1.0, ex - 1 - 23);
+  return 4.0 * (2.0 * 1.7320508075688772 * rc * 1.5 * ulpL + 4.0 * ldexp(rc * rc, -24)) + 1e-6;
+}
+
+// Box-derived header fields (FP32 box, fixed-point scales, screen band) for
+// edges L; the same code runs at upload and after an accepted volume move.
+__host__ __device__ inline void hdr_set_box(ChainHdr& h, const double L[3]) {
+  double Lmax = 0;
+  for (int k = 0; k < 3; k++) {
+    h.L[k] = L[k];
+    h.Lf[k] = (float)L[k];
+    h.fxinv[k] = 4294967296.0 / L[k];
+    h.fxs[k] = (float)(L[k] / 4294967296.0);
+    h.fxinvf[k] = (float)(4294967296.0 / L[k]);
+    h.fxs_lo[k] = (float)(L[k] / 4294967296.0 - (double)h.fxs[k]);
+    Lmax = L[k] > Lmax ? L[k] : Lmax;
+  }
+  const double band = screen_band(h.cutoff, Lmax);
+  h.cut2_lo = (float)(h.cutoff * h.cutoff - band);
+  h.cut2_hi = (float)(h.cutoff * h.cutoff + band);
+}
+
+// One chain's volume move in flight (NPT).
+struct VolMove {
+  double L[3];
+  double dlnv, u;
+  int state, pad;   // 0 not due, 1 evaluate, 2 rejected outright, 3 accepted
+};
 
 struct Pool {
   double *x, *y, *z, *sig, *eps, *q;
@@ -245,6 +286,8 @@ struct Group {
 // batches of 32 entries, so the screen -> list -> pair pipeline needs no
 // group barrier.
 constexpr int kRing = 64;
+// Bytes of one drawn move in shared memory (MoveF, move_f32.cuh).
+constexpr int kPropBytes = 40;
 
 struct GroupSmem {
   // moved molecule
@@ -265,6 +308,7 @@ struct GroupSmem {
   int* misc;                            // [32] broadcast ints
   double* miscd;                        // [32] broadcast doubles
   float4* pc;                           // [cache_n] screen positions of the chain (or null)
+  void* props;                          // [32] drawn moves of the next steps (chain kernel)
 };
 
 struct SmemShape {
@@ -285,6 +329,7 @@ struct SmemShape {
     b += align16(32 * 4);
     b += align16(32 * 8);
     b += align16(cache_n * 16);
+    b += align16(32 * kPropBytes);
     return b;
   }
   __device__ GroupSmem carve(char* base) const {
@@ -307,6 +352,8 @@ struct SmemShape {
     s.misc = (int*)p; p += align16(32 * 4);
     s.miscd = (double*)p; p += align16(32 * 8);
     s.pc = cache_n > 0 ? (float4*)p : nullptr;
+    p += align16(cache_n * 16);
+    s.props = (void*)p;
     return s;
   }
 };

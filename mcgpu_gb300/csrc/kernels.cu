@@ -274,11 +274,14 @@ __global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol
 // re-evaluates both placements with FP64 pairs and decides on that.  Warp
 // 0 commits.  With cache_n > 0 each group keeps its chain's primary screen
 // positions in shared memory.  If trace != nullptr, step st of chain c is
-// recorded at trace[c * trace_stride + trace_off + st].
+// recorded at trace[c * trace_stride + trace_off + st].  Warp 0 draws the
+// moves of 32 steps at once (one per lane) into shared memory.  lanes_cap >
+// 0 caps the lanes per neighbour molecule of every chain.
 __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsigned* queue,
                                                      const int* order, int n_tasks, int gwarps,
                                                      SmemShape shape, mcgpu_trace* trace,
-                                                     int trace_off, int trace_stride) {
+                                                     int trace_off, int trace_stride,
+                                                     int lanes_cap) {
   extern __shared__ __align__(16) char smem[];
   const int gsize = gwarps * 32;
   const int gid = threadIdx.x / gsize;
@@ -301,30 +304,25 @@ __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsign
     long long acc_n = 0, npairs = 0;
     int ties = 0;
     const unsigned long long step0 = H.step;
+    const int T = lanes_cap > 0 ? min(lanes_cap, H.tpm) : H.tpm;
+    MoveF* props = (MoveF*)s.props;
     for (int st = 0; st < n_steps; st++) {
       if (w == 0) {
-        MoveF mv;
-        if (lane == 0)
-          mv = draw_move_f32(H.seed, H.chain_id, step0 + st, H.n_mol, P.mlen + H.mol0,
-                             (float)H.max_t, (float)H.max_r, H.rot_mode);
-        mv.mol = __shfl_sync(~0u, mv.mol, 0);
-        mv.vertex = __shfl_sync(~0u, mv.vertex, 0);
-        mv.dx = __shfl_sync(~0u, mv.dx, 0);
-        mv.dy = __shfl_sync(~0u, mv.dy, 0);
-        mv.dz = __shfl_sync(~0u, mv.dz, 0);
-        mv.qd.w = __shfl_sync(~0u, mv.qd.w, 0);
-        mv.qd.x = __shfl_sync(~0u, mv.qd.x, 0);
-        mv.qd.y = __shfl_sync(~0u, mv.qd.y, 0);
-        mv.qd.z = __shfl_sync(~0u, mv.qd.z, 0);
-        mv.u = __shfl_sync(~0u, mv.u, 0);
-        stage_chain(P, H, mv, s, pcache, lane);
+        if ((st & 31) == 0) {
+          if (st + lane < n_steps)
+            props[lane] = draw_move_f32(H.seed, H.chain_id, step0 + st + lane, H.n_mol,
+                                        P.mlen + H.mol0, (float)H.max_t, (float)H.max_r,
+                                        H.rot_mode);
+          __syncwarp();
+        }
+        stage_chain(P, H, props[st & 31], s, pcache, lane);
       }
       g.sync();
       const MovedInfo mi = load_moved(s);
       // read before the reduction barrier: warp 0 restages the slot after it
       const float u = __int_as_float(s.misc[kMiscU]);
       AccFF acc = {0.f, 0.f, 0.f, 0.f, 0.f, 0};
-      warp_eval_chain(P, H, s, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, H.tpm, acc);
+      warp_eval_chain(P, H, s, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, acc);
       group_reduce_ff(g, s, acc);
       // FP32 decision unless the FP32 dE is within its rounding bound of the
       // threshold; the bound covers the pair terms' rounding (kTieRel of the
@@ -339,7 +337,7 @@ __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsign
         g.sync();
         double eo = 0.0, en = 0.0, ab2 = 0.0;
         long long np2 = 0;
-        warp_eval_chain64(P, H, s, mi, H.mol0, H.mol0 + H.n_mol, w, nw, lane, H.tpm, eo, en);
+        warp_eval_chain64(P, H, s, mi, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, eo, en);
         group_reduce(g, s, eo, en, ab2, np2);
         e_old = eo;
         e_new = en;

@@ -91,7 +91,7 @@ __device__ __forceinline__ float r2_screen(float4 a, float4 b, const ChainHdr& H
 // translated, then the molecule wrapped by its first primary atom
 // (keepMoleculeInBox, :710-729).  Results go to shared memory; scalars to
 // misc/miscd.  The caller synchronises the group afterwards.
-__device__ void stage(const Pool& P, const ChainHdr& H, int m, const Proposal* p,
+__device__ inline void stage(const Pool& P, const ChainHdr& H, int m, const Proposal* p,
                       const GroupSmem& s, int lane) {
   const int a0 = P.mstart[m];
   const int lw = P.mlen[m];
@@ -482,7 +482,7 @@ __device__ __forceinline__ void batch_f64(const Pool& P, const ChainHdr& H, cons
 // its ring and evaluates them in batches of 32.  FP32 pairs accumulate in
 // double-float and are added to the FP64 sums at the end.
 template <bool F64>
-__device__ void warp_eval(const Pool& P, const ChainHdr& H, const GroupSmem& s, const MovedInfo& mi,
+__device__ inline void warp_eval(const Pool& P, const ChainHdr& H, const GroupSmem& s, const MovedInfo& mi,
                           int c_begin, int c_end, int w, int nw, int lane, int T, double& eo,
                           double& en, double& ab, long long& np) {
   int* rj = s.lj + w * kRing;

@@ -125,6 +125,7 @@ struct MoveF {
   QuatF qd;       // rotation of the move (not normalised)
   float u;        // acceptance uniform in (0, 1)
 };
+static_assert(sizeof(MoveF) == kPropBytes, "MoveF size");
 
 constexpr float kDeg2Rad = 0.0174532925199432958f;
 

@@ -1,0 +1,276 @@
+// npt.cu -- isobaric (NPT) volume moves of device-resident chains.
+//
+// A volume move of a chain whose step count is a multiple of its interval:
+//   ln V' = ln V + dlnv,  dlnv uniform in +-max_dlnv (Philox block 3 of the
+//   step's counter), every edge scaled by s = exp(dlnv / 3);
+//   each molecule's centre (its first primary atom, the chain state's
+//   anchor) scales about the origin, c' = s c, its geometry stays rigid.  In
+//   the chain state the anchor is a fixed-point fraction of the edge, so the
+//   scaling is the change of L alone;
+//   accepted when exp(-(dU + P dV)/kT + (N + 1) dlnv) >= u (u from the same
+//   Philox block), with U(V) and U(V') full FP64 system energies (the
+//   reference's pair arithmetic, SimulationStep.cpp:40-71, :317-375) of the
+//   chain state at both volumes.
+// The reference's own NPT path (Ensemble.cpp:9-23, SimulationStep.cpp:476-518)
+// applies a fixed factor 1.1 and no pressure units; this is the standard
+// isobaric ln V move instead.  The running energy is replaced by the FP64
+// total of the volume the chain keeps (a drift reset every interval).
+//
+// Kernels (one volume phase, launched between step launches):
+//   k_vol_propose      per chain: due?, draw, L'
+//   k_vol_pair_sums    per molecule: E(m, j>m) at V and V' (FP64 pairs)
+//   k_vol_sums         per chain: ordered sums
+//   k_vol_decide       per chain: criterion, new box, energy
+//   k_vol_refresh      per molecule of an accepting chain: screen positions
+#include "chain.cuh"
+
+namespace mcgpu {
+
+// exp(x) for |x| <= 0.034 by its Taylor series to x^6 (Horner, every
+// operation rounded once): relative truncation error below 1e-14.  The
+// oracle evaluates the same expression, so the scaled box is bit-identical.
+__device__ __forceinline__ double exp_small(double x) {
+  double p = 1.0 / 720.0;
+  p = __dadd_rn(__dmul_rn(p, x), 1.0 / 120.0);
+  p = __dadd_rn(__dmul_rn(p, x), 1.0 / 24.0);
+  p = __dadd_rn(__dmul_rn(p, x), 1.0 / 6.0);
+  p = __dadd_rn(__dmul_rn(p, x), 0.5);
+  p = __dadd_rn(__dmul_rn(p, x), 1.0);
+  p = __dadd_rn(__dmul_rn(p, x), 1.0);
+  return p;
+}
+
+__global__ void k_vol_propose(Pool P, VolMove* vm) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= P.n_chains) return;
+  const ChainHdr& H = P.hdr[c];
+  VolMove v;
+  v.state = 0;
+  v.pad = 0;
+  v.dlnv = 0.0;
+  v.u = 0.0;
+  for (int k = 0; k < 3; k++) v.L[k] = H.L[k];
+  if (H.vol_interval > 0 && H.step > 0 && H.step % (unsigned long long)H.vol_interval == 0 &&
+      H.error == 0) {
+    const uint2 key = make_uint2((unsigned)H.seed, (unsigned)(H.seed >> 32));
+    const uint4 r = philox4x32_10(
+        make_uint4((unsigned)H.step, (unsigned)(H.step >> 32), (unsigned)H.chain_id, 3u), key);
+    v.dlnv = __dadd_rn(__dmul_rn(2.0 * H.max_dlnv, u01(r.x)), -H.max_dlnv);
+    v.u = u01(r.y);
+    const double s = exp_small(v.dlnv / 3.0);
+    double Lmin = 1e300;
+    for (int k = 0; k < 3; k++) {
+      v.L[k] = __dmul_rn(H.L[k], s);
+      Lmin = fmin(Lmin, v.L[k]);
+    }
+    // molecules must stay within a quarter of an edge (the chain state's
+    // anchor-image rule); the cutoff may exceed half an edge, as in the
+    // reference's single-image minimum convention
+    v.state = ((double)H.rad_max >= 0.25 * Lmin) ? 2 : 1;
+  }
+  vm[c] = v;
+}
+
+// FP64 position of a chain atom at box edge L (anchor fraction scaled).
+__device__ __forceinline__ double3 pos_at(uint4 A, float4 o, const double* L) {
+  return make_double3(chain_coord(A.x, o.x, L[0]), chain_coord(A.y, o.y, L[1]),
+                      chain_coord(A.z, o.z, L[2]));
+}
+
+__device__ __forceinline__ double dist2_at(double3 a, double3 b, const double* L) {
+  const double dx = make_periodic(b.x - a.x, L[0]);
+  const double dy = make_periodic(b.y - a.y, L[1]);
+  const double dz = make_periodic(b.z - a.z, L[2]);
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+constexpr int kVolThreads = 128;
+
+// E(m, j > m) of pool molecule m at V (.x) and V' (.y).  Candidates whose
+// anchors are farther apart than rc + both radii (+ a margin far above the
+// FP32 rounding of the anchor difference) are skipped without an FP64
+// test; every other primary pair takes the reference's FP64 test.
+__global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int* mol_chain,
+                                                               const VolMove* vm, int m_begin,
+                                                               double2* emol2) {
+  __shared__ double sx[2][3][kMaxA];
+  __shared__ double sq[3][kMaxA];
+  __shared__ int spa[kMaxP];
+  __shared__ double2 red[kVolThreads];
+  const int m = m_begin + blockIdx.x;
+  const int c = mol_chain[m];
+  const VolMove v = vm[c];
+  if (v.state != 1) {
+    if (threadIdx.x == 0) emol2[m] = make_double2(0.0, 0.0);
+    return;
+  }
+  const ChainHdr& H = P.hdr[c];
+  const double* Lv[2] = {H.L, v.L};
+  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
+  const int2 pi = P.mpi[m];
+  const uint4 Am = P.mfix[m];
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    const float4 o = P.aoff[a0 + i];
+    for (int w = 0; w < 2; w++) {
+      const double3 x = pos_at(Am, o, Lv[w]);
+      sx[w][0][i] = x.x;
+      sx[w][1][i] = x.y;
+      sx[w][2][i] = x.z;
+    }
+    sq[0][i] = P.sig[a0 + i];
+    sq[1][i] = P.eps[a0 + i];
+    sq[2][i] = P.q[a0 + i];
+  }
+  for (int k = threadIdx.x; k < pi.y; k += blockDim.x) spa[k] = P.pidx[pi.x + k] - a0;
+  __syncthreads();
+  const double s = v.L[0] / H.L[0];
+  const float reach = H.cutoff + H.rad_max * 2.0 + 1e-2;
+  const float reach2 = reach * reach;
+  double eo = 0.0, en = 0.0;
+  for (int j = m + 1 + (int)threadIdx.x; j < H.mol0 + H.n_mol; j += blockDim.x) {
+    const uint4 Aj = P.mfix[j];
+    const float3 D = fixdiff(Aj, Am, H);
+    const float d2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
+    const float sf = (float)s;
+    // V' anchor distance is s |D|; skip only if both are out of reach
+    if (d2 > reach2 && d2 * sf * sf > reach2) continue;
+    const int2 pj = P.mpi[j];
+    bool in[2] = {false, false};
+    for (int w = 0; w < 2; w++) {
+      for (int k2 = 0; k2 < pj.y && !in[w]; k2++) {
+        const double3 b = pos_at(Aj, P.aoff[P.pidx[pj.x + k2]], Lv[w]);
+        for (int k1 = 0; k1 < pi.y && !in[w]; k1++) {
+          const int pa = spa[k1];
+          const double3 a = make_double3(sx[w][0][pa], sx[w][1][pa], sx[w][2][pa]);
+          in[w] = dist2_at(a, b, Lv[w]) <= __dmul_rn(H.cutoff, H.cutoff);
+        }
+      }
+    }
+    if (!in[0] && !in[1]) continue;
+    const int b0 = P.mstart[j], lenj = P.mlen[j] & 255;
+    for (int bb = b0; bb < b0 + lenj; bb++) {
+      const double sb = P.sig[bb], eb = P.eps[bb], qb = P.q[bb];
+      if (!(sb >= 0 && eb >= 0)) continue;
+      const float4 ob = P.aoff[bb];
+      for (int w = 0; w < 2; w++) {
+        if (!in[w]) continue;
+        const double3 xb = pos_at(Aj, ob, Lv[w]);
+        double acc = 0.0;
+        for (int i = 0; i < len; i++) {
+          const double sa = sq[0][i], ea = sq[1][i];
+          if (!(sa >= 0 && ea >= 0)) continue;
+          const double3 xa = make_double3(sx[w][0][i], sx[w][1][i], sx[w][2][i]);
+          acc += pair64(dist2_at(xa, xb, Lv[w]), sa, sb, ea, eb, sq[2][i], qb);
+        }
+        if (w == 0) eo += acc; else en += acc;
+      }
+    }
+  }
+  red[threadIdx.x] = make_double2(eo, en);
+  __syncthreads();
+  for (int off = blockDim.x >> 1; off > 0; off >>= 1) {
+    if ((int)threadIdx.x < off) {
+      red[threadIdx.x].x += red[threadIdx.x + off].x;
+      red[threadIdx.x].y += red[threadIdx.x + off].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) emol2[m] = red[0];
+}
+
+// Ordered per-chain sums of emol2 (one CTA per chain).
+__global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, double2* out) {
+  __shared__ double2 red[256];
+  if (vm[blockIdx.x].state != 1) return;
+  const ChainHdr& H = P.hdr[blockIdx.x];
+  double2 acc = make_double2(0.0, 0.0);
+  for (int i = threadIdx.x; i < H.n_mol; i += blockDim.x) {
+    acc.x += emol2[H.mol0 + i].x;
+    acc.y += emol2[H.mol0 + i].y;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = blockDim.x >> 1; off > 0; off >>= 1) {
+    if ((int)threadIdx.x < off) {
+      red[threadIdx.x].x += red[threadIdx.x + off].x;
+      red[threadIdx.x].y += red[threadIdx.x + off].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+// The isobaric criterion; an accepted move installs the new box.
+__global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, mcgpu_vol_trace* trace,
+                             int trace_slot, int trace_stride) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= P.n_chains) return;
+  VolMove v = vm[c];
+  if (v.state == 0) return;
+  ChainHdr& H = P.hdr[c];
+  H.vol_tried++;
+  double e_old = H.energy, e_new = 0.0;
+  int ok = 0;
+  if (v.state == 1) {
+    e_old = esum[c].x;
+    e_new = esum[c].y;
+    const double vo = H.L[0] * H.L[1] * H.L[2];
+    const double vn = v.L[0] * v.L[1] * v.L[2];
+    const double arg = -((e_new - e_old) + H.pressure * (vn - vo)) / H.kT +
+                       (double)(H.n_mol + 1) * v.dlnv;
+    ok = (arg >= 0.0) || (exp(arg) >= v.u);
+    H.energy = ok ? e_new : e_old;
+  }
+  if (ok) {
+    hdr_set_box(H, v.L);
+    H.vol_accepted++;
+    v.state = 3;
+    vm[c] = v;
+  }
+  if (trace) {
+    mcgpu_vol_trace t;
+    t.step = (int64_t)H.step;
+    t.accepted = ok;
+    t.evaluated = v.state != 2;
+    t.e_old = e_old;
+    t.e_new = e_new;
+    t.dlnv = v.dlnv;
+    t.u = v.u;
+    t.edge = H.L[0];
+    trace[(size_t)c * trace_stride + trace_slot] = t;
+  }
+}
+
+// Screen positions of the primaries of every molecule of an accepting chain.
+__global__ void k_vol_refresh(Pool P, const int* mol_chain, const VolMove* vm, int n_mol_total) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n_mol_total) return;
+  const int c = mol_chain[m];
+  if (vm[c].state != 3) return;
+  const ChainHdr& H = P.hdr[c];
+  const int2 pi = P.mpi[m];
+  const uint4 A = P.mfix[m];
+  for (int k = 0; k < pi.y; k++) {
+    const double3 x = chain_pos3(A, P.aoff[P.pidx[pi.x + k]], H);
+    P.ppos[pi.x + k] = wrap_pos(x.x, x.y, x.z, H);
+  }
+}
+
+// One volume phase on stream st (buffers sized for the pool).
+cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
+                                double2* emol2, double2* esum, mcgpu_vol_trace* trace,
+                                int trace_slot, int trace_stride, cudaStream_t st) {
+  const int nc = P.n_chains;
+  k_vol_propose<<<(nc + 127) / 128, 128, 0, st>>>(P, vm);
+  const int chunk = 1 << 20;
+  for (int m0 = 0; m0 < n_mol_total; m0 += chunk) {
+    const int n = n_mol_total - m0 < chunk ? n_mol_total - m0 : chunk;
+    k_vol_pair_sums<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, emol2);
+  }
+  k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, esum);
+  k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, trace, trace_slot, trace_stride);
+  k_vol_refresh<<<(n_mol_total + 127) / 128, 128, 0, st>>>(P, mol_chain, vm, n_mol_total);
+  return cudaGetLastError();
+}
+
+}  // namespace mcgpu

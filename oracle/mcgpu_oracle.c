@@ -761,3 +761,65 @@ double orc_fchain_run(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step
   if (n_accepted) *n_accepted = acc;
   return e;
 }
+
+/* exp(x) for small |x| by its Taylor series to x^6, Horner's rule, each
+ * operation rounded once (the device evaluates the same expression). */
+static double exp_small(double x) {
+  double p = 1.0 / 720.0;
+  p = p * x + 1.0 / 120.0;
+  p = p * x + 1.0 / 24.0;
+  p = p * x + 1.0 / 6.0;
+  p = p * x + 0.5;
+  p = p * x + 1.0;
+  p = p * x + 1.0;
+  return p;
+}
+
+/* One isobaric ln V move of the chain state at step count `step`: draws
+ * (Philox block 3: dlnv from word 0, u from word 1), every edge scaled by
+ * exp(dlnv / 3) with the anchors' fixed-point fractions unchanged (centres
+ * scale about the origin, geometry rigid), FP64 system energies at both
+ * volumes (orc_system_energy on the state's rows), the isobaric criterion
+ * exp(-(dU + P dV)/kT + (N + 1) dlnv) >= u.  Rejected outright (-1) when an
+ * edge would fall to four times rad_max (the largest molecule radius).  *energy
+ * becomes the FP64 energy of the kept volume (unchanged on -1).  Returns 1
+ * accepted, 0 rejected. */
+int orc_fchain_volume(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step,
+                      double p_kcal, double max_dlnv, float rad_max, double* energy,
+                      double* e_old, double* e_new, double* dlnv_out, double* u_out) {
+  orc_box* b = c->b;
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t ctr[4] = {(uint32_t)step, (uint32_t)(step >> 32), chain, 3u};
+  uint32_t r[4];
+  orc_philox4x32_10(ctr, key, r);
+  const double dlnv = (2.0 * max_dlnv) * u01(r[0]) + (-max_dlnv);
+  const double u = u01(r[1]);
+  if (dlnv_out) *dlnv_out = dlnv;
+  if (u_out) *u_out = u;
+  const double s = exp_small(dlnv / 3.0);
+  double Ln[3], Lo[3], Lmin = 1e300;
+  for (int k = 0; k < 3; k++) {
+    Lo[k] = b->size[k];
+    Ln[k] = Lo[k] * s;
+    if (Ln[k] < Lmin) Lmin = Ln[k];
+  }
+  if ((double)rad_max >= 0.25 * Lmin) return -1;
+  const double eo = orc_system_energy(b);
+  for (int k = 0; k < 3; k++) b->size[k] = Ln[k];
+  for (int m = 0; m < b->n_mol; m++) chain_rows(c, m);
+  const double en = orc_system_energy(b);
+  if (e_old) *e_old = eo;
+  if (e_new) *e_new = en;
+  const double vo = Lo[0] * Lo[1] * Lo[2];
+  const double vn = Ln[0] * Ln[1] * Ln[2];
+  const double arg = -((en - eo) + p_kcal * (vn - vo)) / b->kT + (double)(b->n_mol + 1) * dlnv;
+  const int ok = (arg >= 0.0) || (exp(arg) >= u);
+  if (ok) {
+    *energy = en;
+  } else {
+    for (int k = 0; k < 3; k++) b->size[k] = Lo[k];
+    for (int m = 0; m < b->n_mol; m++) chain_rows(c, m);
+    *energy = eo;
+  }
+  return ok;
+}

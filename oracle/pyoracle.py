@@ -12,6 +12,7 @@ this module, and only as the checker or the timed CPU baseline.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import subprocess
 from pathlib import Path
@@ -118,6 +119,11 @@ def orc_lib() -> C.CDLL:
                                             C.c_uint64, C.c_int, C.c_double, C.POINTER(OrcTrace),
                                             C.POINTER(C.c_longlong)]),
             "orc_sincos_f32": (None, [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+            "orc_fchain_volume": (C.c_int, [C.POINTER(OrcChainS), C.c_uint64, C.c_uint32,
+                                            C.c_uint64, C.c_double, C.c_double, C.c_float,
+                                            C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double)]),
             "orc_accept_volume": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double,
                                             C.c_int, C.c_double, C.c_double]),
         }
@@ -215,6 +221,15 @@ class OracleChain:
         self.q = np.zeros(4 * b.n_mol, dtype=np.float32)
         self.tpl = np.zeros(3 * b.n_atom, dtype=np.float32)
         self.off = np.zeros(3 * b.n_atom, dtype=np.float32)
+        # largest molecule radius about its first primary atom, as the device
+        # header holds it (FP32)
+        rad = 0.0
+        for m in range(b.n_mol):
+            an = int(b.pidx[b.mol_pidx_start[m]])
+            for a in range(int(b.mol_start[m]), int(b.mol_start[m] + b.mol_len[m])):
+                dx, dy, dz = b.x[a] - b.x[an], b.y[a] - b.y[an], b.z[a] - b.z[an]
+                rad = max(rad, math.sqrt(dx * dx + dy * dy + dz * dz))
+        self.rad_max = float(np.float32(rad))
         fp = C.POINTER(C.c_float)
         self.s = OrcChainS(C.pointer(self.ob.s), self.A.ctypes.data_as(C.POINTER(C.c_uint32)),
                            self.q.ctypes.data_as(fp), self.tpl.ctypes.data_as(fp),
@@ -239,6 +254,23 @@ class OracleChain:
 
     def coords(self) -> np.ndarray:
         return self.ob.coords()
+
+    # 1 atm in kcal/mol/A^3 (101325 Pa * 1e-30 m^3/A^3 * N_A / 4184 J/kcal)
+    ATM_KCAL = 101325 * 6.02214076e23 * 1e-30 / 4184
+
+    def volume_move(self, seed: int, chain: int, step: int, pressure_atm: float,
+                    max_dlnv: float, energy: float) -> dict:
+        """One isobaric ln V move at step count `step` (orc_fchain_volume);
+        returns the outcome (1, 0, or -1 for rejected outright), both FP64
+        energies, the draws and the energy after the decision."""
+        e = C.c_double(energy)
+        eo, en, dl, u = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        st = orc_lib().orc_fchain_volume(
+            C.byref(self.s), int(seed) & (2 ** 64 - 1), int(chain), int(step),
+            float(pressure_atm) * self.ATM_KCAL, float(max_dlnv), self.rad_max, C.byref(e),
+            C.byref(eo), C.byref(en), C.byref(dl), C.byref(u))
+        return {"status": st, "e_old": eo.value, "e_new": en.value, "dlnv": dl.value,
+                "u": u.value, "energy": e.value, "edge": float(self.ob.s.size[0])}
 
 
 def sincos_f32(x: float) -> tuple[float, float]:
