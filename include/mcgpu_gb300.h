@@ -231,6 +231,77 @@ int mcgpu_batch_download(mcgpu_batch* batch, int chain, double* x, double* y,
  * out[n_chains]; the running totals are not changed. */
 int mcgpu_batch_system_energy(mcgpu_batch* batch, double* out);
 
+/* ---- serving: continuous batching of simulation jobs ------------------- */
+
+/* A server keeps many jobs (independent chains) resident on one GPU and
+ * advances them together in rounds of round_steps steps of the persistent
+ * chain kernel.  Jobs arriving while others run wait in a FIFO queue and are
+ * admitted between rounds as slots and memory free up (a later, smaller job
+ * may pass a larger one that does not fit yet); a job leaves the pool at the
+ * end of the round in which it reaches its step count.  A job's results
+ * depend only on its own description (box, seed, chain id, steps, ensemble)
+ * and the server's tile: the same alone as in any mix. */
+typedef struct {
+  uint64_t hbm_budget_bytes;  /* admission limit on resident job state       */
+  int64_t max_atoms;          /* arena capacity in atoms (0: from the budget,
+                                 at 4 atoms per molecule)                    */
+  int64_t max_molecules;      /* arena capacity in molecules (0: as above)   */
+  int32_t max_slots;          /* jobs resident at once (1..4096)             */
+  int32_t round_steps;        /* steps per round; NPT jobs make a volume move
+                                 every round_steps steps                     */
+  int32_t max_mol_atoms;      /* largest molecule a job may hold (<= 64)     */
+  int32_t rotation;           /* MCGPU_ROT_EULER or MCGPU_ROT_AXIS          */
+  int32_t threads, chains_per_cta, lanes_per_molecule; /* chain-kernel tile,
+                                 fixed for the server's life (0: defaults)   */
+  int32_t pad0;
+} mcgpu_server_config;
+
+typedef struct {
+  const mcgpu_box_desc* box;  /* copied at submit                          */
+  uint64_t seed;              /* Philox key                                */
+  uint32_t chain_id;          /* Philox counter id                         */
+  int32_t npt;                /* 1: isobaric volume moves                  */
+  int64_t n_steps;            /* trial moves to run                        */
+  double pressure_atm;        /* NPT pressure                              */
+  double max_dlnv;            /* NPT ln V step bound, (0, 0.1]             */
+  double *x_out, *y_out, *z_out; /* final coordinates (n_atom each), may be
+                                 NULL; must stay valid until the job's result
+                                 is taken by mcgpu_server_results          */
+} mcgpu_job_desc;
+
+typedef struct {
+  int64_t job_id;
+  double energy;              /* running total at the end                  */
+  int64_t steps, accepted;
+  int32_t vol_tried, vol_accepted;
+  double box[3];
+  double t_submit, t_admit, t_done; /* seconds on the server's clock        */
+  int64_t footprint_bytes;    /* device bytes the job held                 */
+  int32_t error, ties;
+} mcgpu_job_result;
+
+int mcgpu_server_create(mcgpu_ctx* ctx, const mcgpu_server_config* cfg,
+                        mcgpu_server** out);
+int mcgpu_server_destroy(mcgpu_server* srv);
+/* Queues a job (its rows are copied).  MCGPU_ERR_CAPACITY if the job could
+ * never be admitted (larger than the budget, the arena or the molecule
+ * limit). */
+int mcgpu_server_submit(mcgpu_server* srv, const mcgpu_job_desc* job, int64_t* job_id);
+/* One round: admits what fits (uploads overlap the round in flight), waits
+ * for the round in flight, retires the jobs it finished (coordinates to
+ * x_out/y_out/z_out), admits again and launches the next round
+ * (asynchronously).  Returns without work when nothing is queued or running. */
+int mcgpu_server_step(mcgpu_server* srv);
+/* Steps until every submitted job has finished. */
+int mcgpu_server_drain(mcgpu_server* srv);
+int mcgpu_server_status(mcgpu_server* srv, int* running, int* queued, int64_t* finished,
+                        uint64_t* bytes_in_use);
+/* Moves up to max finished jobs' results to out (oldest first); *n gets the
+ * count. */
+int mcgpu_server_results(mcgpu_server* srv, mcgpu_job_result* out, int max, int* n);
+/* Seconds on the server's clock (the clock of t_submit/t_admit/t_done). */
+double mcgpu_server_clock(const mcgpu_server* srv);
+
 /* ---- no-allocation system energy ---------------------------------------- */
 
 /* No counterpart in the reference: an extra entry point for callers that may

@@ -12,9 +12,10 @@ from ._abi import (PREC_FP64, PREC_MIXED, ROT_AXIS, ROT_EULER, MCGPUError)
 from .workloads import BoxData, bicyclic_box, water_box, water_chains
 from .step import Context, GpuBox, GpuSimulationStep, LibcRand, run_plain
 from .batch import ChainBatch
+from .server import JobServer
 
 __all__ = [
     "PREC_FP64", "PREC_MIXED", "ROT_AXIS", "ROT_EULER", "MCGPUError", "BoxData",
     "bicyclic_box", "water_box", "water_chains", "Context", "GpuBox", "GpuSimulationStep",
-    "LibcRand", "run_plain", "ChainBatch",
+    "LibcRand", "run_plain", "ChainBatch", "JobServer",
 ]

@@ -65,6 +65,28 @@ class Trace(C.Structure):
                 ("fp64", C.c_int32), ("pad0", C.c_int32)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_atoms", C.c_int64),
+                ("max_molecules", C.c_int64), ("max_slots", C.c_int32),
+                ("round_steps", C.c_int32), ("max_mol_atoms", C.c_int32),
+                ("rotation", C.c_int32), ("threads", C.c_int32), ("chains_per_cta", C.c_int32),
+                ("lanes_per_molecule", C.c_int32), ("pad0", C.c_int32)]
+
+
+class JobDesc(C.Structure):
+    _fields_ = [("box", C.POINTER(BoxDesc)), ("seed", C.c_uint64), ("chain_id", C.c_uint32),
+                ("npt", C.c_int32), ("n_steps", C.c_int64), ("pressure_atm", C.c_double),
+                ("max_dlnv", C.c_double), ("x_out", _dp), ("y_out", _dp), ("z_out", _dp)]
+
+
+class JobResult(C.Structure):
+    _fields_ = [("job_id", C.c_int64), ("energy", C.c_double), ("steps", C.c_int64),
+                ("accepted", C.c_int64), ("vol_tried", C.c_int32), ("vol_accepted", C.c_int32),
+                ("box", C.c_double * 3), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("footprint_bytes", C.c_int64), ("error", C.c_int32),
+                ("ties", C.c_int32)]
+
+
 _vp = C.c_void_p
 _PROTOS = {
     "mcgpu_version": (C.c_char_p, []),
@@ -96,6 +118,15 @@ _PROTOS = {
     "mcgpu_batch_download": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
     "mcgpu_batch_system_energy": (C.c_int, [_vp, _dp]),
     "mcgpu_build_centres": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint64, _dp]),
+    "mcgpu_server_create": (C.c_int, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "mcgpu_server_destroy": (C.c_int, [_vp]),
+    "mcgpu_server_submit": (C.c_int, [_vp, C.POINTER(JobDesc), C.POINTER(C.c_int64)]),
+    "mcgpu_server_step": (C.c_int, [_vp]),
+    "mcgpu_server_drain": (C.c_int, [_vp]),
+    "mcgpu_server_status": (C.c_int, [_vp, _ip, _ip, C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_uint64)]),
+    "mcgpu_server_results": (C.c_int, [_vp, C.POINTER(JobResult), C.c_int, _ip]),
+    "mcgpu_server_clock": (C.c_double, [_vp]),
     "mcgpu_system_energy_static": (C.c_int, [C.POINTER(BoxDesc), _vp, _vp]),
 }
 

@@ -15,32 +15,8 @@
 #include <string>
 #include <vector>
 
-#include "device.cuh"
+#include "host.h"
 
-namespace mcgpu {
-__global__ void k_refresh_mirrors(Pool P, const int* mol_chain, int n_mol_total);
-__global__ void k_change_molecule(Pool P, int chain, int mol, Proposal prop, SmemShape shape);
-__global__ void k_rollback(Pool P, int chain, int mol);
-__global__ void k_chain_sums(Pool P, const double* emol, double* out);
-__global__ void k_set_energy(Pool P, const double* e);
-__global__ void k_chain_steps(Pool P, int n_steps, unsigned* queue, const int* order, int n_tasks,
-                              int gwarps, SmemShape shape, mcgpu_trace* trace, int trace_off,
-                              int trace_stride, int lanes_cap);
-__global__ void k_chain_init(Pool P, const int* mol_chain, int n_mol_total);
-__global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol, int n_atom);
-cudaError_t launch_mol_energy(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
-                              Pool P, int chain, int curr, int start, double* partials,
-                              unsigned* counter, double* out);
-cudaError_t launch_move_energies(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
-                                 Pool P, int chain, int mol, Proposal prop, double* partials,
-                                 unsigned* counter, double* out);
-cudaError_t launch_mol_pair_sums(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
-                                 Pool P, const int* mol_chain, int m_begin, double* emol,
-                                 long long* pairs);
-cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
-                                double2* emol2, double2* esum, mcgpu_vol_trace* trace,
-                                int trace_slot, int trace_stride, cudaStream_t st);
-}  // namespace mcgpu
 
 using namespace mcgpu;
 
@@ -48,15 +24,8 @@ using namespace mcgpu;
 
 static thread_local std::string g_err;
 
-struct mcgpu_ctx {
-  int device = 0;
-  int sm_count = 0;
-  cudaStream_t stream = nullptr;   // stream every launch goes to
-  cudaStream_t own = nullptr;      // the context's own stream
-  std::string err;
-};
 
-static int set_err(mcgpu_ctx* ctx, int code, const char* fmt, ...) {
+int set_err(mcgpu_ctx* ctx, int code, const char* fmt, ...) {
   char buf[512];
   va_list ap;
   va_start(ap, fmt);
@@ -72,35 +41,10 @@ namespace mcgpu {
 void note_process_error(const char* msg) { g_err = msg; }
 }  // namespace mcgpu
 
-#define CK(ctx, call)                                                                  \
-  do {                                                                                 \
-    cudaError_t e_ = (call);                                                           \
-    if (e_ != cudaSuccess)                                                             \
-      return set_err((ctx), MCGPU_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
-  } while (0)
 
 // ---- pool ----------------------------------------------------------------------
 
-namespace {
-
-template <class T>
-T* dalloc(size_t n, cudaError_t* e) {
-  T* p = nullptr;
-  cudaError_t r = cudaMalloc((void**)&p, sizeof(T) * std::max<size_t>(n, 1));
-  if (r != cudaSuccess && *e == cudaSuccess) *e = r;
-  return p;
-}
-
-struct HostPool {
-  std::vector<double> x, y, z, sig, eps, q;
-  std::vector<float4> aoff;
-  std::vector<float2> aeq;
-  std::vector<int> mstart, mlen, pidx, mol_chain, atom_mol;
-  std::vector<int2> mpi;
-  std::vector<float> mrad;
-  std::vector<ChainHdr> hdr;
-  int max_len = 0;
-};
+namespace mcgpu {
 
 // Validates one descriptor and appends it as chain `c` of the host pool.
 int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
@@ -222,32 +166,6 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
   return MCGPU_OK;
 }
 
-struct DevPool {
-  Pool P{};
-  int n_chains = 0, n_mol = 0, n_atom = 0, n_pidx = 0, max_len = 0;
-  int* mol_chain = nullptr;
-  int* atom_mol = nullptr;
-  double* emol = nullptr;
-  long long* pairs = nullptr;
-  double* esum = nullptr;
-  std::vector<ChainHdr> hdr;  // host copy of the headers at upload
-  std::vector<int> mstart, mlen;  // host copies (pool-absolute)
-
-  void release() {
-    void* ptrs[] = {P.x, P.y, P.z, P.sig, P.eps, P.q, P.aoff, P.aofl, P.aeq, P.mstart, P.mlen, P.mpi,
-                    P.mfix, P.mrad, P.mq, P.atpl, P.pidx, P.ppos, P.hdr, P.rb, P.trace,
-                    mol_chain, atom_mol, emol, pairs, esum};
-    for (void* p : ptrs)
-      if (p) cudaFree(p);
-    P = Pool{};
-    mol_chain = nullptr;
-    atom_mol = nullptr;
-    emol = nullptr;
-    pairs = nullptr;
-    esum = nullptr;
-  }
-};
-
 int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
   cudaError_t e = cudaSuccess;
   const size_t na = hp.x.size(), nm = hp.mstart.size(), np = hp.pidx.size(), nc = hp.hdr.size();
@@ -288,7 +206,7 @@ int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
   UP(dp.atom_mol, hp.atom_mol);
 #undef UP
   const int wpb = 8;
-  k_refresh_mirrors<<<(int)((nm + wpb - 1) / wpb), wpb * 32, 0, st>>>(P, dp.mol_chain, (int)nm);
+  k_refresh_mirrors<<<(int)((nm + wpb - 1) / wpb), wpb * 32, 0, st>>>(P, dp.mol_chain, 0, (int)nm);
   CK(ctx, cudaGetLastError());
   CK(ctx, cudaStreamSynchronize(st));
   dp.hdr = hp.hdr;
@@ -297,17 +215,13 @@ int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
   return MCGPU_OK;
 }
 
-SmemShape shape_for(int max_len, int nwarps, int cache_n = 0) {
+SmemShape shape_for(int max_len, int nwarps, int cache_n) {
   SmemShape s;
   s.maxA = std::max(max_len, 1);
   s.nwarps = nwarps;
   s.cache_n = cache_n;
   return s;
 }
-
-// Largest chain whose primary screen positions a group caches in shared
-// memory (16 bytes per molecule).
-constexpr int kCacheMax = 4096;
 
 int pool_cache_n(const DevPool& dp) {
   int n = 0;
@@ -321,14 +235,14 @@ int pool_cache_n(const DevPool& dp) {
 // Chain state from the FP64 rows (snaps the rows to it).
 int pool_chain_init(mcgpu_ctx* ctx, DevPool& dp, cudaStream_t st) {
   const int wpb = 8;
-  k_chain_init<<<(dp.n_mol + wpb - 1) / wpb, wpb * 32, 0, st>>>(dp.P, dp.mol_chain, dp.n_mol);
+  k_chain_init<<<(dp.n_mol + wpb - 1) / wpb, wpb * 32, 0, st>>>(dp.P, dp.mol_chain, 0, dp.n_mol);
   CK(ctx, cudaGetLastError());
   return MCGPU_OK;
 }
 
 // FP64 rows from the chain state.
 int pool_chain_export(mcgpu_ctx* ctx, DevPool& dp, cudaStream_t st) {
-  k_chain_export<<<(dp.n_atom + 255) / 256, 256, 0, st>>>(dp.P, dp.mol_chain, dp.atom_mol,
+  k_chain_export<<<(dp.n_atom + 255) / 256, 256, 0, st>>>(dp.P, dp.mol_chain, dp.atom_mol, 0,
                                                          dp.n_atom);
   CK(ctx, cudaGetLastError());
   return MCGPU_OK;
@@ -351,7 +265,7 @@ int pool_system_energy(mcgpu_ctx* ctx, DevPool& dp, bool f64, cudaStream_t st) {
   return MCGPU_OK;
 }
 
-}  // namespace
+}  // namespace mcgpu
 
 // ---- context ---------------------------------------------------------------------
 

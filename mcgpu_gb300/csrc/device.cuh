@@ -73,6 +73,9 @@ struct __align__(16) ChainHdr {
   // step uniform in +-max_dlnv, pressure in kcal/mol/A^3
   double pressure, max_dlnv;
   int vol_interval, vol_tried, vol_accepted, pad6;
+  // step_limit > 0 stops the chain there (a served job's length);
+  // vol_step: step count of the last volume move (one per step count)
+  long long step_limit, vol_step;
 };
 static_assert(sizeof(ChainHdr) % 16 == 0, "ChainHdr alignment");
 
@@ -108,6 +111,17 @@ struct VolMove {
   double L[3];
   double dlnv, u;
   int state, pad;   // 0 not due, 1 evaluate, 2 rejected outright, 3 accepted
+};
+
+// Molecules a volume phase covers: all of the pool (act == nullptr) or the
+// ranges [act_m0[k], act_m0[k] + act_pref[k+1] - act_pref[k]) of n_act
+// active chains, act_pref their prefix sums (device arrays).
+struct MolRanges {
+  const int* act_slot = nullptr;   // chain (slot) of each active range
+  const int* act_m0 = nullptr;
+  const int* act_pref = nullptr;
+  int n_act = 0;
+  int total = 0;
 };
 
 struct Pool {

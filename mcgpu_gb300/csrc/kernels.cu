@@ -17,9 +17,9 @@ namespace mcgpu {
 
 // ---- mirrors ---------------------------------------------------------------
 
-__global__ void k_refresh_mirrors(Pool P, const int* mol_chain, int n_mol_total) {
-  const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (m >= n_mol_total) return;
+__global__ void k_refresh_mirrors(Pool P, const int* mol_chain, int m_begin, int m_end) {
+  const int m = m_begin + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (m >= m_end) return;
   refresh_molecule(P, P.hdr[mol_chain[m]], m, threadIdx.x & 31, 32);
 }
 
@@ -205,6 +205,22 @@ __global__ void k_set_energy(Pool P, const double* e) {
   if (c < P.n_chains) P.hdr[c].energy = e[c];
 }
 
+// Running energy of chain c from its emol terms: the ordered sum of
+// k_chain_sums for one chain (a served job entering the pool).
+__global__ void k_chain_energy1(Pool P, int c, const double* emol) {
+  __shared__ double red[256];
+  ChainHdr& H = P.hdr[c];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < H.n_mol; i += blockDim.x) acc += emol[H.mol0 + i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int off = blockDim.x >> 1; off > 0; off >>= 1) {
+    if ((int)threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) H.energy = red[0];
+}
+
 // ---- device-resident Metropolis -------------------------------------------
 
 // Puts every molecule of the pool in the device-resident chain state:
@@ -212,9 +228,9 @@ __global__ void k_set_energy(Pool P, const double* e) {
 // anchor), template = offsets, quaternion = identity; then snaps the FP64
 // rows to that state (x = anchor + offset, each moved by < 1e-7 A) so both
 // descriptions agree exactly.  One warp per molecule.
-__global__ void k_chain_init(Pool P, const int* mol_chain, int n_mol_total) {
-  const int m = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (m >= n_mol_total) return;
+__global__ void k_chain_init(Pool P, const int* mol_chain, int m_begin, int m_end) {
+  const int m = m_begin + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (m >= m_end) return;
   const ChainHdr& H = P.hdr[mol_chain[m]];
   const int lane = threadIdx.x & 31;
   const int a0 = P.mstart[m], len = P.mlen[m] & 255;
@@ -252,9 +268,10 @@ __global__ void k_chain_init(Pool P, const int* mol_chain, int n_mol_total) {
 
 // FP64 rows of every atom from the chain state (for downloads, FP64
 // recomputes and the plain entry points).  One thread per atom.
-__global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol, int n_atom) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= n_atom) return;
+__global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol, int a_begin,
+                               int a_end) {
+  const int a = a_begin + blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= a_end) return;
   const int m = atom_mol[a];
   const ChainHdr& H = P.hdr[mol_chain[m]];
   const double3 x = chain_pos3(P.mfix[m], P.aoff[a], H);
@@ -306,10 +323,13 @@ __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsign
     const unsigned long long step0 = H.step;
     const int T = lanes_cap > 0 ? min(lanes_cap, H.tpm) : H.tpm;
     MoveF* props = (MoveF*)s.props;
-    for (int st = 0; st < n_steps; st++) {
+    int my_steps = n_steps;
+    if (H.step_limit > 0)
+      my_steps = (int)max(0LL, min((long long)n_steps, H.step_limit - (long long)step0));
+    for (int st = 0; st < my_steps; st++) {
       if (w == 0) {
         if ((st & 31) == 0) {
-          if (st + lane < n_steps)
+          if (st + lane < my_steps)
             props[lane] = draw_move_f32(H.seed, H.chain_id, step0 + st + lane, H.n_mol,
                                         P.mlen + H.mol0, (float)H.max_t, (float)H.max_r,
                                         H.rot_mode);
@@ -383,7 +403,7 @@ __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsign
     }
     if (g.tid == 0) {
       Hp->energy = energy;
-      Hp->step = step0 + n_steps;
+      Hp->step = step0 + my_steps;
       Hp->accepted += acc_n;
       Hp->pairs += npairs;
       Hp->ties += ties;

@@ -40,9 +40,15 @@ __device__ __forceinline__ double exp_small(double x) {
   return p;
 }
 
-__global__ void k_vol_propose(Pool P, VolMove* vm) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= P.n_chains) return;
+// Chain of work item i: i itself, or the i-th active slot.
+__device__ __forceinline__ int range_chain(const MolRanges& R, int i) {
+  return R.act_slot ? R.act_slot[i] : i;
+}
+
+__global__ void k_vol_propose(Pool P, VolMove* vm, MolRanges R, int n_items) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_items) return;
+  const int c = range_chain(R, i);
   const ChainHdr& H = P.hdr[c];
   VolMove v;
   v.state = 0;
@@ -51,7 +57,7 @@ __global__ void k_vol_propose(Pool P, VolMove* vm) {
   v.u = 0.0;
   for (int k = 0; k < 3; k++) v.L[k] = H.L[k];
   if (H.vol_interval > 0 && H.step > 0 && H.step % (unsigned long long)H.vol_interval == 0 &&
-      H.error == 0) {
+      (long long)H.step > H.vol_step && H.error == 0) {
     const uint2 key = make_uint2((unsigned)H.seed, (unsigned)(H.seed >> 32));
     const uint4 r = philox4x32_10(
         make_uint4((unsigned)H.step, (unsigned)(H.step >> 32), (unsigned)H.chain_id, 3u), key);
@@ -90,14 +96,26 @@ constexpr int kVolThreads = 128;
 // anchors are farther apart than rc + both radii (+ a margin far above the
 // FP32 rounding of the anchor difference) are skipped without an FP64
 // test; every other primary pair takes the reference's FP64 test.
+// Pool molecule of work item b: m_begin + b, or the b-th molecule of the
+// active ranges (binary search over their prefix sums).
+__device__ __forceinline__ int range_mol(const MolRanges& R, int m_begin, int b) {
+  if (!R.act_pref) return m_begin + b;
+  int lo = 0, hi = R.n_act - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (R.act_pref[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  return R.act_m0[lo] + (b - R.act_pref[lo]);
+}
+
 __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int* mol_chain,
                                                                const VolMove* vm, int m_begin,
-                                                               double2* emol2) {
+                                                               MolRanges R, double2* emol2) {
   __shared__ double sx[2][3][kMaxA];
   __shared__ double sq[3][kMaxA];
   __shared__ int spa[kMaxP];
   __shared__ double2 red[kVolThreads];
-  const int m = m_begin + blockIdx.x;
+  const int m = range_mol(R, m_begin, blockIdx.x);
   const int c = mol_chain[m];
   const VolMove v = vm[c];
   if (v.state != 1) {
@@ -179,10 +197,12 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
 }
 
 // Ordered per-chain sums of emol2 (one CTA per chain).
-__global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, double2* out) {
+__global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, double2* out,
+                           MolRanges R) {
   __shared__ double2 red[256];
-  if (vm[blockIdx.x].state != 1) return;
-  const ChainHdr& H = P.hdr[blockIdx.x];
+  const int c = range_chain(R, blockIdx.x);
+  if (vm[c].state != 1) return;
+  const ChainHdr& H = P.hdr[c];
   double2 acc = make_double2(0.0, 0.0);
   for (int i = threadIdx.x; i < H.n_mol; i += blockDim.x) {
     acc.x += emol2[H.mol0 + i].x;
@@ -197,18 +217,20 @@ __global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, doub
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+  if (threadIdx.x == 0) out[c] = red[0];
 }
 
 // The isobaric criterion; an accepted move installs the new box.
 __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, mcgpu_vol_trace* trace,
-                             int trace_slot, int trace_stride) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= P.n_chains) return;
+                             int trace_slot, int trace_stride, MolRanges R, int n_items) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_items) return;
+  const int c = range_chain(R, i);
   VolMove v = vm[c];
   if (v.state == 0) return;
   ChainHdr& H = P.hdr[c];
   H.vol_tried++;
+  H.vol_step = (long long)H.step;
   double e_old = H.energy, e_new = 0.0;
   int ok = 0;
   if (v.state == 1) {
@@ -242,9 +264,11 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, mcgpu_vol
 }
 
 // Screen positions of the primaries of every molecule of an accepting chain.
-__global__ void k_vol_refresh(Pool P, const int* mol_chain, const VolMove* vm, int n_mol_total) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= n_mol_total) return;
+__global__ void k_vol_refresh(Pool P, const int* mol_chain, const VolMove* vm, int n_items,
+                              MolRanges R) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_items) return;
+  const int m = range_mol(R, 0, b);
   const int c = mol_chain[m];
   if (vm[c].state != 3) return;
   const ChainHdr& H = P.hdr[c];
@@ -259,17 +283,24 @@ __global__ void k_vol_refresh(Pool P, const int* mol_chain, const VolMove* vm, i
 // One volume phase on stream st (buffers sized for the pool).
 cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
                                 double2* emol2, double2* esum, mcgpu_vol_trace* trace,
-                                int trace_slot, int trace_stride, cudaStream_t st) {
-  const int nc = P.n_chains;
-  k_vol_propose<<<(nc + 127) / 128, 128, 0, st>>>(P, vm);
-  const int chunk = 1 << 20;
-  for (int m0 = 0; m0 < n_mol_total; m0 += chunk) {
-    const int n = n_mol_total - m0 < chunk ? n_mol_total - m0 : chunk;
-    k_vol_pair_sums<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, emol2);
+                                int trace_slot, int trace_stride, cudaStream_t st, MolRanges act) {
+  const int nc = act.act_slot ? act.n_act : P.n_chains;
+  if (nc == 0) return cudaSuccess;
+  k_vol_propose<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, act, nc);
+  const int items = act.act_pref ? act.total : n_mol_total;
+  if (act.act_pref) {
+    if (items > 0) k_vol_pair_sums<<<items, kVolThreads, 0, st>>>(P, mol_chain, vm, 0, act, emol2);
+  } else {
+    const int chunk = 1 << 20;
+    for (int m0 = 0; m0 < n_mol_total; m0 += chunk) {
+      const int n = n_mol_total - m0 < chunk ? n_mol_total - m0 : chunk;
+      k_vol_pair_sums<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2);
+    }
   }
-  k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, esum);
-  k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, trace, trace_slot, trace_stride);
-  k_vol_refresh<<<(n_mol_total + 127) / 128, 128, 0, st>>>(P, mol_chain, vm, n_mol_total);
+  k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, esum, act);
+  k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, trace, trace_slot, trace_stride, act,
+                                                nc);
+  if (items > 0) k_vol_refresh<<<(items + 127) / 128, 128, 0, st>>>(P, mol_chain, vm, items, act);
   return cudaGetLastError();
 }
 
