@@ -89,6 +89,9 @@ typedef struct {
   double box[3];          /* current box edges (they change under NPT)     */
   int32_t vol_tried;      /* volume moves attempted                        */
   int32_t vol_accepted;   /* volume moves accepted                         */
+  int32_t nl_builds;      /* Verlet-list builds                            */
+  int32_t nl_full_scans;  /* steps screened over all molecules while a list
+                             was on (trial beyond skin/2, or list stale)   */
 } mcgpu_chain_stats;
 
 /* One volume move of an NPT chain (for replay checks). */
@@ -120,6 +123,7 @@ typedef struct mcgpu_server mcgpu_server;
 
 /* Creates a context on CUDA device `device` (one GPU per context). */
 int mcgpu_ctx_create(mcgpu_ctx** out, int device);
+/* Destroys the context; destroy its boxes, batches and servers first. */
 int mcgpu_ctx_destroy(mcgpu_ctx* ctx);
 /* Makes the context launch on the caller's CUDA stream (a cudaStream_t
  * passed as a plain pointer; NULL restores the context's own stream).  The
@@ -222,6 +226,17 @@ int mcgpu_batch_run_traced(mcgpu_batch* batch, int n_steps, mcgpu_trace* out,
  * interval 0 makes the batch NVT again.  max_dlnv in (0, 0.1]. */
 int mcgpu_batch_set_npt(mcgpu_batch* batch, int interval, const double* pressure_atm,
                         const double* max_dlnv);
+/* Verlet neighbour lists with the given skin (Angstrom; <= 0 turns them
+ * off) for every chain of a batch, or for the device-resident chain of a
+ * box.  Built on the GPU from a cell list on the molecules' anchors (cells
+ * at least rc + skin + 2 * primary radius wide), rebuilt between launches
+ * once a molecule has moved more than skin/2 since the last build; while a
+ * trial placement is farther than that the step screens all molecules.
+ * The in-range sets, and so the trajectories, are those of the full scan.
+ * Replaces the reference's VerletStep / NLCStep strategies
+ * (VerletStep.cpp:119-207, NLCStep.cpp:125-243) for the chain forms. */
+int mcgpu_batch_set_verlet(mcgpu_batch* batch, double skin);
+int mcgpu_box_set_verlet(mcgpu_box* box, double skin);
 int mcgpu_batch_sync(mcgpu_batch* batch);
 int mcgpu_batch_stats(mcgpu_batch* batch, mcgpu_chain_stats* stats);
 /* Coordinates of chain c (arrays sized like its descriptor). */

@@ -50,7 +50,8 @@ class Move(C.Structure):
 class ChainStats(C.Structure):
     _fields_ = [("energy", C.c_double), ("steps", C.c_int64), ("accepted", C.c_int64),
                 ("pairs", C.c_int64), ("error", C.c_int32), ("ties", C.c_int32),
-                ("box", C.c_double * 3), ("vol_tried", C.c_int32), ("vol_accepted", C.c_int32)]
+                ("box", C.c_double * 3), ("vol_tried", C.c_int32), ("vol_accepted", C.c_int32),
+                ("nl_builds", C.c_int32), ("nl_full_scans", C.c_int32)]
 
 
 class VolTrace(C.Structure):
@@ -114,6 +115,8 @@ _PROTOS = {
     "mcgpu_batch_sync": (C.c_int, [_vp]),
     "mcgpu_batch_run_traced": (C.c_int, [_vp, C.c_int, C.POINTER(Trace), C.POINTER(VolTrace)]),
     "mcgpu_batch_set_npt": (C.c_int, [_vp, C.c_int, _dp, _dp]),
+    "mcgpu_batch_set_verlet": (C.c_int, [_vp, C.c_double]),
+    "mcgpu_box_set_verlet": (C.c_int, [_vp, C.c_double]),
     "mcgpu_batch_stats": (C.c_int, [_vp, C.POINTER(ChainStats)]),
     "mcgpu_batch_download": (C.c_int, [_vp, C.c_int, _dp, _dp, _dp]),
     "mcgpu_batch_system_energy": (C.c_int, [_vp, _dp]),

@@ -25,6 +25,7 @@ class ChainBatch:
         _abi.check(_abi.lib().mcgpu_batch_create(ctx.handle, n, self._descs, self._seeds,
                                                  int(rotation), C.byref(self._h)), ctx.handle)
         self.n_chains = n
+        ctx.adopt(self)
 
     def _check(self, st: int) -> None:
         _abi.check(st, self.ctx.handle)
@@ -62,6 +63,10 @@ class ChainBatch:
         return steps, vols
 
     vol_interval = 0
+
+    def set_verlet(self, skin: float) -> None:
+        """Verlet neighbour lists with this skin (Angstrom); <= 0 turns them off."""
+        self._check(_abi.lib().mcgpu_batch_set_verlet(self._h, float(skin)))
 
     def set_npt(self, interval: int, pressure_atm, max_dlnv) -> None:
         """Isobaric volume moves every `interval` steps (0 = NVT again);

@@ -82,7 +82,7 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
                             : make_float2(0.f, 0.f));
   }
   int max_len = 0;
-  double max_rad = 0;
+  double max_rad = 0, max_prad = 0;
   bool simple = d->n_pidx == d->n_mol;
   for (int m = 0; m < d->n_mol; m++) {
     const int s = d->mol_start[m], len = d->mol_len[m];
@@ -112,6 +112,11 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
     for (int a = s; a < s + len; a++) {
       const double dx = d->x[a] - d->x[an], dy = d->y[a] - d->y[an], dz = d->z[a] - d->z[an];
       rad = std::max(rad, std::sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    for (int k = ps; k < ps + pc; k++) {
+      const int p = d->pidx[k];
+      const double dx = d->x[p] - d->x[an], dy = d->y[p] - d->y[an], dz = d->z[p] - d->z[an];
+      max_prad = std::max(max_prad, std::sqrt(dx * dx + dy * dy + dz * dz));
     }
     max_rad = std::max(max_rad, rad);
     max_len = std::max(max_len, len);
@@ -157,6 +162,7 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
   hdr_set_box(h, d->size);
   h.kTinvf = (float)(1.0 / (d->temperature * kBoltz));
   h.rad_max = (float)max_rad;
+  h.prad = (float)max_prad;
   h.kT = d->temperature * kBoltz;  // SimBoxBuilder.cpp:29
   h.max_t = d->max_translate;
   h.max_r = d->max_rotate;
@@ -245,6 +251,73 @@ int pool_chain_export(mcgpu_ctx* ctx, DevPool& dp, cudaStream_t st) {
   k_chain_export<<<(dp.n_atom + 255) / 256, 256, 0, st>>>(dp.P, dp.mol_chain, dp.atom_mol, 0,
                                                          dp.n_atom);
   CK(ctx, cudaGetLastError());
+  return MCGPU_OK;
+}
+
+int pool_set_verlet(mcgpu_ctx* ctx, DevPool& dp, double skin, cudaStream_t st) {
+  const int nc = dp.n_chains;
+  std::vector<NlCfg> cfg(nc);
+  int cells = 0, max_cells = 0;
+  long long stride = 0;
+  for (int c = 0; c < nc; c++) {
+    const ChainHdr& h = dp.hdr[c];
+    NlCfg& f = cfg[c];
+    std::memset(&f, 0, sizeof(f));
+    if (skin <= 0) continue;
+    const double rl = h.cutoff + skin + 2.0 * h.prad;
+    int cap = 1;
+    for (int k = 0; k < 3; k++) cap *= (int)std::floor(1.25 * h.L[k] / rl) + 1;
+    f.on = 1;
+    f.cell0 = cells;
+    f.cell_cap = cap;
+    f.rlist = (float)rl;
+    f.r2 = (float)((rl + 1e-2) * (rl + 1e-2));
+    const double hs = std::max(0.5 * skin - 1e-2, 0.0);
+    f.half2 = (float)(hs * hs);
+    cells += cap;
+    max_cells = std::max(max_cells, cap);
+    const double rho = h.n_mol / (h.L[0] * h.L[1] * h.L[2]);
+    const double est = rho * 4.18879020478639 * std::pow(rl + 1e-2, 3);
+    stride = std::max<long long>(stride, std::min<long long>((long long)(2 * est) + 64, h.n_mol));
+  }
+  stride = (stride + 31) & ~31LL;
+  Pool& P = dp.P;
+  void* old[] = {P.nl, P.nl_cnt, P.pbuild, P.mcell, P.cell_cnt, P.cell_start, P.cell_mol};
+  for (void* p : old)
+    if (p) cudaFree(p);
+  P.nl = nullptr; P.nl_cnt = nullptr; P.pbuild = nullptr; P.mcell = nullptr;
+  P.cell_cnt = nullptr; P.cell_start = nullptr; P.cell_mol = nullptr;
+  P.nl_stride = 0;
+  dp.nl_on = skin > 0;
+  dp.nl_max_cells = max_cells;
+  cudaError_t e = cudaSuccess;
+  if (dp.nl_on) {
+    P.nl_stride = (int)stride;
+    P.nl = dalloc<int>((size_t)dp.n_mol * stride, &e);
+    P.nl_cnt = dalloc<int>(dp.n_mol, &e);
+    P.pbuild = dalloc<float4>(dp.n_pidx, &e);
+    P.mcell = dalloc<int>(dp.n_mol, &e);
+    P.cell_cnt = dalloc<int>(cells, &e);
+    P.cell_start = dalloc<int>(cells, &e);
+    P.cell_mol = dalloc<int>(dp.n_mol, &e);
+    if (e != cudaSuccess) return set_err(ctx, MCGPU_ERR_NOMEM, "Verlet lists: %s", cudaGetErrorString(e));
+  }
+  NlCfg* dcfg = dalloc<NlCfg>(nc, &e);
+  if (e != cudaSuccess) return set_err(ctx, MCGPU_ERR_NOMEM, "Verlet config: %s", cudaGetErrorString(e));
+  e = cudaMemcpyAsync(dcfg, cfg.data(), sizeof(NlCfg) * nc, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    k_nl_config<<<(nc + 127) / 128, 128, 0, st>>>(P, dcfg);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(dcfg);
+  if (e != cudaSuccess) return set_err(ctx, MCGPU_ERR_CUDA, "Verlet config: %s", cudaGetErrorString(e));
+  return MCGPU_OK;
+}
+
+int pool_nl_rebuild(mcgpu_ctx* ctx, DevPool& dp, cudaStream_t st) {
+  if (!dp.nl_on) return MCGPU_OK;
+  CK(ctx, launch_nl_rebuild(dp.P, dp.mol_chain, dp.n_mol, dp.nl_max_cells, st));
   return MCGPU_OK;
 }
 
@@ -590,9 +663,12 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
   }
   const int nw = std::max(1, std::min(8, dp.n_mol / 256));
   SmemShape sh = shape_for(dp.max_len, nw, pool_cache_n(dp));
-  const int seg = 1024;
+  // with a Verlet list, short launches let stale lists be rebuilt promptly
+  const int seg = dp.nl_on ? 64 : 1024;
   for (int done = 0; done < n_steps; done += seg) {
     const int k = std::min(seg, n_steps - done);
+    int rc = pool_nl_rebuild(ctx, dp, st);
+    if (rc) return rc;
     CK(ctx, cudaMemsetAsync(b->queue, 0, sizeof(unsigned), st));
     Pool P = dp.P;
     P.trace = nullptr;
@@ -614,6 +690,11 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
     stats->pairs = h.pairs;
     stats->error = h.error;
     stats->ties = h.ties;
+    for (int k = 0; k < 3; k++) stats->box[k] = h.L[k];
+    stats->vol_tried = h.vol_tried;
+    stats->vol_accepted = h.vol_accepted;
+    stats->nl_builds = h.nl_builds;
+    stats->nl_full_scans = h.nl_full;
   }
   CK(ctx, cudaStreamSynchronize(st));
   return MCGPU_OK;
@@ -667,6 +748,8 @@ static int batch_launch(mcgpu_batch* bt, int steps, unsigned* q, cudaStream_t st
   const int gw = batch_gwarps(bt);
   SmemShape sh = shape_for(bt->pool.max_len, gw, bt->cache_n);
   bt->rows_stale = true;
+  int rc = pool_nl_rebuild(ctx, bt->pool, st);
+  if (rc) return rc;
   CK(ctx, cudaMemsetAsync(q, 0, sizeof(unsigned), st));
   k_chain_steps<<<grid, bt->threads, smem, st>>>(bt->pool.P, steps, q, bt->order,
                                                  bt->pool.n_chains, gw, sh, trace, trace_off,
@@ -949,6 +1032,19 @@ extern "C" int mcgpu_batch_run_traced(mcgpu_batch* bt, int n_steps, mcgpu_trace*
   return MCGPU_OK;
 }
 
+extern "C" int mcgpu_batch_set_verlet(mcgpu_batch* bt, double skin) {
+  if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
+  if (!std::isfinite(skin)) return set_err(bt->ctx, MCGPU_ERR_INVALID, "skin %g", skin);
+  batch_drop_graph(bt);
+  return pool_set_verlet(bt->ctx, bt->pool, skin, bt->ctx->stream);
+}
+
+extern "C" int mcgpu_box_set_verlet(mcgpu_box* b, double skin) {
+  if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  if (!std::isfinite(skin)) return set_err(b->ctx, MCGPU_ERR_INVALID, "skin %g", skin);
+  return pool_set_verlet(b->ctx, b->pool, skin, b->ctx->stream);
+}
+
 extern "C" int mcgpu_batch_set_npt(mcgpu_batch* bt, int interval, const double* pressure_atm,
                                    const double* max_dlnv) {
   if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
@@ -1012,6 +1108,8 @@ extern "C" int mcgpu_batch_stats(mcgpu_batch* bt, mcgpu_chain_stats* stats) {
     for (int k = 0; k < 3; k++) stats[c].box[k] = h[c].L[k];
     stats[c].vol_tried = h[c].vol_tried;
     stats[c].vol_accepted = h[c].vol_accepted;
+    stats[c].nl_builds = h[c].nl_builds;
+    stats[c].nl_full_scans = h[c].nl_full;
     err |= h[c].error;
   }
   if (err) return set_err(ctx, MCGPU_ERR_DEVICE, "a chain reported device error status %d", err);

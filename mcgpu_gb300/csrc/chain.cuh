@@ -40,8 +40,10 @@ __device__ __forceinline__ float4 chain_screen_pos(uint4 A, float4 o, const Chai
                      __uint2float_rn(z) * H.fxs[2], 0.f);
 }
 
-// misc[] slots written by stage_chain beyond load_moved's
-enum : int { kMiscQn = 16, kMiscU = 20 };
+// misc[] slots written by stage_chain beyond load_moved's: new quaternion,
+// acceptance uniform, "trial placement within skin/2 of the Verlet build"
+// flag; kMiscNlOk: the chain's list is still valid (group-uniform state)
+enum : int { kMiscQn = 16, kMiscU = 20, kMiscNlTrial = 24, kMiscNlOk = 25 };
 
 // Warp 0 stages the proposed FP32 move `mv` of a chain molecule: old and
 // new offsets (o_old, o_new), pair factors and |o|^2 (eq), screen
@@ -93,12 +95,16 @@ __device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF
   }
   for (int off = 16; off > 0; off >>= 1) qsum += __shfl_xor_sync(~0u, qsum, off);
   __syncwarp();
+  bool near = true;
   for (int k = lane; k < pi.y; k += 32) {
     const int slot = P.pidx[pi.x + k] - a0;
     s.pa[k] = slot;
     s.p_old[k] = (k == 0 && pcache) ? pcache[m - H.mol0] : P.ppos[pi.x + k];
-    s.p_new[k] = chain_screen_pos(An, s.o_new[slot], H);
+    const float4 pn = chain_screen_pos(An, s.o_new[slot], H);
+    s.p_new[k] = pn;
+    if (H.nl_on) near = near && r2_screen(pn, P.pbuild[pi.x + k], H) <= H.nl_half2;
   }
+  near = __all_sync(~0u, near);
   if (lane == 0) {
     s.misc[0] = m; s.misc[1] = a0; s.misc[2] = len; s.misc[3] = pi.y;
     s.misc[4] = lw >> 8; s.misc[5] = 3; s.misc[6] = mv.vertex;
@@ -107,6 +113,7 @@ __device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF
     s.misc[kMiscQn] = __float_as_int(qn.w); s.misc[kMiscQn + 1] = __float_as_int(qn.x);
     s.misc[kMiscQn + 2] = __float_as_int(qn.y); s.misc[kMiscQn + 3] = __float_as_int(qn.z);
     s.misc[kMiscU] = __float_as_int(mv.u);
+    s.misc[kMiscNlTrial] = near ? 1 : 0;
     s.miscd[0] = (double)P.mrad[m];
     s.miscd[1] = (double)qsum;
   }
@@ -151,19 +158,22 @@ __device__ __forceinline__ int screen_chain(const Pool& P, const ChainHdr& H, co
   return f;
 }
 
-// One warp screens chain candidates [c_begin, c_end) in warp-strided
-// rounds of 32 (screen positions from the shared-memory cache when given)
-// and evaluates the in-range ones in batches of 32.
+// One warp screens chain candidates [c_begin, c_end) -- or, with a Verlet
+// list, the molecules cand[c_begin .. c_end) -- in warp-strided rounds of 32
+// (screen positions from the shared-memory cache when given) and evaluates
+// the in-range ones in batches of 32.
 __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const GroupSmem& s,
                                 const MovedInfo& mi, const float4* pcache, int c_begin, int c_end,
-                                int w, int nw, int lane, int T, AccFF& acc) {
+                                int w, int nw, int lane, int T, AccFF& acc,
+                                const int* cand = nullptr) {
   int* rj = s.lj + w * kRing;
   int head = 0, tail = 0;
   const unsigned lt = lanemask_lt();
   for (int base = c_begin + w * 32; base < c_end; base += nw * 32) {
-    const int j = base + lane;
+    const int idx = base + lane;
+    const int j = (cand && idx < c_end) ? cand[idx] : idx;
     int f = 0;
-    if (j < c_end && j != mi.mol) {
+    if (idx < c_end && j != mi.mol) {
       float4 q0;
       if (pcache)
         q0 = pcache[j - H.mol0];

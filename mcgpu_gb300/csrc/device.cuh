@@ -76,6 +76,14 @@ struct __align__(16) ChainHdr {
   // step_limit > 0 stops the chain there (a served job's length);
   // vol_step: step count of the last volume move (one per step count)
   long long step_limit, vol_step;
+  // Verlet list: nl_on enables it; nl_valid while every molecule's
+  // primaries are within skin/2 of their positions at the last build;
+  // cells: ncell[k] cells per edge from cell0 in the pool's cell arrays
+  // (at most cell_cap); nl_r2: list radius squared; nl_half2: (skin/2)^2
+  int nl_on, nl_valid, nl_builds, nl_full;
+  int cell0, cell_cap, ncell[3];
+  int nl_overflow;
+  float nl_r2, nl_half2, nl_rlist, prad;
 };
 static_assert(sizeof(ChainHdr) % 16 == 0, "ChainHdr alignment");
 
@@ -105,6 +113,12 @@ __host__ __device__ inline void hdr_set_box(ChainHdr& h, const double L[3]) {
   h.cut2_lo = (float)(h.cutoff * h.cutoff - band);
   h.cut2_hi = (float)(h.cutoff * h.cutoff + band);
 }
+
+// Verlet-list configuration of one chain (host-computed).
+struct NlCfg {
+  int on, cell0, cell_cap, pad;
+  float r2, half2, rlist, pad2;
+};
 
 // One chain's volume move in flight (NPT).
 struct VolMove {
@@ -141,6 +155,15 @@ struct Pool {
   double* rb;          // rollback rows, 3 * max_len per chain
   mcgpu_trace* trace;  // optional step records
   int n_chains;
+  // Verlet lists (null when no chain uses one)
+  int* nl;             // [n_mol * nl_stride] neighbour molecules (pool-absolute)
+  int* nl_cnt;         // [n_mol]
+  float4* pbuild;      // [n_pidx] primary screen positions at the last build
+  int* mcell;          // [n_mol] cell of each molecule (pool cell index)
+  int* cell_cnt;       // [cells] members, then fill counters
+  int* cell_start;     // [cells] first slot in cell_mol
+  int* cell_mol;       // [n_mol] molecules grouped by cell
+  int nl_stride;
 };
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), from the published

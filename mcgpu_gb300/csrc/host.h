@@ -24,6 +24,9 @@ __global__ void k_chain_steps(Pool P, int n_steps, unsigned* queue, const int* o
                               int trace_stride, int lanes_cap);
 __global__ void k_chain_init(Pool P, const int* mol_chain, int m_begin, int m_end);
 __global__ void k_chain_energy1(Pool P, int c, const double* emol);
+__global__ void k_nl_config(Pool P, const NlCfg* cfg);
+cudaError_t launch_nl_rebuild(Pool P, const int* mol_chain, int n_mol, int max_cells,
+                              cudaStream_t st);
 __global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol, int a_begin,
                                int a_end);
 cudaError_t launch_mol_energy(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
@@ -95,10 +98,13 @@ struct DevPool {
   double* esum = nullptr;
   std::vector<ChainHdr> hdr;  // host copy of the headers at upload
   std::vector<int> mstart, mlen;  // host copies (pool-absolute)
+  bool nl_on = false;             // some chain keeps a Verlet list
+  int nl_max_cells = 0;           // largest per-chain cell allocation
 
   void release() {
     void* ptrs[] = {P.x, P.y, P.z, P.sig, P.eps, P.q, P.aoff, P.aofl, P.aeq, P.mstart, P.mlen, P.mpi,
                     P.mfix, P.mrad, P.mq, P.atpl, P.pidx, P.ppos, P.hdr, P.rb, P.trace,
+                    P.nl, P.nl_cnt, P.pbuild, P.mcell, P.cell_cnt, P.cell_start, P.cell_mol,
                     mol_chain, atom_mol, emol, pairs, esum};
     for (void* p : ptrs)
       if (p) cudaFree(p);
@@ -122,5 +128,9 @@ int pool_cache_n(const DevPool& dp);
 int pool_chain_init(mcgpu_ctx* ctx, DevPool& dp, cudaStream_t st);
 int pool_chain_export(mcgpu_ctx* ctx, DevPool& dp, cudaStream_t st);
 int pool_system_energy(mcgpu_ctx* ctx, DevPool& dp, bool f64, cudaStream_t st);
+// Verlet lists with the given skin for every chain (skin <= 0: off).
+int pool_set_verlet(mcgpu_ctx* ctx, DevPool& dp, double skin, cudaStream_t st);
+// Rebuilds the stale lists (no-op launches when none is stale).
+int pool_nl_rebuild(mcgpu_ctx* ctx, DevPool& dp, cudaStream_t st);
 
 }  // namespace mcgpu

@@ -316,7 +316,9 @@ __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsign
     float4* pcache = (s.pc && H.simple_prim && H.n_mol <= shape.cache_n) ? s.pc : nullptr;
     if (pcache)
       for (int i = g.tid; i < H.n_mol; i += gsize) pcache[i] = P.ppos[H.pidx0 + i];
+    if (g.tid == 0) s.misc[kMiscNlOk] = (H.nl_on && H.nl_valid) ? 1 : 0;
     g.sync();
+    int full_scans = 0;
     double energy = H.energy;
     long long acc_n = 0, npairs = 0;
     int ties = 0;
@@ -341,8 +343,16 @@ __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsign
       const MovedInfo mi = load_moved(s);
       // read before the reduction barrier: warp 0 restages the slot after it
       const float u = __int_as_float(s.misc[kMiscU]);
+      // Verlet list while it is valid and the trial placement stays within
+      // skin/2 of the build; the full scan otherwise (same in-range set)
+      const int trial_near = s.misc[kMiscNlTrial];
+      const bool use_list = s.misc[kMiscNlOk] && trial_near;
       AccFF acc = {0.f, 0.f, 0.f, 0.f, 0.f, 0};
-      warp_eval_chain(P, H, s, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, acc);
+      if (use_list)
+        warp_eval_chain(P, H, s, mi, pcache, 0, P.nl_cnt[mi.mol], w, nw, lane, T, acc,
+                        P.nl + (size_t)mi.mol * P.nl_stride);
+      else
+        warp_eval_chain(P, H, s, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, acc);
       group_reduce_ff(g, s, acc);
       // FP32 decision unless the FP32 dE is within its rounding bound of the
       // threshold; the bound covers the pair terms' rounding (kTieRel of the
@@ -382,7 +392,10 @@ __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsign
           if (ok) {
             energy += de;
             acc_n++;
+            // a molecule now beyond skin/2 of the build invalidates the list
+            if (!trial_near) s.misc[kMiscNlOk] = 0;
           }
+          if (H.nl_on && !use_list) full_scans++;
           npairs += acc.np;
           ties += tie;
           if (trace) {
@@ -407,6 +420,10 @@ __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsign
       Hp->accepted += acc_n;
       Hp->pairs += npairs;
       Hp->ties += ties;
+      if (H.nl_on) {
+        Hp->nl_valid = s.misc[kMiscNlOk];
+        Hp->nl_full += full_scans;
+      }
     }
     g.sync();
   }

@@ -246,6 +246,7 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, mcgpu_vol
   if (ok) {
     hdr_set_box(H, v.L);
     H.vol_accepted++;
+    H.nl_valid = 0;  // every centre moved: the Verlet list is rebuilt
     v.state = 3;
     vm[c] = v;
   }

@@ -52,6 +52,7 @@ class JobServer:
         _abi.check(_abi.lib().mcgpu_server_create(ctx.handle, C.byref(cfg), C.byref(self._h)),
                    ctx.handle)
         self._pending: dict[int, _Pending] = {}
+        ctx.adopt(self)
 
     def _check(self, st: int) -> None:
         _abi.check(st, self.ctx.handle)

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -27,13 +28,19 @@ KBOLTZ = 0.00198717  # SimBox.h:16
 
 
 class Context:
-    """One CUDA device context (mcgpu_ctx_create)."""
+    """One CUDA device context (mcgpu_ctx_create).  Boxes, batches and
+    servers made from it register here; closing the context closes them
+    first (the C ABI requires them destroyed before their context)."""
 
     def __init__(self, device: int = 0):
         self._h = C.c_void_p()
+        self._children = weakref.WeakSet()
         L = _abi.lib()
         _abi.check(L.mcgpu_ctx_create(C.byref(self._h), int(device)))
         self.device = device
+
+    def adopt(self, child) -> None:
+        self._children.add(child)
 
     @property
     def handle(self) -> C.c_void_p:
@@ -47,6 +54,8 @@ class Context:
 
     def close(self) -> None:
         if self._h:
+            for child in list(self._children):
+                child.close()
             _abi.lib().mcgpu_ctx_destroy(self._h)
             self._h = C.c_void_p()
 
@@ -91,6 +100,7 @@ class GpuBox:
         _abi.check(_abi.lib().mcgpu_box_upload(ctx.handle, C.byref(self._desc), int(precision),
                                                C.byref(self._h)), ctx.handle)
         self.precision = precision
+        ctx.adopt(self)
 
     def _check(self, st: int) -> None:
         _abi.check(st, self.ctx.handle)
@@ -144,6 +154,10 @@ class GpuBox:
                                                   y.ctypes.data_as(dp), z.ctypes.data_as(dp),
                                                   None))
         return x, y, z
+
+    def set_verlet(self, skin: float) -> None:
+        """Verlet neighbour lists (skin in Angstrom, <= 0 off) for chain_run."""
+        self._check(_abi.lib().mcgpu_box_set_verlet(self._h, float(skin)))
 
     def chain_run(self, seed: int, n_steps: int, chain_id: int = 0,
                   rotation: int = _abi.ROT_AXIS, trace: bool = False):
