@@ -104,6 +104,8 @@ typedef struct {
   double e_old, e_new;    /* FP64 system energies at V and V'              */
   double dlnv, u;         /* the ln V step and the acceptance uniform      */
   double edge;            /* box edge x after the decision                 */
+  int32_t fp64;           /* 1 if FP32 energies were re-taken in FP64      */
+  int32_t pad0;
 } mcgpu_vol_trace;
 
 /* One step of a recorded device trajectory (for replay checks). */
@@ -223,9 +225,16 @@ int mcgpu_batch_run_traced(mcgpu_batch* batch, int n_steps, mcgpu_trace* out,
  * restarts from the FP64 energy of the volume it keeps.  The reference's
  * NPTEnsemble (Ensemble.cpp:9-23, SimulationStep.cpp:476-518) is the
  * counterpart; its fixed factor 1.1 and unitless P dV are not reproduced.
- * interval 0 makes the batch NVT again.  max_dlnv in (0, 0.1]. */
+ * interval 0 makes the batch NVT again.  max_dlnv in (0, 0.1].
+ * precision MCGPU_PREC_FP64 computes U(V), U(V') with FP64 pair terms;
+ * MCGPU_PREC_MIXED with FP32 pair terms summed in double-float, re-taking
+ * in FP64 only the moves whose criterion argument lies within the FP32
+ * rounding bound of ln u (so the decisions are the FP64 ones; the kept
+ * energy carries the FP32-pair error).  GB300 issues FP64 at 1/64 of the
+ * FP32 rate, which makes the FP64 form the dominant cost of frequent volume
+ * moves on large boxes. */
 int mcgpu_batch_set_npt(mcgpu_batch* batch, int interval, const double* pressure_atm,
-                        const double* max_dlnv);
+                        const double* max_dlnv, int precision);
 /* Verlet neighbour lists with the given skin (Angstrom; <= 0 turns them
  * off) for every chain of a batch, or for the device-resident chain of a
  * box.  Built on the GPU from a cell list on the molecules' anchors (cells
@@ -276,6 +285,9 @@ typedef struct {
   uint64_t seed;              /* Philox key                                */
   uint32_t chain_id;          /* Philox counter id                         */
   int32_t npt;                /* 1: isobaric volume moves                  */
+  int32_t vol_precision;      /* NPT energies: MCGPU_PREC_FP64 or _MIXED (see
+                                 mcgpu_batch_set_npt)                      */
+  int32_t pad1;
   int64_t n_steps;            /* trial moves to run                        */
   double pressure_atm;        /* NPT pressure                              */
   double max_dlnv;            /* NPT ln V step bound, (0, 0.1]             */

@@ -57,7 +57,8 @@ class ChainStats(C.Structure):
 class VolTrace(C.Structure):
     _fields_ = [("step", C.c_int64), ("accepted", C.c_int32), ("evaluated", C.c_int32),
                 ("e_old", C.c_double), ("e_new", C.c_double), ("dlnv", C.c_double),
-                ("u", C.c_double), ("edge", C.c_double)]
+                ("u", C.c_double), ("edge", C.c_double), ("fp64", C.c_int32),
+                ("pad0", C.c_int32)]
 
 
 class Trace(C.Structure):
@@ -76,7 +77,8 @@ class ServerConfig(C.Structure):
 
 class JobDesc(C.Structure):
     _fields_ = [("box", C.POINTER(BoxDesc)), ("seed", C.c_uint64), ("chain_id", C.c_uint32),
-                ("npt", C.c_int32), ("n_steps", C.c_int64), ("pressure_atm", C.c_double),
+                ("npt", C.c_int32), ("vol_precision", C.c_int32), ("pad1", C.c_int32),
+                ("n_steps", C.c_int64), ("pressure_atm", C.c_double),
                 ("max_dlnv", C.c_double), ("x_out", _dp), ("y_out", _dp), ("z_out", _dp)]
 
 
@@ -114,7 +116,7 @@ _PROTOS = {
     "mcgpu_batch_get_tile": (C.c_int, [_vp, _ip, _ip, _ip, _ip]),
     "mcgpu_batch_sync": (C.c_int, [_vp]),
     "mcgpu_batch_run_traced": (C.c_int, [_vp, C.c_int, C.POINTER(Trace), C.POINTER(VolTrace)]),
-    "mcgpu_batch_set_npt": (C.c_int, [_vp, C.c_int, _dp, _dp]),
+    "mcgpu_batch_set_npt": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_int]),
     "mcgpu_batch_set_verlet": (C.c_int, [_vp, C.c_double]),
     "mcgpu_box_set_verlet": (C.c_int, [_vp, C.c_double]),
     "mcgpu_batch_stats": (C.c_int, [_vp, C.POINTER(ChainStats)]),

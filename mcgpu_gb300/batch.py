@@ -68,15 +68,17 @@ class ChainBatch:
         """Verlet neighbour lists with this skin (Angstrom); <= 0 turns them off."""
         self._check(_abi.lib().mcgpu_batch_set_verlet(self._h, float(skin)))
 
-    def set_npt(self, interval: int, pressure_atm, max_dlnv) -> None:
+    def set_npt(self, interval: int, pressure_atm, max_dlnv,
+                precision: int = _abi.PREC_FP64) -> None:
         """Isobaric volume moves every `interval` steps (0 = NVT again);
-        pressure_atm and max_dlnv are scalars or one value per chain."""
+        pressure_atm and max_dlnv are scalars or one value per chain;
+        precision of the two system energies: PREC_FP64 or PREC_MIXED."""
         n = self.n_chains
         p = np.broadcast_to(np.asarray(pressure_atm, np.float64), (n,)).copy()
         d = np.broadcast_to(np.asarray(max_dlnv, np.float64), (n,)).copy()
         dp = C.POINTER(C.c_double)
         self._check(_abi.lib().mcgpu_batch_set_npt(self._h, int(interval), p.ctypes.data_as(dp),
-                                                   d.ctypes.data_as(dp)))
+                                                   d.ctypes.data_as(dp), int(precision)))
         self.vol_interval = int(interval)
 
     def sync(self) -> None:

@@ -721,7 +721,10 @@ struct mcgpu_batch {
   int vol_interval = 0;
   VolMove* vm = nullptr;
   double2* emol2 = nullptr;
+  double2* eabs2 = nullptr;
   double2* vsum = nullptr;
+  double2* vsum_abs = nullptr;
+  bool vol_has64 = false, vol_has32 = false;  // precisions of the NPT chains
   // snapshot for the autotuner
   std::vector<void*> snap;
 };
@@ -832,7 +835,9 @@ extern "C" int mcgpu_batch_destroy(mcgpu_batch* bt) {
   if (bt->order) cudaFree(bt->order);
   if (bt->vm) cudaFree(bt->vm);
   if (bt->emol2) cudaFree(bt->emol2);
+  if (bt->eabs2) cudaFree(bt->eabs2);
   if (bt->vsum) cudaFree(bt->vsum);
+  if (bt->vsum_abs) cudaFree(bt->vsum_abs);
   for (void* p : bt->snap)
     if (p) cudaFree(p);
   delete bt;
@@ -892,7 +897,8 @@ static int batch_build_graph(mcgpu_batch* bt, int launches, int interval) {
     }
     if (rc == MCGPU_OK) {
       cudaError_t e = launch_volume_phase(bt->pool.P, bt->pool.mol_chain, bt->pool.n_mol, bt->vm,
-                                          bt->emol2, bt->vsum, nullptr, 0, 0, st);
+                                          bt->emol2, bt->eabs2, bt->vsum, bt->vsum_abs, nullptr, 0,
+                                          0, st, MolRanges(), bt->vol_has64, bt->vol_has32);
       if (e != cudaSuccess) rc = set_err(ctx, MCGPU_ERR_CUDA, "volume phase launch: %s", cudaGetErrorString(e));
     }
   } else {
@@ -985,7 +991,8 @@ static int batch_advance(mcgpu_batch* bt, int n_steps, mcgpu_trace* trace, int t
     bt->steps_done += seg;
     if (bt->steps_done % iv == 0) {
       CK(ctx, launch_volume_phase(bt->pool.P, bt->pool.mol_chain, bt->pool.n_mol, bt->vm, bt->emol2,
-                                  bt->vsum, vtrace, vk, vstride, ctx->stream));
+                                  bt->eabs2, bt->vsum, bt->vsum_abs, vtrace, vk, vstride,
+                                  ctx->stream, MolRanges(), bt->vol_has64, bt->vol_has32));
       vk++;
     }
   }
@@ -1046,13 +1053,16 @@ extern "C" int mcgpu_box_set_verlet(mcgpu_box* b, double skin) {
 }
 
 extern "C" int mcgpu_batch_set_npt(mcgpu_batch* bt, int interval, const double* pressure_atm,
-                                   const double* max_dlnv) {
+                                   const double* max_dlnv, int precision) {
   if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
   mcgpu_ctx* ctx = bt->ctx;
   const int nc = bt->pool.n_chains;
   if (interval < 0) return set_err(ctx, MCGPU_ERR_INVALID, "volume interval %d must be >= 0", interval);
+  if (precision != MCGPU_PREC_FP64 && precision != MCGPU_PREC_MIXED)
+    return set_err(ctx, MCGPU_ERR_INVALID, "unknown volume-move precision %d", precision);
+  const int mixed = interval > 0 && precision == MCGPU_PREC_MIXED;
   std::vector<double> p(nc, 0.0), dl(nc, 0.0);
-  std::vector<int> iv(nc, interval);
+  std::vector<int> iv(nc, interval), vmx(nc, mixed);
   if (interval > 0) {
     if (!pressure_atm || !max_dlnv) return set_err(ctx, MCGPU_ERR_INVALID, "null NPT parameters");
     for (int c = 0; c < nc; c++) {
@@ -1067,7 +1077,9 @@ extern "C" int mcgpu_batch_set_npt(mcgpu_batch* bt, int interval, const double* 
     cudaError_t e = cudaSuccess;
     if (!bt->vm) bt->vm = dalloc<VolMove>(nc, &e);
     if (!bt->emol2) bt->emol2 = dalloc<double2>(bt->pool.n_mol, &e);
+    if (!bt->eabs2) bt->eabs2 = dalloc<double2>(bt->pool.n_mol, &e);
     if (!bt->vsum) bt->vsum = dalloc<double2>(nc, &e);
+    if (!bt->vsum_abs) bt->vsum_abs = dalloc<double2>(nc, &e);
     if (e != cudaSuccess) return set_err(ctx, MCGPU_ERR_NOMEM, "NPT buffers: %s", cudaGetErrorString(e));
   }
   cudaStream_t st = ctx->stream;
@@ -1078,8 +1090,12 @@ extern "C" int mcgpu_batch_set_npt(mcgpu_batch* bt, int interval, const double* 
                             nc, cudaMemcpyHostToDevice, st));
   CK(ctx, cudaMemcpy2DAsync(&h->vol_interval, sizeof(ChainHdr), iv.data(), sizeof(int), sizeof(int),
                             nc, cudaMemcpyHostToDevice, st));
+  CK(ctx, cudaMemcpy2DAsync(&h->vol_mixed, sizeof(ChainHdr), vmx.data(), sizeof(int), sizeof(int),
+                            nc, cudaMemcpyHostToDevice, st));
   CK(ctx, cudaStreamSynchronize(st));
   bt->vol_interval = interval;
+  bt->vol_has64 = interval > 0 && !mixed;
+  bt->vol_has32 = mixed;
   batch_drop_graph(bt);
   return MCGPU_OK;
 }

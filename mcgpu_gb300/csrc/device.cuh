@@ -84,6 +84,8 @@ struct __align__(16) ChainHdr {
   int cell0, cell_cap, ncell[3];
   int nl_overflow;
   float nl_r2, nl_half2, nl_rlist, prad;
+  int vol_mixed;        // volume moves with FP32 pairs (FP64 re-take near threshold)
+  int vol_fp64;         // volume decisions re-taken with FP64 pairs
 };
 static_assert(sizeof(ChainHdr) % 16 == 0, "ChainHdr alignment");
 
@@ -124,7 +126,9 @@ struct NlCfg {
 struct VolMove {
   double L[3];
   double dlnv, u;
-  int state, pad;   // 0 not due, 1 evaluate, 2 rejected outright, 3 accepted
+  int state;   // 0 not due, 1 evaluate, 2 rejected outright, 3 accepted,
+               // 4 FP32 energies too close to the threshold: FP64 re-take
+  int fp64;    // decided on FP64 pair energies
 };
 
 // Molecules a volume phase covers: all of the pool (act == nullptr) or the

@@ -39,9 +39,9 @@ cudaError_t launch_mol_pair_sums(bool f64, int grid, int threads, SmemShape sh, 
                                  Pool P, const int* mol_chain, int m_begin, double* emol,
                                  long long* pairs);
 cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
-                                double2* emol2, double2* esum, mcgpu_vol_trace* trace,
-                                int trace_slot, int trace_stride, cudaStream_t st,
-                                MolRanges act = MolRanges());
+                                double2* emol2, double2* eabs2, double2* esum, double2* esum_abs,
+                                mcgpu_vol_trace* trace, int trace_slot, int trace_stride,
+                                cudaStream_t st, MolRanges act, bool has64, bool has32);
 
 }  // namespace mcgpu
 

@@ -492,7 +492,9 @@ __device__ inline void warp_eval(const Pool& P, const ChainHdr& H, const GroupSm
   for (int base = c_begin + w * 32; base < c_end; base += nw * 32) {
     const int j = base + lane;
     int f = 0;
-    if (j < c_end && j != mi.mol) f = F64 ? screen_f64(P, H, s, mi, j) : screen_mixed(P, H, s, mi, j);
+    // the FP32 screen with the FP64 re-test inside its guard band gives the
+    // FP64 test's in-range set exactly, for FP64 and FP32 pair terms alike
+    if (j < c_end && j != mi.mol) f = screen_mixed(P, H, s, mi, j);
     const unsigned bal = __ballot_sync(~0u, f != 0);
     if (f) rj[(tail + __popc(bal & lt)) & (kRing - 1)] = (j << 4) | f;
     tail += __popc(bal);

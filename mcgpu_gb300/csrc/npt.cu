@@ -16,11 +16,19 @@
 // isobaric ln V move instead.  The running energy is replaced by the FP64
 // total of the volume the chain keeps (a drift reset every interval).
 //
+// With vol_mixed the energies come from FP32 pair terms summed in
+// double-float (k_vol_pair_sums32) and the decision is taken on them unless
+// the criterion's argument lies within their rounding bound of ln u; those
+// chains alone are re-evaluated with FP64 pairs and decided on that, so the
+// decisions are the FP64 ones.
+//
 // Kernels (one volume phase, launched between step launches):
 //   k_vol_propose      per chain: due?, draw, L'
 //   k_vol_pair_sums    per molecule: E(m, j>m) at V and V' (FP64 pairs)
+//   k_vol_pair_sums32  the same with FP32 pairs (vol_mixed chains)
 //   k_vol_sums         per chain: ordered sums
-//   k_vol_decide       per chain: criterion, new box, energy
+//   k_vol_decide       per chain: criterion (or the FP64 re-take mark), new
+//                      box, energy
 //   k_vol_refresh      per molecule of an accepting chain: screen positions
 #include "chain.cuh"
 
@@ -52,7 +60,7 @@ __global__ void k_vol_propose(Pool P, VolMove* vm, MolRanges R, int n_items) {
   const ChainHdr& H = P.hdr[c];
   VolMove v;
   v.state = 0;
-  v.pad = 0;
+  v.fp64 = 0;
   v.dlnv = 0.0;
   v.u = 0.0;
   for (int k = 0; k < 3; k++) v.L[k] = H.L[k];
@@ -108,9 +116,16 @@ __device__ __forceinline__ int range_mol(const MolRanges& R, int m_begin, int b)
   return R.act_m0[lo] + (b - R.act_pref[lo]);
 }
 
+// Chains a pair-sum pass evaluates: pass 0 the due non-mixed chains, pass 1
+// the mixed chains marked for the FP64 re-take.
+__device__ __forceinline__ bool vol_take64(const VolMove& v, const ChainHdr& H, int pass) {
+  return pass == 0 ? (v.state == 1 && !H.vol_mixed) : v.state == 4;
+}
+
 __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int* mol_chain,
                                                                const VolMove* vm, int m_begin,
-                                                               MolRanges R, double2* emol2) {
+                                                               MolRanges R, double2* emol2,
+                                                               int pass) {
   __shared__ double sx[2][3][kMaxA];
   __shared__ double sq[3][kMaxA];
   __shared__ int spa[kMaxP];
@@ -118,11 +133,8 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
   const int m = range_mol(R, m_begin, blockIdx.x);
   const int c = mol_chain[m];
   const VolMove v = vm[c];
-  if (v.state != 1) {
-    if (threadIdx.x == 0) emol2[m] = make_double2(0.0, 0.0);
-    return;
-  }
   const ChainHdr& H = P.hdr[c];
+  if (!vol_take64(v, H, pass)) return;
   const double* Lv[2] = {H.L, v.L};
   const int a0 = P.mstart[m], len = P.mlen[m] & 255;
   const int2 pi = P.mpi[m];
@@ -196,53 +208,232 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
   if (threadIdx.x == 0) emol2[m] = red[0];
 }
 
-// Ordered per-chain sums of emol2 (one CTA per chain).
-__global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, double2* out,
-                           MolRanges R) {
-  __shared__ double2 red[256];
-  const int c = range_chain(R, blockIdx.x);
-  if (vm[c].state != 1) return;
-  const ChainHdr& H = P.hdr[c];
-  double2 acc = make_double2(0.0, 0.0);
-  for (int i = threadIdx.x; i < H.n_mol; i += blockDim.x) {
-    acc.x += emol2[H.mol0 + i].x;
-    acc.y += emol2[H.mol0 + i].y;
+// Box-derived FP32 scales of one of the two volumes of a move.
+struct VolBox {
+  float Lf[3], fxs[3], fxs_lo[3];
+  float cut2_lo, cut2_hi;
+  double L[3];
+};
+
+__device__ inline void volbox_set(VolBox& B, const double* L, double rc) {
+  double Lmax = 0;
+  for (int k = 0; k < 3; k++) {
+    B.L[k] = L[k];
+    B.Lf[k] = (float)L[k];
+    B.fxs[k] = (float)(L[k] / 4294967296.0);
+    B.fxs_lo[k] = (float)(L[k] / 4294967296.0 - (double)B.fxs[k]);
+    Lmax = fmax(Lmax, L[k]);
   }
-  red[threadIdx.x] = acc;
+  const double band = screen_band(rc, Lmax);
+  B.cut2_lo = (float)(rc * rc - band);
+  B.cut2_hi = (float)(rc * rc + band);
+}
+
+// Anchor difference b - a at box B as a double-float (fixdiff_ff's split).
+__device__ __forceinline__ void vol_fixdiff(uint4 b, uint4 a, const VolBox& B, float3& hi,
+                                            float3& lo) {
+  const int d[3] = {(int)(b.x - a.x), (int)(b.y - a.y), (int)(b.z - a.z)};
+  float h[3], l[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int dh = d[k] & ~0xFF;
+    const float fh = (float)dh, fl = (float)(d[k] - dh);
+    const float p = fh * B.fxs[k];
+    const float e = fmaf(fh, B.fxs[k], -p);
+    const float t = fmaf(fh, B.fxs_lo[k], fmaf(fl, B.fxs[k], e));
+    h[k] = p + t;
+    l[k] = t - (h[k] - p);
+  }
+  hi = make_float3(h[0], h[1], h[2]);
+  lo = make_float3(l[0], l[1], l[2]);
+}
+
+// E(m, j > m) at V (.x) and V' (.y) of a mixed chain's molecule m with FP32
+// pair terms (per-pair minimum image, the chain kernel's arithmetic) summed
+// in double-float; eabs2 gets the sums of the terms' magnitudes.  The
+// in-range test is the FP32 screen with the FP64 re-test inside its guard
+// band: the FP64 test's set exactly.
+__global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const int* mol_chain,
+                                                                 const VolMove* vm, int m_begin,
+                                                                 MolRanges R, double2* emol2,
+                                                                 double2* eabs2) {
+  __shared__ float4 so[kMaxA];
+  __shared__ float2 sq[kMaxA];
+  __shared__ int spa[kMaxP];
+  __shared__ VolBox vb[2];
+  __shared__ double2 red[kVolThreads];
+  __shared__ double2 rab[kVolThreads];
+  const int m = range_mol(R, m_begin, blockIdx.x);
+  const int c = mol_chain[m];
+  const VolMove v = vm[c];
+  const ChainHdr& H = P.hdr[c];
+  if (!(v.state == 1 && H.vol_mixed)) return;
+  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
+  const int2 pi = P.mpi[m];
+  const uint4 Am = P.mfix[m];
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    so[i] = P.aoff[a0 + i];
+    sq[i] = P.aeq[a0 + i];
+  }
+  for (int k = threadIdx.x; k < pi.y; k += blockDim.x) spa[k] = P.pidx[pi.x + k] - a0;
+  if (threadIdx.x == 0) volbox_set(vb[0], H.L, H.cutoff);
+  if (threadIdx.x == 1) volbox_set(vb[1], v.L, H.cutoff);
+  __syncthreads();
+  const double* Lv[2] = {H.L, v.L};
+  const float reach = H.cutoff + H.rad_max * 2.0 + 1e-2;
+  const float reach2 = reach * reach;
+  const float sf = (float)(v.L[0] / H.L[0]);
+  float eh[2] = {0.f, 0.f}, el[2] = {0.f, 0.f}, ab[2] = {0.f, 0.f};
+  for (int j = m + 1 + (int)threadIdx.x; j < H.mol0 + H.n_mol; j += blockDim.x) {
+    const uint4 Aj = P.mfix[j];
+    const float3 D0 = fixdiff(Aj, Am, H);
+    const float d2 = fmaf(D0.x, D0.x, fmaf(D0.y, D0.y, D0.z * D0.z));
+    if (d2 > reach2 && d2 * sf * sf > reach2) continue;
+    const int2 pj = P.mpi[j];
+    const int b0 = P.mstart[j], lenj = P.mlen[j] & 255;
+    for (int w = 0; w < 2; w++) {
+      const VolBox& B = vb[w];
+      float3 Dh, Dl;
+      vol_fixdiff(Aj, Am, B, Dh, Dl);
+      bool in = false;
+      for (int k2 = 0; k2 < pj.y && !in; k2++) {
+        const int p2 = P.pidx[pj.x + k2];
+        const float4 op = P.aoff[p2];
+        for (int k1 = 0; k1 < pi.y && !in; k1++) {
+          const float4 oa = so[spa[k1]];
+          const float dx = wrapf((Dh.x + op.x) - oa.x, B.Lf[0]);
+          const float dy = wrapf((Dh.y + op.y) - oa.y, B.Lf[1]);
+          const float dz = wrapf((Dh.z + op.z) - oa.z, B.Lf[2]);
+          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          if (r2 <= B.cut2_lo) {
+            in = true;
+          } else if (r2 <= B.cut2_hi) {
+            in = dist2_at(pos_at(Am, oa, Lv[w]), pos_at(Aj, op, Lv[w]), Lv[w]) <=
+                 __dmul_rn(H.cutoff, H.cutoff);
+          }
+        }
+      }
+      if (!in) continue;
+      float e = 0.f;
+      for (int bb = b0; bb < b0 + lenj; bb++) {
+        const float4 ob = P.aoff[bb];
+        const float2 qb = P.aeq[bb];
+        // b relative to m's anchor as a double-float: two-sum of D + o_b
+        const float bx = Dh.x + ob.x, by = Dh.y + ob.y, bz = Dh.z + ob.z;
+        const float lx = ((Dh.x - (bx - (bx - Dh.x))) + (ob.x - (bx - Dh.x))) + Dl.x;
+        const float ly = ((Dh.y - (by - (by - Dh.y))) + (ob.y - (by - Dh.y))) + Dl.y;
+        const float lz = ((Dh.z - (bz - (bz - Dh.z))) + (ob.z - (bz - Dh.z))) + Dl.z;
+        for (int i = 0; i < len; i++) {
+          const float4 a = so[i];
+          const float2 ea = sq[i];
+          const float dx = wrapf((bx - a.x) + lx, B.Lf[0]);
+          const float dy = wrapf((by - a.y) + ly, B.Lf[1]);
+          const float dz = wrapf((bz - a.z) + lz, B.Lf[2]);
+          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+          if (!(r2 > 0.f)) continue;
+          const float lj = lj32(rcp_nr(r2), a.w, ob.w, ea.x, qb.x);
+          const float cl = (ea.y * qb.y) * rsqrt_nr(r2);
+          e += lj + cl;
+          ab[w] += fabsf(lj) + fabsf(cl);
+        }
+      }
+      ff_add(eh[w], el[w], e);
+    }
+  }
+  red[threadIdx.x] = make_double2((double)eh[0] + (double)el[0], (double)eh[1] + (double)el[1]);
+  rab[threadIdx.x] = make_double2((double)ab[0], (double)ab[1]);
   __syncthreads();
   for (int off = blockDim.x >> 1; off > 0; off >>= 1) {
     if ((int)threadIdx.x < off) {
       red[threadIdx.x].x += red[threadIdx.x + off].x;
       red[threadIdx.x].y += red[threadIdx.x + off].y;
+      rab[threadIdx.x].x += rab[threadIdx.x + off].x;
+      rab[threadIdx.x].y += rab[threadIdx.x + off].y;
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[c] = red[0];
+  if (threadIdx.x == 0) {
+    emol2[m] = red[0];
+    eabs2[m] = rab[0];
+  }
+}
+
+// Ordered per-chain sums of emol2 (and, for FP32 energies, of the term
+// magnitudes eabs2) for the chains in state `want`.
+__global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, const double2* eabs2,
+                           double2* out, double2* out_abs, MolRanges R, int want) {
+  __shared__ double2 red[256];
+  __shared__ double2 rab[256];
+  const int c = range_chain(R, blockIdx.x);
+  if (vm[c].state != want) return;
+  const ChainHdr& H = P.hdr[c];
+  const bool mixed = want == 1 && H.vol_mixed;
+  double2 acc = make_double2(0.0, 0.0), ab = make_double2(0.0, 0.0);
+  for (int i = threadIdx.x; i < H.n_mol; i += blockDim.x) {
+    acc.x += emol2[H.mol0 + i].x;
+    acc.y += emol2[H.mol0 + i].y;
+    if (mixed) {
+      ab.x += eabs2[H.mol0 + i].x;
+      ab.y += eabs2[H.mol0 + i].y;
+    }
+  }
+  red[threadIdx.x] = acc;
+  rab[threadIdx.x] = ab;
+  __syncthreads();
+  for (int off = blockDim.x >> 1; off > 0; off >>= 1) {
+    if ((int)threadIdx.x < off) {
+      red[threadIdx.x].x += red[threadIdx.x + off].x;
+      red[threadIdx.x].y += red[threadIdx.x + off].y;
+      rab[threadIdx.x].x += rab[threadIdx.x + off].x;
+      rab[threadIdx.x].y += rab[threadIdx.x + off].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    out[c] = red[0];
+    out_abs[c] = mixed ? rab[0] : make_double2(0.0, 0.0);
+  }
 }
 
 // The isobaric criterion; an accepted move installs the new box.
-__global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, mcgpu_vol_trace* trace,
-                             int trace_slot, int trace_stride, MolRanges R, int n_items) {
+// Pass 0 decides the due chains (a mixed chain whose FP32 argument lies
+// within its rounding bound of ln u is marked state 4 instead); pass 1
+// decides the marked chains on their FP64 energies.
+__global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const double2* eabs,
+                             mcgpu_vol_trace* trace, int trace_slot, int trace_stride,
+                             MolRanges R, int n_items, int pass) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_items) return;
   const int c = range_chain(R, i);
   VolMove v = vm[c];
-  if (v.state == 0) return;
+  if (pass == 0 ? (v.state != 1 && v.state != 2) : v.state != 4) return;
   ChainHdr& H = P.hdr[c];
-  H.vol_tried++;
-  H.vol_step = (long long)H.step;
   double e_old = H.energy, e_new = 0.0;
   int ok = 0;
-  if (v.state == 1) {
+  if (v.state == 1 || v.state == 4) {
     e_old = esum[c].x;
     e_new = esum[c].y;
     const double vo = H.L[0] * H.L[1] * H.L[2];
     const double vn = v.L[0] * v.L[1] * v.L[2];
     const double arg = -((e_new - e_old) + H.pressure * (vn - vo)) / H.kT +
                        (double)(H.n_mol + 1) * v.dlnv;
+    if (v.state == 1 && H.vol_mixed) {
+      // FP32 pair terms: |error of dU| <= kTieRel * sum of term magnitudes
+      const double bound =
+          (kTieRel * (eabs[c].x + eabs[c].y) + 1e-12 * (fabs(e_old) + fabs(e_new))) / H.kT;
+      if (fabs(arg - log(v.u)) <= bound + 1e-12) {
+        v.state = 4;
+        v.fp64 = 1;
+        vm[c] = v;
+        return;
+      }
+    }
     ok = (arg >= 0.0) || (exp(arg) >= v.u);
     H.energy = ok ? e_new : e_old;
   }
+  H.vol_tried++;
+  H.vol_step = (long long)H.step;
+  if (v.fp64) H.vol_fp64++;
   if (ok) {
     hdr_set_box(H, v.L);
     H.vol_accepted++;
@@ -260,6 +451,8 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, mcgpu_vol
     t.dlnv = v.dlnv;
     t.u = v.u;
     t.edge = H.L[0];
+    t.fp64 = v.fp64;
+    t.pad0 = 0;
     trace[(size_t)c * trace_stride + trace_slot] = t;
   }
 }
@@ -281,26 +474,47 @@ __global__ void k_vol_refresh(Pool P, const int* mol_chain, const VolMove* vm, i
   }
 }
 
-// One volume phase on stream st (buffers sized for the pool).
+// One volume phase on stream st (buffers sized for the pool).  has64 /
+// has32: some due chain uses FP64 / FP32 pair energies (the other pair
+// kernel is skipped).  With active ranges the work items are the ranges'
+// molecules, numbered from 0; otherwise all pool molecules in chunks.
 cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
-                                double2* emol2, double2* esum, mcgpu_vol_trace* trace,
-                                int trace_slot, int trace_stride, cudaStream_t st, MolRanges act) {
+                                double2* emol2, double2* eabs2, double2* esum, double2* esum_abs,
+                                mcgpu_vol_trace* trace, int trace_slot, int trace_stride,
+                                cudaStream_t st, MolRanges act, bool has64, bool has32) {
   const int nc = act.act_slot ? act.n_act : P.n_chains;
   if (nc == 0) return cudaSuccess;
   k_vol_propose<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, act, nc);
   const int items = act.act_pref ? act.total : n_mol_total;
-  if (act.act_pref) {
-    if (items > 0) k_vol_pair_sums<<<items, kVolThreads, 0, st>>>(P, mol_chain, vm, 0, act, emol2);
-  } else {
-    const int chunk = 1 << 20;
-    for (int m0 = 0; m0 < n_mol_total; m0 += chunk) {
-      const int n = n_mol_total - m0 < chunk ? n_mol_total - m0 : chunk;
-      k_vol_pair_sums<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2);
+  auto pairs = [&](bool f64, int pass) {
+    if (items <= 0) return;
+    if (act.act_pref) {
+      if (f64)
+        k_vol_pair_sums<<<items, kVolThreads, 0, st>>>(P, mol_chain, vm, 0, act, emol2, pass);
+      else
+        k_vol_pair_sums32<<<items, kVolThreads, 0, st>>>(P, mol_chain, vm, 0, act, emol2, eabs2);
+      return;
     }
+    const int chunk = 1 << 20;
+    for (int m0 = 0; m0 < items; m0 += chunk) {
+      const int n = items - m0 < chunk ? items - m0 : chunk;
+      if (f64)
+        k_vol_pair_sums<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2, pass);
+      else
+        k_vol_pair_sums32<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2, eabs2);
+    }
+  };
+  if (has64) pairs(true, 0);
+  if (has32) pairs(false, 0);
+  k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 1);
+  k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, trace, trace_slot,
+                                                trace_stride, act, nc, 0);
+  if (has32) {
+    pairs(true, 1);
+    k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 4);
+    k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, trace, trace_slot,
+                                                  trace_stride, act, nc, 1);
   }
-  k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, esum, act);
-  k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, trace, trace_slot, trace_stride, act,
-                                                nc);
   if (items > 0) k_vol_refresh<<<(items + 127) / 128, 128, 0, st>>>(P, mol_chain, vm, items, act);
   return cudaGetLastError();
 }

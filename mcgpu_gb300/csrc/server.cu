@@ -71,7 +71,7 @@ struct Job {
   int64_t id = 0;
   HostPool hp;  // the job's rows as chain 0 at offset 0
   int64_t n_steps = 0;
-  int npt = 0;
+  int npt = 0, vol_mixed = 0;
   double pressure = 0, max_dlnv = 0;
   double *x_out = nullptr, *y_out = nullptr, *z_out = nullptr;
   double t_submit = 0, t_admit = 0;
@@ -106,7 +106,9 @@ struct mcgpu_server {
   int* dlist = nullptr;  // order [slots] | act_slot [slots] | act_m0 [slots] | act_pref [slots+1]
   VolMove* vm = nullptr;
   double2* emol2 = nullptr;
+  double2* eabs2 = nullptr;
   double2* vsum = nullptr;
+  double2* vsum_abs = nullptr;
   // pinned host buffers
   ChainHdr* hmirror = nullptr;
   int* hlist = nullptr;
@@ -153,7 +155,9 @@ int server_alloc(mcgpu_server* s) {
   s->dlist = dalloc<int>(4 * (size_t)nc + 1, &e);
   s->vm = dalloc<VolMove>(nc, &e);
   s->emol2 = dalloc<double2>(nm, &e);
+  s->eabs2 = dalloc<double2>(nm, &e);
   s->vsum = dalloc<double2>(nc, &e);
+  s->vsum_abs = dalloc<double2>(nc, &e);
   if (e == cudaSuccess) e = cudaMemsetAsync(P.hdr, 0, sizeof(ChainHdr) * nc, ctx->stream);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&s->hmirror, sizeof(ChainHdr) * nc);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&s->hlist, sizeof(int) * (4 * (size_t)nc + 1));
@@ -165,7 +169,7 @@ int server_alloc(mcgpu_server* s) {
 
 void server_free(mcgpu_server* s) {
   s->pool.release();
-  void* d[] = {s->qctr, s->dlist, s->vm, s->emol2, s->vsum};
+  void* d[] = {s->qctr, s->dlist, s->vm, s->emol2, s->eabs2, s->vsum, s->vsum_abs};
   for (void* p : d)
     if (p) cudaFree(p);
   if (s->hmirror) cudaFreeHost(s->hmirror);
@@ -241,6 +245,7 @@ int upload_job(mcgpu_server* s, Job* j) {
   h.vol_interval = j->npt ? s->cfg.round_steps : 0;
   h.pressure = j->pressure;
   h.max_dlnv = j->max_dlnv;
+  h.vol_mixed = j->vol_mixed;
   Pool& P = s->pool.P;
   int rc = MCGPU_OK;
 #define SC(dst, vec) \
@@ -376,10 +381,13 @@ int launch_round(mcgpu_server* s) {
   int* am0 = s->hlist + 2 * nc;
   int* apref = s->hlist + 3 * nc;
   int n_npt = 0, total = 0;
+  bool has64 = false, has32 = false;
   for (size_t i = 0; i < act.size(); i++) {
     order[i] = act[i];
     const Job* j = s->slot_job[act[i]];
     if (!j->npt) continue;
+    has64 = has64 || !j->vol_mixed;
+    has32 = has32 || j->vol_mixed;
     aslot[n_npt] = act[i];
     am0[n_npt] = (int)j->m0;
     apref[n_npt] = total;
@@ -407,8 +415,8 @@ int launch_round(mcgpu_server* s) {
     R.act_pref = s->dlist + 3 * nc;
     R.n_act = n_npt;
     R.total = total;
-    CK(ctx, launch_volume_phase(s->pool.P, s->pool.mol_chain, 0, s->vm, s->emol2, s->vsum, nullptr,
-                                0, 0, st, R));
+    CK(ctx, launch_volume_phase(s->pool.P, s->pool.mol_chain, 0, s->vm, s->emol2, s->eabs2,
+                                s->vsum, s->vsum_abs, nullptr, 0, 0, st, R, has64, has32));
   }
   CK(ctx, cudaMemcpyAsync(s->hmirror, s->pool.P.hdr, sizeof(ChainHdr) * nc, cudaMemcpyDeviceToHost, st));
   CK(ctx, cudaEventRecord(s->ev_round, st));
@@ -499,6 +507,8 @@ extern "C" int mcgpu_server_submit(mcgpu_server* s, const mcgpu_job_desc* jd, in
   if (jd->n_steps <= 0) return set_err(ctx, MCGPU_ERR_INVALID, "job step count %lld must be > 0",
                                        (long long)jd->n_steps);
   if (jd->npt) {
+    if (jd->vol_precision != MCGPU_PREC_FP64 && jd->vol_precision != MCGPU_PREC_MIXED)
+      return set_err(ctx, MCGPU_ERR_INVALID, "unknown volume-move precision %d", jd->vol_precision);
     if (!std::isfinite(jd->pressure_atm) || jd->pressure_atm < 0)
       return set_err(ctx, MCGPU_ERR_INVALID, "job pressure %g atm", jd->pressure_atm);
     if (!(jd->max_dlnv > 0 && jd->max_dlnv <= 0.1))
@@ -530,6 +540,7 @@ extern "C" int mcgpu_server_submit(mcgpu_server* s, const mcgpu_job_desc* jd, in
   j->npt = jd->npt ? 1 : 0;
   j->pressure = jd->npt ? jd->pressure_atm * kAtmKcal : 0.0;
   j->max_dlnv = jd->npt ? jd->max_dlnv : 0.0;
+  j->vol_mixed = (jd->npt && jd->vol_precision == MCGPU_PREC_MIXED) ? 1 : 0;
   j->x_out = jd->x_out;
   j->y_out = jd->y_out;
   j->z_out = jd->z_out;

@@ -70,7 +70,7 @@ class JobServer:
 
     def submit(self, box: BoxData, seed: int, n_steps: int, chain_id: int = 0,
                npt: bool = False, pressure_atm: float = 1.0, max_dlnv: float = 0.01,
-               want_coords: bool = True) -> int:
+               want_coords: bool = True, vol_precision: int = _abi.PREC_FP64) -> int:
         b = box.copy().normalise()
         d = b.desc()
         jd = _abi.JobDesc()
@@ -78,6 +78,7 @@ class JobServer:
         jd.seed = int(seed) & (2 ** 64 - 1)
         jd.chain_id = int(chain_id)
         jd.npt = 1 if npt else 0
+        jd.vol_precision = int(vol_precision)
         jd.n_steps = int(n_steps)
         jd.pressure_atm = float(pressure_atm)
         jd.max_dlnv = float(max_dlnv)

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from helpers import load_golden
-from mcgpu_gb300 import JobServer, MCGPUError, ROT_AXIS
+from mcgpu_gb300 import PREC_FP64, PREC_MIXED, JobServer, MCGPUError, ROT_AXIS
 from mcgpu_gb300 import workloads as W
 from oracle.pyoracle import OracleChain
 
@@ -30,7 +30,8 @@ def mixed_jobs(n, seed):
     rng = np.random.default_rng(seed)
     for i, (b, s) in enumerate(zip(boxes, seeds)):
         jobs.append(dict(box=b, seed=int(s), n_steps=int(rng.integers(1, 6)) * 50,
-                         chain_id=i, npt=bool(i % 2), pressure_atm=1.0, max_dlnv=0.02))
+                         chain_id=i, npt=bool(i % 2), pressure_atm=1.0, max_dlnv=0.02,
+                         vol_precision=PREC_MIXED if i % 4 == 1 else PREC_FP64))
     bic = load_golden("bicyclic100")[0]
     jobs.insert(3, dict(box=bic, seed=4242, n_steps=150, chain_id=77, npt=True,
                         pressure_atm=1.0, max_dlnv=0.02))
