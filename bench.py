@@ -222,6 +222,157 @@ def bench_plain(ctx, n_steps: int = 2000) -> dict:
     return out
 
 
+# ---- single chain (4000 x 16-atom bicyclic) and large system (32768 waters) ----------
+
+def timed_chain(g, seed: int, n_steps: int):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st, _ = g.chain_run(seed=seed, n_steps=n_steps)
+    torch.cuda.synchronize()
+    return n_steps / (time.perf_counter() - t0), st
+
+
+def bench_single(ctx, plain_steps: int = 150, chain_steps: int = 4000) -> dict:
+    """4000 rigid 16-atom bicyclic molecules, L = 86.1 A, rc 12 A, 298 K,
+    +-0.2 A / +-10 deg: the plain GPU drop-in (host loop over the
+    SimulationStep contract, FP64 and FP32 pairs) against the device-resident
+    chain (FP32 pairs, FP64 sums, on-device RNG and accept), with and without
+    the Verlet list (skin 1.5 A)."""
+    import mcgpu_gb300 as M
+    box = M.bicyclic_box(4000, L=86.1, seed=4000, atom_dmin=2.5)
+    out = {"workload": "4000 x 16-atom bicyclic, L=86.1 A, rc 12 A, NVT 298 K, single chain"}
+    for name, prec in (("plain_fp64", M.PREC_FP64), ("plain_mixed", M.PREC_MIXED)):
+        g = M.GpuBox(ctx, box, prec)
+        step = M.GpuSimulationStep(g, M.LibcRand(7))
+        M.run_plain(step, 10, fused=True)
+        t0 = time.perf_counter()
+        M.run_plain(step, plain_steps, fused=True)
+        out[name] = plain_steps / (time.perf_counter() - t0)
+        g.close()
+    for name, skin in (("chain_full_scan", 0.0), ("chain_verlet", 1.5)):
+        g = M.GpuBox(ctx, box, M.PREC_MIXED)
+        if skin > 0:
+            g.set_verlet(skin)
+        g.chain_run(seed=11, n_steps=64)
+        out[name], st = timed_chain(g, 11, chain_steps)
+        out[name + "_fp64_retakes"] = st.ties
+        g.close()
+    out["chain_over_plain_fp64"] = out["chain_verlet"] / out["plain_fp64"]
+    out["unit"] = "moves/s"
+    return out
+
+
+def bench_large(ctx, steps: int = 6000) -> dict:
+    """32768 waters (98,304 atoms), L = 99.3 A, rc 12 A, NPT 298 K and
+    1 atm, Verlet list (skin 1.5 A) rebuilt on the skin/2 trigger, a volume
+    move every 500 steps (FP32 pair energies, FP64 re-take near the
+    threshold), then a full FP64 recompute for the drift of the running
+    energy.  Beside it the plain FP64 drop-in for a few steps."""
+    import torch
+    import mcgpu_gb300 as M
+    box = M.water_box(32768, L=99.3, cutoff=12.0, temperature=298.0, seed=32768)
+    out = {"workload": "32768 waters, L=99.3 A, rc 12 A, NPT 298 K / 1 atm, Verlet skin 1.5 A, "
+                       "volume move every 500 steps"}
+    bt = M.ChainBatch(ctx, [box], [0x5EED], rotation=M.ROT_AXIS)
+    bt.set_tile(256, 1, 64)
+    bt.set_verlet(1.5)
+    bt.set_npt(500, 1.0, 0.005, M.PREC_MIXED)
+    bt.run(500)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bt.run(steps)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    st = bt.stats()[0]
+    full = float(bt.system_energies()[0])
+    out.update({"chain_verlet_npt": steps / dt, "unit": "moves/s",
+                "energy_running": st.energy, "energy_fp64_recompute": full,
+                "drift_rel": abs(st.energy - full) / abs(full),
+                "volume_moves": st.vol_tried, "volume_accepted": st.vol_accepted,
+                "edge_A": st.box[0], "density_mol_per_A3": box.n_mol / st.box[0] ** 3,
+                "nl_builds": st.nl_builds, "nl_full_scan_steps": st.nl_full_scans,
+                "fp64_retakes": st.ties, "steps": steps + 500})
+    bt.close()
+    g = M.GpuBox(ctx, box, M.PREC_FP64)
+    step = M.GpuSimulationStep(g, M.LibcRand(3))
+    M.run_plain(step, 5, fused=True)
+    t0 = time.perf_counter()
+    M.run_plain(step, 60, fused=True)
+    out["plain_fp64"] = 60 / (time.perf_counter() - t0)
+    g.close()
+    return out
+
+
+# ---- served request loop ---------------------------------------------------------------
+
+def bench_served(ctx, rate: float = 200.0, window_s: float = 4.0, steps_per_job: int = 20000,
+                 pool_each: int = 12, seed: int = 77) -> dict:
+    """Jobs arrive as a Poisson stream (rate jobs/s over window_s seconds),
+    50/50 water and 16-atom bicyclic, N log-uniform in [128, 8192], NPT at
+    1 atm with T uniform in [280, 360] K, a ln V move (+-0.01) every 100
+    steps, steps_per_job steps each; admitted against a 120 GB budget and
+    advanced by the server's rounds.  Boxes come from a pre-built pool
+    (pool_each per species) with per-job temperature and Philox key."""
+    import numpy as np
+    import mcgpu_gb300 as M
+    rng = np.random.default_rng(seed)
+    pool = []
+    for k in range(pool_each):
+        n = int(round(math.exp(rng.uniform(math.log(128), math.log(8192)))))
+        pool.append(M.water_box(n, cutoff=9.0, seed=1000 + k))
+        n = int(round(math.exp(rng.uniform(math.log(128), math.log(8192)))))
+        pool.append(M.bicyclic_box(n, seed=2000 + k, atom_dmin=2.5))
+    for b in pool:
+        b.cutoff = min(b.cutoff, 0.5 * float(b.size[0]))
+    arrivals = []
+    t = 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > window_s:
+            break
+        arrivals.append(t)
+    srv = M.JobServer(ctx, hbm_budget_bytes=120 << 30, max_slots=512, round_steps=100,
+                      max_mol_atoms=16, max_atoms=24_000_000, max_molecules=4_000_000)
+    jobs = []
+    for i, ta in enumerate(arrivals):
+        b = pool[int(rng.integers(len(pool)))].copy()
+        b.temperature = float(rng.uniform(280.0, 360.0))
+        jobs.append((ta, b, int(rng.integers(1, 2 ** 63)), i))
+    done = {}
+    t0 = srv.clock()
+    nxt = 0
+    while len(done) < len(jobs):
+        now = srv.clock() - t0
+        while nxt < len(jobs) and jobs[nxt][0] <= now:
+            ta, b, sd, i = jobs[nxt]
+            srv.submit(b, sd, steps_per_job, chain_id=i, npt=True, pressure_atm=1.0,
+                       max_dlnv=0.01, want_coords=False, vol_precision=M.PREC_MIXED)
+            nxt += 1
+        st = srv.status()
+        if st["running"] == 0 and st["queued"] == 0 and nxt < len(jobs):
+            time.sleep(max(0.0, jobs[nxt][0] - (srv.clock() - t0)))
+            continue
+        srv.step()
+        done.update(srv.results())
+    lat = sorted(r.result.t_done - r.result.t_submit for r in done.values())
+    t_first = min(r.result.t_submit for r in done.values())
+    t_last = max(r.result.t_done for r in done.values())
+    moves = sum(r.result.steps for r in done.values())
+    errors = sum(1 for r in done.values() if r.result.error)
+    ties = sum(r.result.ties for r in done.values())
+    srv.close()
+    pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]
+    return {"workload": f"Poisson {rate:.0f} jobs/s for {window_s:.0f} s ({len(jobs)} jobs), 50/50 "
+                        "water / 16-atom bicyclic, N log-uniform [128, 8192], NPT 1 atm, "
+                        f"T U[280,360] K, ln V move every 100 steps, {steps_per_job} steps/job",
+            "jobs": len(jobs), "moves_per_s": moves / (t_last - t_first), "unit": "moves/s",
+            "p50_s": pct(0.50), "p99_s": pct(0.99), "max_s": lat[-1],
+            "makespan_s": t_last - t_first, "errors": errors, "fp64_retakes": ties,
+            "note": f"boxes from a pool of {2 * pool_each} pre-built configurations; "
+                    "volume-move energies FP32 pairs with FP64 re-take near the threshold"}
+
+
 # ---- batched ------------------------------------------------------------------------
 
 def main():
@@ -233,6 +384,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-single", action="store_true", help="skip the 4000 x 16-atom chain")
+    ap.add_argument("--no-large", action="store_true", help="skip the 32768-water system")
+    ap.add_argument("--no-served", action="store_true", help="skip the served request loop")
+    ap.add_argument("--served-window", type=float, default=4.0)
+    ap.add_argument("--served-steps", type=int, default=20000)
     ap.add_argument("--tile", default=None,
                     help="threads,chains_per_cta,steps_per_launch,lanes (skips the autotuner)")
     args = ap.parse_args()
@@ -328,6 +484,13 @@ def main():
     plain = None
     if rank == 0 and not args.no_plain:
         plain = bench_plain(ctx)
+    single = large = served = None
+    if rank == 0 and not args.no_single:
+        single = bench_single(ctx)
+    if rank == 0 and not args.no_large:
+        large = bench_large(ctx)
+    if rank == 0 and not args.no_served:
+        served = bench_served(ctx, window_s=args.served_window, steps_per_job=args.served_steps)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(boxes, seeds)
@@ -361,6 +524,11 @@ def main():
         "e2e": e2e,
         "plain_1chain": plain,
         "batched_over_plain": (value / plain["fp64"]["moves_per_s"]) if plain else None,
+        "served": served,
+        "served_over_plain": (served["moves_per_s"] / plain["fp64"]["moves_per_s"])
+                             if (served and plain) else None,
+        "single_chain": single,
+        "large_system": large,
         "cpu_baseline": cpu,
         "wall_s_timed": wall,
     }
