@@ -238,9 +238,12 @@ def bench_single(ctx, plain_steps: int = 150, chain_steps: int = 4000) -> dict:
     +-0.2 A / +-10 deg: the plain GPU drop-in (host loop over the
     SimulationStep contract, FP64 and FP32 pairs) against the device-resident
     chain (FP32 pairs, FP64 sums, on-device RNG and accept), with and without
-    the Verlet list (skin 1.5 A)."""
+    the Verlet list (skin 1.5 A).  Start: FCC lattice (10^3 cells hold the
+    4000 centres exactly), one common orientation, as the reference builds
+    its boxes; random centres at this density put atoms of neighbours on top
+    of each other (energies ~1e19 kcal/mol)."""
     import mcgpu_gb300 as M
-    box = M.bicyclic_box(4000, L=86.1, seed=4000, atom_dmin=2.5)
+    box = M.bicyclic_box(4000, L=86.1, seed=4000, lattice=True)
     out = {"workload": "4000 x 16-atom bicyclic, L=86.1 A, rc 12 A, NVT 298 K, single chain"}
     for name, prec in (("plain_fp64", M.PREC_FP64), ("plain_mixed", M.PREC_MIXED)):
         g = M.GpuBox(ctx, box, prec)
@@ -313,7 +316,8 @@ def bench_served(ctx, rate: float = 200.0, window_s: float = 4.0, steps_per_job:
     1 atm with T uniform in [280, 360] K, a ln V move (+-0.01) every 100
     steps, steps_per_job steps each; admitted against a 120 GB budget and
     advanced by the server's rounds.  Boxes come from a pre-built pool
-    (pool_each per species) with per-job temperature and Philox key."""
+    (pool_each per species; water from random centres, the 16-atom molecule
+    on an FCC lattice) with per-job temperature and Philox key."""
     import numpy as np
     import mcgpu_gb300 as M
     rng = np.random.default_rng(seed)
@@ -322,7 +326,7 @@ def bench_served(ctx, rate: float = 200.0, window_s: float = 4.0, steps_per_job:
         n = int(round(math.exp(rng.uniform(math.log(128), math.log(8192)))))
         pool.append(M.water_box(n, cutoff=9.0, seed=1000 + k))
         n = int(round(math.exp(rng.uniform(math.log(128), math.log(8192)))))
-        pool.append(M.bicyclic_box(n, seed=2000 + k, atom_dmin=2.5))
+        pool.append(M.bicyclic_box(n, seed=2000 + k, lattice=True))
     for b in pool:
         b.cutoff = min(b.cutoff, 0.5 * float(b.size[0]))
     arrivals = []

@@ -195,6 +195,52 @@ def rsa_centres(seed: int, n: int, L: float, dmin: float) -> np.ndarray:
     return out
 
 
+def fcc_centres(seed: int, n: int, L: float) -> np.ndarray:
+    """n sites of a face-centred cubic lattice filling the cubic box: the
+    smallest k with 4 k^3 >= n cells per edge, lattice constant L / k, a
+    seeded random choice of n of the 4 k^3 sites (all of them when they
+    match, e.g. 4000 molecules at k = 10).  The reference builds its boxes
+    on such a lattice (FileUtilities.cpp:550-642)."""
+    k = 1
+    while 4 * k ** 3 < n:
+        k += 1
+    a = L / k
+    base = np.array([[0, 0, 0], [0.5, 0.5, 0], [0.5, 0, 0.5], [0, 0.5, 0.5]])
+    cells = np.array([(i, j, l) for i in range(k) for j in range(k) for l in range(k)], float)
+    sites = ((cells[:, None, :] + base[None]) * a + 0.25 * a).reshape(-1, 3)
+    if sites.shape[0] > n:
+        pick = np.sort(np.random.default_rng(seed).choice(sites.shape[0], n, replace=False))
+        sites = sites[pick]
+    return sites
+
+
+def aligned_rotation(xyz: np.ndarray, a: float, seed: int, tries: int = 4096) -> np.ndarray:
+    """One orientation for every molecule of an FCC lattice of constant a:
+    among `tries` seeded uniform rotations, the one with the largest closest
+    approach between a molecule's atoms and those of its 12 nearest lattice
+    neighbours (farther shells are at least a apart)."""
+    nb = []
+    for v in ((0.5, 0.5, 0.0), (0.5, 0.0, 0.5), (0.0, 0.5, 0.5)):
+        idx = [i for i in range(3) if v[i]]
+        for s1 in (1.0, -1.0):
+            for s2 in (1.0, -1.0):
+                w = np.array(v) * a
+                w[idx[0]] *= s1
+                w[idx[1]] *= s2
+                nb.append(w)
+    nb = np.array(nb)
+    R = random_rotations(np.random.default_rng(seed), tries)
+    best, best_R = -1.0, R[0]
+    for c in range(0, tries, 256):
+        p = np.einsum("rij,aj->rai", R[c:c + 256], xyz)           # (r, atoms, 3)
+        d = p[:, None, :, None, :] + nb[None, :, None, None, :] - p[:, None, None, :, :]
+        m = np.sqrt(np.einsum("rnabk,rnabk->rnab", d, d)).min(axis=(1, 2, 3))
+        k = int(np.argmax(m))
+        if m[k] > best:
+            best, best_R = float(m[k]), R[c + k]
+    return best_R
+
+
 def _close_atom_pairs(pos: np.ndarray, check: np.ndarray, L: float, dmin: float):
     """Molecule pairs (i, j), i in `check`, with an atom pair of different
     molecules closer than dmin (minimum image); pos is (n_mol, a, 3)."""
@@ -237,18 +283,27 @@ def _place(xyz, R, centres):
 
 def build_box(template, n_mol: int, L: float, cutoff: float, temperature: float,
               max_translate: float, max_rotate: float, seed: int, dmin: float,
-              name: str = "", atom_dmin: float = 0.0, overlap_rounds: int = 200) -> BoxData:
+              name: str = "", atom_dmin: float = 0.0, overlap_rounds: int = 200,
+              lattice: bool = False) -> BoxData:
     """Places n_mol copies of a rigid template: centres by random sequential
-    addition at minimum separation dmin, orientations uniform on SO(3).  With
-    atom_dmin > 0, molecules with an atom closer than atom_dmin to another
-    molecule's atom are re-oriented (and after repeated failures re-centred)
-    for up to overlap_rounds rounds; at liquid density some overlaps may
-    remain, as in the reference's own lattice starts."""
+    addition at minimum separation dmin and orientations uniform on SO(3),
+    or (lattice=True) centres on an FCC lattice all in one orientation, the
+    one keeping neighbouring molecules' atoms farthest apart.  With atom_dmin > 0, molecules with an atom closer than
+    atom_dmin to another molecule's atom are re-oriented (and, off the
+    lattice, re-centred after repeated failures) for up to overlap_rounds
+    rounds; at liquid density some overlaps may remain, as in the
+    reference's own lattice starts."""
     xyz, sig, eps, q, prim = template
     a = xyz.shape[0]
     rng = np.random.default_rng(seed)
-    centres = rsa_centres(seed, n_mol, L, dmin)
-    R = random_rotations(rng, n_mol)
+    centres = fcc_centres(seed, n_mol, L) if lattice else rsa_centres(seed, n_mol, L, dmin)
+    if lattice:
+        k = 1
+        while 4 * k ** 3 < n_mol:
+            k += 1
+        R = np.broadcast_to(aligned_rotation(xyz, L / k, seed), (n_mol, 3, 3)).copy()
+    else:
+        R = random_rotations(rng, n_mol)
     # pos[m, i, :] = R[m] @ xyz[i] + centre[m], elementwise (same bits on every host)
     pos = _place(xyz, R, centres)
     if atom_dmin > 0 and n_mol > 1:
@@ -261,7 +316,7 @@ def build_box(template, n_mol: int, L: float, cutoff: float, temperature: float,
             bad = np.unique(np.maximum(i, j))
             tries[bad] += 1
             R[bad] = random_rotations(rng, bad.size)
-            recentre = bad[tries[bad] % 8 == 0]
+            recentre = bad[tries[bad] % 8 == 0] if not lattice else bad[:0]
             if recentre.size:
                 centres[recentre] = rng.random((recentre.size, 3)) * L
             pos[bad] = _place(xyz, R[bad], centres[bad])
@@ -291,7 +346,8 @@ def water_box(n_mol: int = 256, L: float | None = None, cutoff: float = 9.0,
 
 def bicyclic_box(n_mol: int = 4000, L: float | None = None, cutoff: float = 12.0,
                  temperature: float = 298.0, max_translate: float = 0.2, max_rotate: float = 10.0,
-                 seed: int = 4000, dmin: float = 4.0, atom_dmin: float = 0.0) -> BoxData:
+                 seed: int = 4000, dmin: float = 4.0, atom_dmin: float = 0.0,
+                 lattice: bool = False) -> BoxData:
     """The 16-atom bicyclic liquid: random centres at a 4 A minimum centre
     distance, random orientations.  At this density ring atoms of
     neighbouring molecules overlap in the start (as in the reference's own
@@ -300,7 +356,8 @@ def bicyclic_box(n_mol: int = 4000, L: float | None = None, cutoff: float = 12.0
     if L is None:
         L = (n_mol / BICYCLIC_DENSITY) ** (1.0 / 3.0)
     return build_box(bicyclic_template(), n_mol, L, cutoff, temperature, max_translate,
-                     max_rotate, seed, dmin, name=f"bicyclic{n_mol}", atom_dmin=atom_dmin)
+                     max_rotate, seed, dmin, name=f"bicyclic{n_mol}", atom_dmin=atom_dmin,
+                     lattice=lattice)
 
 
 def water_chains(n_chains: int = 512, n_min: int = 64, n_max: int = 2048, seed: int = 2024,

@@ -50,3 +50,20 @@ def test_generators_are_seeded():
     a, b = W.water_box(100, seed=5), W.water_box(100, seed=5)
     assert np.array_equal(a.x, b.x)
     assert not np.array_equal(a.x, W.water_box(100, seed=6).x)
+
+
+def test_fcc_lattice_start():
+    """FCC centres: 4000 molecules fill 10^3 cells exactly at L = 86.1 A,
+    nearest centres a/sqrt(2) apart; one common orientation keeps the 16-atom
+    molecules' atoms apart, so the start energy is finite and small."""
+    from oracle.pyoracle import OracleBox
+    c = W.fcc_centres(1, 4000, 86.1)
+    assert c.shape == (4000, 3)
+    d = c[:200, None, :] - c[None, :, :]
+    d -= 86.1 * np.rint(d / 86.1)
+    r = np.sqrt((d ** 2).sum(-1))
+    r[np.arange(200), np.arange(200)] = np.inf
+    assert abs(r.min() - 8.61 / np.sqrt(2)) < 1e-9
+    box = W.bicyclic_box(500, seed=3, lattice=True)
+    e = OracleBox(box).system_energy()
+    assert np.isfinite(e) and e / box.n_mol < 1e3
