@@ -1080,6 +1080,14 @@ extern "C" int mcgpu_batch_set_npt(mcgpu_batch* bt, int interval, const double* 
     if (!bt->eabs2) bt->eabs2 = dalloc<double2>(bt->pool.n_mol, &e);
     if (!bt->vsum) bt->vsum = dalloc<double2>(nc, &e);
     if (!bt->vsum_abs) bt->vsum_abs = dalloc<double2>(nc, &e);
+    Pool& P = bt->pool.P;
+    if (!P.vc_cnt) {
+      const size_t nm = (size_t)bt->pool.n_mol;
+      P.vc_cnt = dalloc<int>(nm, &e);
+      P.vc_start = dalloc<int>(nm, &e);
+      P.vc_mol = dalloc<int>(nm, &e);
+      P.vc_of = dalloc<int>(nm, &e);
+    }
     if (e != cudaSuccess) return set_err(ctx, MCGPU_ERR_NOMEM, "NPT buffers: %s", cudaGetErrorString(e));
   }
   cudaStream_t st = ctx->stream;

@@ -169,8 +169,20 @@ __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const G
   int* rj = s.lj + w * kRing;
   int head = 0, tail = 0;
   const unsigned lt = lanemask_lt();
-  for (int base = c_begin + w * 32; base < c_end; base += nw * 32) {
-    const int idx = base + lane;
+  // all molecules: warp w screens blocks of 32 consecutive indices; a list
+  // (short, in cell order): warp w takes every nw-th entry, so every warp
+  // gets its share of the in-range neighbours
+  const int rounds = cand ? (c_end - c_begin + 32 * nw - 1) / (32 * nw) : 0;
+  for (int it = 0;; it++) {
+    int idx;
+    if (cand) {
+      if (it >= rounds) break;
+      idx = c_begin + (it * 32 + lane) * nw + w;
+    } else {
+      const int base = c_begin + w * 32 + it * nw * 32;
+      if (base >= c_end) break;
+      idx = base + lane;
+    }
     const int j = (cand && idx < c_end) ? cand[idx] : idx;
     int f = 0;
     if (idx < c_end && j != mi.mol) {

@@ -86,6 +86,8 @@ struct __align__(16) ChainHdr {
   float nl_r2, nl_half2, nl_rlist, prad;
   int vol_mixed;        // volume moves with FP32 pairs (FP64 re-take near threshold)
   int vol_fp64;         // volume decisions re-taken with FP64 pairs
+  int vncell[3];        // cells per edge of the volume move in flight
+  int pad8;
 };
 static_assert(sizeof(ChainHdr) % 16 == 0, "ChainHdr alignment");
 
@@ -168,6 +170,12 @@ struct Pool {
   int* cell_start;     // [cells] first slot in cell_mol
   int* cell_mol;       // [n_mol] molecules grouped by cell
   int nl_stride;
+  // cell grid of a volume move, indexed in the chain's own molecule range
+  // (a chain has at most as many cells as molecules); null without NPT
+  int* vc_cnt;         // [n_mol] members of cell mol0 + c
+  int* vc_start;       // [n_mol] first slot in vc_mol
+  int* vc_mol;         // [n_mol] molecules grouped by cell
+  int* vc_of;          // [n_mol] cell of each molecule
 };
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), from the published

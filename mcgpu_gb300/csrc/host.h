@@ -105,6 +105,7 @@ struct DevPool {
     void* ptrs[] = {P.x, P.y, P.z, P.sig, P.eps, P.q, P.aoff, P.aofl, P.aeq, P.mstart, P.mlen, P.mpi,
                     P.mfix, P.mrad, P.mq, P.atpl, P.pidx, P.ppos, P.hdr, P.rb, P.trace,
                     P.nl, P.nl_cnt, P.pbuild, P.mcell, P.cell_cnt, P.cell_start, P.cell_mol,
+                    P.vc_cnt, P.vc_start, P.vc_mol, P.vc_of,
                     mol_chain, atom_mol, emol, pairs, esum};
     for (void* p : ptrs)
       if (p) cudaFree(p);

@@ -100,10 +100,6 @@ __device__ __forceinline__ double dist2_at(double3 a, double3 b, const double* L
 
 constexpr int kVolThreads = 128;
 
-// E(m, j > m) of pool molecule m at V (.x) and V' (.y).  Candidates whose
-// anchors are farther apart than rc + both radii (+ a margin far above the
-// FP32 rounding of the anchor difference) are skipped without an FP64
-// test; every other primary pair takes the reference's FP64 test.
 // Pool molecule of work item b: m_begin + b, or the b-th molecule of the
 // active ranges (binary search over their prefix sums).
 __device__ __forceinline__ int range_mol(const MolRanges& R, int m_begin, int b) {
@@ -116,96 +112,177 @@ __device__ __forceinline__ int range_mol(const MolRanges& R, int m_begin, int b)
   return R.act_m0[lo] + (b - R.act_pref[lo]);
 }
 
-// Chains a pair-sum pass evaluates: pass 0 the due non-mixed chains, pass 1
-// the mixed chains marked for the FP64 re-take.
-__device__ __forceinline__ bool vol_take64(const VolMove& v, const ChainHdr& H, int pass) {
-  return pass == 0 ? (v.state == 1 && !H.vol_mixed) : v.state == 4;
+// ---- cell grid of a volume move ------------------------------------------
+// Cells at least r = (rc + 2 prad + 0.01) / min(1, s) wide, so every pair
+// with an anchor distance within reach at V or V' lies in neighbouring
+// cells; cell c of a chain is pool entry mol0 + c (at most n_mol cells).
+
+__device__ __forceinline__ float vol_reach(const ChainHdr& H) {
+  return (float)(H.cutoff + 2.0 * (double)H.prad + 1e-2);
 }
 
-__global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int* mol_chain,
-                                                               const VolMove* vm, int m_begin,
-                                                               MolRanges R, double2* emol2,
-                                                               int pass) {
-  __shared__ double sx[2][3][kMaxA];
-  __shared__ double sq[3][kMaxA];
-  __shared__ int spa[kMaxP];
-  __shared__ double2 red[kVolThreads];
-  const int m = range_mol(R, m_begin, blockIdx.x);
+__global__ void k_vc_grid(Pool P, const VolMove* vm, MolRanges R, int n_items) {
+  const int i = blockIdx.x;
+  if (i >= n_items) return;
+  const int c = range_chain(R, i);
+  if (vm[c].state != 1) return;
+  ChainHdr& H = P.hdr[c];
+  __shared__ int nc[3];
+  if (threadIdx.x == 0) {
+    const double s = vm[c].L[0] / H.L[0];
+    const double edge = (double)vol_reach(H) / fmin(1.0, s) * (1.0 + 1e-6);
+    for (int k = 0; k < 3; k++) nc[k] = max(1, (int)floor(H.L[k] / edge));
+    while ((long long)nc[0] * nc[1] * nc[2] > H.n_mol) {
+      int kmax = 0;
+      for (int k = 1; k < 3; k++)
+        if (nc[k] > nc[kmax]) kmax = k;
+      nc[kmax]--;
+    }
+    for (int k = 0; k < 3; k++) H.vncell[k] = nc[k];
+  }
+  __syncthreads();
+  const int n = nc[0] * nc[1] * nc[2];
+  for (int k = threadIdx.x; k < n; k += blockDim.x) P.vc_cnt[H.mol0 + k] = 0;
+}
+
+__device__ __forceinline__ int vcell_of(unsigned a, int n) {
+  return (int)(((unsigned long long)a * (unsigned)n) >> 32);
+}
+
+__global__ void k_vc_count(Pool P, const int* mol_chain, const VolMove* vm, MolRanges R,
+                           int n_items) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_items) return;
+  const int m = range_mol(R, 0, b);
   const int c = mol_chain[m];
-  const VolMove v = vm[c];
+  if (vm[c].state != 1) return;
   const ChainHdr& H = P.hdr[c];
-  if (!vol_take64(v, H, pass)) return;
-  const double* Lv[2] = {H.L, v.L};
-  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
-  const int2 pi = P.mpi[m];
-  const uint4 Am = P.mfix[m];
-  for (int i = threadIdx.x; i < len; i += blockDim.x) {
-    const float4 o = P.aoff[a0 + i];
-    for (int w = 0; w < 2; w++) {
-      const double3 x = pos_at(Am, o, Lv[w]);
-      sx[w][0][i] = x.x;
-      sx[w][1][i] = x.y;
-      sx[w][2][i] = x.z;
-    }
-    sq[0][i] = P.sig[a0 + i];
-    sq[1][i] = P.eps[a0 + i];
-    sq[2][i] = P.q[a0 + i];
-  }
-  for (int k = threadIdx.x; k < pi.y; k += blockDim.x) spa[k] = P.pidx[pi.x + k] - a0;
+  const uint4 A = P.mfix[m];
+  const int cx = vcell_of(A.x, H.vncell[0]), cy = vcell_of(A.y, H.vncell[1]);
+  const int cz = vcell_of(A.z, H.vncell[2]);
+  const int cell = H.mol0 + (cx * H.vncell[1] + cy) * H.vncell[2] + cz;
+  P.vc_of[m] = cell;
+  atomicAdd(&P.vc_cnt[cell], 1);
+}
+
+// Exclusive scan of a chain's cell counts into vc_start (one block of 256
+// threads: contiguous runs per thread, then a scan of the run totals);
+// the counters are reset for the scatter.
+__global__ void k_vc_scan(Pool P, const VolMove* vm, MolRanges R, int n_items) {
+  __shared__ int tot[256];
+  const int i = blockIdx.x;
+  if (i >= n_items) return;
+  const int c = range_chain(R, i);
+  if (vm[c].state != 1) return;
+  const ChainHdr& H = P.hdr[c];
+  const int n = H.vncell[0] * H.vncell[1] * H.vncell[2];
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int k0 = threadIdx.x * per, k1 = min(n, k0 + per);
+  int sum = 0;
+  for (int k = k0; k < k1; k++) sum += P.vc_cnt[H.mol0 + k];
+  tot[threadIdx.x] = sum;
   __syncthreads();
-  const double s = v.L[0] / H.L[0];
-  const float reach = H.cutoff + H.rad_max * 2.0 + 1e-2;
-  const float reach2 = reach * reach;
-  double eo = 0.0, en = 0.0;
-  for (int j = m + 1 + (int)threadIdx.x; j < H.mol0 + H.n_mol; j += blockDim.x) {
-    const uint4 Aj = P.mfix[j];
-    const float3 D = fixdiff(Aj, Am, H);
-    const float d2 = fmaf(D.x, D.x, fmaf(D.y, D.y, D.z * D.z));
-    const float sf = (float)s;
-    // V' anchor distance is s |D|; skip only if both are out of reach
-    if (d2 > reach2 && d2 * sf * sf > reach2) continue;
-    const int2 pj = P.mpi[j];
-    bool in[2] = {false, false};
-    for (int w = 0; w < 2; w++) {
-      for (int k2 = 0; k2 < pj.y && !in[w]; k2++) {
-        const double3 b = pos_at(Aj, P.aoff[P.pidx[pj.x + k2]], Lv[w]);
-        for (int k1 = 0; k1 < pi.y && !in[w]; k1++) {
-          const int pa = spa[k1];
-          const double3 a = make_double3(sx[w][0][pa], sx[w][1][pa], sx[w][2][pa]);
-          in[w] = dist2_at(a, b, Lv[w]) <= __dmul_rn(H.cutoff, H.cutoff);
-        }
-      }
-    }
-    if (!in[0] && !in[1]) continue;
-    const int b0 = P.mstart[j], lenj = P.mlen[j] & 255;
-    for (int bb = b0; bb < b0 + lenj; bb++) {
-      const double sb = P.sig[bb], eb = P.eps[bb], qb = P.q[bb];
-      if (!(sb >= 0 && eb >= 0)) continue;
-      const float4 ob = P.aoff[bb];
-      for (int w = 0; w < 2; w++) {
-        if (!in[w]) continue;
-        const double3 xb = pos_at(Aj, ob, Lv[w]);
-        double acc = 0.0;
-        for (int i = 0; i < len; i++) {
-          const double sa = sq[0][i], ea = sq[1][i];
-          if (!(sa >= 0 && ea >= 0)) continue;
-          const double3 xa = make_double3(sx[w][0][i], sx[w][1][i], sx[w][2][i]);
-          acc += pair64(dist2_at(xa, xb, Lv[w]), sa, sb, ea, eb, sq[2][i], qb);
-        }
-        if (w == 0) eo += acc; else en += acc;
-      }
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int t = 0; t < (int)blockDim.x; t++) {
+      const int v = tot[t];
+      tot[t] = run;
+      run += v;
     }
   }
-  red[threadIdx.x] = make_double2(eo, en);
   __syncthreads();
-  for (int off = blockDim.x >> 1; off > 0; off >>= 1) {
-    if ((int)threadIdx.x < off) {
-      red[threadIdx.x].x += red[threadIdx.x + off].x;
-      red[threadIdx.x].y += red[threadIdx.x + off].y;
-    }
-    __syncthreads();
+  int run = H.mol0 + tot[threadIdx.x];
+  for (int k = k0; k < k1; k++) {
+    P.vc_start[H.mol0 + k] = run;
+    run += P.vc_cnt[H.mol0 + k];
+    P.vc_cnt[H.mol0 + k] = 0;
   }
-  if (threadIdx.x == 0) emol2[m] = red[0];
+}
+
+__global__ void k_vc_scatter(Pool P, const int* mol_chain, const VolMove* vm, MolRanges R,
+                             int n_items) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_items) return;
+  const int m = range_mol(R, 0, b);
+  if (vm[mol_chain[m]].state != 1) return;
+  const int cell = P.vc_of[m];
+  const int pos = atomicAdd(&P.vc_cnt[cell], 1);
+  P.vc_mol[P.vc_start[cell] + pos] = m;
+}
+
+// Sorts each cell's members by index (deterministic candidate order); the
+// work item of molecule mol0 + k sorts cell k.
+__global__ void k_vc_sort(Pool P, const int* mol_chain, const VolMove* vm, MolRanges R,
+                          int n_items) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_items) return;
+  const int m = range_mol(R, 0, b);
+  const int c = mol_chain[m];
+  if (vm[c].state != 1) return;
+  const ChainHdr& H = P.hdr[c];
+  if (m - H.mol0 >= H.vncell[0] * H.vncell[1] * H.vncell[2]) return;
+  int* v = P.vc_mol + P.vc_start[m];
+  const int n = P.vc_cnt[m];
+  for (int a = 1; a < n; a++) {
+    const int key = v[a];
+    int k = a - 1;
+    while (k >= 0 && v[k] > key) {
+      v[k + 1] = v[k];
+      k--;
+    }
+    v[k + 1] = key;
+  }
+}
+
+// The cells around molecule m's (27, or every cell once along an edge of
+// fewer than 3): first slot and member count of each, and prefix sums, in
+// shared memory; threads then take flat candidate indices.
+struct VcStencil {
+  int start[27], cnt[27], pref[28];
+  int n;
+};
+
+__device__ inline void vc_stencil(const Pool& P, const ChainHdr& H, int m, VcStencil& S) {
+  if (threadIdx.x != 0) return;
+  const int local = P.vc_of[m] - H.mol0;
+  const int n1 = H.vncell[1], n2 = H.vncell[2];
+  const int cz = local % n2, cy = (local / n2) % n1, cx = local / (n1 * n2);
+  int sx[3], sy[3], sz[3];
+  const int nc[3] = {H.vncell[0], n1, n2};
+  const int cc[3] = {cx, cy, cz};
+  int* st[3] = {sx, sy, sz};
+  int ns[3];
+  for (int k = 0; k < 3; k++) {
+    if (nc[k] >= 3) {
+      st[k][0] = (cc[k] + nc[k] - 1) % nc[k];
+      st[k][1] = cc[k];
+      st[k][2] = (cc[k] + 1) % nc[k];
+      ns[k] = 3;
+    } else {
+      for (int t = 0; t < nc[k]; t++) st[k][t] = t;
+      ns[k] = nc[k];
+    }
+  }
+  int n = 0, run = 0;
+  for (int a = 0; a < ns[0]; a++)
+    for (int b = 0; b < ns[1]; b++)
+      for (int c = 0; c < ns[2]; c++) {
+        const int cell = H.mol0 + (sx[a] * n1 + sy[b]) * n2 + sz[c];
+        S.start[n] = P.vc_start[cell];
+        S.cnt[n] = P.vc_cnt[cell];
+        S.pref[n] = run;
+        run += S.cnt[n];
+        n++;
+      }
+  S.pref[n] = run;
+  S.n = n;
+}
+
+// Candidate t of the stencil (t < S.pref[S.n]); k is the thread's cursor
+// over the cells (t only grows).
+__device__ __forceinline__ int vc_candidate(const Pool& P, const VcStencil& S, int t, int& k) {
+  while (S.pref[k + 1] <= t) k++;
+  return P.vc_mol[S.start[k] + (t - S.pref[k])];
 }
 
 // Box-derived FP32 scales of one of the two volumes of a move.
@@ -248,6 +325,210 @@ __device__ __forceinline__ void vol_fixdiff(uint4 b, uint4 a, const VolBox& B, f
   lo = make_float3(l[0], l[1], l[2]);
 }
 
+// ---- chunked candidate screening shared by the pair kernels -------------
+// A chunk of kVolChunk candidates is screened (4 per thread); the in-range
+// ones are compacted per warp into shared memory in candidate order (warp
+// w's segment holds its 4 x 32 candidates' hits), then every thread takes
+// (neighbour, neighbour atom) items, so the pair arithmetic runs on full
+// warps whatever the scatter of in-range neighbours over the candidates.
+constexpr int kVolWarps = kVolThreads / 32;
+constexpr int kVolChunk = 4 * kVolThreads;
+constexpr int kVolSeg = kVolChunk / kVolWarps;
+constexpr int kVolFShift = 28;
+constexpr int kVolJMask = (1 << kVolFShift) - 1;
+
+// In-range flags of candidate j at V (bit 0) and V' (bit 1): the FP32
+// screen of every primary pair, the reference's FP64 test inside the guard
+// band.  Candidates whose anchors are out of reach at both volumes are
+// skipped without a test.
+__device__ __forceinline__ int vol_screen(const Pool& P, const ChainHdr& H, const VolBox* vb,
+                                          const float4* so, const int* spa, int npidx, uint4 Am,
+                                          int j, const double* const* Lv, float reach2, float sf) {
+  const uint4 Aj = P.mfix[j];
+  const float3 D0 = fixdiff(Aj, Am, H);
+  const float d2 = fmaf(D0.x, D0.x, fmaf(D0.y, D0.y, D0.z * D0.z));
+  if (d2 > reach2 && d2 * sf * sf > reach2) return 0;
+  const int2 pj = P.mpi[j];
+  int f = 0;
+  for (int w = 0; w < 2; w++) {
+    const VolBox& B = vb[w];
+    float3 Dh, Dl;
+    vol_fixdiff(Aj, Am, B, Dh, Dl);
+    bool in = false;
+    for (int k2 = 0; k2 < pj.y && !in; k2++) {
+      const float4 op = P.aoff[P.pidx[pj.x + k2]];
+      for (int k1 = 0; k1 < npidx && !in; k1++) {
+        const float4 oa = so[spa[k1]];
+        const float dx = wrapf((Dh.x + op.x) - oa.x, B.Lf[0]);
+        const float dy = wrapf((Dh.y + op.y) - oa.y, B.Lf[1]);
+        const float dz = wrapf((Dh.z + op.z) - oa.z, B.Lf[2]);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (r2 <= B.cut2_lo) {
+          in = true;
+        } else if (r2 <= B.cut2_hi) {
+          in = dist2_at(pos_at(Am, oa, Lv[w]), pos_at(Aj, op, Lv[w]), Lv[w]) <=
+               __dmul_rn(H.cutoff, H.cutoff);
+        }
+      }
+    }
+    if (in) f |= 1 << w;
+  }
+  return f;
+}
+
+// Appends this lane's hit (f != 0) to its warp's segment, in lane order.
+__device__ __forceinline__ void vol_append(int* ent, int* wcnt, int j, int f, int r) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (r == 0 && lane == 0) wcnt[w] = 0;
+  __syncwarp();
+  const unsigned bal = __ballot_sync(~0u, f != 0);
+  const int base = wcnt[w];
+  if (f) ent[w * kVolSeg + base + __popc(bal & lanemask_lt())] = j | (f << kVolFShift);
+  __syncwarp();
+  if (lane == 0) wcnt[w] = base + __popc(bal);
+  __syncwarp();
+}
+
+__device__ __forceinline__ void vol_offsets(const int* wcnt, int* woff) {
+  if (threadIdx.x == 0) {
+    woff[0] = 0;
+    for (int w = 0; w < kVolWarps; w++) woff[w + 1] = woff[w] + wcnt[w];
+  }
+}
+
+__device__ __forceinline__ int vol_entry(const int* ent, const int* woff, int e) {
+  int w = 0;
+  while (woff[w + 1] <= e) w++;
+  return ent[w * kVolSeg + (e - woff[w])];
+}
+
+// FP64 pair term with the blending square roots taken per atom
+// (sqrt|s_a| sqrt|s_b| for sqrt|s_a s_b|, equal to within an ulp), one
+// division and one square root per pair; zero at r2 == 0 as the reference.
+__device__ __forceinline__ double pair64f(double r2, double rsa, double rsb, double rea,
+                                          double reb, double qq) {
+  if (r2 == 0.0) return 0.0;
+  const double ir2 = 1.0 / r2;
+  const double sg = rsa * rsb;
+  const double s2 = sg * sg * ir2;
+  const double s6 = s2 * s2 * s2;
+  return 4.0 * (rea * reb) * (s6 * s6 - s6) + qq * sqrt(ir2);
+}
+
+// Chains a pair-sum pass evaluates: pass 0 the due non-mixed chains, pass 1
+// the mixed chains marked for the FP64 re-take.
+__device__ __forceinline__ bool vol_take64(const VolMove& v, const ChainHdr& H, int pass) {
+  return pass == 0 ? (v.state == 1 && !H.vol_mixed) : v.state == 4;
+}
+
+// E(m, j > m) of pool molecule m at V (.x) and V' (.y) with FP64 pair terms
+// (the reference's, SimulationStep.cpp:344-375, with the blending roots per
+// atom).  Candidates from the cell stencil, screened and compacted in
+// chunks (vol_screen: the FP64 test's in-range set exactly).
+__global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int* mol_chain,
+                                                               const VolMove* vm, int m_begin,
+                                                               MolRanges R, double2* emol2,
+                                                               int pass) {
+  __shared__ double sx[2][3][kMaxA];
+  __shared__ double sq[3][kMaxA];
+  __shared__ int spa[kMaxP];
+  __shared__ double2 red[kVolThreads];
+  __shared__ VcStencil S;
+  __shared__ VolBox vb[2];
+  __shared__ float4 so[kMaxA];
+  __shared__ int ent[kVolChunk];
+  __shared__ int wcnt[kVolWarps], woff[kVolWarps + 1];
+  const int m = range_mol(R, m_begin, blockIdx.x);
+  const int c = mol_chain[m];
+  const VolMove v = vm[c];
+  const ChainHdr& H = P.hdr[c];
+  if (!vol_take64(v, H, pass)) return;
+  vc_stencil(P, H, m, S);
+  if (threadIdx.x == 32) volbox_set(vb[0], H.L, H.cutoff);
+  if (threadIdx.x == 33) volbox_set(vb[1], v.L, H.cutoff);
+  const double* Lv[2] = {H.L, v.L};
+  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
+  const int2 pi = P.mpi[m];
+  const uint4 Am = P.mfix[m];
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    const float4 o = P.aoff[a0 + i];
+    so[i] = o;
+    for (int w = 0; w < 2; w++) {
+      const double3 x = pos_at(Am, o, Lv[w]);
+      sx[w][0][i] = x.x;
+      sx[w][1][i] = x.y;
+      sx[w][2][i] = x.z;
+    }
+    const double sg = P.sig[a0 + i], ep = P.eps[a0 + i];
+    // dummy sites (sigma or epsilon < 0) are skipped: marked by -1
+    sq[0][i] = (sg >= 0 && ep >= 0) ? sqrt(sg) : -1.0;
+    sq[1][i] = (sg >= 0 && ep >= 0) ? sqrt(ep) : -1.0;
+    sq[2][i] = P.q[a0 + i] * kCoulomb;
+  }
+  for (int k = threadIdx.x; k < pi.y; k += blockDim.x) spa[k] = P.pidx[pi.x + k] - a0;
+  __syncthreads();
+  const float reach = vol_reach(H);
+  const float reach2 = reach * reach;
+  const float sf = (float)(v.L[0] / H.L[0]);
+  const int maxlen = H.max_len;
+  double eo = 0.0, en = 0.0;
+  const int n_cand = S.pref[S.n];
+  int kc = 0;
+  for (int c0 = 0; c0 < n_cand; c0 += kVolChunk) {
+    // screen: in-range flags of this chunk's candidates, compacted per warp
+    for (int r = 0; r < kVolChunk / kVolThreads; r++) {
+      const int t = c0 + r * kVolThreads + (int)threadIdx.x;
+      int f = 0, j = 0;
+      if (t < n_cand) {
+        j = vc_candidate(P, S, t, kc);
+        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, Lv, reach2, sf);
+      }
+      vol_append(ent, wcnt, j, f, r);
+    }
+    __syncthreads();
+    vol_offsets(wcnt, woff);
+    __syncthreads();
+    // pairs: one (neighbour, neighbour atom) item per thread
+    const int items = woff[kVolWarps] * maxlen;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int e = it / maxlen, bi = it - e * maxlen;
+      const int jf = vol_entry(ent, woff, e);
+      const int j = jf & kVolJMask, f = jf >> kVolFShift;
+      const int b0 = P.mstart[j], lenj = P.mlen[j] & 255;
+      if (bi >= lenj) continue;
+      const int bb = b0 + bi;
+      const double sb = P.sig[bb], eb = P.eps[bb], qb = P.q[bb];
+      if (!(sb >= 0 && eb >= 0)) continue;
+      const double rsb = sqrt(sb), reb = sqrt(eb);
+      const float4 ob = P.aoff[bb];
+      const uint4 Aj = P.mfix[j];
+      for (int w = 0; w < 2; w++) {
+        if (!(f & (1 << w))) continue;
+        const double3 xb = pos_at(Aj, ob, Lv[w]);
+        double acc = 0.0;
+        for (int i = 0; i < len; i++) {
+          const double rsa = sq[0][i];
+          if (rsa < 0) continue;
+          const double3 xa = make_double3(sx[w][0][i], sx[w][1][i], sx[w][2][i]);
+          acc += pair64f(dist2_at(xa, xb, Lv[w]), rsa, rsb, sq[1][i], reb, sq[2][i] * qb);
+        }
+        if (w == 0) eo += acc; else en += acc;
+      }
+    }
+    __syncthreads();
+  }
+  red[threadIdx.x] = make_double2(eo, en);
+  __syncthreads();
+  for (int off = blockDim.x >> 1; off > 0; off >>= 1) {
+    if ((int)threadIdx.x < off) {
+      red[threadIdx.x].x += red[threadIdx.x + off].x;
+      red[threadIdx.x].y += red[threadIdx.x + off].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) emol2[m] = red[0];
+}
+
 // E(m, j > m) at V (.x) and V' (.y) of a mixed chain's molecule m with FP32
 // pair terms (per-pair minimum image, the chain kernel's arithmetic) summed
 // in double-float; eabs2 gets the sums of the terms' magnitudes.  The
@@ -263,11 +544,15 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
   __shared__ VolBox vb[2];
   __shared__ double2 red[kVolThreads];
   __shared__ double2 rab[kVolThreads];
+  __shared__ VcStencil S;
+  __shared__ int ent[kVolChunk];
+  __shared__ int wcnt[kVolWarps], woff[kVolWarps + 1];
   const int m = range_mol(R, m_begin, blockIdx.x);
   const int c = mol_chain[m];
   const VolMove v = vm[c];
   const ChainHdr& H = P.hdr[c];
   if (!(v.state == 1 && H.vol_mixed)) return;
+  vc_stencil(P, H, m, S);
   const int a0 = P.mstart[m], len = P.mlen[m] & 255;
   const int2 pi = P.mpi[m];
   const uint4 Am = P.mfix[m];
@@ -280,65 +565,65 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
   if (threadIdx.x == 1) volbox_set(vb[1], v.L, H.cutoff);
   __syncthreads();
   const double* Lv[2] = {H.L, v.L};
-  const float reach = H.cutoff + H.rad_max * 2.0 + 1e-2;
+  const float reach = vol_reach(H);
   const float reach2 = reach * reach;
   const float sf = (float)(v.L[0] / H.L[0]);
   float eh[2] = {0.f, 0.f}, el[2] = {0.f, 0.f}, ab[2] = {0.f, 0.f};
-  for (int j = m + 1 + (int)threadIdx.x; j < H.mol0 + H.n_mol; j += blockDim.x) {
-    const uint4 Aj = P.mfix[j];
-    const float3 D0 = fixdiff(Aj, Am, H);
-    const float d2 = fmaf(D0.x, D0.x, fmaf(D0.y, D0.y, D0.z * D0.z));
-    if (d2 > reach2 && d2 * sf * sf > reach2) continue;
-    const int2 pj = P.mpi[j];
-    const int b0 = P.mstart[j], lenj = P.mlen[j] & 255;
-    for (int w = 0; w < 2; w++) {
-      const VolBox& B = vb[w];
-      float3 Dh, Dl;
-      vol_fixdiff(Aj, Am, B, Dh, Dl);
-      bool in = false;
-      for (int k2 = 0; k2 < pj.y && !in; k2++) {
-        const int p2 = P.pidx[pj.x + k2];
-        const float4 op = P.aoff[p2];
-        for (int k1 = 0; k1 < pi.y && !in; k1++) {
-          const float4 oa = so[spa[k1]];
-          const float dx = wrapf((Dh.x + op.x) - oa.x, B.Lf[0]);
-          const float dy = wrapf((Dh.y + op.y) - oa.y, B.Lf[1]);
-          const float dz = wrapf((Dh.z + op.z) - oa.z, B.Lf[2]);
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          if (r2 <= B.cut2_lo) {
-            in = true;
-          } else if (r2 <= B.cut2_hi) {
-            in = dist2_at(pos_at(Am, oa, Lv[w]), pos_at(Aj, op, Lv[w]), Lv[w]) <=
-                 __dmul_rn(H.cutoff, H.cutoff);
-          }
-        }
+  const int maxlen = H.max_len;
+  const int n_cand = S.pref[S.n];
+  int kc = 0;
+  for (int c0 = 0; c0 < n_cand; c0 += kVolChunk) {
+    for (int r = 0; r < kVolChunk / kVolThreads; r++) {
+      const int t = c0 + r * kVolThreads + (int)threadIdx.x;
+      int f = 0, j = 0;
+      if (t < n_cand) {
+        j = vc_candidate(P, S, t, kc);
+        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, Lv, reach2, sf);
       }
-      if (!in) continue;
-      float e = 0.f;
-      for (int bb = b0; bb < b0 + lenj; bb++) {
-        const float4 ob = P.aoff[bb];
-        const float2 qb = P.aeq[bb];
+      vol_append(ent, wcnt, j, f, r);
+    }
+    __syncthreads();
+    vol_offsets(wcnt, woff);
+    __syncthreads();
+    const int items = woff[kVolWarps] * maxlen;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int e = it / maxlen, bi = it - e * maxlen;
+      const int jf = vol_entry(ent, woff, e);
+      const int j = jf & kVolJMask, f = jf >> kVolFShift;
+      const int lenj = P.mlen[j] & 255;
+      if (bi >= lenj) continue;
+      const int bb = P.mstart[j] + bi;
+      const float4 ob = P.aoff[bb];
+      const float2 qb = P.aeq[bb];
+      const uint4 Aj = P.mfix[j];
+      for (int w = 0; w < 2; w++) {
+        if (!(f & (1 << w))) continue;
+        const VolBox& B = vb[w];
+        float3 Dh, Dl;
+        vol_fixdiff(Aj, Am, B, Dh, Dl);
         // b relative to m's anchor as a double-float: two-sum of D + o_b
         const float bx = Dh.x + ob.x, by = Dh.y + ob.y, bz = Dh.z + ob.z;
         const float lx = ((Dh.x - (bx - (bx - Dh.x))) + (ob.x - (bx - Dh.x))) + Dl.x;
         const float ly = ((Dh.y - (by - (by - Dh.y))) + (ob.y - (by - Dh.y))) + Dl.y;
         const float lz = ((Dh.z - (bz - (bz - Dh.z))) + (ob.z - (bz - Dh.z))) + Dl.z;
+        float e32 = 0.f;
         for (int i = 0; i < len; i++) {
-          const float4 a = so[i];
+          const float4 a4 = so[i];
           const float2 ea = sq[i];
-          const float dx = wrapf((bx - a.x) + lx, B.Lf[0]);
-          const float dy = wrapf((by - a.y) + ly, B.Lf[1]);
-          const float dz = wrapf((bz - a.z) + lz, B.Lf[2]);
+          const float dx = wrapf((bx - a4.x) + lx, B.Lf[0]);
+          const float dy = wrapf((by - a4.y) + ly, B.Lf[1]);
+          const float dz = wrapf((bz - a4.z) + lz, B.Lf[2]);
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
           if (!(r2 > 0.f)) continue;
-          const float lj = lj32(rcp_nr(r2), a.w, ob.w, ea.x, qb.x);
+          const float lj = lj32(rcp_nr(r2), a4.w, ob.w, ea.x, qb.x);
           const float cl = (ea.y * qb.y) * rsqrt_nr(r2);
-          e += lj + cl;
+          e32 += lj + cl;
           ab[w] += fabsf(lj) + fabsf(cl);
         }
+        ff_add(eh[w], el[w], e32);
       }
-      ff_add(eh[w], el[w], e);
     }
+    __syncthreads();
   }
   red[threadIdx.x] = make_double2((double)eh[0] + (double)el[0], (double)eh[1] + (double)el[1]);
   rab[threadIdx.x] = make_double2((double)ab[0], (double)ab[1]);
@@ -486,6 +771,14 @@ cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, V
   if (nc == 0) return cudaSuccess;
   k_vol_propose<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, act, nc);
   const int items = act.act_pref ? act.total : n_mol_total;
+  if (items > 0) {
+    const int gb = (items + 255) / 256;
+    k_vc_grid<<<nc, 128, 0, st>>>(P, vm, act, nc);
+    k_vc_count<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
+    k_vc_scan<<<nc, 256, 0, st>>>(P, vm, act, nc);
+    k_vc_scatter<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
+    k_vc_sort<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
+  }
   auto pairs = [&](bool f64, int pass) {
     if (items <= 0) return;
     if (act.act_pref) {

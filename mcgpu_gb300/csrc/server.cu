@@ -137,6 +137,8 @@ int server_alloc(mcgpu_server* s) {
   P.mstart = dalloc<int>(nm, &e); P.mlen = dalloc<int>(nm, &e); P.mpi = dalloc<int2>(nm, &e);
   P.mfix = dalloc<uint4>(nm, &e); P.mrad = dalloc<float>(nm, &e); P.mq = dalloc<float4>(nm, &e);
   P.pidx = dalloc<int>(np, &e); P.ppos = dalloc<float4>(np, &e);
+  P.vc_cnt = dalloc<int>(nm, &e); P.vc_start = dalloc<int>(nm, &e);
+  P.vc_mol = dalloc<int>(nm, &e); P.vc_of = dalloc<int>(nm, &e);
   P.hdr = dalloc<ChainHdr>(nc, &e);
   P.rb = dalloc<double>((size_t)nc * 3 * ml, &e);
   P.trace = nullptr;
