@@ -808,14 +808,30 @@ extern "C" int mcgpu_batch_create(mcgpu_ctx* ctx, int n_chains, const mcgpu_box_
     mcgpu_batch_destroy(bt);
     return rc;
   }
-  rc = pool_system_energy(ctx, bt->pool, true, ctx->stream);
-  if (rc) {
-    mcgpu_batch_destroy(bt);
-    return rc;
+  // initial running energies: FP64 system energies over per-chain cell
+  // grids (the volume-move machinery at the chains' own boxes)
+  {
+    cudaError_t e2 = cudaSuccess;
+    Pool& P = bt->pool.P;
+    const size_t nm = (size_t)bt->pool.n_mol;
+    bt->vm = dalloc<VolMove>(n_chains, &e2);
+    bt->emol2 = dalloc<double2>(nm, &e2);
+    bt->eabs2 = dalloc<double2>(nm, &e2);
+    bt->vsum = dalloc<double2>(n_chains, &e2);
+    bt->vsum_abs = dalloc<double2>(n_chains, &e2);
+    P.vc_cnt = dalloc<int>(nm, &e2);
+    P.vc_start = dalloc<int>(nm, &e2);
+    P.vc_mol = dalloc<int>(nm, &e2);
+    P.vc_of = dalloc<int>(nm, &e2);
+    if (e2 == cudaSuccess)
+      e2 = launch_chain_energy(P, bt->pool.mol_chain, bt->pool.n_mol, bt->vm, bt->emol2, bt->eabs2,
+                               bt->vsum, bt->vsum_abs, ctx->stream, MolRanges(), true);
+    if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(ctx->stream);
+    if (e2 != cudaSuccess) {
+      mcgpu_batch_destroy(bt);
+      return set_err(ctx, MCGPU_ERR_CUDA, "initial energies: %s", cudaGetErrorString(e2));
+    }
   }
-  k_set_energy<<<(n_chains + 127) / 128, 128, 0, ctx->stream>>>(bt->pool.P, bt->pool.esum);
-  CK(ctx, cudaGetLastError());
-  CK(ctx, cudaStreamSynchronize(ctx->stream));
   *out = bt;
   return MCGPU_OK;
 }

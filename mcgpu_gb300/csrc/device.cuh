@@ -124,8 +124,18 @@ struct NlCfg {
   float r2, half2, rlist, pad2;
 };
 
-// One chain's volume move in flight (NPT).
+// Box-derived FP32 scales of one of the two volumes of a move.
+struct VolBox {
+  float Lf[3], fxs[3], fxs_lo[3];
+  float cut2_lo, cut2_hi;
+  double L[3];
+};
+
+// One chain's volume move in flight (NPT), with both volumes' FP32 scales
+// and the anchor reach of the pair screen (set once per move).
 struct VolMove {
+  VolBox box[2];
+  float reach, sf;   // rc + 2 prad + 0.01; edge ratio L'/L
   double L[3];
   double dlnv, u;
   int state;   // 0 not due, 1 evaluate, 2 rejected outright, 3 accepted,

@@ -42,6 +42,9 @@ cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, V
                                 double2* emol2, double2* eabs2, double2* esum, double2* esum_abs,
                                 mcgpu_vol_trace* trace, int trace_slot, int trace_stride,
                                 cudaStream_t st, MolRanges act, bool has64, bool has32);
+cudaError_t launch_chain_energy(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
+                                double2* emol2, double2* eabs2, double2* esum, double2* esum_abs,
+                                cudaStream_t st, MolRanges act, bool f64);
 
 }  // namespace mcgpu
 

@@ -53,6 +53,24 @@ __device__ __forceinline__ int range_chain(const MolRanges& R, int i) {
   return R.act_slot ? R.act_slot[i] : i;
 }
 
+__device__ inline void volbox_set(VolBox& B, const double* L, double rc) {
+  double Lmax = 0;
+  for (int k = 0; k < 3; k++) {
+    B.L[k] = L[k];
+    B.Lf[k] = (float)L[k];
+    B.fxs[k] = (float)(L[k] / 4294967296.0);
+    B.fxs_lo[k] = (float)(L[k] / 4294967296.0 - (double)B.fxs[k]);
+    Lmax = fmax(Lmax, L[k]);
+  }
+  const double band = screen_band(rc, Lmax);
+  B.cut2_lo = (float)(rc * rc - band);
+  B.cut2_hi = (float)(rc * rc + band);
+}
+
+__device__ __forceinline__ float vol_reach(const ChainHdr& H) {
+  return (float)(H.cutoff + 2.0 * (double)H.prad + 1e-2);
+}
+
 __global__ void k_vol_propose(Pool P, VolMove* vm, MolRanges R, int n_items) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_items) return;
@@ -77,6 +95,10 @@ __global__ void k_vol_propose(Pool P, VolMove* vm, MolRanges R, int n_items) {
       v.L[k] = __dmul_rn(H.L[k], s);
       Lmin = fmin(Lmin, v.L[k]);
     }
+    volbox_set(v.box[0], H.L, H.cutoff);
+    volbox_set(v.box[1], v.L, H.cutoff);
+    v.reach = vol_reach(H);
+    v.sf = (float)(v.L[0] / H.L[0]);
     // molecules must stay within a quarter of an edge (the chain state's
     // anchor-image rule); the cutoff may exceed half an edge, as in the
     // reference's single-image minimum convention
@@ -117,9 +139,6 @@ __device__ __forceinline__ int range_mol(const MolRanges& R, int m_begin, int b)
 // with an anchor distance within reach at V or V' lies in neighbouring
 // cells; cell c of a chain is pool entry mol0 + c (at most n_mol cells).
 
-__device__ __forceinline__ float vol_reach(const ChainHdr& H) {
-  return (float)(H.cutoff + 2.0 * (double)H.prad + 1e-2);
-}
 
 __global__ void k_vc_grid(Pool P, const VolMove* vm, MolRanges R, int n_items) {
   const int i = blockIdx.x;
@@ -285,26 +304,6 @@ __device__ __forceinline__ int vc_candidate(const Pool& P, const VcStencil& S, i
   return P.vc_mol[S.start[k] + (t - S.pref[k])];
 }
 
-// Box-derived FP32 scales of one of the two volumes of a move.
-struct VolBox {
-  float Lf[3], fxs[3], fxs_lo[3];
-  float cut2_lo, cut2_hi;
-  double L[3];
-};
-
-__device__ inline void volbox_set(VolBox& B, const double* L, double rc) {
-  double Lmax = 0;
-  for (int k = 0; k < 3; k++) {
-    B.L[k] = L[k];
-    B.Lf[k] = (float)L[k];
-    B.fxs[k] = (float)(L[k] / 4294967296.0);
-    B.fxs_lo[k] = (float)(L[k] / 4294967296.0 - (double)B.fxs[k]);
-    Lmax = fmax(Lmax, L[k]);
-  }
-  const double band = screen_band(rc, Lmax);
-  B.cut2_lo = (float)(rc * rc - band);
-  B.cut2_hi = (float)(rc * rc + band);
-}
 
 // Anchor difference b - a at box B as a double-float (fixdiff_ff's split).
 __device__ __forceinline__ void vol_fixdiff(uint4 b, uint4 a, const VolBox& B, float3& hi,
@@ -343,14 +342,15 @@ constexpr int kVolJMask = (1 << kVolFShift) - 1;
 // skipped without a test.
 __device__ __forceinline__ int vol_screen(const Pool& P, const ChainHdr& H, const VolBox* vb,
                                           const float4* so, const int* spa, int npidx, uint4 Am,
-                                          int j, const double* const* Lv, float reach2, float sf) {
+                                          int j, const double* const* Lv, float reach2, float sf,
+                                          int nvol) {
   const uint4 Aj = P.mfix[j];
   const float3 D0 = fixdiff(Aj, Am, H);
   const float d2 = fmaf(D0.x, D0.x, fmaf(D0.y, D0.y, D0.z * D0.z));
   if (d2 > reach2 && d2 * sf * sf > reach2) return 0;
   const int2 pj = P.mpi[j];
   int f = 0;
-  for (int w = 0; w < 2; w++) {
+  for (int w = 0; w < nvol; w++) {
     const VolBox& B = vb[w];
     float3 Dh, Dl;
     vol_fixdiff(Aj, Am, B, Dh, Dl);
@@ -416,8 +416,10 @@ __device__ __forceinline__ double pair64f(double r2, double rsa, double rsb, dou
 }
 
 // Chains a pair-sum pass evaluates: pass 0 the due non-mixed chains, pass 1
-// the mixed chains marked for the FP64 re-take.
+// the mixed chains marked for the FP64 re-take, pass 2 the chains whose
+// energy at their current box is wanted (one volume only).
 __device__ __forceinline__ bool vol_take64(const VolMove& v, const ChainHdr& H, int pass) {
+  if (pass == 2) return v.state == 1;  // a chain's energy at its current box
   return pass == 0 ? (v.state == 1 && !H.vol_mixed) : v.state == 4;
 }
 
@@ -443,9 +445,9 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
   const VolMove v = vm[c];
   const ChainHdr& H = P.hdr[c];
   if (!vol_take64(v, H, pass)) return;
+  const int nvol = pass == 2 ? 1 : 2;
   vc_stencil(P, H, m, S);
-  if (threadIdx.x == 32) volbox_set(vb[0], H.L, H.cutoff);
-  if (threadIdx.x == 33) volbox_set(vb[1], v.L, H.cutoff);
+  if (threadIdx.x < 2) vb[threadIdx.x] = v.box[threadIdx.x];
   const double* Lv[2] = {H.L, v.L};
   const int a0 = P.mstart[m], len = P.mlen[m] & 255;
   const int2 pi = P.mpi[m];
@@ -467,9 +469,8 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
   }
   for (int k = threadIdx.x; k < pi.y; k += blockDim.x) spa[k] = P.pidx[pi.x + k] - a0;
   __syncthreads();
-  const float reach = vol_reach(H);
-  const float reach2 = reach * reach;
-  const float sf = (float)(v.L[0] / H.L[0]);
+  const float reach2 = v.reach * v.reach;
+  const float sf = v.sf;
   const int maxlen = H.max_len;
   double eo = 0.0, en = 0.0;
   const int n_cand = S.pref[S.n];
@@ -481,7 +482,7 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
       int f = 0, j = 0;
       if (t < n_cand) {
         j = vc_candidate(P, S, t, kc);
-        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, Lv, reach2, sf);
+        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, Lv, reach2, sf, nvol);
       }
       vol_append(ent, wcnt, j, f, r);
     }
@@ -537,7 +538,7 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
 __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const int* mol_chain,
                                                                  const VolMove* vm, int m_begin,
                                                                  MolRanges R, double2* emol2,
-                                                                 double2* eabs2) {
+                                                                 double2* eabs2, int init) {
   __shared__ float4 so[kMaxA];
   __shared__ float2 sq[kMaxA];
   __shared__ int spa[kMaxP];
@@ -551,7 +552,9 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
   const int c = mol_chain[m];
   const VolMove v = vm[c];
   const ChainHdr& H = P.hdr[c];
-  if (!(v.state == 1 && H.vol_mixed)) return;
+  // init: a chain's energy at its current box (one volume)
+  if (!(v.state == 1 && (H.vol_mixed || init))) return;
+  const int nvol = init ? 1 : 2;
   vc_stencil(P, H, m, S);
   const int a0 = P.mstart[m], len = P.mlen[m] & 255;
   const int2 pi = P.mpi[m];
@@ -561,13 +564,11 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
     sq[i] = P.aeq[a0 + i];
   }
   for (int k = threadIdx.x; k < pi.y; k += blockDim.x) spa[k] = P.pidx[pi.x + k] - a0;
-  if (threadIdx.x == 0) volbox_set(vb[0], H.L, H.cutoff);
-  if (threadIdx.x == 1) volbox_set(vb[1], v.L, H.cutoff);
+  if (threadIdx.x < 2) vb[threadIdx.x] = v.box[threadIdx.x];
   __syncthreads();
   const double* Lv[2] = {H.L, v.L};
-  const float reach = vol_reach(H);
-  const float reach2 = reach * reach;
-  const float sf = (float)(v.L[0] / H.L[0]);
+  const float reach2 = v.reach * v.reach;
+  const float sf = v.sf;
   float eh[2] = {0.f, 0.f}, el[2] = {0.f, 0.f}, ab[2] = {0.f, 0.f};
   const int maxlen = H.max_len;
   const int n_cand = S.pref[S.n];
@@ -578,7 +579,7 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
       int f = 0, j = 0;
       if (t < n_cand) {
         j = vc_candidate(P, S, t, kc);
-        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, Lv, reach2, sf);
+        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, Lv, reach2, sf, nvol);
       }
       vol_append(ent, wcnt, j, f, r);
     }
@@ -759,6 +760,64 @@ __global__ void k_vol_refresh(Pool P, const int* mol_chain, const VolMove* vm, i
   }
 }
 
+// A "volume move" to the chain's own box: state 1, both boxes the current
+// one, so the cell grid and the pair kernels give the chain's energy.
+__global__ void k_vol_self(Pool P, VolMove* vm, MolRanges R, int n_items) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_items) return;
+  const int c = range_chain(R, i);
+  const ChainHdr& H = P.hdr[c];
+  VolMove v;
+  for (int k = 0; k < 3; k++) v.L[k] = H.L[k];
+  volbox_set(v.box[0], H.L, H.cutoff);
+  v.box[1] = v.box[0];
+  v.reach = vol_reach(H);
+  v.sf = 1.0f;
+  v.dlnv = 0.0;
+  v.u = 0.0;
+  v.fp64 = 0;
+  v.state = H.n_mol > 0 ? 1 : 0;
+  vm[c] = v;
+}
+
+__global__ void k_vol_self_energy(Pool P, const VolMove* vm, const double2* esum, MolRanges R,
+                                  int n_items) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_items) return;
+  const int c = range_chain(R, i);
+  if (vm[c].state == 1) P.hdr[c].energy = esum[c].x;
+}
+
+// Sets the running energy of the chains in act (all when act has no
+// ranges) to their system energy, FP64 or FP32 pair terms (double-float
+// sums), through the volume machinery; vm, emol2, eabs2, esum, esum_abs are
+// scratch of the volume phase (the chains' own entries only).
+cudaError_t launch_chain_energy(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
+                                double2* emol2, double2* eabs2, double2* esum, double2* esum_abs,
+                                cudaStream_t st, MolRanges act, bool f64) {
+  const int nc = act.act_slot ? act.n_act : P.n_chains;
+  const int items = act.act_pref ? act.total : n_mol_total;
+  if (nc == 0 || items == 0) return cudaSuccess;
+  k_vol_self<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, act, nc);
+  const int gb = (items + 255) / 256;
+  k_vc_grid<<<nc, 128, 0, st>>>(P, vm, act, nc);
+  k_vc_count<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
+  k_vc_scan<<<nc, 256, 0, st>>>(P, vm, act, nc);
+  k_vc_scatter<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
+  k_vc_sort<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
+  const int chunk = act.act_pref ? items : (1 << 20);
+  for (int m0 = 0; m0 < items; m0 += chunk) {
+    const int n = items - m0 < chunk ? items - m0 : chunk;
+    if (f64)
+      k_vol_pair_sums<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2, 2);
+    else
+      k_vol_pair_sums32<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2, eabs2, 1);
+  }
+  k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 1);
+  k_vol_self_energy<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, act, nc);
+  return cudaGetLastError();
+}
+
 // One volume phase on stream st (buffers sized for the pool).  has64 /
 // has32: some due chain uses FP64 / FP32 pair energies (the other pair
 // kernel is skipped).  With active ranges the work items are the ranges'
@@ -785,7 +844,7 @@ cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, V
       if (f64)
         k_vol_pair_sums<<<items, kVolThreads, 0, st>>>(P, mol_chain, vm, 0, act, emol2, pass);
       else
-        k_vol_pair_sums32<<<items, kVolThreads, 0, st>>>(P, mol_chain, vm, 0, act, emol2, eabs2);
+        k_vol_pair_sums32<<<items, kVolThreads, 0, st>>>(P, mol_chain, vm, 0, act, emol2, eabs2, 0);
       return;
     }
     const int chunk = 1 << 20;
@@ -794,7 +853,7 @@ cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, V
       if (f64)
         k_vol_pair_sums<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2, pass);
       else
-        k_vol_pair_sums32<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2, eabs2);
+        k_vol_pair_sums32<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2, eabs2, 0);
     }
   };
   if (has64) pairs(true, 0);

@@ -104,6 +104,7 @@ struct mcgpu_server {
   // device scratch
   unsigned* qctr = nullptr;
   int* dlist = nullptr;  // order [slots] | act_slot [slots] | act_m0 [slots] | act_pref [slots+1]
+  int* dinit = nullptr;  // per slot: (slot, m0, 0, n_mol) range of a job being initialised
   VolMove* vm = nullptr;
   double2* emol2 = nullptr;
   double2* eabs2 = nullptr;
@@ -155,6 +156,7 @@ int server_alloc(mcgpu_server* s) {
   dp.max_len = ml;
   s->qctr = dalloc<unsigned>(1, &e);
   s->dlist = dalloc<int>(4 * (size_t)nc + 1, &e);
+  s->dinit = dalloc<int>(4 * (size_t)nc, &e);
   s->vm = dalloc<VolMove>(nc, &e);
   s->emol2 = dalloc<double2>(nm, &e);
   s->eabs2 = dalloc<double2>(nm, &e);
@@ -171,7 +173,7 @@ int server_alloc(mcgpu_server* s) {
 
 void server_free(mcgpu_server* s) {
   s->pool.release();
-  void* d[] = {s->qctr, s->dlist, s->vm, s->emol2, s->eabs2, s->vsum, s->vsum_abs};
+  void* d[] = {s->qctr, s->dlist, s->dinit, s->vm, s->emol2, s->eabs2, s->vsum, s->vsum_abs};
   for (void* p : d)
     if (p) cudaFree(p);
   if (s->hmirror) cudaFreeHost(s->hmirror);
@@ -264,11 +266,19 @@ int upload_job(mcgpu_server* s, Job* j) {
   k_refresh_mirrors<<<(n + wpb - 1) / wpb, wpb * 32, 0, st>>>(P, s->pool.mol_chain, m0, m0 + n);
   k_chain_init<<<(n + wpb - 1) / wpb, wpb * 32, 0, st>>>(P, s->pool.mol_chain, m0, m0 + n);
   CK(ctx, cudaGetLastError());
-  const int nw = 4;
-  CK(ctx, launch_mol_pair_sums(true, n, nw * 32, shape_for(s->cfg.max_mol_atoms, nw), st, P,
-                               s->pool.mol_chain, m0, s->pool.emol, s->pool.pairs));
-  k_chain_energy1<<<1, 256, 0, st>>>(P, slot, s->pool.emol);
-  CK(ctx, cudaGetLastError());
+  // initial running energy: FP64 system energy over the job's cell grid
+  // (its own molecules, slot and scratch entries only)
+  int* dr = s->dinit + 4 * slot;
+  const int rng[4] = {slot, m0, 0, n};
+  if ((rc = stage_copy(s, dr, rng, 4))) return rc;
+  MolRanges R;
+  R.act_slot = dr;
+  R.act_m0 = dr + 1;
+  R.act_pref = dr + 2;
+  R.n_act = 1;
+  R.total = n;
+  CK(ctx, launch_chain_energy(P, s->pool.mol_chain, 0, s->vm, s->emol2, s->eabs2, s->vsum,
+                              s->vsum_abs, st, R, true));
   return MCGPU_OK;
 }
 
