@@ -40,6 +40,11 @@ WORKLOAD = ("512 independent NVT water chains (3-site TIP3P-like, rigid), N log-
             "[64, 2048] at 1.0 g/cc, T uniform in [280, 360] K, cutoff min(9, L/2) A, "
             "+-0.15 A / +-15 deg random-axis moves, Philox proposals, on-device accept")
 FP32_FLOPS_PER_PAIR = 38   # per atom pair, fixed by convention from the reference's arithmetic
+# DRAM bytes (read + write) per launch of k_chain_steps on this workload,
+# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, 3 launches
+# after 6 warm-up launches, L2 flushed between bench steps), by tile
+# (threads, chains per CTA, steps per launch, lanes per molecule).
+CHAIN_TRAFFIC_BYTES = {(256, 1, 64, 1): 49.96e6}
 
 
 def peaks():
@@ -516,7 +521,9 @@ def main():
                          "(~14 MB) is re-read from HBM at each step start",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                     "traffic": CHAIN_TRAFFIC_BYTES.get((threads, cpc, spl, lanes)),
+                     "traffic_unit": "bytes per launch (ncu capture of this tile; null for others)",
                      "kernel": "k_chain_steps",
                      "work": f"{FP32_FLOPS_PER_PAIR} flop x {mean_pairs_per_move:.1f} atom pairs "
                              "per move (device-counted, old+new)",
