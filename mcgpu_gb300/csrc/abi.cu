@@ -84,6 +84,9 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
   int max_len = 0;
   double max_rad = 0, max_prad = 0;
   bool simple = d->n_pidx == d->n_mol;
+  bool uniform = simple;
+  int u_len = -1, u_act = -1, u_prim = -1;
+  float u_mrad = 0.f;
   for (int m = 0; m < d->n_mol; m++) {
     const int s = d->mol_start[m], len = d->mol_len[m];
     const int ps = d->mol_pidx_start[m], pc = d->mol_pidx_count[m];
@@ -126,6 +129,14 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
     hp.mrad.push_back((float)(rad * (1 + 1e-6) + 1e-4));
     hp.mol_chain.push_back(c);
     if (ps != m || pc != 1) simple = false;
+    if (m == 0) {
+      u_len = len;
+      u_act = act;
+      u_prim = an - s;
+    }
+    if (!simple || s != m * u_len || len != u_len || act != u_act || an - s != u_prim)
+      uniform = false;
+    u_mrad = std::max(u_mrad, hp.mrad.back());
   }
   hp.atom_mol.resize(hp.x.size(), -1);
   for (int m = 0; m < d->n_mol; m++)
@@ -156,6 +167,11 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
   h.rot_mode = rot_mode;
   h.chain_id = (int)c;
   h.simple_prim = simple ? 1 : 0;
+  h.uniform = uniform ? 1 : 0;
+  h.ulen = u_len;
+  h.uact = u_act;
+  h.uprim = u_prim;
+  h.umrad = u_mrad;
   h.precise = max_len >= 8 ? 1 : 0;
   const double rc = d->cutoff;
   h.cutoff = rc;

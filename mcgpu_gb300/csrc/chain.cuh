@@ -52,10 +52,18 @@ enum : int { kMiscQn = 16, kMiscU = 20, kMiscNlTrial = 24, kMiscNlOk = 25 };
 __device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF& mv, const GroupSmem& s,
                             const float4* pcache, int lane) {
   const int m = H.mol0 + mv.mol;
-  const int a0 = P.mstart[m];
-  const int lw = P.mlen[m];
+  int a0, lw;
+  int2 pi;
+  if (H.uniform) {
+    a0 = H.atom0 + mv.mol * H.ulen;
+    lw = H.ulen | (H.uact << 8);
+    pi = make_int2(H.pidx0 + mv.mol, 1);
+  } else {
+    a0 = P.mstart[m];
+    lw = P.mlen[m];
+    pi = P.mpi[m];
+  }
   const int len = lw & 255;
-  const int2 pi = P.mpi[m];
   const float4 q4 = P.mq[m];
   const uint4 A = P.mfix[m];
   QuatF q;
@@ -88,16 +96,13 @@ __device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF
     s.l_new[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     s.eq[i] = make_float4(qe.x, qe.y, fmaf(o.x, o.x, fmaf(o.y, o.y, o.z * o.z)),
                           fmaf(on.x, on.x, fmaf(on.y, on.y, on.z * on.z)));
-    s.sd[i] = P.sig[a];
-    s.ed[i] = P.eps[a];
-    s.qd[i] = P.q[a];
     qsum += qe.y;
   }
   for (int off = 16; off > 0; off >>= 1) qsum += __shfl_xor_sync(~0u, qsum, off);
   __syncwarp();
   bool near = true;
   for (int k = lane; k < pi.y; k += 32) {
-    const int slot = P.pidx[pi.x + k] - a0;
+    const int slot = H.uniform ? H.uprim : P.pidx[pi.x + k] - a0;
     s.pa[k] = slot;
     s.p_old[k] = (k == 0 && pcache) ? pcache[m - H.mol0] : P.ppos[pi.x + k];
     const float4 pn = chain_screen_pos(An, s.o_new[slot], H);
@@ -114,7 +119,7 @@ __device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF
     s.misc[kMiscQn + 2] = __float_as_int(qn.y); s.misc[kMiscQn + 3] = __float_as_int(qn.z);
     s.misc[kMiscU] = __float_as_int(mv.u);
     s.misc[kMiscNlTrial] = near ? 1 : 0;
-    s.miscd[0] = (double)P.mrad[m];
+    s.miscd[0] = (double)(H.uniform ? H.umrad : P.mrad[m]);
     s.miscd[1] = (double)qsum;
   }
 }
@@ -253,10 +258,14 @@ __device__ __forceinline__ void group_reduce_ff(const Group& g, const GroupSmem&
 // FP64 re-take of a step near the decision threshold: the reference's pair
 // arithmetic (BruteForceStep.cpp:48-79) on the FP64 positions of the chain
 // state (anchor + offset).  Warp 0 first writes the moved molecule's old
-// and new FP64 coordinates to shared memory; the caller synchronises.
-__device__ inline void stage_chain_f64(const ChainHdr& H, const GroupSmem& s, const MovedInfo& mi,
-                                int lane) {
+// and new FP64 coordinates and its FP64 parameters to shared memory; the
+// caller synchronises.
+__device__ inline void stage_chain_f64(const Pool& P, const ChainHdr& H, const GroupSmem& s,
+                                       const MovedInfo& mi, int lane) {
   for (int i = lane; i < mi.len; i += 32) {
+    s.sd[i] = P.sig[mi.atom0 + i];
+    s.ed[i] = P.eps[mi.atom0 + i];
+    s.qd[i] = P.q[mi.atom0 + i];
     const double3 a = chain_pos3(mi.fx_old, s.o_old[i], H);
     const double3 b = chain_pos3(mi.fx_new, s.o_new[i], H);
     s.ox[i] = a.x; s.oy[i] = a.y; s.oz[i] = a.z;
@@ -343,7 +352,7 @@ __device__ inline void warp_eval_chain64(const Pool& P, const ChainHdr& H, const
 __device__ __forceinline__ void commit_chain(const Pool& P, const ChainHdr& H, const GroupSmem& s,
                                              const MovedInfo& mi, float4* pcache, int lane) {
   for (int i = lane; i < mi.len; i += 32) P.aoff[mi.atom0 + i] = s.o_new[i];
-  const int2 pi = P.mpi[mi.mol];
+  const int2 pi = H.uniform ? make_int2(H.pidx0 + (mi.mol - H.mol0), 1) : P.mpi[mi.mol];
   for (int k = lane; k < mi.npidx; k += 32) P.ppos[pi.x + k] = s.p_new[k];
   if (lane == 0) {
     P.mfix[mi.mol] = mi.fx_new;

@@ -88,6 +88,11 @@ struct __align__(16) ChainHdr {
   int vol_fp64;         // volume decisions re-taken with FP64 pairs
   int vncell[3];        // cells per edge of the volume move in flight
   int pad8;
+  // uniform chain: every molecule ulen atoms (uact active) laid out
+  // contiguously from atom0, one primary at slot uprim, radius <= umrad:
+  // atom and primary indexes follow from the molecule index (no loads)
+  int uniform, ulen, uact, uprim;
+  float umrad, pad9, pad10, pad11;
 };
 static_assert(sizeof(ChainHdr) % 16 == 0, "ChainHdr alignment");
 

@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsign
       const int tie = (de_f >= -bound) && (fabsf(pf - u) <= pf * (1.5f * bound * H.kTinvf) + 1e-6f);
       double e_old, e_new;
       if (tie) {
-        if (w == 0) stage_chain_f64(H, s, mi, lane);
+        if (w == 0) stage_chain_f64(P, H, s, mi, lane);
         g.sync();
         double eo = 0.0, en = 0.0, ab2 = 0.0;
         long long np2 = 0;

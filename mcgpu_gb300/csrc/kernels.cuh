@@ -352,12 +352,22 @@ __device__ __forceinline__ void batch_ff(const Pool& P, const ChainHdr& H, const
       const int jf = rj[(head + e) & (kRing - 1)];
       const int j = jf >> 4;
       f = jf & 15;
-      b0 = P.mstart[j];
-      const int lw = P.mlen[j];
+      float mrj;
+      if (!LO && H.uniform) {
+        // uniform chain: the neighbour's rows follow from its index
+        b0 = H.atom0 + (j - H.mol0) * H.ulen;
+        lenj = H.ulen;
+        actj = H.uact;
+        mrj = H.umrad;
+      } else {
+        b0 = P.mstart[j];
+        const int lw = P.mlen[j];
+        lenj = lw & 255;
+        actj = lw >> 8;
+        mrj = P.mrad[j];
+      }
       const uint4 fj = P.mfix[j];
-      const float rr = mi.rad + P.mrad[j];
-      lenj = lw & 255;
-      actj = lw >> 8;
+      const float rr = mi.rad + mrj;
       if (f & kInOld) {
         if (PRECISE) fixdiff_ff(fj, mi.fx_old, H, Do, Dol); else Do = fixdiff(fj, mi.fx_old, H);
         if (needs_wrap(Do, rr, H)) f |= kWrapOld;
