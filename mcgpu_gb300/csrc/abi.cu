@@ -136,6 +136,11 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
     }
     if (!simple || s != m * u_len || len != u_len || act != u_act || an - s != u_prim)
       uniform = false;
+    // the same species: identical parameters slot by slot
+    for (int k = 0; uniform && k < len; k++)
+      if (d->sigma[s + k] != d->sigma[k] || d->epsilon[s + k] != d->epsilon[k] ||
+          d->charge[s + k] != d->charge[k])
+        uniform = false;
     u_mrad = std::max(u_mrad, hp.mrad.back());
   }
   hp.atom_mol.resize(hp.x.size(), -1);

@@ -178,6 +178,7 @@ __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const G
   // (short, in cell order): warp w takes every nw-th entry, so every warp
   // gets its share of the in-range neighbours
   const int rounds = cand ? (c_end - c_begin + 32 * nw - 1) / (32 * nw) : 0;
+  const bool u1 = H.uniform && T == 1 && H.ulen <= 4 && !H.precise;
   for (int it = 0;; it++) {
     int idx;
     if (cand) {
@@ -205,7 +206,9 @@ __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const G
     tail += __popc(bal);
     if (tail - head >= 32) {
       __syncwarp();
-      if (H.precise)
+      if (u1)
+        batch_u1(P, H, s, mi, rj, head, 32, w, lane, acc);
+      else if (H.precise)
         batch_ff<true, false>(P, H, s, mi, rj, head, 32, lane, T, acc);
       else
         batch_ff<false, false>(P, H, s, mi, rj, head, 32, lane, T, acc);
@@ -215,7 +218,9 @@ __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const G
   }
   __syncwarp();
   if (tail > head) {
-    if (H.precise)
+    if (u1)
+      batch_u1(P, H, s, mi, rj, head, tail - head, w, lane, acc);
+    else if (H.precise)
       batch_ff<true, false>(P, H, s, mi, rj, head, tail - head, lane, T, acc);
     else
       batch_ff<false, false>(P, H, s, mi, rj, head, tail - head, lane, T, acc);

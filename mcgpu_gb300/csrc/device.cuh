@@ -88,9 +88,10 @@ struct __align__(16) ChainHdr {
   int vol_fp64;         // volume decisions re-taken with FP64 pairs
   int vncell[3];        // cells per edge of the volume move in flight
   int pad8;
-  // uniform chain: every molecule ulen atoms (uact active) laid out
-  // contiguously from atom0, one primary at slot uprim, radius <= umrad:
-  // atom and primary indexes follow from the molecule index (no loads)
+  // uniform chain: one species (every molecule ulen atoms, uact active, the
+  // same parameters slot by slot) laid out contiguously from atom0, one
+  // primary at slot uprim, radius <= umrad: atom and primary indexes and
+  // pair factors follow from the molecule index (no loads)
   int uniform, ulen, uact, uprim;
   float umrad, pad9, pad10, pad11;
 };
@@ -373,6 +374,8 @@ struct GroupSmem {
   double* miscd;                        // [32] broadcast doubles
   float4* pc;                           // [cache_n] screen positions of the chain (or null)
   void* props;                          // [32] drawn moves of the next steps (chain kernel)
+  float4* nbuf;                         // [nwarps * 32 * 5] per-lane neighbour rows (async copies)
+  float2* teq;                          // [maxA] pair factors per slot of a uniform chain
 };
 
 struct SmemShape {
@@ -394,6 +397,8 @@ struct SmemShape {
     b += align16(32 * 8);
     b += align16(cache_n * 16);
     b += align16(32 * kPropBytes);
+    b += align16(nwarps * 32 * 5 * 16);
+    b += align16(maxA * 8);
     return b;
   }
   __device__ GroupSmem carve(char* base) const {
@@ -418,6 +423,10 @@ struct SmemShape {
     s.pc = cache_n > 0 ? (float4*)p : nullptr;
     p += align16(cache_n * 16);
     s.props = (void*)p;
+    p += align16(32 * kPropBytes);
+    s.nbuf = (float4*)p;
+    p += align16(nwarps * 32 * 5 * 16);
+    s.teq = (float2*)p;
     return s;
   }
 };

@@ -294,7 +294,7 @@ __global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol
 // recorded at trace[c * trace_stride + trace_off + st].  Warp 0 draws the
 // moves of 32 steps at once (one per lane) into shared memory.  lanes_cap >
 // 0 caps the lanes per neighbour molecule of every chain.
-__global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsigned* queue,
+__global__ void __launch_bounds__(256, 2) k_chain_steps(Pool P, int n_steps, unsigned* queue,
                                                      const int* order, int n_tasks, int gwarps,
                                                      SmemShape shape, mcgpu_trace* trace,
                                                      int trace_off, int trace_stride,
@@ -317,6 +317,8 @@ __global__ void __launch_bounds__(256) k_chain_steps(Pool P, int n_steps, unsign
     if (pcache)
       for (int i = g.tid; i < H.n_mol; i += gsize) pcache[i] = P.ppos[H.pidx0 + i];
     if (g.tid == 0) s.misc[kMiscNlOk] = (H.nl_on && H.nl_valid) ? 1 : 0;
+    if (H.uniform)
+      for (int i = g.tid; i < H.ulen; i += gsize) s.teq[i] = P.aeq[H.atom0 + i];
     g.sync();
     int full_scans = 0;
     double energy = H.energy;

@@ -430,6 +430,78 @@ __device__ __forceinline__ void batch_ff(const Pool& P, const ChainHdr& H, const
   }
 }
 
+// Asynchronous global -> shared copies (cp.async): the data lands in shared
+// memory without passing through registers; each thread waits for its own.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// batch_ff with one lane per entry (T = 1) for a uniform chain of molecules
+// of at most 4 atoms: the entry's anchor and atom offsets follow from the
+// neighbour index, so each lane requests all of them at once with async
+// copies into its own shared-memory slot (one round trip to L2 instead of
+// one per atom, no registers held), and the pair factors come from the
+// chain's per-slot template.  The atoms are summed in batch_ff's order: the
+// sums are batch_ff's bit for bit.
+__device__ __forceinline__ void batch_u1(const Pool& P, const ChainHdr& H, const GroupSmem& s,
+                                         const MovedInfo& mi, const int* rj, int head, int count,
+                                         int w, int lane, AccFF& acc) {
+  if (lane >= count) return;  // lanes are independent: no shuffles below
+  const int jf = rj[(head + lane) & (kRing - 1)];
+  const int j = jf >> 4;
+  int f = jf & 15;
+  const int b0 = H.atom0 + (j - H.mol0) * H.ulen;
+  const int lenj = H.ulen;
+  float4* nb = s.nbuf + (w * 32 + lane) * 5;
+  cp_async16(nb + 4, P.mfix + j);
+  for (int k = 0; k < lenj; k++) cp_async16(nb + k, P.aoff + b0 + k);
+  cp_async_wait_all();
+  const uint4 fj = *reinterpret_cast<const uint4*>(nb + 4);
+  const float rr = mi.rad + H.umrad;
+  float3 Do = make_float3(0.f, 0.f, 0.f), Dn = Do;
+  const float3 z3 = Do;
+  if (f & kInOld) {
+    Do = fixdiff(fj, mi.fx_old, H);
+    if (needs_wrap(Do, rr, H)) f |= kWrapOld;
+  }
+  if (f & kInNew) {
+    Dn = fixdiff(fj, mi.fx_new, H);
+    if (needs_wrap(Dn, rr, H)) f |= kWrapNew;
+  }
+  float so = 0.f, sn = 0.f, sa = 0.f;
+  for (int k = 0; k < lenj; k++) {
+    const float4 ob = nb[k];
+    const float2 qb = s.teq[k];
+    if (f & kInOld) {
+      const float3 bh = make_float3(Do.x + ob.x, Do.y + ob.y, Do.z + ob.z);
+      so += (f & kWrapOld)
+                ? sum_moved32_wrap<false>(s.o_old, s.l_old, s.eq, mi.len, bh, z3, ob.w, qb, H, sa)
+                : sum_moved32_cf<false>(s.o_old, s.l_old, s.eq, mi.len, false, bh, z3, ob.w, qb,
+                                        mi.qm, sa);
+    }
+    if (f & kInNew) {
+      const float3 bh = make_float3(Dn.x + ob.x, Dn.y + ob.y, Dn.z + ob.z);
+      sn += (f & kWrapNew)
+                ? sum_moved32_wrap<false>(s.o_new, s.l_new, s.eq, mi.len, bh, z3, ob.w, qb, H, sa)
+                : sum_moved32_cf<false>(s.o_new, s.l_new, s.eq, mi.len, true, bh, z3, ob.w, qb,
+                                        mi.qm, sa);
+    }
+  }
+  if (f & kInOld) {
+    ff_add(acc.oh, acc.ol, so);
+    acc.np += (long long)mi.act * H.uact;
+  }
+  if (f & kInNew) {
+    ff_add(acc.nh, acc.nl, sn);
+    acc.np += (long long)mi.act * H.uact;
+  }
+  acc.ab += sa;
+}
+
 // FP64 pair terms from the master rows, the reference's per-pair minimum
 // image and dummy-site rule (BruteForceStep.cpp:61-76).
 __device__ __forceinline__ double sum_moved64(const GroupSmem& s, bool use_new, int len, double xb,
