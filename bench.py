@@ -420,7 +420,7 @@ def main():
         bt.set_tile(*[int(v) for v in args.tile.split(",")])
         tile = bt.tile
     else:
-        tile = bt.autotune(64) if not args.no_autotune else bt.tile
+        tile = bt.autotune(128) if not args.no_autotune else bt.tile
     threads, cpc, spl, lanes = tile
     launches_per_step = math.ceil(STEPS_PER_BENCH / spl)
 

@@ -1246,81 +1246,68 @@ extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
   if (rc) return rc;
   const long long steps0 = bt->steps_done;
   struct Tile { int threads, cpc, spl, lanes; };
-  std::vector<Tile> cands;
-  const int tw[] = {64, 128, 256};
-  for (int t : tw)
-    for (int gw = 1; gw <= t / 32; gw *= 2) {
-      const int cpc = (t / 32) / gw;
-      if (gw > 1 && cpc > 15) continue;
-      cands.push_back({t, cpc, 16, 0});
-    }
   cudaEvent_t e0, e1;
   CK(ctx, cudaEventCreate(&e0));
   CK(ctx, cudaEventCreate(&e1));
-  float best = 1e30f;
-  Tile bestT = {bt->threads, bt->cpc, bt->spl, bt->lanes};
-  for (const Tile& T : cands) {
-    if (mcgpu_batch_set_tile(bt, T.threads, T.cpc, T.spl, T.lanes) != MCGPU_OK) continue;
-    rc = batch_snapshot(bt, true);
-    if (rc) break;
+  // time of trial_steps steps with tile T from the saved state: the faster
+  // of two timed runs after a warm-up launch (per-step cost, so runs longer
+  // than trial_steps are scaled)
+  auto trial = [&](const Tile& T, float* out) -> int {
+    *out = 1e30f;
+    if (mcgpu_batch_set_tile(bt, T.threads, T.cpc, T.spl, T.lanes) != MCGPU_OK) return MCGPU_OK;
+    int r = batch_snapshot(bt, true);
+    if (r) return r;
     bt->steps_done = steps0;
-    rc = mcgpu_batch_run(bt, T.spl, 0);  // warm-up
-    if (rc) break;
-    CK(ctx, cudaEventRecord(e0, ctx->stream));
-    rc = mcgpu_batch_run(bt, trial_steps, 0);
-    if (rc) break;
-    CK(ctx, cudaEventRecord(e1, ctx->stream));
-    CK(ctx, cudaEventSynchronize(e1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best) {
-      best = ms;
-      bestT = T;
+    r = mcgpu_batch_run(bt, T.spl, 0);
+    if (r) return r;
+    const int n = std::max(trial_steps, 2 * T.spl);
+    for (int rep = 0; rep < 2; rep++) {
+      CK(ctx, cudaEventRecord(e0, ctx->stream));
+      r = mcgpu_batch_run(bt, n, 0);
+      if (r) return r;
+      CK(ctx, cudaEventRecord(e1, ctx->stream));
+      CK(ctx, cudaEventSynchronize(e1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      *out = std::min(*out, ms * (float)trial_steps / (float)n);
     }
-  }
+    return MCGPU_OK;
+  };
+  float best = 1e30f, ms = 0;
+  Tile bestT = {bt->threads, bt->cpc, bt->spl, bt->lanes};
+  // CTA shape (threads, chains per CTA) with the default lanes
+  const int tw[] = {64, 128, 256};
+  for (int t : tw)
+    for (int gw = 1; gw <= t / 32 && rc == MCGPU_OK; gw *= 2) {
+      const int cpc = (t / 32) / gw;
+      if (gw > 1 && cpc > 15) continue;
+      const Tile T = {t, cpc, 16, 0};
+      rc = trial(T, &ms);
+      if (rc == MCGPU_OK && ms < best) {
+        best = ms;
+        bestT = T;
+      }
+    }
   // lanes per neighbour molecule for the best shape
   int max_tpm = 1;
   for (const ChainHdr& h : bt->pool.hdr) max_tpm = std::max(max_tpm, h.tpm);
   for (int lanes = 1; lanes < max_tpm && rc == MCGPU_OK; lanes <<= 1) {
-    if (mcgpu_batch_set_tile(bt, bestT.threads, bestT.cpc, bestT.spl, lanes) != MCGPU_OK) continue;
-    rc = batch_snapshot(bt, true);
-    if (rc) break;
-    bt->steps_done = steps0;
-    rc = mcgpu_batch_run(bt, bestT.spl, 0);
-    if (rc) break;
-    CK(ctx, cudaEventRecord(e0, ctx->stream));
-    rc = mcgpu_batch_run(bt, trial_steps, 0);
-    if (rc) break;
-    CK(ctx, cudaEventRecord(e1, ctx->stream));
-    CK(ctx, cudaEventSynchronize(e1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best) {
+    const Tile T = {bestT.threads, bestT.cpc, bestT.spl, lanes};
+    rc = trial(T, &ms);
+    if (rc == MCGPU_OK && ms < best) {
       best = ms;
-      bestT.lanes = lanes;
+      bestT = T;
     }
   }
   // steps per launch for the best shape
   const int spls[] = {4, 16, 64};
   for (int spl : spls) {
     if (rc) break;
-    if (mcgpu_batch_set_tile(bt, bestT.threads, bestT.cpc, spl, bestT.lanes) != MCGPU_OK) continue;
-    rc = batch_snapshot(bt, true);
-    if (rc) break;
-    bt->steps_done = steps0;
-    rc = mcgpu_batch_run(bt, spl, 0);
-    if (rc) break;
-    CK(ctx, cudaEventRecord(e0, ctx->stream));
-    rc = mcgpu_batch_run(bt, std::max(trial_steps, 2 * spl), 0);
-    if (rc) break;
-    CK(ctx, cudaEventRecord(e1, ctx->stream));
-    CK(ctx, cudaEventSynchronize(e1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e0, e1);
-    ms *= (float)trial_steps / (float)std::max(trial_steps, 2 * spl);
-    if (ms <= best) {
+    const Tile T = {bestT.threads, bestT.cpc, spl, bestT.lanes};
+    rc = trial(T, &ms);
+    if (rc == MCGPU_OK && ms <= best) {
       best = ms;
-      bestT.spl = spl;
+      bestT = T;
     }
   }
   cudaEventDestroy(e0);

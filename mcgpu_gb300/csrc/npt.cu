@@ -543,8 +543,7 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
   __shared__ float2 sq[kMaxA];
   __shared__ int spa[kMaxP];
   __shared__ VolBox vb[2];
-  __shared__ double2 red[kVolThreads];
-  __shared__ double2 rab[kVolThreads];
+  __shared__ float wred[kVolWarps][6];
   __shared__ VcStencil S;
   __shared__ int ent[kVolChunk];
   __shared__ int wcnt[kVolWarps], woff[kVolWarps + 1];
@@ -626,21 +625,31 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
     }
     __syncthreads();
   }
-  red[threadIdx.x] = make_double2((double)eh[0] + (double)el[0], (double)eh[1] + (double)el[1]);
-  rab[threadIdx.x] = make_double2((double)ab[0], (double)ab[1]);
-  __syncthreads();
-  for (int off = blockDim.x >> 1; off > 0; off >>= 1) {
-    if ((int)threadIdx.x < off) {
-      red[threadIdx.x].x += red[threadIdx.x + off].x;
-      red[threadIdx.x].y += red[threadIdx.x + off].y;
-      rab[threadIdx.x].x += rab[threadIdx.x + off].x;
-      rab[threadIdx.x].y += rab[threadIdx.x + off].y;
+  // double-float reduction (warp butterflies, then the warps in order); one
+  // conversion to FP64 per molecule
+  for (int off = 16; off > 0; off >>= 1) {
+    for (int w = 0; w < 2; w++) {
+      const float h = __shfl_xor_sync(~0u, eh[w], off), l = __shfl_xor_sync(~0u, el[w], off);
+      ff_add2(eh[w], el[w], h, l);
+      ab[w] += __shfl_xor_sync(~0u, ab[w], off);
     }
-    __syncthreads();
   }
+  if ((threadIdx.x & 31) == 0) {
+    const int wi = threadIdx.x >> 5;
+    wred[wi][0] = eh[0]; wred[wi][1] = el[0]; wred[wi][2] = eh[1];
+    wred[wi][3] = el[1]; wred[wi][4] = ab[0]; wred[wi][5] = ab[1];
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    emol2[m] = red[0];
-    eabs2[m] = rab[0];
+    float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, a0 = 0.f, a1 = 0.f;
+    for (int wi = 0; wi < kVolWarps; wi++) {
+      ff_add2(h0, l0, wred[wi][0], wred[wi][1]);
+      ff_add2(h1, l1, wred[wi][2], wred[wi][3]);
+      a0 += wred[wi][4];
+      a1 += wred[wi][5];
+    }
+    emol2[m] = make_double2((double)h0 + (double)l0, (double)h1 + (double)l1);
+    eabs2[m] = make_double2((double)a0, (double)a1);
   }
 }
 
