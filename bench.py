@@ -44,7 +44,7 @@ FP32_FLOPS_PER_PAIR = 38   # per atom pair, fixed by convention from the referen
 # measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, 3 launches
 # after 6 warm-up launches, L2 flushed between bench steps), by tile
 # (threads, chains per CTA, steps per launch, lanes per molecule).
-CHAIN_TRAFFIC_BYTES = {(256, 1, 64, 1): 49.96e6}
+CHAIN_TRAFFIC_BYTES = {(256, 1, 64, 1): 33.57e6}
 
 
 def peaks():
