@@ -251,6 +251,20 @@ int mcgpu_batch_stats(mcgpu_batch* batch, mcgpu_chain_stats* stats);
 /* Coordinates of chain c (arrays sized like its descriptor). */
 int mcgpu_batch_download(mcgpu_batch* batch, int chain, double* x, double* y,
                          double* z);
+/* Checkpoint of a batch: the resumable device state (coordinates, anchors,
+ * orientations, screen positions, every chain header with its running
+ * energy, counters and Philox step counter, the Verlet lists, the NPT
+ * phase) as an opaque host blob.  With buf == NULL only *used is set (the
+ * size).  The reference's resumable state is the text .state file
+ * (StateScanner::outputState, StateScanner.cpp:545-597, read back by
+ * loadBoxData, FileUtilities.cpp:119-163), which keeps six significant
+ * digits and restarts the RNG from the seed; this blob resumes bit for bit. */
+int mcgpu_batch_checkpoint(mcgpu_batch* batch, void* buf, size_t cap, size_t* used);
+/* Restores a checkpoint into a batch created from the same boxes, with the
+ * same Verlet skin and NPT interval set; the batch then continues exactly
+ * as the checkpointed one would have.  MCGPU_ERR_INVALID for a blob of
+ * another layout or settings (nothing is changed then). */
+int mcgpu_batch_restore(mcgpu_batch* batch, const void* buf, size_t len);
 /* Recomputes every chain's total energy from scratch (FP64 accumulate) into
  * out[n_chains]; the running totals are not changed. */
 int mcgpu_batch_system_energy(mcgpu_batch* batch, double* out);

@@ -114,6 +114,21 @@ class ChainBatch:
                                                     y.ctypes.data_as(dp), z.ctypes.data_as(dp)))
         return x, y, z
 
+    def checkpoint(self) -> bytes:
+        """The batch's resumable device state (chain states with their
+        Philox counters, coordinates, Verlet lists, NPT phase) as bytes."""
+        n = C.c_size_t()
+        self._check(_abi.lib().mcgpu_batch_checkpoint(self._h, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        self._check(_abi.lib().mcgpu_batch_checkpoint(self._h, buf, n, C.byref(n)))
+        return buf.raw[:n.value]
+
+    def restore(self, blob: bytes) -> None:
+        """Continues from a checkpoint of a batch built from the same boxes
+        (set the same Verlet skin and NPT interval first)."""
+        buf = C.create_string_buffer(bytes(blob), len(blob))
+        self._check(_abi.lib().mcgpu_batch_restore(self._h, buf, len(blob)))
+
     def system_energies(self) -> np.ndarray:
         out = np.empty(self.n_chains)
         self._check(_abi.lib().mcgpu_batch_system_energy(

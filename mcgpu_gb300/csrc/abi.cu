@@ -1212,22 +1212,152 @@ extern "C" int mcgpu_batch_system_energy(mcgpu_batch* bt, double* out) {
   return MCGPU_OK;
 }
 
-// ---- autotuner ---------------------------------------------------------------------
+// ---- checkpoint / restore -----------------------------------------------------------
 
-// Device state a run changes: coordinates and mirrors of all atoms, the
-// molecule anchors, the screen positions and the chain headers.
-static int batch_snapshot(mcgpu_batch* bt, bool restore) {
+namespace {
+
+struct CkptHead {
+  char magic[8];
+  uint32_t version, n_chains, n_mol, n_atom, n_pidx, nl_stride, nl_on, vol_interval;
+  int64_t steps_done;
+  uint64_t layout, payload, checksum, hdr_bytes;
+};
+constexpr char kCkptMagic[8] = {'M', 'C', 'G', 'P', 'U', 'C', 'K', '1'};
+
+uint64_t fnv1a(uint64_t h, const void* p, size_t n) {
+  const unsigned char* b = (const unsigned char*)p;
+  for (size_t i = 0; i < n; i++) h = (h ^ b[i]) * 1099511628211ull;
+  return h;
+}
+
+// Pool layout a checkpoint belongs to: molecule ranges and chain offsets.
+uint64_t pool_layout(const DevPool& dp) {
+  uint64_t h = 1469598103934665603ull;
+  h = fnv1a(h, dp.mstart.data(), dp.mstart.size() * sizeof(int));
+  h = fnv1a(h, dp.mlen.data(), dp.mlen.size() * sizeof(int));
+  for (const ChainHdr& c : dp.hdr) {
+    const int v[] = {c.atom0, c.mol0, c.pidx0, c.n_mol, c.n_atom, c.n_pidx, c.max_len};
+    h = fnv1a(h, v, sizeof(v));
+  }
+  return h;
+}
+
+struct CkptRow {
+  void* p;
+  size_t bytes;
+};
+
+// Device rows a run changes, in blob order.
+std::vector<CkptRow> ckpt_rows(const DevPool& dp) {
+  std::vector<CkptRow> r = {
+      {dp.P.x, 8ull * dp.n_atom},     {dp.P.y, 8ull * dp.n_atom},
+      {dp.P.z, 8ull * dp.n_atom},     {dp.P.aoff, 16ull * dp.n_atom},
+      {dp.P.mfix, 16ull * dp.n_mol},  {dp.P.mq, 16ull * dp.n_mol},
+      {dp.P.ppos, 16ull * dp.n_pidx}, {dp.P.hdr, sizeof(ChainHdr) * (size_t)dp.n_chains}};
+  if (dp.nl_on) {
+    r.push_back({dp.P.nl, 4ull * dp.n_mol * (size_t)dp.P.nl_stride});
+    r.push_back({dp.P.nl_cnt, 4ull * dp.n_mol});
+    r.push_back({dp.P.pbuild, 16ull * dp.n_pidx});
+  }
+  return r;
+}
+
+}  // namespace
+
+extern "C" int mcgpu_batch_checkpoint(mcgpu_batch* bt, void* buf, size_t cap, size_t* used) {
+  if (!bt || !used) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
   mcgpu_ctx* ctx = bt->ctx;
   DevPool& dp = bt->pool;
-  struct Row { void* p; size_t bytes; } rows[] = {
-      {dp.P.x, 8ull * dp.n_atom}, {dp.P.y, 8ull * dp.n_atom}, {dp.P.z, 8ull * dp.n_atom},
-      {dp.P.aoff, 16ull * dp.n_atom}, {dp.P.mfix, 16ull * dp.n_mol}, {dp.P.ppos, 16ull * dp.n_pidx},
-      {dp.P.mq, 16ull * dp.n_mol},
-      {dp.P.hdr, sizeof(ChainHdr) * (size_t)dp.n_chains}};
-  const int nr = (int)(sizeof(rows) / sizeof(rows[0]));
-  if (bt->snap.empty()) {
+  const std::vector<CkptRow> rows = ckpt_rows(dp);
+  size_t payload = 0;
+  for (const CkptRow& r : rows) payload += r.bytes;
+  *used = sizeof(CkptHead) + payload;
+  if (!buf) return MCGPU_OK;
+  if (cap < *used)
+    return set_err(ctx, MCGPU_ERR_INVALID, "checkpoint needs %zu bytes, buffer has %zu", *used, cap);
+  if (bt->rows_stale) {
+    int rc = pool_chain_export(ctx, dp, ctx->stream);
+    if (rc) return rc;
+    bt->rows_stale = false;
+  }
+  char* out = (char*)buf + sizeof(CkptHead);
+  for (const CkptRow& r : rows) {
+    CK(ctx, cudaMemcpyAsync(out, r.p, r.bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    out += r.bytes;
+  }
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  CkptHead h{};
+  std::memcpy(h.magic, kCkptMagic, 8);
+  h.version = 1;
+  h.n_chains = (uint32_t)dp.n_chains;
+  h.n_mol = (uint32_t)dp.n_mol;
+  h.n_atom = (uint32_t)dp.n_atom;
+  h.n_pidx = (uint32_t)dp.n_pidx;
+  h.nl_stride = dp.nl_on ? (uint32_t)dp.P.nl_stride : 0u;
+  h.nl_on = dp.nl_on ? 1u : 0u;
+  h.vol_interval = (uint32_t)bt->vol_interval;
+  h.steps_done = bt->steps_done;
+  h.layout = pool_layout(dp);
+  h.payload = payload;
+  h.hdr_bytes = sizeof(ChainHdr);
+  h.checksum = fnv1a(1469598103934665603ull, (const char*)buf + sizeof(CkptHead), payload);
+  std::memcpy(buf, &h, sizeof(h));
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_batch_restore(mcgpu_batch* bt, const void* buf, size_t len) {
+  if (!bt || !buf) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = bt->ctx;
+  DevPool& dp = bt->pool;
+  CkptHead h;
+  if (len < sizeof(h)) return set_err(ctx, MCGPU_ERR_INVALID, "checkpoint too short");
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1)
+    return set_err(ctx, MCGPU_ERR_INVALID, "not a checkpoint of this library");
+  if (h.hdr_bytes != sizeof(ChainHdr) || h.n_chains != (uint32_t)dp.n_chains ||
+      h.n_mol != (uint32_t)dp.n_mol || h.n_atom != (uint32_t)dp.n_atom ||
+      h.n_pidx != (uint32_t)dp.n_pidx || h.layout != pool_layout(dp))
+    return set_err(ctx, MCGPU_ERR_INVALID, "checkpoint of another batch layout");
+  if (h.nl_on != (dp.nl_on ? 1u : 0u) || (dp.nl_on && h.nl_stride != (uint32_t)dp.P.nl_stride))
+    return set_err(ctx, MCGPU_ERR_INVALID,
+                   "checkpoint Verlet setting differs (set the same skin before restoring)");
+  if (h.vol_interval != (uint32_t)bt->vol_interval)
+    return set_err(ctx, MCGPU_ERR_INVALID,
+                   "checkpoint NPT interval %u, batch %d (set_npt before restoring)",
+                   h.vol_interval, bt->vol_interval);
+  const std::vector<CkptRow> rows = ckpt_rows(dp);
+  size_t payload = 0;
+  for (const CkptRow& r : rows) payload += r.bytes;
+  if (h.payload != payload || len < sizeof(h) + payload)
+    return set_err(ctx, MCGPU_ERR_INVALID, "checkpoint payload size mismatch");
+  const char* in = (const char*)buf + sizeof(h);
+  if (fnv1a(1469598103934665603ull, in, payload) != h.checksum)
+    return set_err(ctx, MCGPU_ERR_INVALID, "checkpoint checksum mismatch");
+  for (const CkptRow& r : rows) {
+    CK(ctx, cudaMemcpyAsync(r.p, in, r.bytes, cudaMemcpyHostToDevice, ctx->stream));
+    in += r.bytes;
+  }
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  bt->steps_done = h.steps_done;
+  bt->rows_stale = false;
+  return MCGPU_OK;
+}
+
+// ---- autotuner ---------------------------------------------------------------------
+
+// Device-side copy of the rows a checkpoint holds (the Verlet lists
+// included, so a restored batch never screens with lists of another state).
+static int batch_snapshot(mcgpu_batch* bt, bool restore) {
+  mcgpu_ctx* ctx = bt->ctx;
+  const std::vector<CkptRow> rows = ckpt_rows(bt->pool);
+  const int nr = (int)rows.size();
+  if (!restore) {
+    for (void* p : bt->snap)
+      if (p) cudaFree(p);
     bt->snap.assign(nr, nullptr);
     for (int r = 0; r < nr; r++) CK(ctx, cudaMalloc(&bt->snap[r], rows[r].bytes));
+  } else if ((int)bt->snap.size() != nr) {
+    return set_err(ctx, MCGPU_ERR_INVALID, "snapshot taken with other Verlet settings");
   }
   for (int r = 0; r < nr; r++) {
     if (restore)

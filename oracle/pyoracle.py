@@ -325,6 +325,13 @@ class RefHarness:
             "ref_wrap_all": (None, []),
             "ref_get_coords": (None, [_dp, _dp, _dp]),
             "ref_run_plain": (C.c_double, [C.c_int, C.c_double, C.POINTER(C.c_int)]),
+            "ref_load": (C.c_int, [C.c_char_p] + [C.POINTER(C.c_int)] * 3
+                         + [C.POINTER(C.c_long)] * 2),
+            "ref_load_rows": (None, [_dp] * 6 + [_ip] * 6 + [_dp, _dp]),
+            "ref_load_lrc": (C.c_double, []),
+            "ref_load_seed": (C.c_int, []),
+            "ref_load_write_state": (None, [C.c_char_p, C.c_int]),
+            "ref_load_set_coords": (None, [_dp, _dp, _dp]),
         }
         for name, (res, args) in protos.items():
             fn = getattr(L, name)
@@ -346,6 +353,49 @@ class RefHarness:
                               size.ctypes.data_as(_dp), b.cutoff, b.temperature,
                               b.max_translate, b.max_rotate)
         self.n_atom = b.n_atom
+
+    def load_files(self, path: str) -> dict:
+        """The reference's own loader on a .config or .state (run from the
+        file's directory, as metrosim resolves the paths inside it):
+        the SimBox rows it builds, its LRC, seed, start step and steps."""
+        nm, na, npi = C.c_int(), C.c_int(), C.c_int()
+        st, n = C.c_long(), C.c_long()
+        cwd = os.getcwd()
+        d, f = os.path.split(os.path.abspath(path))
+        os.chdir(d)
+        try:
+            rc = self.L.ref_load(f.encode(), C.byref(nm), C.byref(na), C.byref(npi),
+                                 C.byref(st), C.byref(n))
+        finally:
+            os.chdir(cwd)
+        if rc:
+            raise RuntimeError("the reference could not load " + path)
+        na_, nm_ = na.value, nm.value
+        out = {k: np.empty(na_) for k in ("x", "y", "z", "sigma", "epsilon", "charge")}
+        out.update({k: np.empty(nm_, np.int32) for k in ("mol_start", "mol_len", "mol_type",
+                                                         "mol_pidx_start", "mol_pidx_count")})
+        out["pidx"] = np.empty(npi.value, np.int32)
+        out["size"] = np.empty(3)
+        out["params"] = np.empty(5)
+        self.L.ref_load_rows(*(out[k].ctypes.data_as(_dp) for k in
+                               ("x", "y", "z", "sigma", "epsilon", "charge")),
+                             *(out[k].ctypes.data_as(_ip) for k in
+                               ("mol_start", "mol_len", "mol_type", "mol_pidx_start",
+                                "mol_pidx_count", "pidx")),
+                             out["size"].ctypes.data_as(_dp), out["params"].ctypes.data_as(_dp))
+        out["lrc"] = self.L.ref_load_lrc()
+        out["seed"] = self.L.ref_load_seed()
+        out["start_step"] = st.value
+        out["steps"] = n.value
+        return out
+
+    def write_loaded_state(self, path: str, step: int, xyz=None) -> None:
+        """StateScanner::outputState of the loaded box, at its own
+        coordinates or at xyz (n_atom x 3)."""
+        if xyz is not None:
+            c = [np.ascontiguousarray(xyz[:, k], dtype=np.float64) for k in range(3)]
+            self.L.ref_load_set_coords(*(v.ctypes.data_as(_dp) for v in c))
+        self.L.ref_load_write_state(os.path.abspath(path).encode(), int(step))
 
     def coords(self) -> np.ndarray:
         x, y, z = np.empty(self.n_atom), np.empty(self.n_atom), np.empty(self.n_atom)

@@ -10,15 +10,24 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "Metropolis/Box.h"
 #include "Metropolis/BruteForceStep.h"
 #include "Metropolis/GPUCopy.h"
+#include "Metropolis/SerialSim/SerialCalcs.h"
 #include "Metropolis/SimBox.h"
+#include "Metropolis/SimBoxBuilder.h"
+#include "Metropolis/SimulationArgs.h"
 #include "Metropolis/SimulationStep.h"
+#include "Metropolis/Utilities/FileUtilities.h"
 #include "Metropolis/Utilities/MathLibrary.h"
 
 namespace {
 SimBox* g_sb = nullptr;
 BruteForceStep* g_step = nullptr;
+// ref_load: the reference's Box and the SimBox built from it
+Box* g_lbox = nullptr;
+SimBox* g_lsb = nullptr;
+long g_lstart = 0, g_lsteps = 0;
 
 template <class T>
 T* copy_row(const T* src, int n) {
@@ -196,6 +205,94 @@ double ref_run_plain(int steps, double e0, int* accepted) {
   }
   if (accepted) *accepted = acc;
   return e;
+}
+
+// ---- the reference's own file pipeline ---------------------------------------
+//
+// Loads a .config (z-matrix + OPLS table on the FCC lattice) or a .state
+// exactly as Simulation's constructor and run() do before the first step:
+// SerialCalcs::createBox -> loadBoxData (FileUtilities.cpp:19-168), then
+// Box::keepMoleculeInBox for every molecule (Simulation.cpp:70-72) and
+// SimBoxBuilder::build (Simulation.cpp:118-121).  Returns 0 on success and
+// the counts of the built SimBox.
+int ref_load(const char* path, int* n_mol, int* n_atom, int* n_pidx, long* start_step,
+             long* steps) {
+  SimulationArgs args = SimulationArgs();
+  args.filePath = path;
+  std::string p(path);
+  const std::string ext = p.substr(p.find_last_of('.') + 1);
+  args.fileType = ext == "config" ? InputFile::Configuration
+                : ext == "state"  ? InputFile::State
+                                  : InputFile::Unknown;
+  args.strategy = Strategy::Default;
+  SBScanner* sbs = new SBScanner();
+  long st = 0, n = 0;
+  Box* box = SerialCalcs::createBox(args, &st, &n, sbs);
+  if (!box) return 1;
+  for (int m = 0; m < box->environment->numOfMolecules; m++) box->keepMoleculeInBox(m);
+  SimBoxBuilder builder = SimBoxBuilder(false, sbs);
+  g_lbox = box;
+  g_lsb = builder.build(box);
+  g_lstart = st;
+  g_lsteps = n;
+  *n_mol = g_lsb->numMolecules;
+  *n_atom = g_lsb->numAtoms;
+  *n_pidx = g_lsb->numPIdxes;
+  *start_step = st;
+  *steps = n;
+  return 0;
+}
+
+// The loaded SimBox rows (SimBox.h:120-149): coordinates, sigma/epsilon/
+// charge, molecule start/length/type/primary range, primary indexes, box
+// edges and [cutoff, temperature, kT, max translation, max rotation].
+void ref_load_rows(double* x, double* y, double* z, double* sigma, double* epsilon,
+                   double* charge, int* mol_start, int* mol_len, int* mol_type,
+                   int* mol_pidx_start, int* mol_pidx_count, int* pidx, double* size,
+                   double* params) {
+  SimBox* sb = g_lsb;
+  const int na = sb->numAtoms, nm = sb->numMolecules;
+  std::memcpy(x, sb->atomCoordinates[X_COORD], sizeof(double) * na);
+  std::memcpy(y, sb->atomCoordinates[Y_COORD], sizeof(double) * na);
+  std::memcpy(z, sb->atomCoordinates[Z_COORD], sizeof(double) * na);
+  std::memcpy(sigma, sb->atomData[ATOM_SIGMA], sizeof(double) * na);
+  std::memcpy(epsilon, sb->atomData[ATOM_EPSILON], sizeof(double) * na);
+  std::memcpy(charge, sb->atomData[ATOM_CHARGE], sizeof(double) * na);
+  std::memcpy(mol_start, sb->moleculeData[MOL_START], sizeof(int) * nm);
+  std::memcpy(mol_len, sb->moleculeData[MOL_LEN], sizeof(int) * nm);
+  std::memcpy(mol_type, sb->moleculeData[MOL_TYPE], sizeof(int) * nm);
+  std::memcpy(mol_pidx_start, sb->moleculeData[MOL_PIDX_START], sizeof(int) * nm);
+  std::memcpy(mol_pidx_count, sb->moleculeData[MOL_PIDX_COUNT], sizeof(int) * nm);
+  std::memcpy(pidx, sb->primaryIndexes, sizeof(int) * sb->numPIdxes);
+  std::memcpy(size, sb->size, sizeof(double) * 3);
+  params[0] = sb->cutoff;
+  params[1] = sb->temperature;
+  params[2] = sb->kT;
+  params[3] = sb->maxTranslate;
+  params[4] = sb->maxRotate;
+}
+
+// SerialCalcs::calcEnergy_LRC of the loaded box (SerialCalcs.cpp:37-107).
+double ref_load_lrc(void) { return SerialCalcs::calcEnergy_LRC(g_lbox); }
+
+// The loaded environment's seed (Simulation.cpp:45-50 seeds the RNG with it).
+int ref_load_seed(void) { return g_lbox->environment->randomseed; }
+
+// Sets the loaded SimBox's coordinates (e.g. to those of a trajectory the
+// harness ran on a SimBox with the same rows).
+void ref_load_set_coords(const double* x, const double* y, const double* z) {
+  const int na = g_lsb->numAtoms;
+  std::memcpy(g_lsb->atomCoordinates[X_COORD], x, sizeof(double) * na);
+  std::memcpy(g_lsb->atomCoordinates[Y_COORD], y, sizeof(double) * na);
+  std::memcpy(g_lsb->atomCoordinates[Z_COORD], z, sizeof(double) * na);
+}
+
+// StateScanner::outputState of the loaded box at the loaded SimBox
+// coordinates (Simulation.cpp:353-375).
+void ref_load_write_state(const char* path, int step) {
+  StateScanner ss = StateScanner("");
+  ss.outputState(g_lbox->getEnvironment(), g_lbox->getMolecules(), g_lbox->getMoleculeCount(),
+                 step, path, g_lsb->atomCoordinates);
 }
 
 }  // extern "C"
