@@ -987,6 +987,9 @@ static int batch_advance(mcgpu_batch* bt, int n_steps, mcgpu_trace* trace, int t
   mcgpu_ctx* ctx = bt->ctx;
   const int spl = bt->spl;
   const int iv = bt->vol_interval;
+  // graph replays do not pass through batch_launch: mark the FP64 rows
+  // stale here for every path
+  if (n_steps > 0) bt->rows_stale = true;
   if (iv <= 0) {
     const int full = n_steps / spl;
     const int per_graph = std::min(bt->max_slots, 32);

@@ -173,14 +173,14 @@ def run(argv=None, out=sys.stdout) -> RunResult | None:
                              state_dir, save_state, written, out)
     finally:
         ctx.close()
-    energy, acc, rej, coords, edges = res
+    energy, acc, rej, coords, edges, start = res
     run_time = time.perf_counter() - t0
     lrc = lrc0 * V0 / (edges[0] * edges[1] * edges[2])
     env.x, env.y, env.z = (float(v) for v in edges)
     pdb = F.pdb_path(name, pdb_dir)
     F.write_pdb(pdb, box, coords)
     written.append(pdb)
-    end = inp.start_step + steps
+    end = start + steps
     if a.state_interval >= 0:
         save_state(end, coords, edges)
     _log("\nFinished running %d steps\n" % steps, out)
@@ -195,11 +195,11 @@ def run(argv=None, out=sys.stdout) -> RunResult | None:
     _log("Acceptance Ratio: %.2f%%\n" % (100.0 * acc / max(1, acc + rej)), out)
     results = (name or "run") + ".results"
     with open(results, "w") as f:
-        f.write(F.format_results(sim_name=name, mode="GPU", start_step=inp.start_step,
+        f.write(F.format_results(sim_name=name, mode="GPU", start_step=start,
                                  steps=steps, n_molecules=env.n_molecules, energy=energy,
                                  run_time=run_time, accepted=acc, rejected=rej))
     written.append(results)
-    return RunResult(energy, lrc, acc, rej, inp.start_step, steps, tuple(edges), run_time,
+    return RunResult(energy, lrc, acc, rej, start, steps, tuple(edges), run_time,
                      written)
 
 
@@ -230,7 +230,7 @@ def _run_plain(a, ctx, inp, steps, lrc0, save_state, out):
             step.rollback(idx)
     coords = g.download()
     g.close()
-    return energy, acc, rej, coords, edges
+    return energy, acc, rej, coords, edges, start
 
 
 def _run_chain(a, ctx, inp, steps, lrc0, ensemble, vol_interval, strategy, base, state_dir,
@@ -292,7 +292,7 @@ def _run_chain(a, ctx, inp, steps, lrc0, ensemble, vol_interval, strategy, base,
         written.append(p)
     coords = bt.download(0)
     bt.close()
-    return energy, acc, rej, coords, edges
+    return energy, acc, rej, coords, edges, start
 
 
 def main(argv=None) -> int:
