@@ -245,6 +245,13 @@ int mcgpu_batch_set_npt(mcgpu_batch* batch, int interval, const double* pressure
  * Replaces the reference's VerletStep / NLCStep strategies
  * (VerletStep.cpp:119-207, NLCStep.cpp:125-243) for the chain forms. */
 int mcgpu_batch_set_verlet(mcgpu_batch* batch, double skin);
+/* Long-range LJ correction in the isobaric criterion: lrc_v[c] = E_LRC * V
+ * of chain c (kcal/mol * A^3; the correction scales as 1/V at fixed N), so a
+ * volume move adds lrc_v (1/V' - 1/V) to dU.  0 (the default) leaves it out.
+ * The reference computes E_LRC once at the start (SerialCalcs.cpp:37-107,
+ * Simulation.cpp:81) and never on a volume change.  Running energies stay
+ * pair energies; E_LRC at the current box is lrc_v / V. */
+int mcgpu_batch_set_lrc(mcgpu_batch* batch, const double* lrc_v);
 int mcgpu_box_set_verlet(mcgpu_box* box, double skin);
 int mcgpu_batch_sync(mcgpu_batch* batch);
 int mcgpu_batch_stats(mcgpu_batch* batch, mcgpu_chain_stats* stats);

@@ -81,6 +81,13 @@ class ChainBatch:
                                                    d.ctypes.data_as(dp), int(precision)))
         self.vol_interval = int(interval)
 
+    def set_lrc(self, lrc_v) -> None:
+        """Long-range LJ correction in the volume-move criterion: E_LRC * V
+        per chain (scalar or one per chain, kcal/mol * A^3; 0 = none)."""
+        v = np.broadcast_to(np.asarray(lrc_v, np.float64), (self.n_chains,)).copy()
+        self._check(_abi.lib().mcgpu_batch_set_lrc(self._h, v.ctypes.data_as(
+            C.POINTER(C.c_double))))
+
     def sync(self) -> None:
         self._check(_abi.lib().mcgpu_batch_sync(self._h))
 

@@ -1086,6 +1086,22 @@ extern "C" int mcgpu_batch_set_verlet(mcgpu_batch* bt, double skin) {
   return pool_set_verlet(bt->ctx, bt->pool, skin, bt->ctx->stream);
 }
 
+extern "C" int mcgpu_batch_set_lrc(mcgpu_batch* bt, const double* lrc_v) {
+  if (!bt || !lrc_v) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = bt->ctx;
+  const int n = bt->pool.n_chains;
+  for (int c = 0; c < n; c++)
+    if (!std::isfinite(lrc_v[c]))
+      return set_err(ctx, MCGPU_ERR_INVALID, "lrc_v[%d] is not finite", c);
+  // one strided copy into the lrc_v field of every device header
+  CK(ctx, cudaMemcpy2DAsync((char*)bt->pool.P.hdr + offsetof(ChainHdr, lrc_v), sizeof(ChainHdr),
+                            lrc_v, sizeof(double), sizeof(double), (size_t)n,
+                            cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int c = 0; c < n; c++) bt->pool.hdr[c].lrc_v = lrc_v[c];
+  return MCGPU_OK;
+}
+
 extern "C" int mcgpu_box_set_verlet(mcgpu_box* b, double skin) {
   if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
   if (!std::isfinite(skin)) return set_err(b->ctx, MCGPU_ERR_INVALID, "skin %g", skin);

@@ -65,7 +65,8 @@ struct __align__(16) ChainHdr {
                                       // rad_max: largest molecule radius
   double L[3], cutoff;
   double fxinv[3], kT;                // Angstrom -> fixed point scale
-  double max_t, max_r, energy, pad1;
+  double max_t, max_r, energy;
+  double lrc_v;                       // long-range LJ correction x volume (NPT term)
   unsigned long long seed, step;
   long long accepted, pairs;
   int error, ties, pad3, pad4;        // ties: decisions re-taken with FP64 pairs

@@ -710,7 +710,9 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
     e_new = esum[c].y;
     const double vo = H.L[0] * H.L[1] * H.L[2];
     const double vn = v.L[0] * v.L[1] * v.L[2];
-    const double arg = -((e_new - e_old) + H.pressure * (vn - vo)) / H.kT +
+    // the tail correction E_LRC = lrc_v / V changes with the volume
+    const double d_lrc = H.lrc_v / vn - H.lrc_v / vo;
+    const double arg = -((e_new - e_old) + d_lrc + H.pressure * (vn - vo)) / H.kT +
                        (double)(H.n_mol + 1) * v.dlnv;
     if (v.state == 1 && H.vol_mixed) {
       // FP32 pair terms: |error of dU| <= kTieRel * sum of term magnitudes

@@ -248,6 +248,8 @@ def _run_chain(a, ctx, inp, steps, lrc0, ensemble, vol_interval, strategy, base,
         # the reference's pressure is in kcal/mol/A^3 (SimulationStep.cpp:476-488)
         bt.set_npt(vol_interval, env.pressure / 1.4583972574259083e-05, a.max_dlnv,
                    _abi.PREC_MIXED)
+        # the tail correction follows the volume (E_LRC * V is constant)
+        bt.set_lrc([lrc0 * V0])
     start = inp.start_step
     if a.resume:
         with open(a.resume, "rb") as f:

@@ -780,12 +780,13 @@ static double exp_small(double x) {
  * exp(dlnv / 3) with the anchors' fixed-point fractions unchanged (centres
  * scale about the origin, geometry rigid), FP64 system energies at both
  * volumes (orc_system_energy on the state's rows), the isobaric criterion
- * exp(-(dU + P dV)/kT + (N + 1) dlnv) >= u.  Rejected outright (-1) when an
+ * exp(-(dU + P dV)/kT + (N + 1) dlnv) >= u, with dU including the change of
+ * the long-range correction lrc_v / V (lrc_v = E_LRC * V; 0 for none).  Rejected outright (-1) when an
  * edge would fall to four times rad_max (the largest molecule radius).  *energy
  * becomes the FP64 energy of the kept volume (unchanged on -1).  Returns 1
  * accepted, 0 rejected. */
 int orc_fchain_volume(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step,
-                      double p_kcal, double max_dlnv, float rad_max, double* energy,
+                      double p_kcal, double max_dlnv, float rad_max, double lrc_v, double* energy,
                       double* e_old, double* e_new, double* dlnv_out, double* u_out) {
   orc_box* b = c->b;
   uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
@@ -812,7 +813,9 @@ int orc_fchain_volume(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step
   if (e_new) *e_new = en;
   const double vo = Lo[0] * Lo[1] * Lo[2];
   const double vn = Ln[0] * Ln[1] * Ln[2];
-  const double arg = -((en - eo) + p_kcal * (vn - vo)) / b->kT + (double)(b->n_mol + 1) * dlnv;
+  const double d_lrc = lrc_v / vn - lrc_v / vo;
+  const double arg =
+      -((en - eo) + d_lrc + p_kcal * (vn - vo)) / b->kT + (double)(b->n_mol + 1) * dlnv;
   const int ok = (arg >= 0.0) || (exp(arg) >= u);
   if (ok) {
     *energy = en;

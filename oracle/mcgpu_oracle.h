@@ -118,7 +118,7 @@ double orc_fchain_run(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step
                      int n_steps, double e0, orc_trace* trace, long long* n_accepted);
 void orc_sincos_f32(float x, float* s, float* c);
 int orc_fchain_volume(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step,
-                      double p_kcal, double max_dlnv, float rad_max, double* energy,
+                      double p_kcal, double max_dlnv, float rad_max, double lrc_v, double* energy,
                       double* e_old, double* e_new, double* dlnv_out, double* u_out);
 
 #ifdef __cplusplus

@@ -121,6 +121,7 @@ def orc_lib() -> C.CDLL:
             "orc_sincos_f32": (None, [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
             "orc_fchain_volume": (C.c_int, [C.POINTER(OrcChainS), C.c_uint64, C.c_uint32,
                                             C.c_uint64, C.c_double, C.c_double, C.c_float,
+                                            C.c_double,
                                             C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_double), C.POINTER(C.c_double),
                                             C.POINTER(C.c_double)]),
@@ -259,7 +260,7 @@ class OracleChain:
     ATM_KCAL = 101325 * 6.02214076e23 * 1e-30 / 4184
 
     def volume_move(self, seed: int, chain: int, step: int, pressure_atm: float,
-                    max_dlnv: float, energy: float) -> dict:
+                    max_dlnv: float, energy: float, lrc_v: float = 0.0) -> dict:
         """One isobaric ln V move at step count `step` (orc_fchain_volume);
         returns the outcome (1, 0, or -1 for rejected outright), both FP64
         energies, the draws and the energy after the decision."""
@@ -267,7 +268,8 @@ class OracleChain:
         eo, en, dl, u = C.c_double(), C.c_double(), C.c_double(), C.c_double()
         st = orc_lib().orc_fchain_volume(
             C.byref(self.s), int(seed) & (2 ** 64 - 1), int(chain), int(step),
-            float(pressure_atm) * self.ATM_KCAL, float(max_dlnv), self.rad_max, C.byref(e),
+            float(pressure_atm) * self.ATM_KCAL, float(max_dlnv), self.rad_max, float(lrc_v),
+            C.byref(e),
             C.byref(eo), C.byref(en), C.byref(dl), C.byref(u))
         return {"status": st, "e_old": eo.value, "e_new": en.value, "dlnv": dl.value,
                 "u": u.value, "energy": e.value, "edge": float(self.ob.s.size[0])}

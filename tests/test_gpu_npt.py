@@ -30,7 +30,7 @@ def npt_boxes():
     return boxes, list(seeds) + [99]
 
 
-def oracle_npt(box, seed, chain, n_steps, interval, pressure, max_dlnv):
+def oracle_npt(box, seed, chain, n_steps, interval, pressure, max_dlnv, lrc_v=0.0):
     """The oracle run of one NPT chain: segments of `interval` steps, each
     followed by a volume move at the chain's step count."""
     oc = OracleChain(box, ROT_AXIS)
@@ -43,7 +43,7 @@ def oracle_npt(box, seed, chain, n_steps, interval, pressure, max_dlnv):
         steps += tr
         done += k
         if done % interval == 0:
-            r = oc.volume_move(seed, chain, done, pressure, max_dlnv, e)
+            r = oc.volume_move(seed, chain, done, pressure, max_dlnv, e, lrc_v)
             e = r["energy"]
             vols.append(r)
     return oc, e, steps, vols
@@ -93,6 +93,36 @@ def test_npt_batch_replay(ctx, prec):
         scale = sum(oc.ob.mol_energy_abs(m, m) for m in range(b.n_mol))
         assert abs(st.energy - e) <= 1e-5 * max(abs(e), 1e-3 * scale) + interval * 1e-9 * scale
     assert 0 < n_acc < len(boxes) * (steps // interval)
+
+
+def test_npt_lrc_term(ctx):
+    """The long-range correction in the volume criterion: decisions, boxes
+    and coordinates equal the oracle's with the term, and the term changes
+    some decision (an exaggerated E_LRC * V so it matters every move)."""
+    boxes, seeds = npt_boxes()
+    interval, steps, dl = 25, 200, 0.02
+    lrc = []
+    for b in boxes:
+        V = float(b.size[0] * b.size[1] * b.size[2])
+        # E_LRC of one-site LJ water at this density is O(-0.1 N) kcal/mol
+        lrc.append(-40.0 * b.n_mol * V)
+    bt = ChainBatch(ctx, boxes, seeds, rotation=ROT_AXIS)
+    bt.set_tile(128, 1, 16)
+    bt.set_npt(interval, 1.0, dl, PREC_MIXED)
+    bt.set_lrc(lrc)
+    _, vtr = bt.run_traced(steps, volume=True)
+    stats = bt.stats()
+    differs = 0
+    for c, b in enumerate(boxes):
+        oc, e, _, ovol = oracle_npt(b, seeds[c], c, steps, interval, 1.0, dl, lrc[c])
+        _, _, _, plain = oracle_npt(b, seeds[c], c, steps, interval, 1.0, dl, 0.0)
+        for k, (t, r) in enumerate(zip(vtr[c], ovol)):
+            assert bool(t.accepted) == (r["status"] == 1) and t.edge == r["edge"], (c, k)
+        differs += sum(1 for p, q in zip(ovol, plain) if p["status"] != q["status"])
+        assert tuple(stats[c].box) == tuple(oc.ob.s.size)
+        x, y, z = bt.download(c)
+        assert np.array_equal(np.stack([x, y, z], 1), oc.coords()), c
+    assert differs > 0
 
 
 def scale_of(ob, b):
