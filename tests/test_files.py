@@ -270,3 +270,25 @@ def test_reference_loader_live():
     for name in CONFIGS:
         ref = R.load_files(str(FILES / (name + ".config")))
         assert_rows(load(name + ".config"), ref)
+
+
+@pytest.mark.parametrize("name", ["demo", "indole267", "meoh500"])
+def test_reference_example_configs_live(tmp_path, name):
+    """The reference's own example configurations (its z-matrices and OPLS
+    table), where its sources and compiled loader are present: rows and LRC
+    bit-identical."""
+    import shutil
+    from oracle.pyoracle import REF_SO, REFERENCE_SRC, RefHarness
+    res = REFERENCE_SRC / "resources"
+    if not REF_SO.exists() or not res.is_dir():
+        pytest.skip("reference sources or compiled reference not present")
+    shutil.copytree(res, tmp_path / "resources")
+    src = res / (name + ".config")
+    if not src.exists():
+        src = res / "exampleFiles" / (name + ".config")
+    shutil.copy(src, tmp_path / (name + ".config"))
+    ref = RefHarness().load_files(str(tmp_path / (name + ".config")))
+    with cwd(tmp_path):
+        si = F.load(name + ".config")
+    assert_rows(si, ref)
+    assert F.energy_lrc(si.box.env, si.box.molecules) == ref["lrc"]
