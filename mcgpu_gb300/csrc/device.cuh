@@ -95,6 +95,9 @@ struct __align__(16) ChainHdr {
   // pair factors follow from the molecule index (no loads)
   int uniform, ulen, uact, uprim;
   float umrad, pad9, pad10, pad11;
+  // bound on |energy - FP64 system energy of the current state|: the sum of
+  // the FP32 step bounds since the energy was last set from a fresh total
+  double run_err, pad12;
 };
 static_assert(sizeof(ChainHdr) % 16 == 0, "ChainHdr alignment");
 

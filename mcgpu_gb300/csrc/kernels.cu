@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(256, 2) k_chain_steps(Pool P, int n_steps, uns
       for (int i = g.tid; i < H.ulen; i += gsize) s.teq[i] = P.aeq[H.atom0 + i];
     g.sync();
     int full_scans = 0;
-    double energy = H.energy;
+    double energy = H.energy, err = 0.0;
     long long acc_n = 0, npairs = 0;
     int ties = 0;
     const unsigned long long step0 = H.step;
@@ -393,6 +393,7 @@ __global__ void __launch_bounds__(256, 2) k_chain_steps(Pool P, int n_steps, uns
         if (lane == 0) {
           if (ok) {
             energy += de;
+            err += tie ? 1e-12 * (double)acc.ab : (double)bound;
             acc_n++;
             // a molecule now beyond skin/2 of the build invalidates the list
             if (!trial_near) s.misc[kMiscNlOk] = 0;
@@ -418,6 +419,7 @@ __global__ void __launch_bounds__(256, 2) k_chain_steps(Pool P, int n_steps, uns
     }
     if (g.tid == 0) {
       Hp->energy = energy;
+      Hp->run_err += err;
       Hp->step = step0 + my_steps;
       Hp->accepted += acc_n;
       Hp->pairs += npairs;

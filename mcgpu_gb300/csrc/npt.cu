@@ -261,40 +261,41 @@ struct VcStencil {
   int n;
 };
 
+// The (up to 27) stencil cells of molecule m's cell, in x-, y-, z-nested
+// order (c-1, c, c+1 per edge with at least 3 cells, else every cell once),
+// with their members' prefix sums.  Warp 0 builds it: one cell per lane, so
+// the cells' counts and starts arrive in one round trip.
 __device__ inline void vc_stencil(const Pool& P, const ChainHdr& H, int m, VcStencil& S) {
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x >= 32) return;
+  const int lane = threadIdx.x;
   const int local = P.vc_of[m] - H.mol0;
-  const int n1 = H.vncell[1], n2 = H.vncell[2];
+  const int n0 = H.vncell[0], n1 = H.vncell[1], n2 = H.vncell[2];
   const int cz = local % n2, cy = (local / n2) % n1, cx = local / (n1 * n2);
-  int sx[3], sy[3], sz[3];
-  const int nc[3] = {H.vncell[0], n1, n2};
-  const int cc[3] = {cx, cy, cz};
-  int* st[3] = {sx, sy, sz};
-  int ns[3];
-  for (int k = 0; k < 3; k++) {
-    if (nc[k] >= 3) {
-      st[k][0] = (cc[k] + nc[k] - 1) % nc[k];
-      st[k][1] = cc[k];
-      st[k][2] = (cc[k] + 1) % nc[k];
-      ns[k] = 3;
-    } else {
-      for (int t = 0; t < nc[k]; t++) st[k][t] = t;
-      ns[k] = nc[k];
-    }
+  const int s0 = n0 >= 3 ? 3 : n0, s1 = n1 >= 3 ? 3 : n1, s2 = n2 >= 3 ? 3 : n2;
+  const int n = s0 * s1 * s2;
+  int start = 0, cnt = 0;
+  if (lane < n) {
+    const int a = lane / (s1 * s2), b = (lane / s2) % s1, c = lane % s2;
+    const int x = n0 >= 3 ? (cx + n0 - 1 + a) % n0 : a;
+    const int y = n1 >= 3 ? (cy + n1 - 1 + b) % n1 : b;
+    const int z = n2 >= 3 ? (cz + n2 - 1 + c) % n2 : c;
+    const int cell = H.mol0 + (x * n1 + y) * n2 + z;
+    start = P.vc_start[cell];
+    cnt = P.vc_cnt[cell];
   }
-  int n = 0, run = 0;
-  for (int a = 0; a < ns[0]; a++)
-    for (int b = 0; b < ns[1]; b++)
-      for (int c = 0; c < ns[2]; c++) {
-        const int cell = H.mol0 + (sx[a] * n1 + sy[b]) * n2 + sz[c];
-        S.start[n] = P.vc_start[cell];
-        S.cnt[n] = P.vc_cnt[cell];
-        S.pref[n] = run;
-        run += S.cnt[n];
-        n++;
-      }
-  S.pref[n] = run;
-  S.n = n;
+  int incl = cnt;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int v = __shfl_up_sync(~0u, incl, off);
+    if (lane >= off) incl += v;
+  }
+  if (lane < n) {
+    S.start[lane] = start;
+    S.cnt[lane] = cnt;
+    S.pref[lane] = incl - cnt;
+  }
+  if (lane == n - 1) S.pref[n] = incl;
+  if (lane == 0) S.n = n;
 }
 
 // Candidate t of the stencil (t < S.pref[S.n]); k is the thread's cursor
@@ -342,15 +343,14 @@ constexpr int kVolJMask = (1 << kVolFShift) - 1;
 // skipped without a test.
 __device__ __forceinline__ int vol_screen(const Pool& P, const ChainHdr& H, const VolBox* vb,
                                           const float4* so, const int* spa, int npidx, uint4 Am,
-                                          int j, const double* const* Lv, float reach2, float sf,
-                                          int nvol) {
+                                          int j, float reach2, float sf, int w0, int nvol) {
   const uint4 Aj = P.mfix[j];
   const float3 D0 = fixdiff(Aj, Am, H);
   const float d2 = fmaf(D0.x, D0.x, fmaf(D0.y, D0.y, D0.z * D0.z));
   if (d2 > reach2 && d2 * sf * sf > reach2) return 0;
   const int2 pj = P.mpi[j];
   int f = 0;
-  for (int w = 0; w < nvol; w++) {
+  for (int w = w0; w < w0 + nvol; w++) {
     const VolBox& B = vb[w];
     float3 Dh, Dl;
     vol_fixdiff(Aj, Am, B, Dh, Dl);
@@ -366,7 +366,7 @@ __device__ __forceinline__ int vol_screen(const Pool& P, const ChainHdr& H, cons
         if (r2 <= B.cut2_lo) {
           in = true;
         } else if (r2 <= B.cut2_hi) {
-          in = dist2_at(pos_at(Am, oa, Lv[w]), pos_at(Aj, op, Lv[w]), Lv[w]) <=
+          in = dist2_at(pos_at(Am, oa, B.L), pos_at(Aj, op, B.L), B.L) <=
                __dmul_rn(H.cutoff, H.cutoff);
         }
       }
@@ -442,19 +442,20 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
   __shared__ int wcnt[kVolWarps], woff[kVolWarps + 1];
   const int m = range_mol(R, m_begin, blockIdx.x);
   const int c = mol_chain[m];
-  const VolMove v = vm[c];
+  const VolMove& v = vm[c];
   const ChainHdr& H = P.hdr[c];
   if (!vol_take64(v, H, pass)) return;
   const int nvol = pass == 2 ? 1 : 2;
   vc_stencil(P, H, m, S);
   if (threadIdx.x < 2) vb[threadIdx.x] = v.box[threadIdx.x];
-  const double* Lv[2] = {H.L, v.L};
+  const double* Lv[2] = {H.L, v.L};   // before the barrier that publishes vb
   const int a0 = P.mstart[m], len = P.mlen[m] & 255;
   const int2 pi = P.mpi[m];
   const uint4 Am = P.mfix[m];
   for (int i = threadIdx.x; i < len; i += blockDim.x) {
     const float4 o = P.aoff[a0 + i];
     so[i] = o;
+#pragma unroll
     for (int w = 0; w < 2; w++) {
       const double3 x = pos_at(Am, o, Lv[w]);
       sx[w][0][i] = x.x;
@@ -482,7 +483,7 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
       int f = 0, j = 0;
       if (t < n_cand) {
         j = vc_candidate(P, S, t, kc);
-        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, Lv, reach2, sf, nvol);
+        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, 0, nvol);
       }
       vol_append(ent, wcnt, j, f, r);
     }
@@ -503,15 +504,17 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
       const double rsb = sqrt(sb), reb = sqrt(eb);
       const float4 ob = P.aoff[bb];
       const uint4 Aj = P.mfix[j];
+#pragma unroll
       for (int w = 0; w < 2; w++) {
         if (!(f & (1 << w))) continue;
-        const double3 xb = pos_at(Aj, ob, Lv[w]);
+        const double* L = vb[w].L;
+        const double3 xb = pos_at(Aj, ob, L);
         double acc = 0.0;
         for (int i = 0; i < len; i++) {
           const double rsa = sq[0][i];
           if (rsa < 0) continue;
           const double3 xa = make_double3(sx[w][0][i], sx[w][1][i], sx[w][2][i]);
-          acc += pair64f(dist2_at(xa, xb, Lv[w]), rsa, rsb, sq[1][i], reb, sq[2][i] * qb);
+          acc += pair64f(dist2_at(xa, xb, L), rsa, rsb, sq[1][i], reb, sq[2][i] * qb);
         }
         if (w == 0) eo += acc; else en += acc;
       }
@@ -530,12 +533,41 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
   if (threadIdx.x == 0) emol2[m] = red[0];
 }
 
-// E(m, j > m) at V (.x) and V' (.y) of a mixed chain's molecule m with FP32
-// pair terms (per-pair minimum image, the chain kernel's arithmetic) summed
-// in double-float; eabs2 gets the sums of the terms' magnitudes.  The
-// in-range test is the FP32 screen with the FP64 re-test inside its guard
-// band: the FP64 test's set exactly.
-__global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const int* mol_chain,
+// FP32 pair terms of neighbour atom b (at bx + lx etc. relative to the moved
+// molecule's anchor, double-float) with every atom of the molecule staged in
+// so/sq.  WRAP takes each pair's own minimum image; without it the pair
+// distances are used as they are, which gives the same r2 bit for bit when
+// every |d| stays below half an edge (the caller's |D| + radii test).
+template <bool WRAP>
+__device__ __forceinline__ void vol_atoms32(const float4* so, const float2* sq, int len, float bx,
+                                            float by, float bz, float lx, float ly, float lz,
+                                            float sig_b, float2 qb, const VolBox& B, float& e32,
+                                            float& a32) {
+  for (int i = 0; i < len; i++) {
+    const float4 a4 = so[i];
+    const float2 ea = sq[i];
+    float dx = (bx - a4.x) + lx, dy = (by - a4.y) + ly, dz = (bz - a4.z) + lz;
+    if (WRAP) {
+      dx = wrapf(dx, B.Lf[0]);
+      dy = wrapf(dy, B.Lf[1]);
+      dz = wrapf(dz, B.Lf[2]);
+    }
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (!(r2 > 0.f)) continue;
+    const float lj = lj32(rcp_nr(r2), a4.w, sig_b, ea.x, qb.x);
+    const float cl = (ea.y * qb.y) * rsqrt_nr(r2);
+    e32 += lj + cl;
+    a32 += fabsf(lj) + fabsf(cl);
+  }
+}
+
+// E(m, j > m) of a mixed chain's molecule m at V' (.y; a volume move, whose
+// U(V) is the chain's running energy) or, with init, at V (.x; any chain in
+// state 1), with FP32 pair terms (per-pair minimum image, the chain kernel's
+// arithmetic) summed in double-float; eabs2 gets the sums of the terms'
+// magnitudes.  The in-range test is the FP32 screen with the FP64 re-test
+// inside its guard band: the FP64 test's set exactly.
+__global__ void __launch_bounds__(kVolThreads, 7) k_vol_pair_sums32(Pool P, const int* mol_chain,
                                                                  const VolMove* vm, int m_begin,
                                                                  MolRanges R, double2* emol2,
                                                                  double2* eabs2, int init) {
@@ -549,11 +581,11 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
   __shared__ int wcnt[kVolWarps], woff[kVolWarps + 1];
   const int m = range_mol(R, m_begin, blockIdx.x);
   const int c = mol_chain[m];
-  const VolMove v = vm[c];
+  const VolMove& v = vm[c];
   const ChainHdr& H = P.hdr[c];
-  // init: a chain's energy at its current box (one volume)
+  // init: a chain's energy at its current box; else U(V') of a mixed move
   if (!(v.state == 1 && (H.vol_mixed || init))) return;
-  const int nvol = init ? 1 : 2;
+  const int w0 = init ? 0 : 1;
   vc_stencil(P, H, m, S);
   const int a0 = P.mstart[m], len = P.mlen[m] & 255;
   const int2 pi = P.mpi[m];
@@ -565,9 +597,9 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
   for (int k = threadIdx.x; k < pi.y; k += blockDim.x) spa[k] = P.pidx[pi.x + k] - a0;
   if (threadIdx.x < 2) vb[threadIdx.x] = v.box[threadIdx.x];
   __syncthreads();
-  const double* Lv[2] = {H.L, v.L};
   const float reach2 = v.reach * v.reach;
   const float sf = v.sf;
+  const float rad_m = P.mrad[m];
   float eh[2] = {0.f, 0.f}, el[2] = {0.f, 0.f}, ab[2] = {0.f, 0.f};
   const int maxlen = H.max_len;
   const int n_cand = S.pref[S.n];
@@ -578,7 +610,7 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
       int f = 0, j = 0;
       if (t < n_cand) {
         j = vc_candidate(P, S, t, kc);
-        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, Lv, reach2, sf, nvol);
+        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, w0, 1);
       }
       vol_append(ent, wcnt, j, f, r);
     }
@@ -596,6 +628,8 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
       const float4 ob = P.aoff[bb];
       const float2 qb = P.aeq[bb];
       const uint4 Aj = P.mfix[j];
+      const float rad_j = P.mrad[j];
+#pragma unroll
       for (int w = 0; w < 2; w++) {
         if (!(f & (1 << w))) continue;
         const VolBox& B = vb[w];
@@ -606,21 +640,15 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums32(Pool P, const i
         const float lx = ((Dh.x - (bx - (bx - Dh.x))) + (ob.x - (bx - Dh.x))) + Dl.x;
         const float ly = ((Dh.y - (by - (by - Dh.y))) + (ob.y - (by - Dh.y))) + Dl.y;
         const float lz = ((Dh.z - (bz - (bz - Dh.z))) + (ob.z - (bz - Dh.z))) + Dl.z;
-        float e32 = 0.f;
-        for (int i = 0; i < len; i++) {
-          const float4 a4 = so[i];
-          const float2 ea = sq[i];
-          const float dx = wrapf((bx - a4.x) + lx, B.Lf[0]);
-          const float dy = wrapf((by - a4.y) + ly, B.Lf[1]);
-          const float dz = wrapf((bz - a4.z) + lz, B.Lf[2]);
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          if (!(r2 > 0.f)) continue;
-          const float lj = lj32(rcp_nr(r2), a4.w, ob.w, ea.x, qb.x);
-          const float cl = (ea.y * qb.y) * rsqrt_nr(r2);
-          e32 += lj + cl;
-          ab[w] += fabsf(lj) + fabsf(cl);
-        }
+        float e32 = 0.f, a32 = 0.f;
+        const float rr = rad_m + rad_j;
+        if (fabsf(Dh.x) + rr > 0.5f * B.Lf[0] - 1e-3f || fabsf(Dh.y) + rr > 0.5f * B.Lf[1] - 1e-3f ||
+            fabsf(Dh.z) + rr > 0.5f * B.Lf[2] - 1e-3f)
+          vol_atoms32<true>(so, sq, len, bx, by, bz, lx, ly, lz, ob.w, qb, B, e32, a32);
+        else
+          vol_atoms32<false>(so, sq, len, bx, by, bz, lx, ly, lz, ob.w, qb, B, e32, a32);
         ff_add(eh[w], el[w], e32);
+        ab[w] += a32;
       }
     }
     __syncthreads();
@@ -662,7 +690,7 @@ __global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, cons
   const int c = range_chain(R, blockIdx.x);
   if (vm[c].state != want) return;
   const ChainHdr& H = P.hdr[c];
-  const bool mixed = want == 1 && H.vol_mixed;
+  const bool mixed = want == 1;
   double2 acc = make_double2(0.0, 0.0), ab = make_double2(0.0, 0.0);
   for (int i = threadIdx.x; i < H.n_mol; i += blockDim.x) {
     acc.x += emol2[H.mol0 + i].x;
@@ -706,7 +734,10 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
   double e_old = H.energy, e_new = 0.0;
   int ok = 0;
   if (v.state == 1 || v.state == 4) {
-    e_old = esum[c].x;
+    // a mixed move's U(V) is the running energy (error bound run_err), its
+    // U(V') the FP32 total; otherwise both are FP64 totals
+    const bool mixed = v.state == 1 && H.vol_mixed;
+    e_old = mixed ? H.energy : esum[c].x;
     e_new = esum[c].y;
     const double vo = H.L[0] * H.L[1] * H.L[2];
     const double vn = v.L[0] * v.L[1] * v.L[2];
@@ -714,10 +745,11 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
     const double d_lrc = H.lrc_v / vn - H.lrc_v / vo;
     const double arg = -((e_new - e_old) + d_lrc + H.pressure * (vn - vo)) / H.kT +
                        (double)(H.n_mol + 1) * v.dlnv;
-    if (v.state == 1 && H.vol_mixed) {
-      // FP32 pair terms: |error of dU| <= kTieRel * sum of term magnitudes
+    const double new_err = mixed ? kTieRel * eabs[c].y : 0.0;
+    if (mixed) {
+      // |error of dU| <= kTieRel * (sum of V' term magnitudes) + run_err
       const double bound =
-          (kTieRel * (eabs[c].x + eabs[c].y) + 1e-12 * (fabs(e_old) + fabs(e_new))) / H.kT;
+          (new_err + H.run_err + 1e-12 * (fabs(e_old) + fabs(e_new))) / H.kT;
       if (fabs(arg - log(v.u)) <= bound + 1e-12) {
         v.state = 4;
         v.fp64 = 1;
@@ -726,7 +758,13 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
       }
     }
     ok = (arg >= 0.0) || (exp(arg) >= v.u);
-    H.energy = ok ? e_new : e_old;
+    if (ok) {
+      H.energy = e_new;
+      H.run_err = new_err;
+    } else if (!mixed) {
+      H.energy = e_old;
+      H.run_err = 0.0;
+    }
   }
   H.vol_tried++;
   H.vol_step = (long long)H.step;
@@ -791,12 +829,14 @@ __global__ void k_vol_self(Pool P, VolMove* vm, MolRanges R, int n_items) {
   vm[c] = v;
 }
 
-__global__ void k_vol_self_energy(Pool P, const VolMove* vm, const double2* esum, MolRanges R,
-                                  int n_items) {
+__global__ void k_vol_self_energy(Pool P, const VolMove* vm, const double2* esum,
+                                  const double2* esum_abs, MolRanges R, int n_items, int f64) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_items) return;
   const int c = range_chain(R, i);
-  if (vm[c].state == 1) P.hdr[c].energy = esum[c].x;
+  if (vm[c].state != 1) return;
+  P.hdr[c].energy = esum[c].x;
+  P.hdr[c].run_err = f64 ? 0.0 : kTieRel * esum_abs[c].x;
 }
 
 // Sets the running energy of the chains in act (all when act has no
@@ -825,7 +865,7 @@ cudaError_t launch_chain_energy(Pool P, const int* mol_chain, int n_mol_total, V
       k_vol_pair_sums32<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2, eabs2, 1);
   }
   k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 1);
-  k_vol_self_energy<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, act, nc);
+  k_vol_self_energy<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, act, nc, f64 ? 1 : 0);
   return cudaGetLastError();
 }
 
