@@ -745,6 +745,7 @@ struct mcgpu_batch {
   double2* eabs2 = nullptr;
   double2* vsum = nullptr;
   double2* vsum_abs = nullptr;
+  int* vlist = nullptr;                   // chains of a re-take (3 * n_chains + 3)
   bool vol_has64 = false, vol_has32 = false;  // precisions of the NPT chains
   // snapshot for the autotuner
   std::vector<void*> snap;
@@ -875,6 +876,7 @@ extern "C" int mcgpu_batch_destroy(mcgpu_batch* bt) {
   if (bt->eabs2) cudaFree(bt->eabs2);
   if (bt->vsum) cudaFree(bt->vsum);
   if (bt->vsum_abs) cudaFree(bt->vsum_abs);
+  if (bt->vlist) cudaFree(bt->vlist);
   for (void* p : bt->snap)
     if (p) cudaFree(p);
   delete bt;
@@ -934,7 +936,8 @@ static int batch_build_graph(mcgpu_batch* bt, int launches, int interval) {
     }
     if (rc == MCGPU_OK) {
       cudaError_t e = launch_volume_phase(bt->pool.P, bt->pool.mol_chain, bt->pool.n_mol, bt->vm,
-                                          bt->emol2, bt->eabs2, bt->vsum, bt->vsum_abs, nullptr, 0,
+                                          bt->emol2, bt->eabs2, bt->vsum, bt->vsum_abs, bt->vlist,
+                                          nullptr, 0,
                                           0, st, MolRanges(), bt->vol_has64, bt->vol_has32);
       if (e != cudaSuccess) rc = set_err(ctx, MCGPU_ERR_CUDA, "volume phase launch: %s", cudaGetErrorString(e));
     }
@@ -1031,7 +1034,7 @@ static int batch_advance(mcgpu_batch* bt, int n_steps, mcgpu_trace* trace, int t
     bt->steps_done += seg;
     if (bt->steps_done % iv == 0) {
       CK(ctx, launch_volume_phase(bt->pool.P, bt->pool.mol_chain, bt->pool.n_mol, bt->vm, bt->emol2,
-                                  bt->eabs2, bt->vsum, bt->vsum_abs, vtrace, vk, vstride,
+                                  bt->eabs2, bt->vsum, bt->vsum_abs, bt->vlist, vtrace, vk, vstride,
                                   ctx->stream, MolRanges(), bt->vol_has64, bt->vol_has32));
       vk++;
     }
@@ -1136,6 +1139,7 @@ extern "C" int mcgpu_batch_set_npt(mcgpu_batch* bt, int interval, const double* 
     if (!bt->eabs2) bt->eabs2 = dalloc<double2>(bt->pool.n_mol, &e);
     if (!bt->vsum) bt->vsum = dalloc<double2>(nc, &e);
     if (!bt->vsum_abs) bt->vsum_abs = dalloc<double2>(nc, &e);
+    if (!bt->vlist) bt->vlist = dalloc<int>(3 * (size_t)nc + 3, &e);
     Pool& P = bt->pool.P;
     if (!P.vc_cnt) {
       const size_t nm = (size_t)bt->pool.n_mol;

@@ -43,6 +43,9 @@ constexpr double kAtmKcal = 1.4583972574259083e-05;
 // the sum of the magnitudes of its FP32 terms (observed worst case ~1e-8;
 // the bound keeps a 100x margin).
 constexpr double kTieRel = 1e-6;
+// The same for double-float pair terms (about 1e-13 observed; the bound
+// keeps a 1000x margin).
+constexpr double kDfRel = 1e-10;
 
 // Device error status words (ChainHdr::error, Pool::error).
 enum : int {
@@ -149,6 +152,7 @@ struct VolMove {
   double L[3];
   double dlnv, u;
   int state;   // 0 not due, 1 evaluate, 2 rejected outright, 3 accepted,
+               // 5 double-float re-take too close to call: FP64 re-take,
                // 4 FP32 energies too close to the threshold: FP64 re-take
   int fp64;    // decided on FP64 pair energies
 };
@@ -332,6 +336,52 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float v) {
 __device__ __forceinline__ void ff_add2(float& hi, float& lo, float h2, float l2) {
   ff_add(hi, lo, h2);
   lo = __fadd_rn(lo, l2);
+}
+
+// ---- double-float arithmetic ----------------------------------------------
+// A value h + l with |l| <= ulp(h)/2 (about 48 significant bits) on FP32
+// instructions: Knuth's two-sum, the FMA two-product, and the usual
+// renormalised sum and product (Dekker 1971; Hida, Li, Bailey 2001).
+// Relative error of an operation about 2^-44.
+struct df {
+  float h, l;
+};
+
+__device__ __forceinline__ df df_of(double x) {
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ df df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ df df_quick(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = df_two_sum(a.h, b.h);
+  const df t = df_two_sum(a.l, b.l);
+  s = df_quick(s.h, __fadd_rn(s.l, t.h));
+  return df_quick(s.h, __fadd_rn(s.l, t.l));
+}
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, {-b.h, -b.l}); }
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = fmaf(a.h, b.h, -p);
+  e = fmaf(a.h, b.l, e);
+  e = fmaf(a.l, b.h, e);
+  return df_quick(p, e);
+}
+// 1/sqrt(a) for a > 0: an FP32 estimate refined by one Newton step
+// y + (y/2)(1 - a y^2) in double-float (error ~1e-14 relative).
+__device__ __forceinline__ df df_rsqrt(df a) {
+  const float y = rsqrtf(a.h);
+  const float y2 = __fmul_rn(y, y);
+  const df ay2 = df_mul(a, {y2, fmaf(y, y, -y2)});
+  const df r = df_sub({1.0f, 0.0f}, ay2);
+  return df_add({y, 0.0f}, df_mul(r, {0.5f * y, 0.0f}));
 }
 
 // ---- groups: the warps that advance one chain --------------------------

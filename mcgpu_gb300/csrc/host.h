@@ -38,10 +38,14 @@ cudaError_t launch_move_energies(bool f64, int grid, int threads, SmemShape sh, 
 cudaError_t launch_mol_pair_sums(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
                                  Pool P, const int* mol_chain, int m_begin, double* emol,
                                  long long* pairs);
+// One volume phase of the chains in act (all when act has no ranges) on
+// stream st: proposals, cell grids, FP32 / FP64 totals, decisions, the
+// double-float and FP64 re-takes; vlist holds 3 * (chains) + 3 ints.
 cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
                                 double2* emol2, double2* eabs2, double2* esum, double2* esum_abs,
-                                mcgpu_vol_trace* trace, int trace_slot, int trace_stride,
-                                cudaStream_t st, MolRanges act, bool has64, bool has32);
+                                int* vlist, mcgpu_vol_trace* trace, int trace_slot,
+                                int trace_stride, cudaStream_t st, MolRanges act, bool has64,
+                                bool has32);
 cudaError_t launch_chain_energy(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
                                 double2* emol2, double2* eabs2, double2* esum, double2* esum_abs,
                                 cudaStream_t st, MolRanges act, bool f64);

@@ -121,6 +121,8 @@ __device__ __forceinline__ double dist2_at(double3 a, double3 b, const double* L
 }
 
 constexpr int kVolThreads = 128;
+// CTAs of the grid-strided re-take kernels (a few per SM)
+constexpr int kVolListGrid = 152 * 4;
 
 // Pool molecule of work item b: m_begin + b, or the b-th molecule of the
 // active ranges (binary search over their prefix sums).
@@ -403,35 +405,79 @@ __device__ __forceinline__ int vol_entry(const int* ent, const int* woff, int e)
 }
 
 // FP64 pair term with the blending square roots taken per atom
-// (sqrt|s_a| sqrt|s_b| for sqrt|s_a s_b|, equal to within an ulp), one
-// division and one square root per pair; zero at r2 == 0 as the reference.
+// (sqrt|s_a| sqrt|s_b| for sqrt|s_a s_b|, equal to within an ulp) and one
+// reciprocal square root per pair (1/r and 1/r^2 = (1/r)^2 within a few
+// ulps of the division and square root of the reference's arithmetic, at
+// about half their FP64 cost); zero at r2 == 0 as the reference.
 __device__ __forceinline__ double pair64f(double r2, double rsa, double rsb, double rea,
                                           double reb, double qq) {
   if (r2 == 0.0) return 0.0;
-  const double ir2 = 1.0 / r2;
+  const double ir = rsqrt(r2);
+  const double ir2 = ir * ir;
   const double sg = rsa * rsb;
   const double s2 = sg * sg * ir2;
   const double s6 = s2 * s2 * s2;
-  return 4.0 * (rea * reb) * (s6 * s6 - s6) + qq * sqrt(ir2);
+  return 4.0 * (rea * reb) * (s6 * s6 - s6) + qq * ir;
 }
 
 // Chains a pair-sum pass evaluates: pass 0 the due non-mixed chains, pass 1
-// the mixed chains marked for the FP64 re-take, pass 2 the chains whose
-// energy at their current box is wanted (one volume only).
+// the mixed chains whose double-float re-take was still too close to call
+// (state 5), pass 2 the chains whose energy at their current box is wanted
+// (one volume only).
 __device__ __forceinline__ bool vol_take64(const VolMove& v, const ChainHdr& H, int pass) {
   if (pass == 2) return v.state == 1;  // a chain's energy at its current box
-  return pass == 0 ? (v.state == 1 && !H.vol_mixed) : v.state == 4;
+  return pass == 0 ? (v.state == 1 && !H.vol_mixed) : v.state == 5;
+}
+
+// The chains of a volume phase in state `want`, compacted: list[0] = their
+// count k, list[1] = their molecules, then at list + 2, + 2 + cap and
+// + 2 + 2 cap (cap = the phase's chain count) each one's slot, first pool
+// molecule and molecule prefix sum (pref[k] = the total).  One warp.
+__global__ void k_vol_list(Pool P, const VolMove* vm, MolRanges R, int nc, int want, int* list) {
+  const int lane = threadIdx.x;
+  if (lane >= 32) return;
+  int k = 0, total = 0;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int c0 = 0; c0 < nc; c0 += 32) {
+    const int i = c0 + lane;
+    int slot = 0, n = 0;
+    bool flag = false;
+    if (i < nc) {
+      slot = range_chain(R, i);
+      flag = vm[slot].state == want;
+      if (flag) n = P.hdr[slot].n_mol;
+    }
+    int incl = n;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int v = __shfl_up_sync(~0u, incl, off);
+      if (lane >= off) incl += v;
+    }
+    const unsigned bal = __ballot_sync(~0u, flag);
+    if (flag) {
+      const int pos = k + __popc(bal & lt);
+      list[2 + pos] = slot;
+      list[2 + nc + pos] = P.hdr[slot].mol0;
+      list[2 + 2 * nc + pos] = total + incl - n;
+    }
+    total += __shfl_sync(~0u, incl, 31);
+    k += __popc(bal);
+  }
+  if (lane == 0) {
+    list[0] = k;
+    list[1] = total;
+    list[2 + 2 * nc + k] = total;
+  }
 }
 
 // E(m, j > m) of pool molecule m at V (.x) and V' (.y) with FP64 pair terms
 // (the reference's, SimulationStep.cpp:344-375, with the blending roots per
 // atom).  Candidates from the cell stencil, screened and compacted in
 // chunks (vol_screen: the FP64 test's in-range set exactly).
-__global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int* mol_chain,
-                                                               const VolMove* vm, int m_begin,
-                                                               MolRanges R, double2* emol2,
-                                                               int pass) {
-  __shared__ double sx[2][3][kMaxA];
+__device__ __forceinline__ void vol_f64_mol(const Pool& P, const int* mol_chain,
+                                            const VolMove* vm, int m, double2* emol2,
+                                            int pass) {
+  __shared__ double sx[3][kMaxA];
   __shared__ double sq[3][kMaxA];
   __shared__ int spa[kMaxP];
   __shared__ double2 red[kVolThreads];
@@ -440,7 +486,6 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
   __shared__ float4 so[kMaxA];
   __shared__ int ent[kVolChunk];
   __shared__ int wcnt[kVolWarps], woff[kVolWarps + 1];
-  const int m = range_mol(R, m_begin, blockIdx.x);
   const int c = mol_chain[m];
   const VolMove& v = vm[c];
   const ChainHdr& H = P.hdr[c];
@@ -448,20 +493,16 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
   const int nvol = pass == 2 ? 1 : 2;
   vc_stencil(P, H, m, S);
   if (threadIdx.x < 2) vb[threadIdx.x] = v.box[threadIdx.x];
-  const double* Lv[2] = {H.L, v.L};   // before the barrier that publishes vb
   const int a0 = P.mstart[m], len = P.mlen[m] & 255;
   const int2 pi = P.mpi[m];
   const uint4 Am = P.mfix[m];
   for (int i = threadIdx.x; i < len; i += blockDim.x) {
     const float4 o = P.aoff[a0 + i];
     so[i] = o;
-#pragma unroll
-    for (int w = 0; w < 2; w++) {
-      const double3 x = pos_at(Am, o, Lv[w]);
-      sx[w][0][i] = x.x;
-      sx[w][1][i] = x.y;
-      sx[w][2][i] = x.z;
-    }
+    // positions relative to the molecule's anchor (rigid: both volumes)
+    sx[0][i] = (double)o.x;
+    sx[1][i] = (double)o.y;
+    sx[2][i] = (double)o.z;
     const double sg = P.sig[a0 + i], ep = P.eps[a0 + i];
     // dummy sites (sigma or epsilon < 0) are skipped: marked by -1
     sq[0][i] = (sg >= 0 && ep >= 0) ? sqrt(sg) : -1.0;
@@ -472,6 +513,7 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
   __syncthreads();
   const float reach2 = v.reach * v.reach;
   const float sf = v.sf;
+  const float rad_m = P.mrad[m];
   const int maxlen = H.max_len;
   double eo = 0.0, en = 0.0;
   const int n_cand = S.pref[S.n];
@@ -504,17 +546,34 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
       const double rsb = sqrt(sb), reb = sqrt(eb);
       const float4 ob = P.aoff[bb];
       const uint4 Aj = P.mfix[j];
+      const float rr = rad_m + P.mrad[j];
 #pragma unroll
       for (int w = 0; w < 2; w++) {
         if (!(f & (1 << w))) continue;
-        const double* L = vb[w].L;
-        const double3 xb = pos_at(Aj, ob, L);
+        const VolBox& B = vb[w];
+        // b relative to m's anchor: the anchors' minimum-image difference
+        // (fixed point) at this volume plus b's offset
+        const int d[3] = {(int)(Aj.x - Am.x), (int)(Aj.y - Am.y), (int)(Aj.z - Am.z)};
+        const double bx = (double)d[0] * (B.L[0] * 0x1p-32) + (double)ob.x;
+        const double by = (double)d[1] * (B.L[1] * 0x1p-32) + (double)ob.y;
+        const double bz = (double)d[2] * (B.L[2] * 0x1p-32) + (double)ob.z;
+        // every pair within half an edge: no image to take
+        const bool wrap = fabsf((float)d[0] * B.fxs[0]) + rr > 0.5f * B.Lf[0] - 1e-3f ||
+                          fabsf((float)d[1] * B.fxs[1]) + rr > 0.5f * B.Lf[1] - 1e-3f ||
+                          fabsf((float)d[2] * B.fxs[2]) + rr > 0.5f * B.Lf[2] - 1e-3f;
         double acc = 0.0;
         for (int i = 0; i < len; i++) {
           const double rsa = sq[0][i];
           if (rsa < 0) continue;
-          const double3 xa = make_double3(sx[w][0][i], sx[w][1][i], sx[w][2][i]);
-          acc += pair64f(dist2_at(xa, xb, L), rsa, rsb, sq[1][i], reb, sq[2][i] * qb);
+          double dx = bx - sx[0][i], dy = by - sx[1][i], dz = bz - sx[2][i];
+          if (wrap) {
+            dx = make_periodic(dx, B.L[0]);
+            dy = make_periodic(dy, B.L[1]);
+            dz = make_periodic(dz, B.L[2]);
+          }
+          const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                      __dmul_rn(dz, dz));
+          acc += pair64f(r2, rsa, rsb, sq[1][i], reb, sq[2][i] * qb);
         }
         if (w == 0) eo += acc; else en += acc;
       }
@@ -531,6 +590,200 @@ __global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums(Pool P, const int
     __syncthreads();
   }
   if (threadIdx.x == 0) emol2[m] = red[0];
+}
+
+
+__global__ void __launch_bounds__(kVolThreads, 4) k_vol_pair_sums(Pool P, const int* mol_chain,
+                                                               const VolMove* vm, int m_begin,
+                                                               MolRanges R, double2* emol2,
+                                                               int pass) {
+  vol_f64_mol(P, mol_chain, vm, range_mol(R, m_begin, blockIdx.x), emol2, pass);
+}
+
+// The molecules of the chains a volume list holds (k_vol_list), grid-strided.
+__device__ __forceinline__ int list_mol(const int* list, int cap, int b) {
+  const int cnt = list[0];
+  const int* m0 = list + 2 + cap;
+  const int* pref = list + 2 + 2 * cap;
+  int lo = 0, hi = cnt - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pref[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  return m0[lo] + (b - pref[lo]);
+}
+
+// FP64 re-take (pass 1: chains in state 5) over the listed chains only.
+__global__ void __launch_bounds__(kVolThreads, 4) k_vol_pair_sums_list(Pool P,
+                                                                    const int* mol_chain,
+                                                                    const VolMove* vm,
+                                                                    const int* list, int cap,
+                                                                    double2* emol2) {
+  const int total = list[1];
+  for (int b = blockIdx.x; b < total; b += gridDim.x) {
+    vol_f64_mol(P, mol_chain, vm, list_mol(list, cap, b), emol2, 1);
+    __syncthreads();
+  }
+}
+
+// E(m, j > m) at V (.x) and V' (.y) of a chain whose FP32 volume decision
+// was too close to call (state 4), with pair terms in double-float
+// arithmetic from the FP64 rows' parameters and the exact anchor-relative
+// positions (anchor difference as a double-float plus FP32 offsets); eabs2
+// gets the sums of the terms' magnitudes for the re-take's own bound.  The
+// in-range set is the FP64 test's (vol_screen), the arithmetic the
+// reference's (SimulationStep.cpp:344-375, BruteForceStep.cpp:61-76) to
+// about 1e-13 relative, at a fraction of the FP64 pipe's cost.
+__device__ __forceinline__ void vol_df_mol(const Pool& P, const int* mol_chain,
+                                           const VolMove* vm, int m, double2* emol2,
+                                           double2* eabs2) {
+  __shared__ float4 so[kMaxA];
+  __shared__ df ssg[kMaxA], sep4[kMaxA], sqc[kMaxA];
+  __shared__ int spa[kMaxP];
+  __shared__ VolBox vb[2];
+  __shared__ float wred[kVolWarps][6];
+  __shared__ VcStencil S;
+  __shared__ int ent[kVolChunk];
+  __shared__ int wcnt[kVolWarps], woff[kVolWarps + 1];
+  const int c = mol_chain[m];
+  const VolMove& v = vm[c];
+  const ChainHdr& H = P.hdr[c];
+  if (v.state != 4) return;
+  vc_stencil(P, H, m, S);
+  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
+  const int2 pi = P.mpi[m];
+  const uint4 Am = P.mfix[m];
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    so[i] = P.aoff[a0 + i];
+    const double sg = P.sig[a0 + i], ep = P.eps[a0 + i];
+    // dummy sites (sigma or epsilon < 0) are skipped: sigma marked -1
+    const bool real = sg >= 0 && ep >= 0;
+    ssg[i] = real ? df_of(sg) : df{-1.0f, 0.0f};
+    sep4[i] = df_of(real ? 4.0 * sqrt(ep) : 0.0);
+    sqc[i] = df_of(P.q[a0 + i] * kCoulomb);
+  }
+  for (int k = threadIdx.x; k < pi.y; k += blockDim.x) spa[k] = P.pidx[pi.x + k] - a0;
+  if (threadIdx.x < 2) vb[threadIdx.x] = v.box[threadIdx.x];
+  __syncthreads();
+  const float reach2 = v.reach * v.reach;
+  const float sf = v.sf;
+  const float rad_m = P.mrad[m];
+  df acc[2] = {{0.f, 0.f}, {0.f, 0.f}};
+  float ab[2] = {0.f, 0.f};
+  const int maxlen = H.max_len;
+  const int n_cand = S.pref[S.n];
+  int kc = 0;
+  for (int c0 = 0; c0 < n_cand; c0 += kVolChunk) {
+    for (int r = 0; r < kVolChunk / kVolThreads; r++) {
+      const int t = c0 + r * kVolThreads + (int)threadIdx.x;
+      int f = 0, j = 0;
+      if (t < n_cand) {
+        j = vc_candidate(P, S, t, kc);
+        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, 0, 2);
+      }
+      vol_append(ent, wcnt, j, f, r);
+    }
+    __syncthreads();
+    vol_offsets(wcnt, woff);
+    __syncthreads();
+    const int items = woff[kVolWarps] * maxlen;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int e = it / maxlen, bi = it - e * maxlen;
+      const int jf = vol_entry(ent, woff, e);
+      const int j = jf & kVolJMask, f = jf >> kVolFShift;
+      const int lenj = P.mlen[j] & 255;
+      if (bi >= lenj) continue;
+      const int bb = P.mstart[j] + bi;
+      const double sgb = P.sig[bb], epb = P.eps[bb];
+      if (!(sgb >= 0 && epb >= 0)) continue;
+      const df sb = df_of(sgb), eb = df_of(epb), qb = df_of(P.q[bb]);
+      // sqrt(eps_b) = eps_b / sqrt(eps_b)
+      const df reb = eb.h > 0.f ? df_mul(eb, df_rsqrt(eb)) : df{0.f, 0.f};
+      const float4 ob = P.aoff[bb];
+      const uint4 Aj = P.mfix[j];
+      const float rr = rad_m + P.mrad[j];
+#pragma unroll
+      for (int w = 0; w < 2; w++) {
+        if (!(f & (1 << w))) continue;
+        const VolBox& B = vb[w];
+        float3 Dh, Dl;
+        vol_fixdiff(Aj, Am, B, Dh, Dl);
+        // b relative to m's anchor, double-float
+        const df bx = df_add(df_two_sum(Dh.x, ob.x), {Dl.x, 0.f});
+        const df by = df_add(df_two_sum(Dh.y, ob.y), {Dl.y, 0.f});
+        const df bz = df_add(df_two_sum(Dh.z, ob.z), {Dl.z, 0.f});
+        const bool wrap = fabsf(Dh.x) + rr > 0.5f * B.Lf[0] - 1e-3f ||
+                          fabsf(Dh.y) + rr > 0.5f * B.Lf[1] - 1e-3f ||
+                          fabsf(Dh.z) + rr > 0.5f * B.Lf[2] - 1e-3f;
+        for (int i = 0; i < len; i++) {
+          const df sa = ssg[i];
+          if (sa.h < 0.f) continue;
+          const float4 oa = so[i];
+          df d[3] = {df_sub(bx, {oa.x, 0.f}), df_sub(by, {oa.y, 0.f}), df_sub(bz, {oa.z, 0.f})};
+          if (wrap) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+              // SimCalcs::makePeriodic on the double-float difference
+              const double L = B.L[k];
+              const double x = (double)d[k].h + (double)d[k].l;
+              if (x < -0.5 * L) d[k] = df_add(d[k], df_of(L));
+              else if (x > 0.5 * L) d[k] = df_sub(d[k], df_of(L));
+            }
+          }
+          const df r2 = df_add(df_add(df_mul(d[0], d[0]), df_mul(d[1], d[1])), df_mul(d[2], d[2]));
+          if (!(r2.h > 0.f)) continue;
+          const df ir = df_rsqrt(r2);
+          const df ir2 = df_mul(ir, ir);
+          const df s2 = df_mul(df_mul(sa, sb), ir2);
+          const df s6 = df_mul(df_mul(s2, s2), s2);
+          const df lj = df_mul(df_mul(sep4[i], reb), df_sub(df_mul(s6, s6), s6));
+          const df cl = df_mul(df_mul(sqc[i], qb), ir);
+          acc[w] = df_add(acc[w], df_add(lj, cl));
+          ab[w] += fabsf(lj.h) + fabsf(cl.h);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // reduction: warp butterflies in double-float, then the warps in order
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int w = 0; w < 2; w++) {
+      const df o = {__shfl_xor_sync(~0u, acc[w].h, off), __shfl_xor_sync(~0u, acc[w].l, off)};
+      acc[w] = df_add(acc[w], o);
+      ab[w] += __shfl_xor_sync(~0u, ab[w], off);
+    }
+  }
+  if ((threadIdx.x & 31) == 0) {
+    const int wi = threadIdx.x >> 5;
+    wred[wi][0] = acc[0].h; wred[wi][1] = acc[0].l; wred[wi][2] = acc[1].h;
+    wred[wi][3] = acc[1].l; wred[wi][4] = ab[0]; wred[wi][5] = ab[1];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    df s0 = {0.f, 0.f}, s1 = {0.f, 0.f};
+    float a0s = 0.f, a1s = 0.f;
+    for (int wi = 0; wi < kVolWarps; wi++) {
+      s0 = df_add(s0, {wred[wi][0], wred[wi][1]});
+      s1 = df_add(s1, {wred[wi][2], wred[wi][3]});
+      a0s += wred[wi][4];
+      a1s += wred[wi][5];
+    }
+    emol2[m] = make_double2((double)s0.h + (double)s0.l, (double)s1.h + (double)s1.l);
+    eabs2[m] = make_double2((double)a0s, (double)a1s);
+  }
+}
+
+
+__global__ void __launch_bounds__(kVolThreads) k_vol_pair_sums_df(Pool P, const int* mol_chain,
+                                                                  const VolMove* vm,
+                                                                  const int* list, int cap,
+                                                                  double2* emol2, double2* eabs2) {
+  const int total = list[1];
+  for (int b = blockIdx.x; b < total; b += gridDim.x) {
+    vol_df_mol(P, mol_chain, vm, list_mol(list, cap, b), emol2, eabs2);
+    __syncthreads();
+  }
 }
 
 // FP32 pair terms of neighbour atom b (at bx + lx etc. relative to the moved
@@ -690,7 +943,7 @@ __global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, cons
   const int c = range_chain(R, blockIdx.x);
   if (vm[c].state != want) return;
   const ChainHdr& H = P.hdr[c];
-  const bool mixed = want == 1;
+  const bool mixed = want == 1 || want == 4;
   double2 acc = make_double2(0.0, 0.0), ab = make_double2(0.0, 0.0);
   for (int i = threadIdx.x; i < H.n_mol; i += blockDim.x) {
     acc.x += emol2[H.mol0 + i].x;
@@ -729,14 +982,17 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
   if (i >= n_items) return;
   const int c = range_chain(R, i);
   VolMove v = vm[c];
-  if (pass == 0 ? (v.state != 1 && v.state != 2) : v.state != 4) return;
+  if (pass == 0 ? (v.state != 1 && v.state != 2) : v.state != (pass == 1 ? 4 : 5)) return;
   ChainHdr& H = P.hdr[c];
   double e_old = H.energy, e_new = 0.0;
   int ok = 0;
-  if (v.state == 1 || v.state == 4) {
-    // a mixed move's U(V) is the running energy (error bound run_err), its
-    // U(V') the FP32 total; otherwise both are FP64 totals
+  if (v.state != 2) {
+    // a mixed move's U(V) is the running energy (error bound run_err) and
+    // its U(V') the FP32 total; a re-take has both totals in double-float
+    // (state 4) or, when that is still too close to call, in FP64 (state 5);
+    // an FP64 chain has both FP64 totals
     const bool mixed = v.state == 1 && H.vol_mixed;
+    const bool dfl = v.state == 4;
     e_old = mixed ? H.energy : esum[c].x;
     e_new = esum[c].y;
     const double vo = H.L[0] * H.L[1] * H.L[2];
@@ -745,13 +1001,19 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
     const double d_lrc = H.lrc_v / vn - H.lrc_v / vo;
     const double arg = -((e_new - e_old) + d_lrc + H.pressure * (vn - vo)) / H.kT +
                        (double)(H.n_mol + 1) * v.dlnv;
-    const double new_err = mixed ? kTieRel * eabs[c].y : 0.0;
+    double err_old = 0.0, err_new = 0.0;
     if (mixed) {
-      // |error of dU| <= kTieRel * (sum of V' term magnitudes) + run_err
-      const double bound =
-          (new_err + H.run_err + 1e-12 * (fabs(e_old) + fabs(e_new))) / H.kT;
+      err_old = H.run_err;
+      err_new = kTieRel * eabs[c].y;
+    } else if (dfl) {
+      err_old = kDfRel * eabs[c].x;
+      err_new = kDfRel * eabs[c].y;
+    }
+    if (mixed || dfl) {
+      // |error of dU| <= err_old + err_new
+      const double bound = (err_old + err_new + 1e-12 * (fabs(e_old) + fabs(e_new))) / H.kT;
       if (fabs(arg - log(v.u)) <= bound + 1e-12) {
-        v.state = 4;
+        v.state = mixed ? 4 : 5;
         v.fp64 = 1;
         vm[c] = v;
         return;
@@ -760,10 +1022,10 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
     ok = (arg >= 0.0) || (exp(arg) >= v.u);
     if (ok) {
       H.energy = e_new;
-      H.run_err = new_err;
+      H.run_err = err_new;
     } else if (!mixed) {
       H.energy = e_old;
-      H.run_err = 0.0;
+      H.run_err = err_old;
     }
   }
   H.vol_tried++;
@@ -875,8 +1137,9 @@ cudaError_t launch_chain_energy(Pool P, const int* mol_chain, int n_mol_total, V
 // molecules, numbered from 0; otherwise all pool molecules in chunks.
 cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, VolMove* vm,
                                 double2* emol2, double2* eabs2, double2* esum, double2* esum_abs,
-                                mcgpu_vol_trace* trace, int trace_slot, int trace_stride,
-                                cudaStream_t st, MolRanges act, bool has64, bool has32) {
+                                int* vlist, mcgpu_vol_trace* trace, int trace_slot,
+                                int trace_stride, cudaStream_t st, MolRanges act, bool has64,
+                                bool has32) {
   const int nc = act.act_slot ? act.n_act : P.n_chains;
   if (nc == 0) return cudaSuccess;
   k_vol_propose<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, act, nc);
@@ -913,10 +1176,20 @@ cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, V
   k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, trace, trace_slot,
                                                 trace_stride, act, nc, 0);
   if (has32) {
-    pairs(true, 1);
+    // too close to call in FP32: double-float re-take, and FP64 for what
+    // is still too close after that
+    // the re-takes run over the listed chains' molecules only (grid-strided)
+    const int grid = kVolListGrid;
+    k_vol_list<<<1, 32, 0, st>>>(P, vm, act, nc, 4, vlist);
+    k_vol_pair_sums_df<<<grid, kVolThreads, 0, st>>>(P, mol_chain, vm, vlist, nc, emol2, eabs2);
     k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 4);
     k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, trace, trace_slot,
                                                   trace_stride, act, nc, 1);
+    k_vol_list<<<1, 32, 0, st>>>(P, vm, act, nc, 5, vlist);
+    k_vol_pair_sums_list<<<grid, kVolThreads, 0, st>>>(P, mol_chain, vm, vlist, nc, emol2);
+    k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 5);
+    k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, trace, trace_slot,
+                                                  trace_stride, act, nc, 2);
   }
   if (items > 0) k_vol_refresh<<<(items + 127) / 128, 128, 0, st>>>(P, mol_chain, vm, items, act);
   return cudaGetLastError();

@@ -110,6 +110,7 @@ struct mcgpu_server {
   double2* eabs2 = nullptr;
   double2* vsum = nullptr;
   double2* vsum_abs = nullptr;
+  int* vlist = nullptr;        // chains of a re-take (3 * slots + 3)
   // pinned host buffers
   ChainHdr* hmirror = nullptr;
   int* hlist = nullptr;
@@ -162,6 +163,7 @@ int server_alloc(mcgpu_server* s) {
   s->eabs2 = dalloc<double2>(nm, &e);
   s->vsum = dalloc<double2>(nc, &e);
   s->vsum_abs = dalloc<double2>(nc, &e);
+  s->vlist = dalloc<int>(3 * (size_t)nc + 3, &e);
   if (e == cudaSuccess) e = cudaMemsetAsync(P.hdr, 0, sizeof(ChainHdr) * nc, ctx->stream);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&s->hmirror, sizeof(ChainHdr) * nc);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&s->hlist, sizeof(int) * (4 * (size_t)nc + 1));
@@ -173,7 +175,8 @@ int server_alloc(mcgpu_server* s) {
 
 void server_free(mcgpu_server* s) {
   s->pool.release();
-  void* d[] = {s->qctr, s->dlist, s->dinit, s->vm, s->emol2, s->eabs2, s->vsum, s->vsum_abs};
+  void* d[] = {s->qctr, s->dlist, s->dinit, s->vm, s->emol2, s->eabs2, s->vsum, s->vsum_abs,
+               s->vlist};
   for (void* p : d)
     if (p) cudaFree(p);
   if (s->hmirror) cudaFreeHost(s->hmirror);
@@ -266,8 +269,9 @@ int upload_job(mcgpu_server* s, Job* j) {
   k_refresh_mirrors<<<(n + wpb - 1) / wpb, wpb * 32, 0, st>>>(P, s->pool.mol_chain, m0, m0 + n);
   k_chain_init<<<(n + wpb - 1) / wpb, wpb * 32, 0, st>>>(P, s->pool.mol_chain, m0, m0 + n);
   CK(ctx, cudaGetLastError());
-  // initial running energy: FP64 system energy over the job's cell grid
-  // (its own molecules, slot and scratch entries only)
+  // initial running energy over the job's cell grid (its own molecules,
+  // slot and scratch entries only): FP64, or for a job whose volume moves
+  // take FP32 pair terms FP32 pairs with their error bound (run_err)
   int* dr = s->dinit + 4 * slot;
   const int rng[4] = {slot, m0, 0, n};
   if ((rc = stage_copy(s, dr, rng, 4))) return rc;
@@ -278,7 +282,7 @@ int upload_job(mcgpu_server* s, Job* j) {
   R.n_act = 1;
   R.total = n;
   CK(ctx, launch_chain_energy(P, s->pool.mol_chain, 0, s->vm, s->emol2, s->eabs2, s->vsum,
-                              s->vsum_abs, st, R, true));
+                              s->vsum_abs, st, R, !(j->npt && j->vol_mixed)));
   return MCGPU_OK;
 }
 
@@ -428,7 +432,8 @@ int launch_round(mcgpu_server* s) {
     R.n_act = n_npt;
     R.total = total;
     CK(ctx, launch_volume_phase(s->pool.P, s->pool.mol_chain, 0, s->vm, s->emol2, s->eabs2,
-                                s->vsum, s->vsum_abs, nullptr, 0, 0, st, R, has64, has32));
+                                s->vsum, s->vsum_abs, s->vlist, nullptr, 0, 0, st, R, has64,
+                                has32));
   }
   CK(ctx, cudaMemcpyAsync(s->hmirror, s->pool.P.hdr, sizeof(ChainHdr) * nc, cudaMemcpyDeviceToHost, st));
   CK(ctx, cudaEventRecord(s->ev_round, st));
