@@ -338,6 +338,13 @@ __device__ __forceinline__ void ff_add2(float& hi, float& lo, float h2, float l2
   lo = __fadd_rn(lo, l2);
 }
 
+// Exact int -> float for |x| < 2^22 by integer arithmetic on the bits of
+// 1.5 * 2^23 (no conversion instruction: on this part those issue on the
+// slow FP64 pipe).
+__device__ __forceinline__ float small_i2f(int x) {
+  return __int_as_float(0x4B400000 + x) - 12582912.0f;
+}
+
 // ---- double-float arithmetic ----------------------------------------------
 // A value h + l with |l| <= ulp(h)/2 (about 48 significant bits) on FP32
 // instructions: Knuth's two-sum, the FMA two-product, and the usual

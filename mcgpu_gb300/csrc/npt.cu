@@ -261,26 +261,41 @@ __global__ void k_vc_sort(Pool P, const int* mol_chain, const VolMove* vm, MolRa
 struct VcStencil {
   int start[27], cnt[27], pref[28];
   int n;
+  int half;   // cell 0 is the molecule's own (pairs j > m), cells 1.. the
+              // forward half of the neighbours (every pair): each pair once
 };
 
-// The (up to 27) stencil cells of molecule m's cell, in x-, y-, z-nested
-// order (c-1, c, c+1 per edge with at least 3 cells, else every cell once),
-// with their members' prefix sums.  Warp 0 builds it: one cell per lane, so
-// the cells' counts and starts arrive in one round trip.
+// The stencil cells of molecule m's cell with their members' prefix sums.
+// With at least 3 cells per edge: the own cell, then the 13 neighbours of
+// the forward half (offsets after (0,0,0) in x-, y-, z-nested order) --
+// each pair of molecules is met once, from the molecule whose cell comes
+// first, or within a cell from the lower index.  Otherwise every cell once
+// (c-1, c, c+1 per edge with at least 3 cells, else all) with pairs j > m.
+// Warp 0 builds it: one cell per lane, so the counts and starts arrive in
+// one round trip.
 __device__ inline void vc_stencil(const Pool& P, const ChainHdr& H, int m, VcStencil& S) {
   if (threadIdx.x >= 32) return;
   const int lane = threadIdx.x;
   const int local = P.vc_of[m] - H.mol0;
   const int n0 = H.vncell[0], n1 = H.vncell[1], n2 = H.vncell[2];
   const int cz = local % n2, cy = (local / n2) % n1, cx = local / (n1 * n2);
+  const bool half = n0 >= 3 && n1 >= 3 && n2 >= 3;
   const int s0 = n0 >= 3 ? 3 : n0, s1 = n1 >= 3 ? 3 : n1, s2 = n2 >= 3 ? 3 : n2;
-  const int n = s0 * s1 * s2;
+  const int n = half ? 14 : s0 * s1 * s2;
   int start = 0, cnt = 0;
   if (lane < n) {
-    const int a = lane / (s1 * s2), b = (lane / s2) % s1, c = lane % s2;
-    const int x = n0 >= 3 ? (cx + n0 - 1 + a) % n0 : a;
-    const int y = n1 >= 3 ? (cy + n1 - 1 + b) % n1 : b;
-    const int z = n2 >= 3 ? (cz + n2 - 1 + c) % n2 : c;
+    int x, y, z;
+    if (half) {
+      const int t = lane == 0 ? 13 : 13 + lane;   // 13 is the offset (0,0,0)
+      x = (cx + n0 + t / 9 - 1) % n0;
+      y = (cy + n1 + (t / 3) % 3 - 1) % n1;
+      z = (cz + n2 + t % 3 - 1) % n2;
+    } else {
+      const int a = lane / (s1 * s2), b = (lane / s2) % s1, c = lane % s2;
+      x = n0 >= 3 ? (cx + n0 - 1 + a) % n0 : a;
+      y = n1 >= 3 ? (cy + n1 - 1 + b) % n1 : b;
+      z = n2 >= 3 ? (cz + n2 - 1 + c) % n2 : c;
+    }
     const int cell = H.mol0 + (x * n1 + y) * n2 + z;
     start = P.vc_start[cell];
     cnt = P.vc_cnt[cell];
@@ -297,7 +312,15 @@ __device__ inline void vc_stencil(const Pool& P, const ChainHdr& H, int m, VcSte
     S.pref[lane] = incl - cnt;
   }
   if (lane == n - 1) S.pref[n] = incl;
-  if (lane == 0) S.n = n;
+  if (lane == 0) {
+    S.n = n;
+    S.half = half ? 1 : 0;
+  }
+}
+
+// Whether molecule m takes candidate j found in stencil cell k.
+__device__ __forceinline__ bool vc_takes(const VcStencil& S, int k, int j, int m) {
+  return S.half ? (k > 0 || j > m) : j > m;
 }
 
 // Candidate t of the stencil (t < S.pref[S.n]); k is the thread's cursor
@@ -315,8 +338,8 @@ __device__ __forceinline__ void vol_fixdiff(uint4 b, uint4 a, const VolBox& B, f
   float h[3], l[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    const int dh = d[k] & ~0xFF;
-    const float fh = (float)dh, fl = (float)(d[k] - dh);
+    // d = (d >> 9) 2^9 + (d & 511): both parts exact in FP32
+    const float fh = small_i2f(d[k] >> 9) * 512.0f, fl = small_i2f(d[k] & 511);
     const float p = fh * B.fxs[k];
     const float e = fmaf(fh, B.fxs[k], -p);
     const float t = fmaf(fh, B.fxs_lo[k], fmaf(fl, B.fxs[k], e));
@@ -347,7 +370,10 @@ __device__ __forceinline__ int vol_screen(const Pool& P, const ChainHdr& H, cons
                                           const float4* so, const int* spa, int npidx, uint4 Am,
                                           int j, float reach2, float sf, int w0, int nvol) {
   const uint4 Aj = P.mfix[j];
-  const float3 D0 = fixdiff(Aj, Am, H);
+  // coarse anchor distance for the reach test (error <= 2^9 L / 2^32)
+  const float3 D0 = make_float3(small_i2f((int)(Aj.x - Am.x) >> 9) * (512.0f * H.fxs[0]),
+                                small_i2f((int)(Aj.y - Am.y) >> 9) * (512.0f * H.fxs[1]),
+                                small_i2f((int)(Aj.z - Am.z) >> 9) * (512.0f * H.fxs[2]));
   const float d2 = fmaf(D0.x, D0.x, fmaf(D0.y, D0.y, D0.z * D0.z));
   if (d2 > reach2 && d2 * sf * sf > reach2) return 0;
   const int2 pj = P.mpi[j];
@@ -525,7 +551,7 @@ __device__ __forceinline__ void vol_f64_mol(const Pool& P, const int* mol_chain,
       int f = 0, j = 0;
       if (t < n_cand) {
         j = vc_candidate(P, S, t, kc);
-        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, 0, nvol);
+        if (vc_takes(S, kc, j, m)) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, 0, nvol);
       }
       vol_append(ent, wcnt, j, f, r);
     }
@@ -679,7 +705,7 @@ __device__ __forceinline__ void vol_df_mol(const Pool& P, const int* mol_chain,
       int f = 0, j = 0;
       if (t < n_cand) {
         j = vc_candidate(P, S, t, kc);
-        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, 0, 2);
+        if (vc_takes(S, kc, j, m)) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, 0, 2);
       }
       vol_append(ent, wcnt, j, f, r);
     }
@@ -863,7 +889,7 @@ __global__ void __launch_bounds__(kVolThreads, 7) k_vol_pair_sums32(Pool P, cons
       int f = 0, j = 0;
       if (t < n_cand) {
         j = vc_candidate(P, S, t, kc);
-        if (j > m) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, w0, 1);
+        if (vc_takes(S, kc, j, m)) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, w0, 1);
       }
       vol_append(ent, wcnt, j, f, r);
     }
