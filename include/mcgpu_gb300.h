@@ -315,6 +315,9 @@ typedef struct {
   double *x_out, *y_out, *z_out; /* final coordinates (n_atom each), may be
                                  NULL; must stay valid until the job's result
                                  is taken by mcgpu_server_results          */
+  double lrc_v;               /* NPT: E_LRC * V of the job's long-range LJ
+                                 correction in the volume criterion (see
+                                 mcgpu_batch_set_lrc); 0 for none           */
 } mcgpu_job_desc;
 
 typedef struct {

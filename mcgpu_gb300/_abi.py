@@ -79,7 +79,8 @@ class JobDesc(C.Structure):
     _fields_ = [("box", C.POINTER(BoxDesc)), ("seed", C.c_uint64), ("chain_id", C.c_uint32),
                 ("npt", C.c_int32), ("vol_precision", C.c_int32), ("pad1", C.c_int32),
                 ("n_steps", C.c_int64), ("pressure_atm", C.c_double),
-                ("max_dlnv", C.c_double), ("x_out", _dp), ("y_out", _dp), ("z_out", _dp)]
+                ("max_dlnv", C.c_double), ("x_out", _dp), ("y_out", _dp), ("z_out", _dp),
+                ("lrc_v", C.c_double)]
 
 
 class JobResult(C.Structure):

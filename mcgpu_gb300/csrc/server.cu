@@ -72,7 +72,7 @@ struct Job {
   HostPool hp;  // the job's rows as chain 0 at offset 0
   int64_t n_steps = 0;
   int npt = 0, vol_mixed = 0;
-  double pressure = 0, max_dlnv = 0;
+  double pressure = 0, max_dlnv = 0, lrc_v = 0;
   double *x_out = nullptr, *y_out = nullptr, *z_out = nullptr;
   double t_submit = 0, t_admit = 0;
   long long bytes = 0;
@@ -252,6 +252,7 @@ int upload_job(mcgpu_server* s, Job* j) {
   h.vol_interval = j->npt ? s->cfg.round_steps : 0;
   h.pressure = j->pressure;
   h.max_dlnv = j->max_dlnv;
+  h.lrc_v = j->lrc_v;
   h.vol_mixed = j->vol_mixed;
   Pool& P = s->pool.P;
   int rc = MCGPU_OK;
@@ -530,6 +531,8 @@ extern "C" int mcgpu_server_submit(mcgpu_server* s, const mcgpu_job_desc* jd, in
       return set_err(ctx, MCGPU_ERR_INVALID, "job pressure %g atm", jd->pressure_atm);
     if (!(jd->max_dlnv > 0 && jd->max_dlnv <= 0.1))
       return set_err(ctx, MCGPU_ERR_INVALID, "job max ln V step %g outside (0, 0.1]", jd->max_dlnv);
+    if (!std::isfinite(jd->lrc_v))
+      return set_err(ctx, MCGPU_ERR_INVALID, "job lrc_v is not finite");
   }
   Job* j = new Job();
   int rc = append_chain(ctx, j->hp, jd->box, 0, jd->seed, s->cfg.rotation);
@@ -557,6 +560,7 @@ extern "C" int mcgpu_server_submit(mcgpu_server* s, const mcgpu_job_desc* jd, in
   j->npt = jd->npt ? 1 : 0;
   j->pressure = jd->npt ? jd->pressure_atm * kAtmKcal : 0.0;
   j->max_dlnv = jd->npt ? jd->max_dlnv : 0.0;
+  j->lrc_v = jd->npt ? jd->lrc_v : 0.0;
   j->vol_mixed = (jd->npt && jd->vol_precision == MCGPU_PREC_MIXED) ? 1 : 0;
   j->x_out = jd->x_out;
   j->y_out = jd->y_out;

@@ -70,7 +70,8 @@ class JobServer:
 
     def submit(self, box: BoxData, seed: int, n_steps: int, chain_id: int = 0,
                npt: bool = False, pressure_atm: float = 1.0, max_dlnv: float = 0.01,
-               want_coords: bool = True, vol_precision: int = _abi.PREC_FP64) -> int:
+               want_coords: bool = True, vol_precision: int = _abi.PREC_FP64,
+               lrc_v: float = 0.0) -> int:
         b = box.copy().normalise()
         d = b.desc()
         jd = _abi.JobDesc()
@@ -82,6 +83,7 @@ class JobServer:
         jd.n_steps = int(n_steps)
         jd.pressure_atm = float(pressure_atm)
         jd.max_dlnv = float(max_dlnv)
+        jd.lrc_v = float(lrc_v)
         xyz = None
         if want_coords:
             xyz = tuple(np.empty(b.n_atom) for _ in range(3))

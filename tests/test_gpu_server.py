@@ -70,6 +70,10 @@ def test_server_matches_oracle(ctx):
     """Served jobs (NVT and NPT) replayed by the oracle: same coordinates bit
     for bit, same volume decisions, energies within the FP32-pair rule."""
     jobs = mixed_jobs(4, seed=9)[:4]
+    for j in jobs:
+        if j["npt"]:   # a tail correction in the volume criterion (E_LRC * V)
+            b = j["box"]
+            j["lrc_v"] = -2.0 * b.n_mol * float(b.size[0] * b.size[1] * b.size[2])
     outs = run_server(ctx, jobs, hbm_budget_bytes=64 * MB, max_slots=8, round_steps=50)
     for j, out in zip(jobs, outs):
         oc = OracleChain(j["box"], ROT_AXIS)
@@ -81,7 +85,7 @@ def test_server_matches_oracle(ctx):
             done += k
             if j["npt"] and done % 50 == 0:
                 r = oc.volume_move(j["seed"], j["chain_id"], done, j["pressure_atm"],
-                                   j["max_dlnv"], e)
+                                   j["max_dlnv"], e, j.get("lrc_v", 0.0))
                 e = r["energy"]
                 vacc += r["status"] == 1
         assert np.array_equal(out.coords, oc.coords())
