@@ -299,11 +299,12 @@ def _run_chain(a, ctx, inp, steps, lrc0, ensemble, vol_interval, strategy, base,
 
 def main(argv=None) -> int:
     try:
-        run(argv)
+        res = run(argv)
     except F.FileFormatError as e:
         sys.stderr.write(str(e) + "\n")
         return 1
-    _log("Finishing simulation...\n\n", sys.stdout)
+    if res is not None:
+        _log("Finishing simulation...\n\n", sys.stdout)
     return 0
 
 
