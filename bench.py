@@ -486,7 +486,7 @@ def main():
         b2.close()
         e2e = {"value": moves_local / dt_e2e, "unit": "moves/s",
                "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
-               "note": "create batch from host boxes (incl. initial FP64 system energies), "
+               "note": "create batch from host boxes (incl. initial FP32-pair system energies), "
                        f"{STEPS_PER_BENCH * args.steps} steps per chain, all coordinates and "
                        "stats back"}
 

@@ -187,7 +187,10 @@ int mcgpu_chain_run(mcgpu_box* box, uint64_t seed, uint32_t chain_id,
 
 /* Uploads n_chains independent boxes (uneven sizes and temperatures allowed)
  * into one device pool; chain c uses Philox key seeds[c] and counter
- * chain id c.  precision is MCGPU_PREC_MIXED in this build. */
+ * chain id c.  precision is MCGPU_PREC_MIXED in this build.  The running
+ * energies start from FP32-pair system energies (double-float sums; their
+ * error bound is carried with the chain); mcgpu_batch_system_energy gives
+ * FP64 totals. */
 int mcgpu_batch_create(mcgpu_ctx* ctx, int n_chains, const mcgpu_box_desc* descs,
                        const uint64_t* seeds, int rotation, mcgpu_batch** out);
 int mcgpu_batch_destroy(mcgpu_batch* batch);

@@ -824,14 +824,17 @@ extern "C" int mcgpu_batch_create(mcgpu_ctx* ctx, int n_chains, const mcgpu_box_
   }
   bt->cache_n = pool_cache_n(bt->pool);
   // device-resident chain state (rows snapped to it), then the initial
-  // running energies: full FP64 system energy of every chain
+  // running energies
   rc = pool_chain_init(ctx, bt->pool, ctx->stream);
   if (rc) {
     mcgpu_batch_destroy(bt);
     return rc;
   }
-  // initial running energies: FP64 system energies over per-chain cell
-  // grids (the volume-move machinery at the chains' own boxes)
+  // initial running energies: FP32-pair system energies (double-float
+  // sums) over per-chain cell grids, the volume-move machinery at the
+  // chains' own boxes; each chain's run_err starts at their error bound.
+  // The chains compute in FP32 pairs throughout; FP64 enters where a
+  // decision is too close to call.
   {
     cudaError_t e2 = cudaSuccess;
     Pool& P = bt->pool.P;
@@ -847,7 +850,7 @@ extern "C" int mcgpu_batch_create(mcgpu_ctx* ctx, int n_chains, const mcgpu_box_
     P.vc_of = dalloc<int>(nm, &e2);
     if (e2 == cudaSuccess)
       e2 = launch_chain_energy(P, bt->pool.mol_chain, bt->pool.n_mol, bt->vm, bt->emol2, bt->eabs2,
-                               bt->vsum, bt->vsum_abs, ctx->stream, MolRanges(), true);
+                               bt->vsum, bt->vsum_abs, ctx->stream, MolRanges(), false);
     if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(ctx->stream);
     if (e2 != cudaSuccess) {
       mcgpu_batch_destroy(bt);
