@@ -480,8 +480,7 @@ def main():
         b2.set_tile(threads, cpc, spl, lanes)
         b2.run(STEPS_PER_BENCH * args.steps, sync=True)
         st_e2e = b2.stats()
-        for c in range(N_CHAINS):
-            b2.download(c)
+        b2.download_all()
         dt_e2e = time.perf_counter() - t0
         b2.close()
         e2e = {"value": moves_local / dt_e2e, "unit": "moves/s",

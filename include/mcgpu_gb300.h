@@ -261,6 +261,9 @@ int mcgpu_batch_stats(mcgpu_batch* batch, mcgpu_chain_stats* stats);
 /* Coordinates of chain c (arrays sized like its descriptor). */
 int mcgpu_batch_download(mcgpu_batch* batch, int chain, double* x, double* y,
                          double* z);
+/* Coordinates of every chain, concatenated in chain order (arrays of the
+ * batch's total atom count): three copies for the whole batch. */
+int mcgpu_batch_download_all(mcgpu_batch* batch, double* x, double* y, double* z);
 /* Checkpoint of a batch: the resumable device state (coordinates, anchors,
  * orientations, screen positions, every chain header with its running
  * energy, counters and Philox step counter, the Verlet lists, the NPT

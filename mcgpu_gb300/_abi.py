@@ -126,6 +126,7 @@ _PROTOS = {
     "mcgpu_batch_checkpoint": (C.c_int, [_vp, _vp, C.c_size_t, C.POINTER(C.c_size_t)]),
     "mcgpu_batch_restore": (C.c_int, [_vp, _vp, C.c_size_t]),
     "mcgpu_batch_set_lrc": (C.c_int, [_vp, _dp]),
+    "mcgpu_batch_download_all": (C.c_int, [_vp, _dp, _dp, _dp]),
     "mcgpu_build_centres": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint64, _dp]),
     "mcgpu_server_create": (C.c_int, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "mcgpu_server_destroy": (C.c_int, [_vp]),

@@ -12,19 +12,68 @@ from .step import Context
 from .workloads import BoxData
 
 
+_F64 = ("x", "y", "z", "sigma", "epsilon", "charge")
+_I32 = ("mol_start", "mol_len", "mol_pidx_start", "mol_pidx_count", "pidx")
+
+
+def _desc_dtype() -> np.dtype:
+    """mcgpu_box_desc as a numpy record (pointers as 64-bit addresses)."""
+    names, formats, offsets = [], [], []
+    for name, ctype in _abi.BoxDesc._fields_:
+        names.append(name)
+        offsets.append(getattr(_abi.BoxDesc, name).offset)
+        if ctype is C.c_int32:
+            formats.append(np.int32)
+        elif ctype is C.c_double:
+            formats.append(np.float64)
+        elif ctype is C.c_double * 3:
+            formats.append((np.float64, 3))
+        else:
+            assert C.sizeof(ctype) == 8
+            formats.append(np.uint64)
+    return np.dtype({"names": names, "formats": formats, "offsets": offsets,
+                     "itemsize": C.sizeof(_abi.BoxDesc)})
+
+
 class ChainBatch:
     def __init__(self, ctx: Context, boxes: list[BoxData], seeds, rotation: int = _abi.ROT_AXIS):
+        """Uploads the boxes as one pool (their rows are copied by the
+        library).  The descriptors are filled as one numpy record array that
+        points at the boxes' own arrays (converted only where they are not
+        contiguous FP64 / int32 already)."""
         self.ctx = ctx
-        self.boxes = [b.copy().normalise() for b in boxes]
-        n = len(self.boxes)
-        self._descs = (_abi.BoxDesc * n)()
-        for i, b in enumerate(self.boxes):
-            self._descs[i] = b.desc()
+        n = len(boxes)
+        self.n_chains = n
+        self.n_atom = np.array([b.n_atom for b in boxes], np.int64)
+        self._atom0 = np.concatenate([[0], np.cumsum(self.n_atom)])
+        d = np.zeros(n, _desc_dtype())
+        d["n_mol"] = [b.n_mol for b in boxes]
+        d["n_atom"] = self.n_atom
+        d["n_pidx"] = [b.n_pidx for b in boxes]
+        keep = []
+        addr = np.empty((n, len(_F64) + len(_I32)), np.uint64)
+        for i, b in enumerate(boxes):
+            row = addr[i]
+            for f, k in enumerate(_F64 + _I32):
+                a = getattr(b, k)
+                dt = np.float64 if f < len(_F64) else np.int32
+                if not (isinstance(a, np.ndarray) and a.dtype == dt and a.flags.c_contiguous):
+                    a = np.ascontiguousarray(a, dt)
+                keep.append(a)
+                row[f] = a.__array_interface__["data"][0]
+        for f, k in enumerate(_F64 + _I32):
+            d[k] = addr[:, f]
+        d["size"] = np.array([np.asarray(b.size, np.float64)[:3] for b in boxes]).reshape(n, 3)
+        d["cutoff"] = [float(b.cutoff) for b in boxes]
+        d["temperature"] = [float(b.temperature) for b in boxes]
+        d["max_translate"] = [float(b.max_translate) for b in boxes]
+        d["max_rotate"] = [float(b.max_rotate) for b in boxes]
         self._seeds = (C.c_uint64 * n)(*[int(s) & (2 ** 64 - 1) for s in seeds])
         self._h = C.c_void_p()
-        _abi.check(_abi.lib().mcgpu_batch_create(ctx.handle, n, self._descs, self._seeds,
-                                                 int(rotation), C.byref(self._h)), ctx.handle)
-        self.n_chains = n
+        _abi.check(_abi.lib().mcgpu_batch_create(
+            ctx.handle, n, C.cast(d.ctypes.data, C.POINTER(_abi.BoxDesc)), self._seeds,
+            int(rotation), C.byref(self._h)), ctx.handle)
+        del keep        # the pool holds its own copy now
         ctx.adopt(self)
 
     def _check(self, st: int) -> None:
@@ -114,12 +163,24 @@ class ChainBatch:
         return list(arr)
 
     def download(self, chain: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
-        n = self.boxes[chain].n_atom
+        n = int(self.n_atom[chain])
         x, y, z = np.empty(n), np.empty(n), np.empty(n)
         dp = C.POINTER(C.c_double)
         self._check(_abi.lib().mcgpu_batch_download(self._h, int(chain), x.ctypes.data_as(dp),
                                                     y.ctypes.data_as(dp), z.ctypes.data_as(dp)))
         return x, y, z
+
+    def download_all(self) -> list:
+        """Coordinates of every chain, (x, y, z) per chain, in three copies."""
+        tot = int(self._atom0[-1])
+        x, y, z = np.empty(tot), np.empty(tot), np.empty(tot)
+        dp = C.POINTER(C.c_double)
+        self._check(_abi.lib().mcgpu_batch_download_all(self._h, x.ctypes.data_as(dp),
+                                                        y.ctypes.data_as(dp),
+                                                        z.ctypes.data_as(dp)))
+        a = self._atom0
+        return [(x[a[c]:a[c + 1]], y[a[c]:a[c + 1]], z[a[c]:a[c + 1]])
+                for c in range(self.n_chains)]
 
     def checkpoint(self) -> bytes:
         """The batch's resumable device state (chain states with their

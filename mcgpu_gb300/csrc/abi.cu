@@ -1222,6 +1222,22 @@ extern "C" int mcgpu_batch_download(mcgpu_batch* bt, int chain, double* x, doubl
   return MCGPU_OK;
 }
 
+extern "C" int mcgpu_batch_download_all(mcgpu_batch* bt, double* x, double* y, double* z) {
+  if (!bt || !x || !y || !z) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = bt->ctx;
+  if (bt->rows_stale) {
+    int rc = pool_chain_export(ctx, bt->pool, ctx->stream);
+    if (rc) return rc;
+    bt->rows_stale = false;
+  }
+  const size_t n = (size_t)bt->pool.n_atom;
+  CK(ctx, cudaMemcpyAsync(x, bt->pool.P.x, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(y, bt->pool.P.y, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(z, bt->pool.P.z, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MCGPU_OK;
+}
+
 extern "C" int mcgpu_batch_system_energy(mcgpu_batch* bt, double* out) {
   if (!bt || !out) return set_err(bt ? bt->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
   mcgpu_ctx* ctx = bt->ctx;

@@ -204,3 +204,15 @@ def test_batch_restore_rejects_other_layout(ctx):
         a.restore(bytes(bad))           # checksum
     for bt in (a, other, same):
         bt.close()
+
+
+def test_batch_download_all_equals_per_chain(ctx):
+    boxes, seeds = W.water_chains(5, n_min=64, n_max=300, seed=8)
+    bt = ChainBatch(ctx, boxes, seeds)
+    bt.run(64)
+    allc = bt.download_all()
+    for c in range(len(boxes)):
+        x, y, z = bt.download(c)
+        ax, ay, az = allc[c]
+        assert np.array_equal(x, ax) and np.array_equal(y, ay) and np.array_equal(z, az)
+    bt.close()
