@@ -792,6 +792,16 @@ extern "C" int mcgpu_batch_create(mcgpu_ctx* ctx, int n_chains, const mcgpu_box_
     return set_err(ctx, MCGPU_ERR_INVALID, "unknown rotation form %d", rotation);
   CK(ctx, cudaSetDevice(ctx->device));
   HostPool hp;
+  {
+    size_t na = 0, nm = 0, np = 0;
+    for (int c = 0; c < n_chains; c++) {
+      na += descs[c].n_atom > 0 ? (size_t)descs[c].n_atom : 0;
+      nm += descs[c].n_mol > 0 ? (size_t)descs[c].n_mol : 0;
+      np += descs[c].n_pidx > 0 ? (size_t)descs[c].n_pidx : 0;
+    }
+    if (na <= (1ull << 30) && nm <= (1ull << 26) && np <= (1ull << 28))
+      hp.reserve(na, nm, np, (size_t)n_chains);
+  }
   for (int c = 0; c < n_chains; c++) {
     int rc = append_chain(ctx, hp, &descs[c], c, seeds[c], rotation);
     if (rc) return rc;

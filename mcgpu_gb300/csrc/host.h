@@ -89,6 +89,18 @@ struct HostPool {
   std::vector<float> mrad;
   std::vector<ChainHdr> hdr;
   int max_len = 0;
+  // capacity for the given totals (one allocation per row instead of growth)
+  void reserve(size_t atoms, size_t mols, size_t pidxs, size_t chains) {
+    for (auto* v : {&x, &y, &z, &sig, &eps, &q}) v->reserve(atoms);
+    aoff.reserve(atoms);
+    aeq.reserve(atoms);
+    atom_mol.reserve(atoms);
+    for (auto* v : {&mstart, &mlen, &mol_chain}) v->reserve(mols);
+    mpi.reserve(mols);
+    mrad.reserve(mols);
+    pidx.reserve(pidxs);
+    hdr.reserve(chains);
+  }
 };
 
 // Validates one descriptor and appends it as chain `c` of the host pool.
