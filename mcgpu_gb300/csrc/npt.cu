@@ -846,7 +846,7 @@ __device__ __forceinline__ void vol_atoms32(const float4* so, const float2* sq, 
 // arithmetic) summed in double-float; eabs2 gets the sums of the terms'
 // magnitudes.  The in-range test is the FP32 screen with the FP64 re-test
 // inside its guard band: the FP64 test's set exactly.
-__global__ void __launch_bounds__(kVolThreads, 7) k_vol_pair_sums32(Pool P, const int* mol_chain,
+__global__ void __launch_bounds__(kVolThreads, 8) k_vol_pair_sums32(Pool P, const int* mol_chain,
                                                                  const VolMove* vm, int m_begin,
                                                                  MolRanges R, double2* emol2,
                                                                  double2* eabs2, int init) {
