@@ -283,7 +283,7 @@ def bench_large(ctx, steps: int = 6000) -> dict:
     out = {"workload": "32768 waters, L=99.3 A, rc 12 A, NPT 298 K / 1 atm, Verlet skin 1.5 A, "
                        "volume move every 500 steps"}
     bt = M.ChainBatch(ctx, [box], [0x5EED], rotation=M.ROT_AXIS)
-    bt.set_tile(256, 1, 64)
+    bt.set_tile(512, 1, 64)          # one chain: one group of 16 warps
     bt.set_verlet(1.5)
     bt.set_npt(500, 1.0, 0.005, M.PREC_MIXED)
     bt.run(500)

@@ -391,6 +391,8 @@ extern "C" int mcgpu_ctx_create(mcgpu_ctx** out, int device) {
   }
   c->stream = c->own;
   if (cudaFuncSetAttribute(k_chain_steps, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           200 * 1024) != cudaSuccess ||
+      cudaFuncSetAttribute(k_chain_steps_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            200 * 1024) != cudaSuccess) {
     cudaStreamDestroy(c->own);
     delete c;
@@ -682,7 +684,8 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
     CK(ctx, cudaMalloc((void**)&b->dtrace, sizeof(mcgpu_trace) * (size_t)n_steps));
     b->trace_cap = n_steps;
   }
-  const int nw = std::max(1, std::min(8, dp.n_mol / 256));
+  // one group for the chain: up to 16 warps (the wide kernel above 8)
+  const int nw = std::max(1, std::min(16, dp.n_mol / 256));
   SmemShape sh = shape_for(dp.max_len, nw, pool_cache_n(dp));
   // with a Verlet list, short launches let stale lists be rebuilt promptly
   const int seg = dp.nl_on ? 64 : 1024;
@@ -693,8 +696,12 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
     CK(ctx, cudaMemsetAsync(b->queue, 0, sizeof(unsigned), st));
     Pool P = dp.P;
     P.trace = nullptr;
-    k_chain_steps<<<1, nw * 32, sh.bytes(), st>>>(P, k, b->queue, b->order, 1, nw, sh,
-                                                  trace ? b->dtrace : nullptr, done, 0, 0);
+    if (nw > 8)
+      k_chain_steps_wide<<<1, nw * 32, sh.bytes(), st>>>(P, k, b->queue, b->order, 1, nw, sh,
+                                                         trace ? b->dtrace : nullptr, done, 0, 0);
+    else
+      k_chain_steps<<<1, nw * 32, sh.bytes(), st>>>(P, k, b->queue, b->order, 1, nw, sh,
+                                                    trace ? b->dtrace : nullptr, done, 0, 0);
     CK(ctx, cudaGetLastError());
     b->rows_stale = true;
   }
@@ -759,7 +766,8 @@ static int batch_grid(mcgpu_batch* bt, int* smem_out) {
   const int smem = sh.bytes() * bt->cpc;
   *smem_out = smem;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chain_steps, bt->threads, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, bt->threads > 256 ? k_chain_steps_wide : k_chain_steps, bt->threads, smem);
   per_sm = std::max(per_sm, 1);
   const int need = (bt->pool.n_chains + bt->cpc - 1) / bt->cpc;
   return std::max(1, std::min(need, per_sm * bt->ctx->sm_count));
@@ -776,9 +784,14 @@ static int batch_launch(mcgpu_batch* bt, int steps, unsigned* q, cudaStream_t st
   int rc = pool_nl_rebuild(ctx, bt->pool, st);
   if (rc) return rc;
   CK(ctx, cudaMemsetAsync(q, 0, sizeof(unsigned), st));
-  k_chain_steps<<<grid, bt->threads, smem, st>>>(bt->pool.P, steps, q, bt->order,
-                                                 bt->pool.n_chains, gw, sh, trace, trace_off,
-                                                 trace_stride, bt->lanes);
+  if (bt->threads > 256)
+    k_chain_steps_wide<<<grid, bt->threads, smem, st>>>(bt->pool.P, steps, q, bt->order,
+                                                        bt->pool.n_chains, gw, sh, trace,
+                                                        trace_off, trace_stride, bt->lanes);
+  else
+    k_chain_steps<<<grid, bt->threads, smem, st>>>(bt->pool.P, steps, q, bt->order,
+                                                   bt->pool.n_chains, gw, sh, trace, trace_off,
+                                                   trace_stride, bt->lanes);
   CK(ctx, cudaGetLastError());
   return MCGPU_OK;
 }
@@ -1458,7 +1471,7 @@ extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
   float best = 1e30f, ms = 0;
   Tile bestT = {bt->threads, bt->cpc, bt->spl, bt->lanes};
   // CTA shape (threads, chains per CTA) with the default lanes
-  const int tw[] = {64, 128, 256};
+  const int tw[] = {64, 128, 256, 512};
   for (int t : tw)
     for (int gw = 1; gw <= t / 32 && rc == MCGPU_OK; gw *= 2) {
       const int cpc = (t / 32) / gw;

@@ -22,6 +22,9 @@ __global__ void k_set_energy(Pool P, const double* e);
 __global__ void k_chain_steps(Pool P, int n_steps, unsigned* queue, const int* order, int n_tasks,
                               int gwarps, SmemShape shape, mcgpu_trace* trace, int trace_off,
                               int trace_stride, int lanes_cap);
+__global__ void k_chain_steps_wide(Pool P, int n_steps, unsigned* queue, const int* order,
+                                   int n_tasks, int gwarps, SmemShape shape, mcgpu_trace* trace,
+                                   int trace_off, int trace_stride, int lanes_cap);
 __global__ void k_chain_init(Pool P, const int* mol_chain, int m_begin, int m_end);
 __global__ void k_chain_energy1(Pool P, int c, const double* emol);
 __global__ void k_nl_config(Pool P, const NlCfg* cfg);

@@ -294,12 +294,10 @@ __global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol
 // recorded at trace[c * trace_stride + trace_off + st].  Warp 0 draws the
 // moves of 32 steps at once (one per lane) into shared memory.  lanes_cap >
 // 0 caps the lanes per neighbour molecule of every chain.
-__global__ void __launch_bounds__(256, 2) k_chain_steps(Pool P, int n_steps, unsigned* queue,
-                                                     const int* order, int n_tasks, int gwarps,
-                                                     SmemShape shape, mcgpu_trace* trace,
-                                                     int trace_off, int trace_stride,
-                                                     int lanes_cap) {
-  extern __shared__ __align__(16) char smem[];
+__device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue,
+                                            const int* order, int n_tasks, int gwarps,
+                                            SmemShape shape, mcgpu_trace* trace, int trace_off,
+                                            int trace_stride, int lanes_cap, char* smem) {
   const int gsize = gwarps * 32;
   const int gid = threadIdx.x / gsize;
   Group g{(int)threadIdx.x - gid * gsize, gsize, 1 + gid};
@@ -431,6 +429,29 @@ __global__ void __launch_bounds__(256, 2) k_chain_steps(Pool P, int n_steps, uns
     }
     g.sync();
   }
+}
+
+__global__ void __launch_bounds__(256, 2) k_chain_steps(Pool P, int n_steps, unsigned* queue,
+                                                     const int* order, int n_tasks, int gwarps,
+                                                     SmemShape shape, mcgpu_trace* trace,
+                                                     int trace_off, int trace_stride,
+                                                     int lanes_cap) {
+  extern __shared__ __align__(16) char smem[];
+  chain_steps(P, n_steps, queue, order, n_tasks, gwarps, shape, trace, trace_off, trace_stride,
+              lanes_cap, smem);
+}
+
+// The same for one group of up to 16 warps per CTA (a single large chain:
+// more warps per step, one CTA per SM).
+__global__ void __launch_bounds__(512, 1) k_chain_steps_wide(Pool P, int n_steps,
+                                                          unsigned* queue, const int* order,
+                                                          int n_tasks, int gwarps,
+                                                          SmemShape shape, mcgpu_trace* trace,
+                                                          int trace_off, int trace_stride,
+                                                          int lanes_cap) {
+  extern __shared__ __align__(16) char smem[];
+  chain_steps(P, n_steps, queue, order, n_tasks, gwarps, shape, trace, trace_off, trace_stride,
+              lanes_cap, smem);
 }
 
 // ---- host launchers (template kernels are instantiated here) --------------

@@ -122,6 +122,23 @@ def test_chain_run_replay(ctx, name, mode):
           f"FP64 re-takes {retakes}")
 
 
+@pytest.mark.parametrize("verlet", [0.0, 1.5])
+def test_wide_group_chain_replay(ctx, verlet):
+    """A chain of 2600 molecules runs as one group of 10 warps (the 512-thread
+    kernel): the oracle's trajectory bit for bit, with and without Verlet lists."""
+    box = W.water_box(2600, seed=61)
+    g = GpuBox(ctx, box, PREC_MIXED)
+    if verlet:
+        g.set_verlet(verlet)
+    st, tr = g.chain_run(seed=4321, n_steps=400, rotation=ROT_AXIS, trace=True)
+    assert st.error == 0
+    oc, e, _, _, retakes = replay(box, 4321, 0, tr, ROT_AXIS)
+    x, y, z = g.download()
+    assert np.array_equal(np.stack([x, y, z], 1), oc.coords())
+    assert st.ties == retakes
+    g.close()
+
+
 def test_batch_replay_uneven_chains(ctx):
     """A batch of uneven chains (sizes, temperatures, one 16-atom chain):
     every chain's trace equals the oracle's run of the same chain."""
@@ -143,7 +160,8 @@ def test_batch_replay_uneven_chains(ctx):
         assert abs(stats[c].energy - e) <= 1e-5 * max(abs(e), 1e-3 * scale) + steps * 1e-9 * scale
 
 
-@pytest.mark.parametrize("tile", [(64, 2, 4), (128, 1, 16), (256, 4, 32), (256, 8, 8)])
+@pytest.mark.parametrize("tile", [(64, 2, 4), (128, 1, 16), (256, 4, 32), (256, 8, 8),
+                                  (512, 1, 16), (512, 4, 16)])
 def test_batch_tiles_agree(ctx, tile):
     """Every tile shape gives the same trajectories (per-chain Philox streams
     make results independent of packing)."""
