@@ -1476,6 +1476,9 @@ extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
     for (int gw = 1; gw <= t / 32 && rc == MCGPU_OK; gw *= 2) {
       const int cpc = (t / 32) / gw;
       if (gw > 1 && cpc > 15) continue;
+      // 512 threads only as one 16-warp group (smaller groups repeat the
+      // 256-thread shapes with fewer CTAs per SM)
+      if (t == 512 && cpc != 1) continue;
       const Tile T = {t, cpc, 16, 0};
       rc = trial(T, &ms);
       if (rc == MCGPU_OK && ms < best) {
