@@ -421,7 +421,12 @@ int launch_round(mcgpu_server* s) {
   CK(ctx, cudaMemsetAsync(s->qctr, 0, sizeof(unsigned), st));
   const int need = ((int)act.size() + s->cfg.chains_per_cta - 1) / s->cfg.chains_per_cta;
   const int grid = std::max(1, std::min(need, s->grid));
-  k_chain_steps<<<grid, s->cfg.threads, s->smem, st>>>(s->pool.P, s->cfg.round_steps, s->qctr,
+  if (s->cfg.threads > 256)
+    k_chain_steps_wide<<<grid, s->cfg.threads, s->smem, st>>>(s->pool.P, s->cfg.round_steps, s->qctr,
+                                                      s->dlist, (int)act.size(), s->gw, s->shape,
+                                                      nullptr, 0, 0, s->cfg.lanes_per_molecule);
+  else
+    k_chain_steps<<<grid, s->cfg.threads, s->smem, st>>>(s->pool.P, s->cfg.round_steps, s->qctr,
                                                       s->dlist, (int)act.size(), s->gw, s->shape,
                                                       nullptr, 0, 0, s->cfg.lanes_per_molecule);
   CK(ctx, cudaGetLastError());
@@ -503,7 +508,8 @@ extern "C" int mcgpu_server_create(mcgpu_ctx* ctx, const mcgpu_server_config* cf
     return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "tile needs %d B shared memory", s->smem);
   }
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chain_steps, c.threads, s->smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, c.threads > 256 ? k_chain_steps_wide : k_chain_steps, c.threads, s->smem);
   s->grid = std::max(1, per_sm) * ctx->sm_count;
   *out = s;
   return MCGPU_OK;

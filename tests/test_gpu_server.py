@@ -138,3 +138,16 @@ def test_server_overlapping_arrivals(ctx):
     alone = run_server(ctx, [jobs[5]], hbm_budget_bytes=64 * MB, max_slots=6, round_steps=50)
     same(alone[0], res[ids[5]])
     srv.close()
+
+
+@pytest.mark.parametrize("tile", [(512, 1, 0), (512, 2, 0)])
+def test_server_wide_tiles_agree(ctx, tile):
+    """Rounds with 512-thread CTAs (the wide chain kernel) give the same jobs."""
+    jobs = mixed_jobs(4, seed=21)[:5]
+    base = run_server(ctx, jobs, hbm_budget_bytes=64 * MB, max_slots=8, round_steps=50)
+    wide = run_server(ctx, jobs, hbm_budget_bytes=64 * MB, max_slots=8, round_steps=50,
+                      tile=tile)
+    for a, b in zip(base, wide):
+        assert a.result.accepted == b.result.accepted
+        assert np.array_equal(a.coords, b.coords)
+        assert abs(a.result.energy - b.result.energy) <= 1e-9 * max(1.0, abs(a.result.energy))
