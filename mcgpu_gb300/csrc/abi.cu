@@ -7,12 +7,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "host.h"
@@ -46,40 +49,57 @@ void note_process_error(const char* msg) { g_err = msg; }
 
 namespace mcgpu {
 
-// Validates one descriptor and appends it as chain `c` of the host pool.
-int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
-                 unsigned long long seed, int rot_mode) {
-  if (!d) return set_err(ctx, MCGPU_ERR_INVALID, "null box descriptor");
-  if (d->n_mol <= 0 || d->n_atom <= 0 || d->n_pidx <= 0)
-    return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: empty box (n_mol=%d n_atom=%d n_pidx=%d)", c,
-                   d->n_mol, d->n_atom, d->n_pidx);
+// Sizes of descriptor d (chain c), validated: 0 or an error code with err.
+static int chain_sizes(const mcgpu_box_desc* d, int c, std::string* err) {
+  char buf[512];
+  if (!d) {
+    *err = "null box descriptor";
+    return MCGPU_ERR_INVALID;
+  }
+  if (d->n_mol <= 0 || d->n_atom <= 0 || d->n_pidx <= 0) {
+    snprintf(buf, sizeof(buf), "chain %d: empty box (n_mol=%d n_atom=%d n_pidx=%d)", c, d->n_mol,
+             d->n_atom, d->n_pidx);
+    *err = buf;
+    return MCGPU_ERR_INVALID;
+  }
+  return MCGPU_OK;
+}
+
+// Validates descriptor d (chain c) and writes it into the host pool at
+// atom0 / mol0 / pidx0 and header slot `slot` (the rows are sized already).
+// On failure returns the error code with its text in err.
+static int fill_chain(HostPool& hp, const mcgpu_box_desc* d, int c, int slot, int atom0, int mol0,
+                      int pidx0, unsigned long long seed, int rot_mode, std::string* err) {
+  char ebuf[512];
+  auto fail = [&](int code, const char* fmt, auto... args) {
+    snprintf(ebuf, sizeof(ebuf), fmt, args...);
+    *err = ebuf;
+    return code;
+  };
   if (!d->x || !d->y || !d->z || !d->sigma || !d->epsilon || !d->charge || !d->mol_start ||
       !d->mol_len || !d->mol_pidx_start || !d->mol_pidx_count || !d->pidx)
-    return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: null row pointer", c);
+    return fail(MCGPU_ERR_INVALID, "chain %d: null row pointer", c);
   for (int k = 0; k < 3; k++)
     if (!(d->size[k] > 0) || !std::isfinite(d->size[k]))
-      return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: box edge %d is %g", c, k, d->size[k]);
+      return fail(MCGPU_ERR_INVALID, "chain %d: box edge %d is %g", c, k, d->size[k]);
   if (!(d->cutoff > 0) || !(d->temperature > 0))
-    return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: cutoff %g / temperature %g must be > 0", c,
+    return fail(MCGPU_ERR_INVALID, "chain %d: cutoff %g / temperature %g must be > 0", c,
                    d->cutoff, d->temperature);
-  const int atom0 = (int)hp.x.size(), mol0 = (int)hp.mstart.size(), pidx0 = (int)hp.pidx.size();
-  const long long tot_atoms = (long long)atom0 + d->n_atom;
-  if (tot_atoms > (1LL << 30) || (long long)mol0 + d->n_mol > (1LL << 26))
-    return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "pool too large");
   for (int a = 0; a < d->n_atom; a++) {
-    hp.x.push_back(d->x[a]);
-    hp.y.push_back(d->y[a]);
-    hp.z.push_back(d->z[a]);
-    hp.sig.push_back(d->sigma[a]);
-    hp.eps.push_back(d->epsilon[a]);
-    hp.q.push_back(d->charge[a]);
+    const size_t at = (size_t)atom0 + a;
+    hp.x[at] = d->x[a];
+    hp.y[at] = d->y[a];
+    hp.z[at] = d->z[a];
+    hp.sig[at] = d->sigma[a];
+    hp.eps[at] = d->epsilon[a];
+    hp.q[at] = d->charge[a];
     if (!std::isfinite(d->x[a]) || !std::isfinite(d->y[a]) || !std::isfinite(d->z[a]))
-      return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: non-finite coordinate at atom %d", c, a);
+      return fail(MCGPU_ERR_INVALID, "chain %d: non-finite coordinate at atom %d", c, a);
     const bool active = d->sigma[a] >= 0 && d->epsilon[a] >= 0;  // BruteForceStep.cpp:64-65
-    hp.aoff.push_back(make_float4(0.f, 0.f, 0.f, active ? (float)d->sigma[a] : 0.f));
-    hp.aeq.push_back(active ? make_float2((float)(2.0 * std::sqrt(std::fabs(d->epsilon[a]))),
-                                          (float)(d->charge[a] * std::sqrt(kCoulomb)))
-                            : make_float2(0.f, 0.f));
+    hp.aoff[at] = make_float4(0.f, 0.f, 0.f, active ? (float)d->sigma[a] : 0.f);
+    hp.aeq[at] = active ? make_float2((float)(2.0 * std::sqrt(std::fabs(d->epsilon[a]))),
+                                      (float)(d->charge[a] * std::sqrt(kCoulomb)))
+                        : make_float2(0.f, 0.f);
   }
   int max_len = 0;
   double max_rad = 0, max_prad = 0;
@@ -91,23 +111,23 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
     const int s = d->mol_start[m], len = d->mol_len[m];
     const int ps = d->mol_pidx_start[m], pc = d->mol_pidx_count[m];
     if (len < 1 || len > kMaxA)
-      return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "chain %d molecule %d: %d atoms (limit %d)", c, m,
+      return fail(MCGPU_ERR_UNSUPPORTED, "chain %d molecule %d: %d atoms (limit %d)", c, m,
                      len, kMaxA);
     if (s < 0 || s + len > d->n_atom)
-      return set_err(ctx, MCGPU_ERR_INVALID, "chain %d molecule %d: atoms [%d,%d) outside [0,%d)",
+      return fail(MCGPU_ERR_INVALID, "chain %d molecule %d: atoms [%d,%d) outside [0,%d)",
                      c, m, s, s + len, d->n_atom);
     if (pc < 1 || pc > kMaxP)
-      return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "chain %d molecule %d: %d primary indexes (1..%d)",
+      return fail(MCGPU_ERR_UNSUPPORTED, "chain %d molecule %d: %d primary indexes (1..%d)",
                      c, m, pc, kMaxP);
     if (ps < 0 || ps + pc > d->n_pidx)
-      return set_err(ctx, MCGPU_ERR_INVALID, "chain %d molecule %d: primary range outside pidx", c,
+      return fail(MCGPU_ERR_INVALID, "chain %d molecule %d: primary range outside pidx", c,
                      m);
     int act = 0;
     for (int a = s; a < s + len; a++) act += (d->sigma[a] >= 0 && d->epsilon[a] >= 0);
     for (int k = ps; k < ps + pc; k++) {
       const int p = d->pidx[k];
       if (p < s || p >= s + len)
-        return set_err(ctx, MCGPU_ERR_INVALID,
+        return fail(MCGPU_ERR_INVALID,
                        "chain %d molecule %d: primary index %d outside its atoms", c, m, p);
     }
     const int an = d->pidx[ps];
@@ -123,11 +143,12 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
     }
     max_rad = std::max(max_rad, rad);
     max_len = std::max(max_len, len);
-    hp.mstart.push_back(atom0 + s);
-    hp.mlen.push_back(len | (act << 8));
-    hp.mpi.push_back(make_int2(pidx0 + ps, pc));
-    hp.mrad.push_back((float)(rad * (1 + 1e-6) + 1e-4));
-    hp.mol_chain.push_back(c);
+    const size_t mo = (size_t)mol0 + m;
+    hp.mstart[mo] = atom0 + s;
+    hp.mlen[mo] = len | (act << 8);
+    hp.mpi[mo] = make_int2(pidx0 + ps, pc);
+    hp.mrad[mo] = (float)(rad * (1 + 1e-6) + 1e-4);
+    hp.mol_chain[mo] = c;
     if (ps != m || pc != 1) simple = false;
     if (m == 0) {
       u_len = len;
@@ -141,21 +162,21 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
       if (d->sigma[s + k] != d->sigma[k] || d->epsilon[s + k] != d->epsilon[k] ||
           d->charge[s + k] != d->charge[k])
         uniform = false;
-    u_mrad = std::max(u_mrad, hp.mrad.back());
+    u_mrad = std::max(u_mrad, hp.mrad[mo]);
   }
-  hp.atom_mol.resize(hp.x.size(), -1);
+  for (int a = 0; a < d->n_atom; a++) hp.atom_mol[(size_t)atom0 + a] = -1;
   for (int m = 0; m < d->n_mol; m++)
     for (int a = d->mol_start[m]; a < d->mol_start[m] + d->mol_len[m]; a++)
       hp.atom_mol[atom0 + a] = mol0 + m;
   for (int a = 0; a < d->n_atom; a++)
     if (hp.atom_mol[atom0 + a] < 0)
-      return set_err(ctx, MCGPU_ERR_INVALID, "chain %d: atom %d belongs to no molecule", c, a);
+      return fail(MCGPU_ERR_INVALID, "chain %d: atom %d belongs to no molecule", c, a);
   const double Lmin = std::min(d->size[0], std::min(d->size[1], d->size[2]));
   if (max_rad >= 0.25 * Lmin)
-    return set_err(ctx, MCGPU_ERR_UNSUPPORTED,
+    return fail(MCGPU_ERR_UNSUPPORTED,
                    "chain %d: molecule radius %.3f A reaches a quarter of the box edge %.3f A", c,
                    max_rad, Lmin);
-  for (int k = 0; k < d->n_pidx; k++) hp.pidx.push_back(atom0 + d->pidx[k]);
+  for (int k = 0; k < d->n_pidx; k++) hp.pidx[(size_t)pidx0 + k] = atom0 + d->pidx[k];
 
   ChainHdr h;
   std::memset(&h, 0, sizeof(h));
@@ -188,8 +209,82 @@ int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
   h.max_t = d->max_translate;
   h.max_r = d->max_rotate;
   h.seed = seed;
-  hp.hdr.push_back(h);
-  hp.max_len = std::max(hp.max_len, max_len);
+  hp.hdr[slot] = h;
+  return MCGPU_OK;
+}
+
+// Validates one descriptor and appends it as chain `c` of the host pool.
+int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
+                 unsigned long long seed, int rot_mode) {
+  std::string err;
+  int rc = chain_sizes(d, c, &err);
+  if (rc) return set_err(ctx, rc, "%s", err.c_str());
+  const size_t atom0 = hp.x.size(), mol0 = hp.mstart.size(), pidx0 = hp.pidx.size();
+  if (atom0 + d->n_atom > (1ull << 30) || mol0 + d->n_mol > (1ull << 26) ||
+      pidx0 + d->n_pidx > (1ull << 30))
+    return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "pool too large");
+  const size_t slot = hp.hdr.size();
+  hp.resize(atom0 + d->n_atom, mol0 + d->n_mol, pidx0 + d->n_pidx, slot + 1);
+  rc = fill_chain(hp, d, c, (int)slot, (int)atom0, (int)mol0, (int)pidx0, seed, rot_mode, &err);
+  if (rc) {
+    hp.resize(atom0, mol0, pidx0, slot);
+    return set_err(ctx, rc, "%s", err.c_str());
+  }
+  hp.max_len = std::max(hp.max_len, hp.hdr[slot].max_len);
+  return MCGPU_OK;
+}
+
+// The host pool of n chains: sizes and offsets first, then the chains
+// filled in parallel on the host's cores (one thread per chain, so each
+// chain's checks run in their usual order). The error reported is the one a
+// chain-by-chain build meets first: the lowest chain that fails.
+int build_pool(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* descs, int n,
+               const uint64_t* seeds, int rot_mode) {
+  std::vector<size_t> a0(n + 1, 0), m0(n + 1, 0), p0(n + 1, 0);
+  std::string size_err;
+  int size_rc = MCGPU_OK, n_ok = n;
+  for (int c = 0; c < n; c++) {
+    size_rc = chain_sizes(&descs[c], c, &size_err);
+    if (!size_rc) {
+      a0[c + 1] = a0[c] + descs[c].n_atom;
+      m0[c + 1] = m0[c] + descs[c].n_mol;
+      p0[c + 1] = p0[c] + descs[c].n_pidx;
+      if (a0[c + 1] > (1ull << 30) || m0[c + 1] > (1ull << 26) || p0[c + 1] > (1ull << 30)) {
+        size_rc = MCGPU_ERR_UNSUPPORTED;
+        size_err = "pool too large";
+      }
+    }
+    if (size_rc) {
+      n_ok = c;
+      break;
+    }
+  }
+  hp.resize(a0[n_ok], m0[n_ok], p0[n_ok], (size_t)n_ok);
+  std::vector<int> codes(n_ok, MCGPU_OK);
+  std::vector<std::string> errs(n_ok);
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int c = next++; c < n_ok; c = next++)
+      codes[c] = fill_chain(hp, &descs[c], c, c, (int)a0[c], (int)m0[c], (int)p0[c], seeds[c],
+                            rot_mode, &errs[c]);
+  };
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = std::min<size_t>({(size_t)hw, (size_t)16, (size_t)std::max(n_ok, 1),
+                                      a0[n_ok] / 20000 + 1});
+  std::vector<std::thread> pool;
+  for (size_t t = 1; t < nt; t++) {
+    try {
+      pool.emplace_back(work);
+    } catch (const std::system_error&) {
+      break;  // fewer helpers; the calling thread takes what is left
+    }
+  }
+  work();
+  for (std::thread& th : pool) th.join();
+  for (int c = 0; c < n_ok; c++)
+    if (codes[c]) return set_err(ctx, codes[c], "%s", errs[c].c_str());
+  if (size_rc) return set_err(ctx, size_rc, "%s", size_err.c_str());
+  for (int c = 0; c < n; c++) hp.max_len = std::max(hp.max_len, hp.hdr[c].max_len);
   return MCGPU_OK;
 }
 
@@ -805,20 +900,7 @@ extern "C" int mcgpu_batch_create(mcgpu_ctx* ctx, int n_chains, const mcgpu_box_
     return set_err(ctx, MCGPU_ERR_INVALID, "unknown rotation form %d", rotation);
   CK(ctx, cudaSetDevice(ctx->device));
   HostPool hp;
-  {
-    size_t na = 0, nm = 0, np = 0;
-    for (int c = 0; c < n_chains; c++) {
-      na += descs[c].n_atom > 0 ? (size_t)descs[c].n_atom : 0;
-      nm += descs[c].n_mol > 0 ? (size_t)descs[c].n_mol : 0;
-      np += descs[c].n_pidx > 0 ? (size_t)descs[c].n_pidx : 0;
-    }
-    if (na <= (1ull << 30) && nm <= (1ull << 26) && np <= (1ull << 28))
-      hp.reserve(na, nm, np, (size_t)n_chains);
-  }
-  for (int c = 0; c < n_chains; c++) {
-    int rc = append_chain(ctx, hp, &descs[c], c, seeds[c], rotation);
-    if (rc) return rc;
-  }
+  if (int rc = build_pool(ctx, hp, descs, n_chains, seeds, rotation)) return rc;
   mcgpu_batch* bt = new mcgpu_batch();
   bt->ctx = ctx;
   int rc = upload_pool(ctx, hp, bt->pool);

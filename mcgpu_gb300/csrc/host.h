@@ -104,11 +104,27 @@ struct HostPool {
     pidx.reserve(pidxs);
     hdr.reserve(chains);
   }
+  // rows of exactly the given totals (new entries value-initialised)
+  void resize(size_t atoms, size_t mols, size_t pidxs, size_t chains) {
+    for (auto* v : {&x, &y, &z, &sig, &eps, &q}) v->resize(atoms);
+    aoff.resize(atoms);
+    aeq.resize(atoms);
+    atom_mol.resize(atoms);
+    for (auto* v : {&mstart, &mlen, &mol_chain}) v->resize(mols);
+    mpi.resize(mols);
+    mrad.resize(mols);
+    pidx.resize(pidxs);
+    hdr.resize(chains);
+  }
 };
 
 // Validates one descriptor and appends it as chain `c` of the host pool.
 int append_chain(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* d, int c,
                  unsigned long long seed, int rot_mode);
+// The host pool of descs[0..n) (chain c seeded with seeds[c]), built on
+// several host threads; errors as append_chain reports them chain by chain.
+int build_pool(mcgpu_ctx* ctx, HostPool& hp, const mcgpu_box_desc* descs, int n,
+               const uint64_t* seeds, int rot_mode);
 
 struct DevPool {
   Pool P{};

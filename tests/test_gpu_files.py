@@ -216,3 +216,21 @@ def test_batch_download_all_equals_per_chain(ctx):
         ax, ay, az = allc[c]
         assert np.array_equal(x, ax) and np.array_equal(y, ay) and np.array_equal(z, az)
     bt.close()
+
+
+def test_batch_create_reports_lowest_failing_chain(ctx):
+    """The pool is filled on several host threads; the error is still the
+    one a chain-by-chain build meets first."""
+    boxes, seeds = W.water_chains(40, n_min=600, n_max=1200, seed=12)
+    boxes[17].x = boxes[17].x.copy()
+    boxes[17].x[5] = np.nan
+    boxes[31].mol_len = boxes[31].mol_len.copy()
+    boxes[31].mol_len[0] = 0
+    with pytest.raises(MCGPUError, match="chain 17: non-finite coordinate at atom 5"):
+        ChainBatch(ctx, boxes, seeds)
+    boxes[17].x[5] = 0.5
+    with pytest.raises(MCGPUError, match="chain 31 molecule 0"):
+        ChainBatch(ctx, boxes, seeds)
+    boxes[3].pidx = np.zeros(0, np.int32)
+    with pytest.raises(MCGPUError, match="chain 3: empty box"):
+        ChainBatch(ctx, boxes, seeds)
