@@ -45,12 +45,13 @@ __device__ __forceinline__ float4 chain_screen_pos(uint4 A, float4 o, const Chai
 // flag; kMiscNlOk: the chain's list is still valid (group-uniform state)
 enum : int { kMiscQn = 16, kMiscU = 20, kMiscNlTrial = 24, kMiscNlOk = 25 };
 
-// Warp 0 stages the proposed FP32 move `mv` of a chain molecule: old and
-// new offsets (o_old, o_new), pair factors and |o|^2 (eq), screen
-// positions of the primaries (p_old, p_new), old and new fixed-point
-// anchors, the new quaternion.  No FP64.
-__device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF& mv, const GroupSmem& s,
-                            const float4* pcache, int lane) {
+// One warp stages the proposed FP32 move `mv` of a chain molecule into
+// slot s: old and new offsets (o_old, o_new), pair factors and |o|^2 (eq),
+// screen positions of the primaries (p_old, p_new), old and new fixed-point
+// anchors, the new quaternion.  No FP64.  It reads the molecule's rows
+// only, so a move staged ahead stays valid until a commit of that molecule.
+__device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF& mv,
+                                   const StageSlot& s, const float4* pcache, int lane) {
   const int m = H.mol0 + mv.mol;
   int a0, lw;
   int2 pi;
@@ -122,6 +123,27 @@ __device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF
     s.miscd[0] = (double)(H.uniform ? H.umrad : P.mrad[m]);
     s.miscd[1] = (double)qsum;
   }
+}
+
+// Warp-wide copy of a move staged ahead into the current slot (misc up to
+// kMiscNlTrial: the slots above it are group state).
+__device__ __forceinline__ void adopt_staged(const StageSlot& from, const StageSlot& to,
+                                             int lane) {
+  const int len = from.misc[2], np = from.misc[3];
+  for (int i = lane; i < len; i += 32) {
+    to.o_old[i] = from.o_old[i];
+    to.o_new[i] = from.o_new[i];
+    to.l_old[i] = from.l_old[i];
+    to.l_new[i] = from.l_new[i];
+    to.eq[i] = from.eq[i];
+  }
+  for (int k = lane; k < np; k += 32) {
+    to.p_old[k] = from.p_old[k];
+    to.p_new[k] = from.p_new[k];
+    to.pa[k] = from.pa[k];
+  }
+  if (lane <= kMiscNlTrial) to.misc[lane] = from.misc[lane];
+  if (lane < 2) to.miscd[lane] = from.miscd[lane];
 }
 
 // Screen of candidate j against the staged molecule (both placements):

@@ -437,7 +437,27 @@ struct GroupSmem {
   void* props;                          // [32] drawn moves of the next steps (chain kernel)
   float4* nbuf;                         // [nwarps * 32 * 5] per-lane neighbour rows (async copies)
   float2* teq;                          // [maxA] pair factors per slot of a uniform chain
+  char* ahead;                          // a second staging slot (the chain kernel's next move)
 };
+
+// The rows a staged move occupies: offsets, pair factors, primaries, the
+// broadcast ints and doubles.  A group has two: its current move's (inside
+// GroupSmem) and the one the chain kernel stages the next move into ahead
+// of time.
+struct StageSlot {
+  float4* o_old; float4* o_new;
+  float4* l_old; float4* l_new;
+  float4* eq;
+  float4* p_old; float4* p_new;
+  int* pa;
+  int* misc;
+  double* miscd;
+};
+
+__device__ __forceinline__ StageSlot current_slot(const GroupSmem& s) {
+  return StageSlot{s.o_old, s.o_new, s.l_old, s.l_new, s.eq, s.p_old, s.p_new, s.pa, s.misc,
+                   s.miscd};
+}
 
 struct SmemShape {
   int maxA, nwarps, cache_n;
@@ -460,7 +480,23 @@ struct SmemShape {
     b += align16(32 * kPropBytes);
     b += align16(nwarps * 32 * 5 * 16);
     b += align16(maxA * 8);
+    b += ahead_bytes();
     return b;
+  }
+  // the second staging slot: offsets and factors, primaries, misc, miscd
+  __host__ __device__ int ahead_bytes() const {
+    return align16(5 * maxA * 16) + align16(2 * kMaxP * 16) + align16(kMaxP * 4) + align16(32 * 4) +
+           align16(32 * 8);
+  }
+  __device__ StageSlot ahead_slot(char* p) const {
+    StageSlot t;
+    t.o_old = (float4*)p; t.o_new = t.o_old + maxA; t.l_old = t.o_new + maxA;
+    t.l_new = t.l_old + maxA; t.eq = t.l_new + maxA; p += align16(5 * maxA * 16);
+    t.p_old = (float4*)p; t.p_new = t.p_old + kMaxP; p += align16(2 * kMaxP * 16);
+    t.pa = (int*)p; p += align16(kMaxP * 4);
+    t.misc = (int*)p; p += align16(32 * 4);
+    t.miscd = (double*)p;
+    return t;
   }
   __device__ GroupSmem carve(char* base) const {
     GroupSmem s;
@@ -488,6 +524,8 @@ struct SmemShape {
     s.nbuf = (float4*)p;
     p += align16(nwarps * 32 * 5 * 16);
     s.teq = (float2*)p;
+    p += align16(maxA * 8);
+    s.ahead = p;
     return s;
   }
 };

@@ -282,17 +282,20 @@ __global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol
 
 // Persistent kernel: groups of `gwarps` warps pull chain tasks from `queue`
 // (task k runs chain order[k]) and advance each by n_steps steps on the
-// chain state.  A step: warp 0 draws the Philox move and stages it in FP32
+// chain state.  A step: the move staged in FP32 during the previous step
 // (one group barrier); every warp screens its share of the candidates and
-// evaluates the in-range ones (FP32 pair terms, double-float sums); one
+// evaluates the in-range ones (FP32 pair terms, double-float sums), the
+// last warp then stages the next move into the second slot; one
 // group reduction gives E_old, E_new.  Outside a guard band around the
 // acceptance threshold the decision (dE < 0, else exp(-dE/kT) >= u,
 // SimulationStep.cpp:794-803) is taken in FP32; inside it the group
 // re-evaluates both placements with FP64 pairs and decides on that.  Warp
 // 0 commits.  With cache_n > 0 each group keeps its chain's primary screen
 // positions in shared memory.  If trace != nullptr, step st of chain c is
-// recorded at trace[c * trace_stride + trace_off + st].  Warp 0 draws the
-// moves of 32 steps at once (one per lane) into shared memory.  lanes_cap >
+// recorded at trace[c * trace_stride + trace_off + st].  The staging warp
+// draws the moves of 32 steps at once (one per lane) into shared memory;
+// after the commit warp 0 copies the staged move into the current slot, or
+// stages it again when the commit moved that molecule.  lanes_cap >
 // 0 caps the lanes per neighbour molecule of every chain.
 __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue,
                                             const int* order, int n_tasks, int gwarps,
@@ -328,17 +331,19 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
     int my_steps = n_steps;
     if (H.step_limit > 0)
       my_steps = (int)max(0LL, min((long long)n_steps, H.step_limit - (long long)step0));
+    const StageSlot cur = current_slot(s), nxt = shape.ahead_slot(s.ahead);
+    // moves are drawn 32 steps at a time (one per lane) by the staging warp
+    auto draw32 = [&](int st0) {
+      if (st0 + lane < my_steps)
+        props[lane] = draw_move_f32(H.seed, H.chain_id, step0 + st0 + lane, H.n_mol,
+                                    P.mlen + H.mol0, (float)H.max_t, (float)H.max_r, H.rot_mode);
+      __syncwarp();
+    };
+    if (w == 0 && my_steps > 0) {
+      draw32(0);
+      stage_chain(P, H, props[0], cur, pcache, lane);
+    }
     for (int st = 0; st < my_steps; st++) {
-      if (w == 0) {
-        if ((st & 31) == 0) {
-          if (st + lane < my_steps)
-            props[lane] = draw_move_f32(H.seed, H.chain_id, step0 + st + lane, H.n_mol,
-                                        P.mlen + H.mol0, (float)H.max_t, (float)H.max_r,
-                                        H.rot_mode);
-          __syncwarp();
-        }
-        stage_chain(P, H, props[st & 31], s, pcache, lane);
-      }
       g.sync();
       const MovedInfo mi = load_moved(s);
       // read before the reduction barrier: warp 0 restages the slot after it
@@ -353,6 +358,14 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
                         P.nl + (size_t)mi.mol * P.nl_stride);
       else
         warp_eval_chain(P, H, s, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, acc);
+      // the last warp (with the fewest screen blocks) stages the next move
+      // while the others finish their share; staging reads rows this step's
+      // commit changes only if the next move is of the same molecule (warp 0
+      // then stages it again)
+      if (w == nw - 1 && st + 1 < my_steps) {
+        if (((st + 1) & 31) == 0) draw32(st + 1);
+        stage_chain(P, H, props[(st + 1) & 31], nxt, pcache, lane);
+      }
       group_reduce_ff(g, s, acc);
       // FP32 decision unless the FP32 dE is within its rounding bound of the
       // threshold; the bound covers the pair terms' rounding (kTieRel of the
@@ -413,6 +426,13 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
           }
         }
         __syncwarp();
+        if (st + 1 < my_steps) {
+          if (ok && H.mol0 + props[(st + 1) & 31].mol == mi.mol)
+            stage_chain(P, H, props[(st + 1) & 31], cur, pcache, lane);
+          else
+            adopt_staged(nxt, cur, lane);
+          __syncwarp();
+        }
       }
     }
     if (g.tid == 0) {
