@@ -41,10 +41,10 @@ WORKLOAD = ("512 independent NVT water chains (3-site TIP3P-like, rigid), N log-
             "+-0.15 A / +-15 deg random-axis moves, Philox proposals, on-device accept")
 FP32_FLOPS_PER_PAIR = 38   # per atom pair, fixed by convention from the reference's arithmetic
 # DRAM bytes (read + write) per launch of k_chain_steps on this workload,
-# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, 3 launches
-# after 6 warm-up launches, L2 flushed between bench steps), by tile
+# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum of the 7th
+# launch, L2 flushed between bench steps), by tile
 # (threads, chains per CTA, steps per launch, lanes per molecule).
-CHAIN_TRAFFIC_BYTES = {(256, 1, 64, 1): 33.57e6}
+CHAIN_TRAFFIC_BYTES = {(256, 1, 64, 1): 33.61e6, (160, 1, 64, 1): 33.72e6}
 
 
 def peaks():
@@ -315,6 +315,7 @@ def bench_large(ctx, steps: int = 6000) -> dict:
 # ---- served request loop ---------------------------------------------------------------
 
 def bench_served(ctx, rate: float = 200.0, window_s: float = 4.0, steps_per_job: int = 20000,
+                 tile=(256, 1, 0),
                  pool_each: int = 12, seed: int = 77) -> dict:
     """Jobs arrive as a Poisson stream (rate jobs/s over window_s seconds),
     50/50 water and 16-atom bicyclic, N log-uniform in [128, 8192], NPT at
@@ -342,7 +343,8 @@ def bench_served(ctx, rate: float = 200.0, window_s: float = 4.0, steps_per_job:
             break
         arrivals.append(t)
     srv = M.JobServer(ctx, hbm_budget_bytes=120 << 30, max_slots=512, round_steps=100,
-                      max_mol_atoms=16, max_atoms=24_000_000, max_molecules=4_000_000)
+                      max_mol_atoms=16, max_atoms=24_000_000, max_molecules=4_000_000,
+                      tile=tile)
     jobs = []
     for i, ta in enumerate(arrivals):
         b = pool[int(rng.integers(len(pool)))].copy()
@@ -378,6 +380,7 @@ def bench_served(ctx, rate: float = 200.0, window_s: float = 4.0, steps_per_job:
             "jobs": len(jobs), "moves_per_s": moves / (t_last - t_first), "unit": "moves/s",
             "p50_s": pct(0.50), "p99_s": pct(0.99), "max_s": lat[-1],
             "makespan_s": t_last - t_first, "errors": errors, "fp64_retakes": ties,
+            "tile": {"threads": tile[0], "chains_per_cta": tile[1], "lanes_per_molecule": tile[2]},
             "note": f"boxes from a pool of {2 * pool_each} pre-built configurations; "
                     "volume-move energies FP32 pairs with FP64 re-take near the threshold"}
 
@@ -398,6 +401,8 @@ def main():
     ap.add_argument("--no-served", action="store_true", help="skip the served request loop")
     ap.add_argument("--served-window", type=float, default=4.0)
     ap.add_argument("--served-steps", type=int, default=20000)
+    ap.add_argument("--served-tile", default="256,1,0",
+                    help="threads,chains_per_cta,lanes of the serving loop's chain kernel")
     ap.add_argument("--tile", default=None,
                     help="threads,chains_per_cta,steps_per_launch,lanes (skips the autotuner)")
     args = ap.parse_args()
@@ -498,7 +503,8 @@ def main():
     if rank == 0 and not args.no_large:
         large = bench_large(ctx)
     if rank == 0 and not args.no_served:
-        served = bench_served(ctx, window_s=args.served_window, steps_per_job=args.served_steps)
+        served = bench_served(ctx, window_s=args.served_window, steps_per_job=args.served_steps,
+                              tile=tuple(int(v) for v in args.served_tile.split(",")))
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(boxes, seeds)
@@ -515,9 +521,12 @@ def main():
                    "steps_per_bench_step": STEPS_PER_BENCH,
                    "tile": {"threads": threads, "chains_per_cta": cpc, "steps_per_launch": spl,
                             "lanes_per_molecule": lanes},
-                   "precision": "FP32 pair terms, FP64 per-neighbour sums, dE and totals",
-                   "l2": "flushed between timed steps (256 MiB write); the chains' state "
-                         "(~14 MB) is re-read from HBM at each step start",
+                   "precision": "FP32 pair terms with double-float sums; FP32 decision "
+                                "outside a guard band around the threshold, FP64 re-take "
+                                "inside it; FP64 running energies",
+                   "l2": "flushed between timed steps (256 MiB write); the rows a launch "
+                         "reads (anchors, offsets, screen positions: 22.5 MB) come from "
+                         "HBM at each step start",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak,

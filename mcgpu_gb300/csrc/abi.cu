@@ -1526,8 +1526,19 @@ extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
   cudaEvent_t e0, e1;
   CK(ctx, cudaEventCreate(&e0));
   CK(ctx, cudaEventCreate(&e1));
-  // time of trial_steps steps with tile T from the saved state: the faster
-  // of two timed runs after a warm-up launch (per-step cost, so runs longer
+  // Every timed launch starts with L2 cleared (a write of twice its size),
+  // as it does for a state larger than L2 or a batch run between other
+  // work; without the scratch buffer the launches run as they come.
+  int l2 = 0;
+  cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device);
+  void* flush = nullptr;
+  const size_t flush_bytes = 2 * (size_t)std::max(l2, 0);
+  if (flush_bytes && cudaMalloc(&flush, flush_bytes) != cudaSuccess) {
+    flush = nullptr;
+    cudaGetLastError();
+  }
+  // time of trial_steps steps with tile T from the saved state: the fastest
+  // of three timed runs after a warm-up launch (per-step cost, so runs longer
   // than trial_steps are scaled)
   auto trial = [&](const Tile& T, float* out) -> int {
     *out = 1e30f;
@@ -1538,47 +1549,54 @@ extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
     r = mcgpu_batch_run(bt, T.spl, 0);
     if (r) return r;
     const int n = std::max(trial_steps, 2 * T.spl);
-    for (int rep = 0; rep < 2; rep++) {
-      CK(ctx, cudaEventRecord(e0, ctx->stream));
-      r = mcgpu_batch_run(bt, n, 0);
-      if (r) return r;
-      CK(ctx, cudaEventRecord(e1, ctx->stream));
-      CK(ctx, cudaEventSynchronize(e1));
-      float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
-      *out = std::min(*out, ms * (float)trial_steps / (float)n);
+    for (int rep = 0; rep < 3; rep++) {
+      float total = 0;
+      for (int done = 0; done < n; done += T.spl) {
+        if (flush) CK(ctx, cudaMemsetAsync(flush, rep + 1, flush_bytes, ctx->stream));
+        CK(ctx, cudaEventRecord(e0, ctx->stream));
+        r = mcgpu_batch_run(bt, std::min(T.spl, n - done), 0);
+        if (r) return r;
+        CK(ctx, cudaEventRecord(e1, ctx->stream));
+        CK(ctx, cudaEventSynchronize(e1));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        total += ms;
+      }
+      *out = std::min(*out, total * (float)trial_steps / (float)n);
     }
     return MCGPU_OK;
   };
   float best = 1e30f, ms = 0;
   Tile bestT = {bt->threads, bt->cpc, bt->spl, bt->lanes};
-  // CTA shape (threads, chains per CTA) with the default lanes
+  // CTA shape (threads, chains per CTA) and lanes per neighbour molecule
+  // together (the best width depends on the lanes), at 64 steps a launch
+  // (shorter launches weigh the launch tail, which the final steps-per-launch
+  // search settles)
+  std::vector<Tile> shapes;
   const int tw[] = {64, 128, 256, 512};
   for (int t : tw)
-    for (int gw = 1; gw <= t / 32 && rc == MCGPU_OK; gw *= 2) {
+    for (int gw = 1; gw <= t / 32; gw *= 2) {
       const int cpc = (t / 32) / gw;
       if (gw > 1 && cpc > 15) continue;
       // 512 threads only as one 16-warp group (smaller groups repeat the
       // 256-thread shapes with fewer CTAs per SM)
       if (t == 512 && cpc != 1) continue;
-      const Tile T = {t, cpc, 16, 0};
+      shapes.push_back({t, cpc, 64, 0});
+    }
+  // one group of 3, 5, 6 or 7 warps per CTA (at 128 registers a thread,
+  // 5-warp CTAs fit three to an SM: three chains in flight instead of two)
+  for (int t : {96, 160, 192, 224}) shapes.push_back({t, 1, 64, 0});
+  int max_tpm = 1;
+  for (const ChainHdr& h : bt->pool.hdr) max_tpm = std::max(max_tpm, h.tpm);
+  for (const Tile& S : shapes)
+    for (int lanes = 0; lanes < max_tpm && rc == MCGPU_OK; lanes = lanes ? lanes << 1 : 1) {
+      const Tile T = {S.threads, S.cpc, S.spl, lanes};
       rc = trial(T, &ms);
       if (rc == MCGPU_OK && ms < best) {
         best = ms;
         bestT = T;
       }
     }
-  // lanes per neighbour molecule for the best shape
-  int max_tpm = 1;
-  for (const ChainHdr& h : bt->pool.hdr) max_tpm = std::max(max_tpm, h.tpm);
-  for (int lanes = 1; lanes < max_tpm && rc == MCGPU_OK; lanes <<= 1) {
-    const Tile T = {bestT.threads, bestT.cpc, bestT.spl, lanes};
-    rc = trial(T, &ms);
-    if (rc == MCGPU_OK && ms < best) {
-      best = ms;
-      bestT = T;
-    }
-  }
   // steps per launch for the best shape
   const int spls[] = {4, 16, 64};
   for (int spl : spls) {
@@ -1592,6 +1610,7 @@ extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (flush) cudaFree(flush);
   if (rc) return rc;
   rc = mcgpu_batch_set_tile(bt, bestT.threads, bestT.cpc, bestT.spl, bestT.lanes);
   if (rc) return rc;

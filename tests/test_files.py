@@ -261,14 +261,19 @@ def test_metrosim_needs_the_gpu(tmp_path):
             M.run(["wat.config", "-n", "5"], out=None)
 
 
-def test_reference_loader_live():
-    """Where the compiled reference is present, its loader is run directly."""
+def test_reference_loader_live(tmp_path):
+    """Where the compiled reference is present, its loader is run directly
+    (on a copy of the inputs: it writes a log file where it runs)."""
+    import shutil
     from oracle.pyoracle import REF_SO, RefHarness
     if not REF_SO.exists():
         pytest.skip("compiled reference not present")
+    for f in FILES.iterdir():
+        if f.is_file():
+            shutil.copy(f, tmp_path / f.name)
     R = RefHarness()
     for name in CONFIGS:
-        ref = R.load_files(str(FILES / (name + ".config")))
+        ref = R.load_files(str(tmp_path / (name + ".config")))
         assert_rows(load(name + ".config"), ref)
 
 

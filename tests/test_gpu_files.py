@@ -234,3 +234,26 @@ def test_batch_create_reports_lowest_failing_chain(ctx):
     boxes[3].pidx = np.zeros(0, np.int32)
     with pytest.raises(MCGPUError, match="chain 3: empty box"):
         ChainBatch(ctx, boxes, seeds)
+
+
+def test_autotune_keeps_state(ctx):
+    """The autotuner times tiles on saved copies of the rows: afterwards the
+    batch is where it was and continues as a batch given the chosen tile."""
+    boxes, seeds = W.water_chains(12, n_min=64, n_max=600, seed=44)
+    a = ChainBatch(ctx, boxes, seeds, rotation=ROT_AXIS)
+    t0 = a.tile
+    a.run(32)
+    before = _stats(a)
+    tile = a.autotune(32)
+    assert a.tile == tile and _stats(a) == before
+    a.run(64)
+    c = ChainBatch(ctx, boxes, seeds, rotation=ROT_AXIS)
+    c.set_tile(*t0)
+    c.run(32)
+    c.set_tile(*tile)
+    c.run(64)
+    assert _stats(a) == _stats(c)
+    for k in range(len(boxes)):
+        assert all(np.array_equal(u, v) for u, v in zip(a.download(k), c.download(k)))
+    a.close()
+    c.close()
