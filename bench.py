@@ -45,6 +45,11 @@ FP32_FLOPS_PER_PAIR = 38   # per atom pair, fixed by convention from the referen
 # launch, L2 flushed between bench steps), by tile
 # (threads, chains per CTA, steps per launch, lanes per molecule).
 CHAIN_TRAFFIC_BYTES = {(256, 1, 64, 1): 33.61e6, (160, 1, 64, 1): 33.72e6}
+# L2 sector throughput peak implied by the same captures: lts__t_sectors.sum.per_second
+# (32 B sectors) over lts__t_sectors.sum.pct_of_peak_sustained_elapsed (36.25 and 36.37
+# TB/s on the two tiles); MEASURED_PEAKS.json holds no L2 figure
+L2_PEAK_GBS = 36300.0
+ATOMS_PER_WATER = 3
 
 
 def peaks():
@@ -472,6 +477,8 @@ def main():
     fp32_peak = sm_count * 128 * 2 * 2.07e9 / 1e12
     achieved = flops_per_launch / kernel_s_per_launch / 1e12
     mean_pairs_per_move = pairs / moves_local
+    # 2 n_in a^2 pairs per move (a = 3 on water): 2 n_in a = pairs / a atom rows
+    l2_bytes_move = (mean_pairs_per_move / ATOMS_PER_WATER + 2 * ATOMS_PER_WATER) * 16
 
     ctx.set_stream(None)
     # end to end through the public API: boxes from host memory, run, results back
@@ -537,7 +544,16 @@ def main():
                              "per move (device-counted, old+new)",
                      "peak_source": "nominal FP32 CUDA-core peak at 2070 MHz "
                                     "(no measured FP32 figure in MEASURED_PEAKS.json)",
-                     "hbm_peak_gbs": pk.get("hbm_gbs"), "hbm_peak_source": src},
+                     "hbm_peak_gbs": pk.get("hbm_gbs"), "hbm_peak_source": src,
+                     "l2": {"bytes_per_move": l2_bytes_move,
+                            "achieved_gbs": value * l2_bytes_move / 1e9,
+                            "peak_gbs": L2_PEAK_GBS,
+                            "frac": value * l2_bytes_move / 1e9 / L2_PEAK_GBS,
+                            "work": "2 n_in a 16 + 2 a 16 bytes per move (float4 rows of the "
+                                    "in-range neighbours' atoms and of the moved molecule, "
+                                    "both placements)",
+                            "peak_source": "ncu L2 sector throughput peak of the k_chain_steps "
+                                           "captures"}},
         "gpu_launches": args.steps * launches_per_step,
         "clocks": clocks,
         "e2e": e2e,

@@ -14,6 +14,19 @@ from .workloads import BoxData
 
 _F64 = ("x", "y", "z", "sigma", "epsilon", "charge")
 _I32 = ("mol_start", "mol_len", "mol_pidx_start", "mol_pidx_count", "pidx")
+_ROWS = tuple((k, np.dtype(np.float64)) for k in _F64) + \
+    tuple((k, np.dtype(np.int32)) for k in _I32)
+
+
+def _row_address(a, dt: np.dtype, keep: list) -> int:
+    """Address of row a as a C-contiguous array of dt (converted, and kept
+    alive in keep, only where it is not one already)."""
+    if not (type(a) is np.ndarray and a.dtype == dt and a.flags.c_contiguous):
+        a = np.ascontiguousarray(a, dt)
+        keep.append(a)
+    if a.flags.writeable and a.size:
+        return C.addressof(C.c_char.from_buffer(a))   # the cheaper route
+    return a.ctypes.data
 
 
 def _desc_dtype() -> np.dtype:
@@ -50,18 +63,10 @@ class ChainBatch:
         d["n_mol"] = [b.n_mol for b in boxes]
         d["n_atom"] = self.n_atom
         d["n_pidx"] = [b.n_pidx for b in boxes]
-        keep = []
-        addr = np.empty((n, len(_F64) + len(_I32)), np.uint64)
-        for i, b in enumerate(boxes):
-            row = addr[i]
-            for f, k in enumerate(_F64 + _I32):
-                a = getattr(b, k)
-                dt = np.float64 if f < len(_F64) else np.int32
-                if not (isinstance(a, np.ndarray) and a.dtype == dt and a.flags.c_contiguous):
-                    a = np.ascontiguousarray(a, dt)
-                keep.append(a)
-                row[f] = a.__array_interface__["data"][0]
-        for f, k in enumerate(_F64 + _I32):
+        keep: list = []
+        addr = np.array([[_row_address(getattr(b, k), dt, keep) for k, dt in _ROWS]
+                         for b in boxes], np.uint64).reshape(n, len(_ROWS))
+        for f, (k, _) in enumerate(_ROWS):
             d[k] = addr[:, f]
         d["size"] = np.array([np.asarray(b.size, np.float64)[:3] for b in boxes]).reshape(n, 3)
         d["cutoff"] = [float(b.cutoff) for b in boxes]
