@@ -331,9 +331,9 @@ int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
   k_refresh_mirrors<<<(int)((nm + wpb - 1) / wpb), wpb * 32, 0, st>>>(P, dp.mol_chain, 0, (int)nm);
   CK(ctx, cudaGetLastError());
   CK(ctx, cudaStreamSynchronize(st));
-  dp.hdr = hp.hdr;
-  dp.mstart = hp.mstart;
-  dp.mlen = hp.mlen;
+  dp.hdr.assign(hp.hdr.begin(), hp.hdr.end());
+  dp.mstart.assign(hp.mstart.begin(), hp.mstart.end());
+  dp.mlen.assign(hp.mlen.begin(), hp.mlen.end());
   return MCGPU_OK;
 }
 

@@ -6,7 +6,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <memory>
 #include <string>
+#include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "device.cuh"
@@ -83,14 +86,38 @@ T* dalloc(size_t n, cudaError_t* e) {
   return p;
 }
 
+// Allocator whose construction without a value leaves trivial types
+// uninitialised: resize() of the host rows costs no fill (the pool build
+// writes every entry afterwards).
+template <class T>
+struct NoFillAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoFillAlloc<U>;
+  };
+  NoFillAlloc() = default;
+  template <class U>
+  NoFillAlloc(const NoFillAlloc<U>&) noexcept {}
+  template <class U>
+  void construct(U* p) noexcept(std::is_nothrow_default_constructible<U>::value) {
+    ::new ((void*)p) U;
+  }
+  template <class U, class... A>
+  void construct(U* p, A&&... a) {
+    ::new ((void*)p) U(std::forward<A>(a)...);
+  }
+};
+template <class T>
+using HostRow = std::vector<T, NoFillAlloc<T>>;
+
 struct HostPool {
-  std::vector<double> x, y, z, sig, eps, q;
-  std::vector<float4> aoff;
-  std::vector<float2> aeq;
-  std::vector<int> mstart, mlen, pidx, mol_chain, atom_mol;
-  std::vector<int2> mpi;
-  std::vector<float> mrad;
-  std::vector<ChainHdr> hdr;
+  HostRow<double> x, y, z, sig, eps, q;
+  HostRow<float4> aoff;
+  HostRow<float2> aeq;
+  HostRow<int> mstart, mlen, pidx, mol_chain, atom_mol;
+  HostRow<int2> mpi;
+  HostRow<float> mrad;
+  HostRow<ChainHdr> hdr;
   int max_len = 0;
   // capacity for the given totals (one allocation per row instead of growth)
   void reserve(size_t atoms, size_t mols, size_t pidxs, size_t chains) {

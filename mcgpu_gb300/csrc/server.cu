@@ -235,8 +235,9 @@ int upload_job(mcgpu_server* s, Job* j) {
   mcgpu_ctx* ctx = s->ctx;
   HostPool& hp = j->hp;
   const int a0 = (int)j->a0, m0 = (int)j->m0, p0 = (int)j->p0, slot = j->slot;
-  std::vector<int> mstart(hp.mstart), pidx(hp.pidx), mol_chain(j->n_mol, slot), atom_mol(hp.atom_mol);
-  std::vector<int2> mpi(hp.mpi);
+  std::vector<int> mstart(hp.mstart.begin(), hp.mstart.end()), pidx(hp.pidx.begin(), hp.pidx.end()),
+      mol_chain(j->n_mol, slot), atom_mol(hp.atom_mol.begin(), hp.atom_mol.end());
+  std::vector<int2> mpi(hp.mpi.begin(), hp.mpi.end());
   for (int& v : mstart) v += a0;
   for (int& v : pidx) v += a0;
   for (int& v : atom_mol) v += m0;
