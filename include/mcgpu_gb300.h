@@ -198,8 +198,12 @@ int mcgpu_batch_destroy(mcgpu_batch* batch);
  * replayed from a captured CUDA graph).  Asynchronous on the batch stream
  * unless sync != 0. */
 int mcgpu_batch_run(mcgpu_batch* batch, int n_steps, int sync);
-/* Chooses steps_per_launch, chains per CTA and threads per molecule by timing
- * candidate tiles on this batch (state is saved and restored). */
+/* Chooses threads per CTA, chains per CTA, lanes per neighbour molecule and
+ * steps per launch by timing candidate tiles on this batch, trial_steps
+ * steps each, every timed launch starting from a cleared L2 (the rows are
+ * saved first and restored after every trial and at the end, so the batch
+ * continues from where it was).  Allocates a scratch buffer of twice the L2
+ * size for the duration of the call. */
 int mcgpu_batch_autotune(mcgpu_batch* batch, int trial_steps);
 /* Sets the tile explicitly: threads per CTA (32..512, a multiple of 32),
  * chains per CTA (dividing its warps), steps per launch (>= 1), and lanes
