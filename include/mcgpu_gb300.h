@@ -104,7 +104,10 @@ typedef struct {
   double e_old, e_new;    /* FP64 system energies at V and V'              */
   double dlnv, u;         /* the ln V step and the acceptance uniform      */
   double edge;            /* box edge x after the decision                 */
-  int32_t fp64;           /* 1 if FP32 energies were re-taken in FP64      */
+  int32_t fp64;           /* 0: FP32 energies (mixed) or FP64 (FP64 form);
+                             1: both re-taken (double-float, then FP64);
+                             2: e_new re-taken in double-float, e_old the
+                             running energy                                 */
   int32_t pad0;
 } mcgpu_vol_trace;
 

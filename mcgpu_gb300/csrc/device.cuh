@@ -151,9 +151,10 @@ struct VolMove {
   float reach, sf;   // rc + 2 prad + 0.01; edge ratio L'/L
   double L[3];
   double dlnv, u;
-  int state;   // 0 not due, 1 evaluate, 2 rejected outright, 3 accepted,
-               // 5 double-float re-take too close to call: FP64 re-take,
-               // 4 FP32 energies too close to the threshold: FP64 re-take
+  int state;   // 0 not due, 1 evaluate, 2 rejected outright, 3 accepted;
+               // too close to the threshold: 6 after the FP32 U(V'), re-take
+               // U(V') in double-float; 4 after that, re-take both totals in
+               // double-float; 5 after that, re-take both in FP64
   int fp64;    // decided on FP64 pair energies
 };
 

@@ -16,11 +16,12 @@
 // isobaric ln V move instead.  The running energy is replaced by the FP64
 // total of the volume the chain keeps (a drift reset every interval).
 //
-// With vol_mixed the energies come from FP32 pair terms summed in
-// double-float (k_vol_pair_sums32) and the decision is taken on them unless
-// the criterion's argument lies within their rounding bound of ln u; those
-// chains alone are re-evaluated with FP64 pairs and decided on that, so the
-// decisions are the FP64 ones.
+// With vol_mixed U(V) is the running energy and U(V') comes from FP32 pair
+// terms summed in double-float (k_vol_pair_sums32); the decision is taken on
+// them unless the criterion's argument lies within their error bound of
+// ln u.  Those chains alone are re-evaluated -- U(V') in double-float, then
+// both totals in double-float, then both in FP64, each tier only for what the
+// last left too close to call -- so the decisions are the FP64 ones.
 //
 // Kernels (one volume phase, launched between step launches):
 //   k_vol_propose      per chain: due?, draw, L'
@@ -674,7 +675,9 @@ __device__ __forceinline__ void vol_df_mol(const Pool& P, const int* mol_chain,
   const int c = mol_chain[m];
   const VolMove& v = vm[c];
   const ChainHdr& H = P.hdr[c];
-  if (v.state != 4) return;
+  if (v.state != 4 && v.state != 6) return;
+  // state 6 re-takes U(V') only (.x stays 0)
+  const int w0 = v.state == 6 ? 1 : 0, nvol = v.state == 6 ? 1 : 2;
   vc_stencil(P, H, m, S);
   const int a0 = P.mstart[m], len = P.mlen[m] & 255;
   const int2 pi = P.mpi[m];
@@ -705,7 +708,8 @@ __device__ __forceinline__ void vol_df_mol(const Pool& P, const int* mol_chain,
       int f = 0, j = 0;
       if (t < n_cand) {
         j = vc_candidate(P, S, t, kc);
-        if (vc_takes(S, kc, j, m)) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, 0, 2);
+        if (vc_takes(S, kc, j, m))
+          f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, w0, nvol);
       }
       vol_append(ent, wcnt, j, f, r);
     }
@@ -969,7 +973,7 @@ __global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, cons
   const int c = range_chain(R, blockIdx.x);
   if (vm[c].state != want) return;
   const ChainHdr& H = P.hdr[c];
-  const bool mixed = want == 1 || want == 4;
+  const bool mixed = want == 1 || want == 4 || want == 6;
   double2 acc = make_double2(0.0, 0.0), ab = make_double2(0.0, 0.0);
   for (int i = threadIdx.x; i < H.n_mol; i += blockDim.x) {
     acc.x += emol2[H.mol0 + i].x;
@@ -999,8 +1003,10 @@ __global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, cons
 
 // The isobaric criterion; an accepted move installs the new box.
 // Pass 0 decides the due chains (a mixed chain whose FP32 argument lies
-// within its rounding bound of ln u is marked state 4 instead); pass 1
-// decides the marked chains on their FP64 energies.
+// within its error bound of ln u is marked state 6 instead); pass 3 decides
+// state 6 on the double-float U(V') (still too close: state 4), pass 1 state
+// 4 on double-float totals at both volumes (still too close: state 5), pass
+// 2 state 5 on FP64 totals.
 __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const double2* eabs,
                              mcgpu_vol_trace* trace, int trace_slot, int trace_stride,
                              MolRanges R, int n_items, int pass) {
@@ -1008,18 +1014,20 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
   if (i >= n_items) return;
   const int c = range_chain(R, i);
   VolMove v = vm[c];
-  if (pass == 0 ? (v.state != 1 && v.state != 2) : v.state != (pass == 1 ? 4 : 5)) return;
+  const int want = pass == 1 ? 4 : (pass == 2 ? 5 : 6);
+  if (pass == 0 ? (v.state != 1 && v.state != 2) : v.state != want) return;
   ChainHdr& H = P.hdr[c];
   double e_old = H.energy, e_new = 0.0;
   int ok = 0;
   if (v.state != 2) {
     // a mixed move's U(V) is the running energy (error bound run_err) and
-    // its U(V') the FP32 total; a re-take has both totals in double-float
-    // (state 4) or, when that is still too close to call, in FP64 (state 5);
-    // an FP64 chain has both FP64 totals
+    // its U(V') the FP32 total; too close to call, U(V') is taken again in
+    // double-float (state 6), then both totals in double-float (state 4),
+    // then both in FP64 (state 5); an FP64 chain has both FP64 totals
     const bool mixed = v.state == 1 && H.vol_mixed;
+    const bool vprime = v.state == 6;
     const bool dfl = v.state == 4;
-    e_old = mixed ? H.energy : esum[c].x;
+    e_old = (mixed || vprime) ? H.energy : esum[c].x;
     e_new = esum[c].y;
     const double vo = H.L[0] * H.L[1] * H.L[2];
     const double vn = v.L[0] * v.L[1] * v.L[2];
@@ -1031,16 +1039,19 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
     if (mixed) {
       err_old = H.run_err;
       err_new = kTieRel * eabs[c].y;
+    } else if (vprime) {
+      err_old = H.run_err;
+      err_new = kDfRel * eabs[c].y;
     } else if (dfl) {
       err_old = kDfRel * eabs[c].x;
       err_new = kDfRel * eabs[c].y;
     }
-    if (mixed || dfl) {
+    if (mixed || vprime || dfl) {
       // |error of dU| <= err_old + err_new
       const double bound = (err_old + err_new + 1e-12 * (fabs(e_old) + fabs(e_new))) / H.kT;
       if (fabs(arg - log(v.u)) <= bound + 1e-12) {
-        v.state = mixed ? 4 : 5;
-        v.fp64 = 1;
+        v.state = mixed ? 6 : (vprime ? 4 : 5);
+        v.fp64 = mixed ? 2 : 1;   // 2: only U(V') is taken again
         vm[c] = v;
         return;
       }
@@ -1049,7 +1060,7 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
     if (ok) {
       H.energy = e_new;
       H.run_err = err_new;
-    } else if (!mixed) {
+    } else if (!mixed && !vprime) {
       H.energy = e_old;
       H.run_err = err_old;
     }
@@ -1206,6 +1217,11 @@ cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, V
     // is still too close after that
     // the re-takes run over the listed chains' molecules only (grid-strided)
     const int grid = kVolListGrid;
+    k_vol_list<<<1, 32, 0, st>>>(P, vm, act, nc, 6, vlist);
+    k_vol_pair_sums_df<<<grid, kVolThreads, 0, st>>>(P, mol_chain, vm, vlist, nc, emol2, eabs2);
+    k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 6);
+    k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, trace, trace_slot,
+                                                  trace_stride, act, nc, 3);
     k_vol_list<<<1, 32, 0, st>>>(P, vm, act, nc, 4, vlist);
     k_vol_pair_sums_df<<<grid, kVolThreads, 0, st>>>(P, mol_chain, vm, vlist, nc, emol2, eabs2);
     k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 4);
