@@ -36,6 +36,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"]
 N_CHAINS = 512
 STEPS_PER_BENCH = 64
+E2E_BENCH_STEPS = 40
 WORKLOAD = ("512 independent NVT water chains (3-site TIP3P-like, rigid), N log-uniform in "
             "[64, 2048] at 1.0 g/cc, T uniform in [280, 360] K, cutoff min(9, L/2) A, "
             "+-0.15 A / +-15 deg random-axis moves, Philox proposals, on-device accept")
@@ -76,7 +77,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
@@ -395,7 +396,7 @@ def bench_served(ctx, rate: float = 200.0, window_s: float = 4.0, steps_per_job:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -487,18 +488,22 @@ def main():
         torch.cuda.synchronize()
         h2d = sum(b.n_atom * (6 * 8) + b.n_mol * 16 + b.n_pidx * 4 for b in boxes)
         d2h = sum(b.n_atom * 24 for b in boxes) + N_CHAINS * 40
+        # a set length (40 bench steps: 2560 moves a chain) whatever --steps
+        # is, so the batch creation weighs the same in every run
+        e2e_steps = E2E_BENCH_STEPS
         t0 = time.perf_counter()
         b2 = M.ChainBatch(ctx, boxes, seeds, rotation=M.ROT_AXIS)
         b2.set_tile(threads, cpc, spl, lanes)
-        b2.run(STEPS_PER_BENCH * args.steps, sync=True)
+        b2.run(STEPS_PER_BENCH * e2e_steps, sync=True)
         st_e2e = b2.stats()
         b2.download_all()
         dt_e2e = time.perf_counter() - t0
         b2.close()
-        e2e = {"value": moves_local / dt_e2e, "unit": "moves/s",
-               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+        e2e = {"value": N_CHAINS * STEPS_PER_BENCH * e2e_steps / dt_e2e, "unit": "moves/s",
+               "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
+               "steps": e2e_steps,
                "note": "create batch from host boxes (incl. initial FP32-pair system energies), "
-                       f"{STEPS_PER_BENCH * args.steps} steps per chain, all coordinates and "
+                       f"{STEPS_PER_BENCH * e2e_steps} steps per chain, all coordinates and "
                        "stats back"}
 
     plain = None
