@@ -72,3 +72,32 @@ def test_build_centres_min_distance():
     r = np.sqrt((d ** 2).sum(-1))
     np.fill_diagonal(r, 99)
     assert r.min() >= 2.5
+
+
+def test_batch_descriptor_rows():
+    """The batch descriptor record matches mcgpu_box_desc field for field, and
+    the row addresses it takes are the arrays' own (converted copies only
+    for rows that are not contiguous FP64 / int32, kept alive by the caller)."""
+    from mcgpu_gb300 import batch as B
+    dt = B._desc_dtype()
+    assert dt.itemsize == C.sizeof(_abi.BoxDesc)
+    for name, _ in _abi.BoxDesc._fields_:
+        assert dt.fields[name][1] == getattr(_abi.BoxDesc, name).offset
+    f64, i32 = np.dtype(np.float64), np.dtype(np.int32)
+    a = np.arange(12.0)
+    keep = []
+    assert B._row_address(a, f64, keep) == a.ctypes.data and keep == []
+    ro = np.arange(6.0)
+    ro.flags.writeable = False
+    assert B._row_address(ro, f64, keep) == ro.ctypes.data and keep == []
+    empty = np.zeros(0)
+    assert B._row_address(empty, f64, keep) == empty.ctypes.data and keep == []
+    strided = np.arange(20.0)[::2]
+    addr = B._row_address(strided, f64, keep)
+    assert len(keep) == 1 and addr == keep[0].ctypes.data
+    assert np.array_equal(keep[0], strided) and keep[0].flags.c_contiguous
+    addr = B._row_address([1, 2, 3], i32, keep)
+    assert len(keep) == 2 and keep[1].dtype == i32 and addr == keep[1].ctypes.data
+    ints64 = np.arange(4, dtype=np.int64)
+    B._row_address(ints64, i32, keep)
+    assert keep[2].dtype == i32 and np.array_equal(keep[2], ints64)
