@@ -211,9 +211,10 @@ int mcgpu_batch_autotune(mcgpu_batch* batch, int trial_steps);
 /* Sets the tile explicitly: threads per CTA (32..512, a multiple of 32),
  * chains per CTA (dividing its warps), steps per launch (>= 1), and lanes
  * per neighbour molecule (a power of two <= 32 capping every chain's
- * default, the power of two at or above its largest molecule; 0 keeps the
- * defaults).  Results do not depend on the first three; the lanes change the
- * FP32 summation order and so the last bits of the energies. */
+ * default; 0 keeps the defaults: one lane for a chain of one species of at
+ * most 4 atoms, else the power of two at or above its largest molecule).
+ * Results do not depend on the first three; the lanes change the FP32
+ * summation order and so the last bits of the energies. */
 int mcgpu_batch_set_tile(mcgpu_batch* batch, int threads, int chains_per_cta,
                          int steps_per_launch, int lanes_per_molecule);
 int mcgpu_batch_get_tile(mcgpu_batch* batch, int* threads, int* chains_per_cta,

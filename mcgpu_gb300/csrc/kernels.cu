@@ -326,7 +326,11 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
     long long acc_n = 0, npairs = 0;
     int ties = 0;
     const unsigned long long step0 = H.step;
-    const int T = lanes_cap > 0 ? min(lanes_cap, H.tpm) : H.tpm;
+    // lanes per neighbour molecule: the cap, else one lane for a chain of
+    // one species of at most 4 atoms (the single-lane pair batch), else the
+    // power of two at or above its largest molecule
+    const int T = lanes_cap > 0 ? min(lanes_cap, H.tpm)
+                                : ((H.uniform && H.ulen <= 4 && !H.precise) ? 1 : H.tpm);
     MoveF* props = (MoveF*)s.props;
     int my_steps = n_steps;
     if (H.step_limit > 0)
