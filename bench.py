@@ -33,7 +33,8 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"]
+METRIC = ("MC moves/s: batched+served vs plain 1-chain on same GB300 at \u0394E rel err"
+          "\u22641e-5; p99 job")
 N_CHAINS = 512
 STEPS_PER_BENCH = 64
 E2E_BENCH_STEPS = 40
