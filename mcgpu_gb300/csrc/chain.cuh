@@ -42,8 +42,8 @@ __device__ __forceinline__ float4 chain_screen_pos(uint4 A, float4 o, const Chai
 
 // misc[] slots written by stage_chain beyond load_moved's: new quaternion,
 // acceptance uniform, "trial placement within skin/2 of the Verlet build"
-// flag; kMiscNlOk: the chain's list is still valid (group-uniform state)
-enum : int { kMiscQn = 16, kMiscU = 20, kMiscNlTrial = 24, kMiscNlOk = 25 };
+// flag
+enum : int { kMiscQn = 16, kMiscU = 20, kMiscNlTrial = 24 };
 
 // One warp stages the proposed FP32 move `mv` of a chain molecule into
 // slot s: old and new offsets (o_old, o_new), pair factors and |o|^2 (eq),
@@ -123,27 +123,6 @@ __device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF
     s.miscd[0] = (double)(H.uniform ? H.umrad : P.mrad[m]);
     s.miscd[1] = (double)qsum;
   }
-}
-
-// Warp-wide copy of a move staged ahead into the current slot (misc up to
-// kMiscNlTrial: the slots above it are group state).
-__device__ __forceinline__ void adopt_staged(const StageSlot& from, const StageSlot& to,
-                                             int lane) {
-  const int len = from.misc[2], np = from.misc[3];
-  for (int i = lane; i < len; i += 32) {
-    to.o_old[i] = from.o_old[i];
-    to.o_new[i] = from.o_new[i];
-    to.l_old[i] = from.l_old[i];
-    to.l_new[i] = from.l_new[i];
-    to.eq[i] = from.eq[i];
-  }
-  for (int k = lane; k < np; k += 32) {
-    to.p_old[k] = from.p_old[k];
-    to.p_new[k] = from.p_new[k];
-    to.pa[k] = from.pa[k];
-  }
-  if (lane <= kMiscNlTrial) to.misc[lane] = from.misc[lane];
-  if (lane < 2) to.miscd[lane] = from.miscd[lane];
 }
 
 // Screen of candidate j against the staged molecule (both placements):
@@ -252,7 +231,8 @@ __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const G
 
 // Group-wide deterministic double-float sum: warp butterflies, then every
 // thread adds the per-warp values in warp order.
-__device__ __forceinline__ void group_reduce_ff(const Group& g, const GroupSmem& s, AccFF& a) {
+__device__ __forceinline__ void group_reduce_ff(const Group& g, const GroupSmem& s, AccFF& a,
+                                                int par = 0) {
   for (int off = 16; off > 0; off >>= 1) {
     const float oh = __shfl_xor_sync(~0u, a.oh, off), ol = __shfl_xor_sync(~0u, a.ol, off);
     const float nh = __shfl_xor_sync(~0u, a.nh, off), nl = __shfl_xor_sync(~0u, a.nl, off);
@@ -262,14 +242,16 @@ __device__ __forceinline__ void group_reduce_ff(const Group& g, const GroupSmem&
     a.np += __shfl_xor_sync(~0u, a.np, off);
   }
   const int nw = g.nwarps();
-  float* red = (float*)s.red;   // 5 floats per warp fit the 3 doubles reserved per warp
+  // buffer `par` of two; 5 floats per warp fit the 3 doubles reserved per warp
+  float* red = (float*)(s.red + par * 3 * nw);
+  long long* redl = s.redl + par * nw;
   if ((g.tid & 31) == 0) {
     red[5 * g.warp() + 0] = a.oh;
     red[5 * g.warp() + 1] = a.ol;
     red[5 * g.warp() + 2] = a.nh;
     red[5 * g.warp() + 3] = a.nl;
     red[5 * g.warp() + 4] = a.ab;
-    s.redl[g.warp()] = a.np;
+    redl[g.warp()] = a.np;
   }
   g.sync();
   a.oh = a.ol = a.nh = a.nl = a.ab = 0.f;
@@ -278,7 +260,7 @@ __device__ __forceinline__ void group_reduce_ff(const Group& g, const GroupSmem&
     ff_add2(a.oh, a.ol, red[5 * w + 0], red[5 * w + 1]);
     ff_add2(a.nh, a.nl, red[5 * w + 2], red[5 * w + 3]);
     a.ab += red[5 * w + 4];
-    a.np += s.redl[w];
+    a.np += redl[w];
   }
 }
 

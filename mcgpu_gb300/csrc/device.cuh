@@ -430,21 +430,21 @@ struct GroupSmem {
   int* lj;                              // (j << 4) | flags
   float4* lA;                           // (Dold.xyz, Dnew.x)
   float2* lB;                           // (Dnew.y, Dnew.z)
-  double* red;                          // [3 * nwarps] reduction scratch
-  long long* redl;                      // [nwarps]
+  double* red;                          // [2][3 * nwarps] reduction scratch (two buffers)
+  long long* redl;                      // [2][nwarps]
   int* misc;                            // [32] broadcast ints
   double* miscd;                        // [32] broadcast doubles
   float4* pc;                           // [cache_n] screen positions of the chain (or null)
   void* props;                          // [32] drawn moves of the next steps (chain kernel)
   float4* nbuf;                         // [nwarps * 32 * 5] per-lane neighbour rows (async copies)
   float2* teq;                          // [maxA] pair factors per slot of a uniform chain
-  char* ahead;                          // a second staging slot (the chain kernel's next move)
+  char* ahead;                          // three more staging slots (the chain kernel's moves)
 };
 
 // The rows a staged move occupies: offsets, pair factors, primaries, the
-// broadcast ints and doubles.  A group has two: its current move's (inside
-// GroupSmem) and the one the chain kernel stages the next move into ahead
-// of time.
+// broadcast ints and doubles: the ones inside GroupSmem, and three more the
+// chain kernel rotates through (a step's move, the next one staged ahead,
+// and the one before, which slower warps may still be committing).
 struct StageSlot {
   float4* o_old; float4* o_new;
   float4* l_old; float4* l_new;
@@ -455,9 +455,11 @@ struct StageSlot {
   double* miscd;
 };
 
-__device__ __forceinline__ StageSlot current_slot(const GroupSmem& s) {
-  return StageSlot{s.o_old, s.o_new, s.l_old, s.l_new, s.eq, s.p_old, s.p_new, s.pa, s.misc,
-                   s.miscd};
+// s with its staging rows replaced by slot t's.
+__device__ __forceinline__ GroupSmem with_slot(GroupSmem s, const StageSlot& t) {
+  s.o_old = t.o_old; s.o_new = t.o_new; s.l_old = t.l_old; s.l_new = t.l_new; s.eq = t.eq;
+  s.p_old = t.p_old; s.p_new = t.p_new; s.pa = t.pa; s.misc = t.misc; s.miscd = t.miscd;
+  return s;
 }
 
 struct SmemShape {
@@ -473,15 +475,15 @@ struct SmemShape {
     b += align16(nwarps * kRing * 4);
     b += align16(nwarps * kRing * 16);
     b += align16(nwarps * kRing * 8);
-    b += align16(3 * nwarps * 8);
-    b += align16(nwarps * 8);
+    b += align16(6 * nwarps * 8);
+    b += align16(2 * nwarps * 8);
     b += align16(32 * 4);
     b += align16(32 * 8);
     b += align16(cache_n * 16);
     b += align16(32 * kPropBytes);
     b += align16(nwarps * 32 * 5 * 16);
     b += align16(maxA * 8);
-    b += ahead_bytes();
+    b += 3 * ahead_bytes();
     return b;
   }
   // the second staging slot: offsets and factors, primaries, misc, miscd
@@ -514,8 +516,8 @@ struct SmemShape {
     s.lj = (int*)p; p += align16(nwarps * kRing * 4);
     s.lA = (float4*)p; p += align16(nwarps * kRing * 16);
     s.lB = (float2*)p; p += align16(nwarps * kRing * 8);
-    s.red = (double*)p; p += align16(3 * nwarps * 8);
-    s.redl = (long long*)p; p += align16(nwarps * 8);
+    s.red = (double*)p; p += align16(6 * nwarps * 8);
+    s.redl = (long long*)p; p += align16(2 * nwarps * 8);
     s.misc = (int*)p; p += align16(32 * 4);
     s.miscd = (double*)p; p += align16(32 * 8);
     s.pc = cache_n > 0 ? (float4*)p : nullptr;

@@ -282,21 +282,23 @@ __global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol
 
 // Persistent kernel: groups of `gwarps` warps pull chain tasks from `queue`
 // (task k runs chain order[k]) and advance each by n_steps steps on the
-// chain state.  A step: the move staged in FP32 during the previous step
-// (one group barrier); every warp screens its share of the candidates and
-// evaluates the in-range ones (FP32 pair terms, double-float sums), the
-// last warp then stages the next move into the second slot; one
-// group reduction gives E_old, E_new.  Outside a guard band around the
-// acceptance threshold the decision (dE < 0, else exp(-dE/kT) >= u,
-// SimulationStep.cpp:794-803) is taken in FP32; inside it the group
-// re-evaluates both placements with FP64 pairs and decides on that.  Warp
-// 0 commits.  With cache_n > 0 each group keeps its chain's primary screen
-// positions in shared memory.  If trace != nullptr, step st of chain c is
-// recorded at trace[c * trace_stride + trace_off + st].  The staging warp
-// draws the moves of 32 steps at once (one per lane) into shared memory;
-// after the commit warp 0 copies the staged move into the current slot, or
-// stages it again when the commit moved that molecule.  lanes_cap >
-// 0 caps the lanes per neighbour molecule of every chain.
+// chain state.  A step: every warp screens its share of the candidates
+// against the move staged in FP32 during the previous step and evaluates
+// the in-range ones (FP32 pair terms, double-float sums); the last warp then
+// stages the next move into the next of three shared-memory slots; one
+// group reduction (the step's barrier) gives every thread E_old, E_new.
+// Outside a guard band around the acceptance threshold the decision
+// (dE < 0, else exp(-dE/kT) >= u, SimulationStep.cpp:794-803) is taken in
+// FP32; inside it the group re-evaluates both placements with FP64 pairs and
+// decides on that.  Every warp takes the decision and writes the accepted
+// placement itself and goes on to the next step; warp 0 keeps the running
+// energy and the counters.  With cache_n > 0 each group keeps its chain's
+// primary screen positions in shared memory.  If trace != nullptr, step st
+// of chain c is recorded at trace[c * trace_stride + trace_off + st].  The
+// staging warp draws the moves of 32 steps at once (one per lane) into
+// shared memory; when a commit moves the molecule of the move staged next,
+// warp 0 stages it again (one more barrier).  lanes_cap > 0 caps the lanes
+// per neighbour molecule of every chain.
 __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue,
                                             const int* order, int n_tasks, int gwarps,
                                             SmemShape shape, mcgpu_trace* trace, int trace_off,
@@ -317,7 +319,6 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
     float4* pcache = (s.pc && H.simple_prim && H.n_mol <= shape.cache_n) ? s.pc : nullptr;
     if (pcache)
       for (int i = g.tid; i < H.n_mol; i += gsize) pcache[i] = P.ppos[H.pidx0 + i];
-    if (g.tid == 0) s.misc[kMiscNlOk] = (H.nl_on && H.nl_valid) ? 1 : 0;
     if (H.uniform)
       for (int i = g.tid; i < H.ulen; i += gsize) s.teq[i] = P.aeq[H.atom0 + i];
     g.sync();
@@ -326,6 +327,9 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
     long long acc_n = 0, npairs = 0;
     int ties = 0;
     const unsigned long long step0 = H.step;
+    // the Verlet list stays valid while no accepted molecule has moved beyond
+    // skin/2 of the build (every thread keeps the same flag)
+    bool nl_ok = H.nl_on && H.nl_valid;
     // lanes per neighbour molecule: the cap, else one lane for a chain of
     // one species of at most 4 atoms (the single-lane pair batch), else the
     // power of two at or above its largest molecule
@@ -335,7 +339,12 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
     int my_steps = n_steps;
     if (H.step_limit > 0)
       my_steps = (int)max(0LL, min((long long)n_steps, H.step_limit - (long long)step0));
-    const StageSlot cur = current_slot(s), nxt = shape.ahead_slot(s.ahead);
+    // step st's move is staged in slot st % 3 (the last warp stages step
+    // st + 1 during step st; slot (st + 2) % 3 = (st - 1) % 3 is rewritten
+    // only after every warp has passed step st's reduction barrier, so no
+    // warp still commits from it)
+    const int sb = shape.ahead_bytes();
+    auto slot = [&](int k) { return shape.ahead_slot(s.ahead + k * sb); };
     // moves are drawn 32 steps at a time (one per lane) by the staging warp
     auto draw32 = [&](int st0) {
       if (st0 + lane < my_steps)
@@ -345,32 +354,32 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
     };
     if (w == 0 && my_steps > 0) {
       draw32(0);
-      stage_chain(P, H, props[0], cur, pcache, lane);
+      stage_chain(P, H, props[0], slot(0), pcache, lane);
     }
+    g.sync();
     for (int st = 0; st < my_steps; st++) {
-      g.sync();
-      const MovedInfo mi = load_moved(s);
-      // read before the reduction barrier: warp 0 restages the slot after it
-      const float u = __int_as_float(s.misc[kMiscU]);
+      const int k = st % 3, kn = k == 2 ? 0 : k + 1;
+      const GroupSmem ss = with_slot(s, slot(k));
+      const MovedInfo mi = load_moved(ss);
+      const float u = __int_as_float(ss.misc[kMiscU]);
       // Verlet list while it is valid and the trial placement stays within
       // skin/2 of the build; the full scan otherwise (same in-range set)
-      const int trial_near = s.misc[kMiscNlTrial];
-      const bool use_list = s.misc[kMiscNlOk] && trial_near;
+      const int trial_near = ss.misc[kMiscNlTrial];
+      const bool use_list = nl_ok && trial_near;
       AccFF acc = {0.f, 0.f, 0.f, 0.f, 0.f, 0};
       if (use_list)
-        warp_eval_chain(P, H, s, mi, pcache, 0, P.nl_cnt[mi.mol], w, nw, lane, T, acc,
+        warp_eval_chain(P, H, ss, mi, pcache, 0, P.nl_cnt[mi.mol], w, nw, lane, T, acc,
                         P.nl + (size_t)mi.mol * P.nl_stride);
       else
-        warp_eval_chain(P, H, s, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, acc);
+        warp_eval_chain(P, H, ss, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, acc);
       // the last warp (with the fewest screen blocks) stages the next move
-      // while the others finish their share; staging reads rows this step's
-      // commit changes only if the next move is of the same molecule (warp 0
-      // then stages it again)
+      // while the others finish their share
       if (w == nw - 1 && st + 1 < my_steps) {
         if (((st + 1) & 31) == 0) draw32(st + 1);
-        stage_chain(P, H, props[(st + 1) & 31], nxt, pcache, lane);
+        stage_chain(P, H, props[(st + 1) & 31], slot(kn), pcache, lane);
       }
-      group_reduce_ff(g, s, acc);
+      // the step's one barrier; every thread ends with the same totals
+      group_reduce_ff(g, ss, acc, st & 1);
       // FP32 decision unless the FP32 dE is within its rounding bound of the
       // threshold; the bound covers the pair terms' rounding (kTieRel of the
       // sum of magnitudes) and the FP32 difference of the two totals.
@@ -378,65 +387,61 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
       const float bound = (float)kTieRel * acc.ab + 2.4e-7f * (fabsf(acc.nh) + fabsf(acc.oh)) + 1e-9f;
       const float pf = expf(-fmaxf(de_f, 0.f) * H.kTinvf);
       const int tie = (de_f >= -bound) && (fabsf(pf - u) <= pf * (1.5f * bound * H.kTinvf) + 1e-6f);
-      double e_old, e_new;
+      double e_old = 0.0, e_new = 0.0;
+      int ok;
       if (tie) {
-        if (w == 0) stage_chain_f64(P, H, s, mi, lane);
+        if (w == 0) stage_chain_f64(P, H, ss, mi, lane);
         g.sync();
         double eo = 0.0, en = 0.0, ab2 = 0.0;
         long long np2 = 0;
-        warp_eval_chain64(P, H, s, mi, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, eo, en);
-        group_reduce(g, s, eo, en, ab2, np2);
+        warp_eval_chain64(P, H, ss, mi, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, eo, en);
+        group_reduce(g, ss, eo, en, ab2, np2, st & 1);
         e_old = eo;
         e_new = en;
+        const double d64 = e_new - e_old;
+        ok = (d64 < 0) || (exp(-d64 / H.kT) >= (double)u);
+      } else {
+        ok = (de_f < 0.f) || (pf >= u);
       }
-      if (w == 0) {
-        int ok = 0;
-        double de = 0.0;
-        if (lane == 0) {
-          if (!tie) {
-            e_old = (double)acc.oh + (double)acc.ol;
-            e_new = (double)acc.nh + (double)acc.nl;
-            ok = (de_f < 0.f) || (pf >= u);
-          } else {
-            const double d64 = e_new - e_old;
-            ok = (d64 < 0) || (exp(-d64 / H.kT) >= (double)u);
-          }
-          de = e_new - e_old;
+      // every warp takes the same decision and writes the same new placement,
+      // so each sees it in its next screen without waiting for the others
+      if (ok) commit_chain(P, H, ss, mi, pcache, lane);
+      __syncwarp();
+      if (ok && !trial_near) nl_ok = false;
+      if (w == 0 && lane == 0) {
+        if (!tie) {
+          e_old = (double)acc.oh + (double)acc.ol;
+          e_new = (double)acc.nh + (double)acc.nl;
         }
-        ok = __shfl_sync(~0u, ok, 0);
-        if (ok) commit_chain(P, H, s, mi, pcache, lane);
-        if (lane == 0) {
-          if (ok) {
-            energy += de;
-            err += tie ? 1e-12 * (double)acc.ab : (double)bound;
-            acc_n++;
-            // a molecule now beyond skin/2 of the build invalidates the list
-            if (!trial_near) s.misc[kMiscNlOk] = 0;
-          }
-          if (H.nl_on && !use_list) full_scans++;
-          npairs += acc.np;
-          ties += tie;
-          if (trace) {
-            mcgpu_trace t;
-            t.mol = mi.mol - H.mol0;
-            t.accepted = ok;
-            t.e_old = e_old;
-            t.e_new = e_new;
-            t.de = de;
-            t.u = (double)u;
-            t.fp64 = tie;
-            t.pad0 = 0;
-            trace[(size_t)c * trace_stride + trace_off + st] = t;
-          }
+        const double de = e_new - e_old;
+        if (ok) {
+          energy += de;
+          err += tie ? 1e-12 * (double)acc.ab : (double)bound;
+          acc_n++;
         }
-        __syncwarp();
-        if (st + 1 < my_steps) {
-          if (ok && H.mol0 + props[(st + 1) & 31].mol == mi.mol)
-            stage_chain(P, H, props[(st + 1) & 31], cur, pcache, lane);
-          else
-            adopt_staged(nxt, cur, lane);
-          __syncwarp();
+        if (H.nl_on && !use_list) full_scans++;
+        npairs += acc.np;
+        ties += tie;
+        if (trace) {
+          mcgpu_trace t;
+          t.mol = mi.mol - H.mol0;
+          t.accepted = ok;
+          t.e_old = e_old;
+          t.e_new = e_new;
+          t.de = de;
+          t.u = (double)u;
+          t.fp64 = tie;
+          t.pad0 = 0;
+          trace[(size_t)c * trace_stride + trace_off + st] = t;
         }
+      }
+      // the next move was staged from rows this commit changes only if it
+      // moves the same molecule (read from its slot: the staging warp may
+      // already be drawing over props): warp 0 stages it again, all warps
+      // wait (the condition is the same in every thread)
+      if (st + 1 < my_steps && ok && slot(kn).misc[0] == mi.mol) {
+        if (w == 0) stage_chain(P, H, props[(st + 1) & 31], slot(kn), pcache, lane);
+        g.sync();
       }
     }
     if (g.tid == 0) {
@@ -447,7 +452,7 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
       Hp->pairs += npairs;
       Hp->ties += ties;
       if (H.nl_on) {
-        Hp->nl_valid = s.misc[kMiscNlOk];
+        Hp->nl_valid = nl_ok ? 1 : 0;
         Hp->nl_full += full_scans;
       }
     }

@@ -614,7 +614,7 @@ __device__ inline void warp_eval(const Pool& P, const ChainHdr& H, const GroupSm
 // thread adds the per-warp values in warp order.  Two calls must be
 // separated by a group barrier (the scratch is reused).
 __device__ __forceinline__ void group_reduce(const Group& g, const GroupSmem& s, double& a,
-                                             double& b, double& d, long long& c) {
+                                             double& b, double& d, long long& c, int par = 0) {
   for (int off = 16; off > 0; off >>= 1) {
     a += __shfl_xor_sync(~0u, a, off);
     b += __shfl_xor_sync(~0u, b, off);
@@ -622,11 +622,13 @@ __device__ __forceinline__ void group_reduce(const Group& g, const GroupSmem& s,
     c += __shfl_xor_sync(~0u, c, off);
   }
   const int nw = g.nwarps();
+  double* red = s.red + par * 3 * nw;   // buffer `par` of two
+  long long* redl = s.redl + par * nw;
   if ((g.tid & 31) == 0) {
-    s.red[g.warp()] = a;
-    s.red[nw + g.warp()] = b;
-    s.red[2 * nw + g.warp()] = d;
-    s.redl[g.warp()] = c;
+    red[g.warp()] = a;
+    red[nw + g.warp()] = b;
+    red[2 * nw + g.warp()] = d;
+    redl[g.warp()] = c;
   }
   g.sync();
   a = 0.0;
@@ -634,10 +636,10 @@ __device__ __forceinline__ void group_reduce(const Group& g, const GroupSmem& s,
   d = 0.0;
   c = 0;
   for (int w = 0; w < nw; w++) {
-    a += s.red[w];
-    b += s.red[nw + w];
-    d += s.red[2 * nw + w];
-    c += s.redl[w];
+    a += red[w];
+    b += red[nw + w];
+    d += red[2 * nw + w];
+    c += redl[w];
   }
 }
 
