@@ -169,39 +169,62 @@ def dist_sum(dist, v: float) -> float:
 
 # ---- CPU baseline -------------------------------------------------------------
 
+CPU_STEPS_PER_CALL = 200   # MC steps of every chain per timed call of the CPU path
+
+
 def cpu_baseline(boxes, seeds, target_s: float = 12.0, threads: int | None = None) -> dict:
     """The reference's algorithm (FP64 restatement, oracle/) on the host
     cores: every chain of the workload advanced by the same Philox moves,
-    chains spread over all threads; a bounded sample sized to about
-    target_s seconds."""
+    chains spread over all threads, CPU_STEPS_PER_CALL steps of every chain
+    per call; calls repeated until about target_s seconds (a bounded
+    sample)."""
     from oracle.pyoracle import OracleBox, chains_run_mt
     threads = threads or os.cpu_count() or 1
     obs = [OracleBox(b) for b in boxes]
+    chains_run_mt(obs, seeds, 1, 1, threads, step0=0)    # warm-up: one step per chain
+    step, moves, calls = 1, 0, 0
     t0 = time.perf_counter()
-    chains_run_mt(obs, seeds, 1, 1, threads, step0=0)  # calibration: 1 step per chain
-    dt = time.perf_counter() - t0
-    steps = max(1, min(200, int(target_s / max(dt, 1e-6))))
-    t0 = time.perf_counter()
-    moves = chains_run_mt(obs, seeds, steps, 1, threads, step0=1)
-    dt = time.perf_counter() - t0
+    while True:
+        moves += chains_run_mt(obs, seeds, CPU_STEPS_PER_CALL, 1, threads, step0=step)
+        step += CPU_STEPS_PER_CALL
+        calls += 1
+        dt = time.perf_counter() - t0
+        if dt >= target_s:
+            break
     return {"value": moves / dt, "unit": "moves/s", "cores": threads, "kind": "port",
-            "sample": f"{len(boxes)} chains x {steps} steps ({moves} moves) in {dt:.2f} s"}
+            "sample": f"{len(boxes)} chains x {calls} x {CPU_STEPS_PER_CALL} steps "
+                      f"({moves} moves) in {dt:.2f} s"}
+
+
+def _product_library_mapped() -> bool:
+    """True if this process has the product's CUDA library mapped."""
+    try:
+        return "libmcgpu_gb300" in Path("/proc/self/maps").read_text()
+    except OSError:
+        return False
 
 
 def run_reference(args, ws, rank):
-    """--impl reference: rank 0 times the reference's CPU path on the host."""
+    """--impl reference: rank 0 times the reference's CPU path on the host:
+    the FP64 restatement (oracle/, bit-identical to the reference compiled
+    from its sources) on the same 512-chain workload, every bench step one
+    call advancing every chain by CPU_STEPS_PER_CALL steps on all host
+    threads.  The workload is built with the oracle's own centre builder, so
+    this arm never loads the product library (checked)."""
     if rank != 0:
         return
     from mcgpu_gb300 import workloads as W
-    boxes, seeds = W.water_chains(N_CHAINS, seed=2024)
-    from oracle.pyoracle import OracleBox, chains_run_mt
+    from oracle.pyoracle import OracleBox, build_centres, chains_run_mt
+    boxes, seeds = W.batch_water_512(seed=2024, centres=build_centres)
+    if _product_library_mapped():
+        raise RuntimeError("the reference arm must not load the product library")
     threads = os.cpu_count() or 1
     obs = [OracleBox(b) for b in boxes]
-    per_step = 2          # MC steps of every chain per bench step (bounded sample)
+    per_step = CPU_STEPS_PER_CALL
     step = 0
     for _ in range(args.warmup):
-        chains_run_mt(obs, seeds, 1, 1, threads, step0=step)
-        step += 1
+        chains_run_mt(obs, seeds, per_step, 1, threads, step0=step)
+        step += per_step
     t0 = time.perf_counter()
     moves = 0
     for _ in range(args.steps):
@@ -217,10 +240,12 @@ def run_reference(args, ws, rank):
         "config": {"workload": WORKLOAD, "chains": N_CHAINS,
                    "steps_per_bench_step": per_step,
                    "note": "reference CPU path as its FP64 restatement (oracle/mcgpu_oracle.c, "
-                           "bit-identical to the compiled reference); chains over all host "
-                           "threads"},
+                           "bit-identical to the compiled reference, which is built only where "
+                           "the reference sources are); chains over all host threads; workload "
+                           "built without the product library"},
         "cpu_baseline": {"value": v, "unit": "moves/s", "cores": threads, "kind": "port",
-                         "sample": f"{N_CHAINS} chains x {per_step * args.steps} steps"},
+                         "sample": f"{N_CHAINS} chains x {args.steps} x {per_step} steps "
+                                   f"({moves} moves) in {dt:.2f} s"},
         "e2e": {"value": v, "unit": "moves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -270,7 +295,7 @@ def bench_single(ctx, plain_steps: int = 150, chain_steps: int = 4000) -> dict:
     its boxes; random centres at this density put atoms of neighbours on top
     of each other (energies ~1e19 kcal/mol)."""
     import mcgpu_gb300 as M
-    box = M.bicyclic_box(4000, L=86.1, seed=4000, lattice=True)
+    box = M.workloads.bicyclic_4000()
     out = {"workload": "4000 x 16-atom bicyclic, L=86.1 A, rc 12 A, NVT 298 K, single chain"}
     for name, prec in (("plain_fp64", M.PREC_FP64), ("plain_mixed", M.PREC_MIXED)):
         g = M.GpuBox(ctx, box, prec)
@@ -301,7 +326,7 @@ def bench_large(ctx, steps: int = 6000) -> dict:
     energy.  Beside it the plain FP64 drop-in for a few steps."""
     import torch
     import mcgpu_gb300 as M
-    box = M.water_box(32768, L=99.3, cutoff=12.0, temperature=298.0, seed=32768)
+    box = M.workloads.water_32768()
     out = {"workload": "32768 waters, L=99.3 A, rc 12 A, NPT 298 K / 1 atm, Verlet skin 1.5 A, "
                        "volume move every 500 steps"}
     bt = M.ChainBatch(ctx, [box], [0x5EED], rotation=M.ROT_AXIS)
@@ -441,7 +466,7 @@ def main():
     torch.cuda.set_device(local)
     ctx = M.Context(local)
 
-    boxes, seeds = M.water_chains(N_CHAINS, seed=2024 + 7919 * rank)
+    boxes, seeds = M.workloads.batch_water_512(seed=2024 + 7919 * rank)
     bt = M.ChainBatch(ctx, boxes, seeds, rotation=M.ROT_AXIS)
     if args.tile:
         bt.set_tile(*[int(v) for v in args.tile.split(",")])

@@ -284,7 +284,7 @@ def _place(xyz, R, centres):
 def build_box(template, n_mol: int, L: float, cutoff: float, temperature: float,
               max_translate: float, max_rotate: float, seed: int, dmin: float,
               name: str = "", atom_dmin: float = 0.0, overlap_rounds: int = 200,
-              lattice: bool = False) -> BoxData:
+              lattice: bool = False, centres=None) -> BoxData:
     """Places n_mol copies of a rigid template: centres by random sequential
     addition at minimum separation dmin and orientations uniform on SO(3),
     or (lattice=True) centres on an FCC lattice all in one orientation, the
@@ -292,11 +292,15 @@ def build_box(template, n_mol: int, L: float, cutoff: float, temperature: float,
     atom_dmin to another molecule's atom are re-oriented (and, off the
     lattice, re-centred after repeated failures) for up to overlap_rounds
     rounds; at liquid density some overlaps may remain, as in the
-    reference's own lattice starts."""
+    reference's own lattice starts.  `centres(seed, n, L, dmin)` replaces
+    the random-sequential-addition builder (it must place the same points)."""
     xyz, sig, eps, q, prim = template
     a = xyz.shape[0]
     rng = np.random.default_rng(seed)
-    centres = fcc_centres(seed, n_mol, L) if lattice else rsa_centres(seed, n_mol, L, dmin)
+    if lattice:
+        centres = fcc_centres(seed, n_mol, L)
+    else:
+        centres = (centres or rsa_centres)(seed, n_mol, L, dmin)
     if lattice:
         k = 1
         while 4 * k ** 3 < n_mol:
@@ -337,11 +341,11 @@ def build_box(template, n_mol: int, L: float, cutoff: float, temperature: float,
 
 def water_box(n_mol: int = 256, L: float | None = None, cutoff: float = 9.0,
               temperature: float = 298.15, max_translate: float = 0.15, max_rotate: float = 15.0,
-              seed: int = 12345, dmin: float = 2.5) -> BoxData:
+              seed: int = 12345, dmin: float = 2.5, centres=None) -> BoxData:
     if L is None:
         L = (n_mol / WATER_DENSITY) ** (1.0 / 3.0)
     return build_box(water_template(), n_mol, L, cutoff, temperature, max_translate, max_rotate,
-                     seed, dmin, name=f"water{n_mol}")
+                     seed, dmin, name=f"water{n_mol}", centres=centres)
 
 
 def bicyclic_box(n_mol: int = 4000, L: float | None = None, cutoff: float = 12.0,
@@ -362,10 +366,11 @@ def bicyclic_box(n_mol: int = 4000, L: float | None = None, cutoff: float = 12.0
 
 def water_chains(n_chains: int = 512, n_min: int = 64, n_max: int = 2048, seed: int = 2024,
                  t_range=(280.0, 360.0), max_translate: float = 0.15,
-                 max_rotate: float = 15.0) -> tuple[list[BoxData], np.ndarray]:
+                 max_rotate: float = 15.0, centres=None) -> tuple[list[BoxData], np.ndarray]:
     """Independent water chains: N log-uniform in [n_min, n_max], L for
     1.0 g/cc, cutoff min(9, L/2), T uniform in t_range; returns the boxes and
-    one 64-bit Philox key per chain."""
+    one 64-bit Philox key per chain.  `centres` replaces the centre builder
+    (same signature as rsa_centres)."""
     rng = np.random.default_rng(seed)
     sizes = np.rint(np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_chains))).astype(int)
     temps = rng.uniform(t_range[0], t_range[1], n_chains)
@@ -376,5 +381,30 @@ def water_chains(n_chains: int = 512, n_min: int = 64, n_max: int = 2048, seed: 
         L = (n / WATER_DENSITY) ** (1.0 / 3.0)
         boxes.append(water_box(n, L=L, cutoff=min(9.0, L / 2), temperature=float(temps[c]),
                                max_translate=max_translate, max_rotate=max_rotate,
-                               seed=int(seed * 100003 + c)))
+                               seed=int(seed * 100003 + c), centres=centres))
     return boxes, seeds
+
+
+# ---- the measured workloads, by name --------------------------------------------
+#
+# One constructor per measured configuration, so the benchmark and the parity
+# tests build bit-identical inputs.
+
+def batch_water_512(seed: int = 2024, centres=None) -> tuple[list[BoxData], np.ndarray]:
+    """512 independent NVT water chains, N log-uniform in [64, 2048] at
+    1.0 g/cc, T uniform in [280, 360] K, cutoff min(9, L/2), +-0.15 A /
+    +-15 deg moves: the batched headline workload."""
+    return water_chains(512, n_min=64, n_max=2048, seed=seed, centres=centres)
+
+
+def bicyclic_4000() -> BoxData:
+    """4000 rigid 16-atom bicyclic molecules, L = 86.1 A, rc 12 A, 298 K,
+    +-0.2 A / +-10 deg, on an FCC lattice (10^3 cells hold the 4000 centres
+    exactly) in one common orientation: the single-chain workload."""
+    return bicyclic_box(4000, L=86.1, seed=4000, lattice=True)
+
+
+def water_32768() -> BoxData:
+    """32,768 waters (98,304 atoms), L = 99.3 A, rc 12 A, 298 K: the large
+    single system (NPT at 1 atm with Verlet lists in its measurement)."""
+    return water_box(32768, L=99.3, cutoff=12.0, temperature=298.0, seed=32768)

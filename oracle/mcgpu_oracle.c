@@ -826,3 +826,97 @@ int orc_fchain_volume(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step
   }
   return ok;
 }
+
+/* ---- synthetic initial configuration (input generation, not the path) ---
+ *
+ * Centres by random sequential addition: points uniform in [0, L)^3, each
+ * candidate closer than dmin (minimum image) to a placed one redrawn, drawn
+ * from xoshiro256** seeded by splitmix64 (Blackman & Vigna 2018, restated
+ * from their published description).  It places the same points as the
+ * product's input builder for the same arguments, so the CPU baseline can
+ * build its workload without loading the product library.  Returns 0, 1
+ * (bad argument) or 2 (no room). */
+static uint64_t orc_splitmix64(uint64_t* s) {
+  uint64_t z = (*s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+static uint64_t orc_rotl64(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static double orc_xoshiro_u01(uint64_t st[4]) {
+  const uint64_t r = orc_rotl64(st[1] * 5, 7) * 9;
+  const uint64_t t = st[1] << 17;
+  st[2] ^= st[0];
+  st[3] ^= st[1];
+  st[1] ^= st[2];
+  st[0] ^= st[3];
+  st[2] ^= t;
+  st[3] = orc_rotl64(st[3], 45);
+  return (double)(r >> 11) * 0x1.0p-53;
+}
+
+int orc_build_centres(int n, double L, double dmin, uint64_t seed, double* out) {
+  if (n < 0 || !(L > 0) || !(dmin >= 0) || (n > 0 && !out)) return 1;
+  if (n == 0) return 0;
+  int nc = dmin > 0 ? (int)floor(L / dmin) : 1;
+  if (nc < 3) nc = 1;
+  if (nc > 512) nc = 512;
+  const double cw = L / nc;
+  const size_t ncell = (size_t)nc * nc * nc;
+  /* per-cell singly linked lists of placed points (head per cell, next per point) */
+  int* head = (int*)malloc(sizeof(int) * ncell);
+  int* next = (int*)malloc(sizeof(int) * (size_t)n);
+  if (!head || !next) {
+    free(head);
+    free(next);
+    return 2;
+  }
+  for (size_t i = 0; i < ncell; i++) head[i] = -1;
+  uint64_t st[4], sd = seed;
+  for (int i = 0; i < 4; i++) st[i] = orc_splitmix64(&sd);
+  const double d2 = dmin * dmin;
+  const long long max_tries = 2000LL * n + 100000;
+  long long tries = 0;
+  int k = 0, rc = 0;
+  while (k < n) {
+    if (++tries > max_tries) {
+      rc = 2;
+      break;
+    }
+    double p[3];
+    for (int d = 0; d < 3; d++) p[d] = orc_xoshiro_u01(st) * L;
+    int c[3];
+    for (int d = 0; d < 3; d++) {
+      c[d] = (int)(p[d] / cw);
+      if (c[d] >= nc) c[d] = nc - 1;
+      if (nc < 3) c[d] = 0;
+    }
+    int ok = 1;
+    const int span = nc >= 3 ? 1 : 0;
+    for (int a = -span; a <= span && ok; a++)
+      for (int b = -span; b <= span && ok; b++)
+        for (int e = -span; e <= span && ok; e++) {
+          const int ca = (c[0] + a + nc) % nc, cb = (c[1] + b + nc) % nc, ce = (c[2] + e + nc) % nc;
+          for (int j = head[((size_t)ca * nc + cb) * nc + ce]; j >= 0 && ok; j = next[j]) {
+            double r2 = 0;
+            for (int d = 0; d < 3; d++) {
+              double dx = out[3 * j + d] - p[d];
+              dx -= L * nearbyint(dx / L);
+              r2 += dx * dx;
+            }
+            if (r2 < d2) ok = 0;
+          }
+        }
+    if (!ok) continue;
+    const size_t cell = ((size_t)c[0] * nc + c[1]) * nc + c[2];
+    next[k] = head[cell];
+    head[cell] = k;
+    for (int d = 0; d < 3; d++) out[3 * k + d] = p[d];
+    k++;
+  }
+  free(head);
+  free(next);
+  return rc;
+}

@@ -121,6 +121,10 @@ int orc_fchain_volume(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step
                       double p_kcal, double max_dlnv, float rad_max, double lrc_v, double* energy,
                       double* e_old, double* e_new, double* dlnv_out, double* u_out);
 
+/* Synthetic input generation: molecule centres by random sequential
+ * addition (the same points as the product's input builder). */
+int orc_build_centres(int n, double L, double dmin, uint64_t seed, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -127,6 +127,8 @@ def orc_lib() -> C.CDLL:
                                             C.POINTER(C.c_double)]),
             "orc_accept_volume": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double,
                                             C.c_int, C.c_double, C.c_double]),
+            "orc_build_centres": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint64,
+                                            _dp]),
         }
         for name, (res, args) in protos.items():
             fn = getattr(L, name)
@@ -273,6 +275,18 @@ class OracleChain:
             C.byref(eo), C.byref(en), C.byref(dl), C.byref(u))
         return {"status": st, "e_old": eo.value, "e_new": en.value, "dlnv": dl.value,
                 "u": u.value, "energy": e.value, "edge": float(self.ob.s.size[0])}
+
+
+def build_centres(seed: int, n: int, L: float, dmin: float) -> np.ndarray:
+    """Molecule centres by random sequential addition (orc_build_centres):
+    the same points as the product's input builder, without loading the
+    product library (for the CPU baseline's workload)."""
+    out = np.empty((n, 3), dtype=np.float64)
+    rc = orc_lib().orc_build_centres(int(n), float(L), float(dmin), int(seed) & (2 ** 64 - 1),
+                                     out.ctypes.data_as(_dp))
+    if rc != 0:
+        raise RuntimeError(f"could not place {n} centres at dmin {dmin} in L {L} (status {rc})")
+    return out
 
 
 def sincos_f32(x: float) -> tuple[float, float]:

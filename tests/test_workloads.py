@@ -67,3 +67,17 @@ def test_fcc_lattice_start():
     box = W.bicyclic_box(500, seed=3, lattice=True)
     e = OracleBox(box).system_energy()
     assert np.isfinite(e) and e / box.n_mol < 1e3
+
+
+def test_oracle_centre_builder_places_the_same_points():
+    """The CPU baseline builds its workload with the oracle's centre builder
+    (so it never loads the product library); it must give the product
+    builder's points, hence bit-identical boxes."""
+    from oracle.pyoracle import build_centres
+    for n, L, dmin, seed in [(100, 15.0, 2.5, 5), (2048, 39.4, 2.5, 7), (300, 10.0, 0.0, 3),
+                             (64, 12.3, 2.5, 2024 * 100003)]:
+        assert np.array_equal(build_centres(seed, n, L, dmin), W.rsa_centres(seed, n, L, dmin))
+    a, _ = W.water_chains(6, seed=11)
+    b, _ = W.water_chains(6, seed=11, centres=build_centres)
+    for x, y in zip(a, b):
+        assert np.array_equal(x.x, y.x) and np.array_equal(x.z, y.z)
