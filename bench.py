@@ -37,6 +37,7 @@ METRIC = ("MC moves/s: batched+served vs plain 1-chain on same GB300 at \u0394E 
           "\u22641e-5; p99 job")
 N_CHAINS = 512
 STEPS_PER_BENCH = 64
+CHAIN_STEPS = 20000        # steps of each chain of the batched workload
 E2E_BENCH_STEPS = 40
 WORKLOAD = ("512 independent NVT water chains (3-site TIP3P-like, rigid), N log-uniform in "
             "[64, 2048] at 1.0 g/cc, T uniform in [280, 360] K, cutoff min(9, L/2) A, "
@@ -326,9 +327,15 @@ def bench_large(ctx, steps: int = 6000) -> dict:
     energy.  Beside it the plain FP64 drop-in for a few steps."""
     import torch
     import mcgpu_gb300 as M
-    box = M.workloads.water_32768()
+    from mcgpu_gb300.prepare import relaxed_water_32768
+    t0 = time.perf_counter()
+    box = relaxed_water_32768(ctx)
+    t_relax = time.perf_counter() - t0
     out = {"workload": "32768 waters, L=99.3 A, rc 12 A, NPT 298 K / 1 atm, Verlet skin 1.5 A, "
-                       "volume move every 500 steps"}
+                       "volume move every 500 steps",
+           "start": "512 waters relaxed by the chain kernel (400 sweeps, NVT 298 K, rc 9 A) at "
+                    "the same density, replicated 4 x 4 x 4",
+           "relax_s": t_relax}
     bt = M.ChainBatch(ctx, [box], [0x5EED], rotation=M.ROT_AXIS)
     bt.set_tile(512, 1, 64)          # one chain: one group of 16 warps
     bt.set_verlet(1.5)
@@ -347,6 +354,8 @@ def bench_large(ctx, steps: int = 6000) -> dict:
                 "volume_moves": st.vol_tried, "volume_accepted": st.vol_accepted,
                 "edge_A": st.box[0], "density_mol_per_A3": box.n_mol / st.box[0] ** 3,
                 "nl_builds": st.nl_builds, "nl_full_scan_steps": st.nl_full_scans,
+                "acceptance": st.accepted / (steps + 500),
+                "energy_per_molecule": st.energy / box.n_mol,
                 "fp64_retakes": st.ties, "steps": steps + 500})
     bt.close()
     g = M.GpuBox(ctx, box, M.PREC_FP64)
@@ -468,6 +477,12 @@ def main():
 
     boxes, seeds = M.workloads.batch_water_512(seed=2024 + 7919 * rank)
     bt = M.ChainBatch(ctx, boxes, seeds, rotation=M.ROT_AXIS)
+    # Each chain runs CHAIN_STEPS steps: the untimed steps before the warm-up
+    # and timed ones come first, so the timed steps are the last of every
+    # chain's run (relaxed from its random start), not its first.
+    pre_steps = max(0, CHAIN_STEPS - (args.warmup + args.steps) * STEPS_PER_BENCH)
+    pre_steps -= pre_steps % STEPS_PER_BENCH
+    bt.run(pre_steps, sync=True)
     if args.tile:
         bt.set_tile(*[int(v) for v in args.tile.split(",")])
         tile = bt.tile
@@ -506,6 +521,8 @@ def main():
             dist.barrier()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     st1 = bt.stats()
+    acc_rate = (sum(s.accepted for s in st1) - sum(s.accepted for s in st0)) / (
+        N_CHAINS * STEPS_PER_BENCH * args.steps)
     pairs = sum(s.pairs for s in st1) - pairs0
     t_local = sum(step_ms) / 1000.0
     t_max = dist_max(dist, t_local)
@@ -573,6 +590,9 @@ def main():
         "config": {"workload": WORKLOAD, "chains": N_CHAINS,
                    "molecules": sum(b.n_mol for b in boxes),
                    "steps_per_bench_step": STEPS_PER_BENCH,
+                   "steps_before_timing": pre_steps + args.warmup * STEPS_PER_BENCH,
+                   "chain_steps": CHAIN_STEPS,
+                   "acceptance": acc_rate,
                    "tile": {"threads": threads, "chains_per_cta": cpc, "steps_per_launch": spl,
                             "lanes_per_molecule": lanes},
                    "precision": "FP32 pair terms with double-float sums; FP32 decision "

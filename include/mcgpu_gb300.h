@@ -390,9 +390,15 @@ double mcgpu_server_clock(const mcgpu_server* srv);
  * array, so two calls that can run at the same time on one device (two
  * streams without ordering, two host threads) race and give wrong sums.  The
  * first call on each device looks up the array's address with that device
- * current; make that first call before any stream capture.  Rows that index
- * out of range give NaN instead of being read.  Errors: MCGPU_ERR_INVALID,
- * MCGPU_ERR_UNSUPPORTED, MCGPU_ERR_CUDA; text via mcgpu_last_error(NULL). */
+ * current; make that first call before any stream capture.  The address is
+ * cached per device together with the id of the context it was found in: a
+ * call made after the application reset the device or re-created its
+ * primary context looks it up again (that call is then a first call too).
+ * Rows that index out of range give NaN instead of being read; a molecule
+ * with no primary indexes contributes nothing, as in moleculesInRange.  A
+ * CUDA error the caller left pending is neither cleared nor reported as
+ * this call's.  Errors: MCGPU_ERR_INVALID, MCGPU_ERR_UNSUPPORTED,
+ * MCGPU_ERR_CUDA; text via mcgpu_last_error(NULL). */
 int mcgpu_system_energy_static(const mcgpu_box_desc* rows, double* out, void* stream);
 
 /* ---- initial configuration (host only, no GPU) -------------------------- */

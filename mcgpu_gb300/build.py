@@ -46,7 +46,8 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 def build(verbose: bool = False, force: bool = False, extra: list[str] | None = None) -> Path:
     """Compiles (if stale) and returns the path of the shared library."""
     BUILD.mkdir(exist_ok=True)
-    headers = sorted(CSRC.glob("*.cuh")) + [ROOT / "include" / "mcgpu_gb300.h"]
+    headers = sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + \
+        [ROOT / "include" / "mcgpu_gb300.h"]
     flags = NVCC_FLAGS + (extra or [])
     objs = []
     jobs = []

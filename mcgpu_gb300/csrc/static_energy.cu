@@ -21,12 +21,17 @@
 // streams, no ordering) race on it.  The first call on each device looks up
 // the array's device address (cudaGetSymbolAddress) with that device
 // current and caches it; make that first call before any stream capture.
+// The cache is keyed on the current context's id: after a device reset or a
+// new primary context the next call looks the address up again (that call
+// is then a first call, with the same rule on capture).
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
 #include <mutex>
 
 #include "../../include/mcgpu_gb300.h"
+#include "static_scratch_cache.h"
 
 namespace mcgpu {
 void note_process_error(const char* msg);  // abi.cu: text for mcgpu_last_error(NULL)
@@ -65,9 +70,12 @@ __device__ __forceinline__ double dist2(const Rows& r, int a1, int a2) {
   return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
 }
 
+// Row ranges of molecule m inside the arrays.  A molecule without primary
+// indexes (pc == 0) is valid: moleculesInRange is false for it
+// (SimulationStep.cpp:317-330), so it contributes nothing.
 __device__ __forceinline__ bool valid_mol(const Rows& r, int m) {
   const int s = r.mstart[m], n = r.mlen[m], ps = r.mps[m], pc = r.mpc[m];
-  return s >= 0 && n >= 1 && s + n <= r.n_atom && ps >= 0 && pc >= 1 && ps + pc <= r.n_pidx;
+  return s >= 0 && n >= 1 && s + n <= r.n_atom && ps >= 0 && pc >= 0 && ps + pc <= r.n_pidx;
 }
 
 // E(m, j > m) per CTA m: threads stride over candidates j; the reference's
@@ -141,12 +149,39 @@ __global__ void k_static_sum(const double* emol, int n, double* out) {
   if (threadIdx.x == 0) *out = red[0];
 }
 
-std::mutex g_mu;
-double* g_emol_addr[kMaxDevices] = {};  // device address of the scratch, per device
+mcgpu::ScratchAddressCache<kMaxDevices> g_emol_cache;  // device address of the scratch
 
 int fail(int code, const char* msg) {
   mcgpu::note_process_error(msg);
   return code;
+}
+
+// Id of the calling thread's current context (0 if none or unknown), through
+// the driver's cuCtxGetCurrent / cuCtxGetId fetched from the runtime (no link
+// against the driver library).
+typedef int (*PfnCtxGetCurrent)(void**);
+typedef int (*PfnCtxGetId)(void*, unsigned long long*);
+
+unsigned long long current_context_id() {
+  static std::once_flag once;
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = (PfnCtxGetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = (PfnCtxGetId)f;
+  });
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx) return 0;
+  if (get_id(ctx, &id) != 0) return 0;
+  return id;
 }
 
 }  // namespace
@@ -166,18 +201,11 @@ extern "C" int mcgpu_system_energy_static(const mcgpu_box_desc* rows, double* ou
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return fail(MCGPU_ERR_CUDA, "no current CUDA device");
-  double* emol = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_emol_addr[dev]) {
-      void* p = nullptr;
-      const cudaError_t e = cudaGetSymbolAddress(&p, g_static_emol);
-      if (e != cudaSuccess || !p)
-        return fail(MCGPU_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed");
-      g_emol_addr[dev] = (double*)p;
-    }
-    emol = g_emol_addr[dev];
-  }
+  double* emol = (double*)g_emol_cache.get(
+      dev, current_context_id(),
+      [](void** p) { return cudaGetSymbolAddress(p, g_static_emol) == cudaSuccess; },
+      [] { return current_context_id(); });
+  if (!emol) return fail(MCGPU_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed");
   Rows r;
   r.x = rows->x; r.y = rows->y; r.z = rows->z;
   r.sig = rows->sigma; r.eps = rows->epsilon; r.q = rows->charge;
@@ -187,9 +215,24 @@ extern "C" int mcgpu_system_energy_static(const mcgpu_box_desc* rows, double* ou
   for (int k = 0; k < 3; k++) r.L[k] = rows->size[k];
   r.cutoff = rows->cutoff;
   cudaStream_t st = (cudaStream_t)stream;
+  // An error the caller's own code left pending stays the caller's: it is
+  // neither cleared nor reported as this call's.
+  const cudaError_t prior = cudaPeekAtLastError();
+  auto launch_error = [prior]() {
+    const cudaError_t e = prior == cudaSuccess ? cudaGetLastError() : cudaPeekAtLastError();
+    return e == prior ? cudaSuccess : e;
+  };
   k_static_pair_sums<<<r.n_mol, 256, 0, st>>>(r, emol);
-  if (cudaGetLastError() != cudaSuccess) return fail(MCGPU_ERR_CUDA, "launch failed");
-  k_static_sum<<<1, 256, 0, st>>>(emol, r.n_mol, out);
-  if (cudaGetLastError() != cudaSuccess) return fail(MCGPU_ERR_CUDA, "launch failed");
+  cudaError_t e = launch_error();
+  if (e == cudaSuccess) {
+    k_static_sum<<<1, 256, 0, st>>>(emol, r.n_mol, out);
+    e = launch_error();
+  }
+  if (e != cudaSuccess) {
+    static thread_local char msg[256];
+    snprintf(msg, sizeof(msg), "mcgpu_system_energy_static: launch failed: %s",
+             cudaGetErrorString(e));
+    return fail(MCGPU_ERR_CUDA, msg);
+  }
   return MCGPU_OK;
 }

@@ -1,0 +1,214 @@
+"""GPU parity at the benchmarked configurations, against the oracle.
+
+* The 512-chain water batch of the headline measurement (batch_water_512,
+  seed 2024: N log-uniform in [64, 2048]) on every single-group tile the
+  autotuner can choose (96, 160, 192, 224 and 256 threads, one chain per CTA,
+  64 steps a launch, lanes 0/1/2), two multi-group tiles, and the tile that
+  autotune() returns: 128 traced steps of ALL 512 chains replayed by the
+  oracle (molecule, uniform and decision of every step equal, coordinates bit
+  for bit), then 2048 more steps through the captured CUDA graph (one replay
+  of 32 launches) for 16 chains spread over the sizes (the smallest and the
+  largest among them): coordinates bit for bit and accepted counts equal.
+  The worst per-step dE error as a fraction of the FP32-pair tolerance
+  (|dE_gpu - dE_ref| <= 1e-5 max(|dE_ref|, 1e-3 sum k|terms|)) is printed.
+* The 4000 x 16-atom chain (bicyclic_4000), full scan and Verlet lists.
+* The 32,768-water NPT chain with Verlet lists and volume moves.
+
+The oracle's decisions are the reference's FP64 decisions
+(SimulationStep.cpp:794-803) on the reference's FP64 energies
+(BruteForceStep.cpp:15-79); coordinates come from the chain form's FP32
+moves, restated in the oracle."""
+import numpy as np
+import pytest
+
+from helpers import tol_mixed
+from mcgpu_gb300 import PREC_MIXED, ROT_AXIS, ChainBatch, Context, GpuBox
+from mcgpu_gb300 import workloads as W
+from oracle.pyoracle import OracleChain
+
+pytestmark = pytest.mark.gpu
+
+TRACE_STEPS = 128
+GRAPH_STEPS = 2048       # 32 launches of 64 steps: one replay of the captured graph
+N_SAMPLE = 16
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module")
+def c2():
+    """The workload, the oracle's trace of every chain's first 128 steps and
+    its coordinates there, and for the sampled chains the per-step FP32
+    tolerance scale, the coordinates after 128 + 2048 steps and the accepted
+    count."""
+    boxes, seeds = W.batch_water_512(seed=2024)
+    n = [b.n_mol for b in boxes]
+    rank = np.argsort(n, kind="stable")
+    sample = sorted(set(int(rank[int(round(i * (len(n) - 1) / (N_SAMPLE - 1)))])
+                        for i in range(N_SAMPLE)))
+    assert min(n[c] for c in sample) == min(n) and max(n[c] for c in sample) == max(n)
+    traces, coords128, acc128 = [], [], []
+    scale, coords_end, acc_end = {}, {}, {}
+    for c, b in enumerate(boxes):
+        oc = OracleChain(b, ROT_AXIS)
+        e0 = oc.system_energy()
+        e, acc, tr = oc.run(int(seeds[c]), c, TRACE_STEPS, e0)
+        traces.append(tr)
+        coords128.append(oc.coords())
+        acc128.append(acc)
+        if c in sample:
+            _, acc2, _ = oc.run(int(seeds[c]), c, GRAPH_STEPS, e, step0=TRACE_STEPS)
+            coords_end[c] = oc.coords()
+            acc_end[c] = acc + acc2
+            # sum k|terms| of the old placement at every traced step
+            o2 = OracleChain(b, ROT_AXIS)
+            sc = []
+            for s in range(TRACE_STEPS):
+                mv = o2.draw(int(seeds[c]), c, s)
+                sc.append(o2.ob.mol_energy_abs(mv.mol, 0))
+                o2.run(int(seeds[c]), c, 1, 0.0, step0=s)
+            scale[c] = sc
+    return dict(boxes=boxes, seeds=seeds, sample=sample, traces=traces, coords128=coords128,
+                acc128=acc128, scale=scale, coords_end=coords_end, acc_end=acc_end)
+
+
+def check_batch(ctx, c2, tile=None, autotune=False):
+    boxes, seeds = c2["boxes"], c2["seeds"]
+    bt = ChainBatch(ctx, boxes, seeds, rotation=ROT_AXIS)
+    if autotune:
+        tile = bt.autotune(128)
+    else:
+        bt.set_tile(*tile)
+    assert bt.tile == tuple(tile)
+    tr = bt.run_traced(TRACE_STEPS)
+    st = bt.stats()
+    worst, retakes = 0.0, 0
+    for c in range(len(boxes)):
+        assert st[c].error == 0 and st[c].steps == TRACE_STEPS
+        for s, (t, r) in enumerate(zip(tr[c], c2["traces"][c])):
+            assert t.mol == r.mol and t.u == r.u, (tile, c, s)
+            assert bool(t.accepted) == bool(r.accepted), (tile, c, s, t.de, r.de, r.u)
+            retakes += t.fp64
+            if t.fp64:
+                tl = 1e-9 * max(1.0, abs(r.e_old) + abs(r.e_new))
+                assert abs(t.e_old - r.e_old) <= tl and abs(t.e_new - r.e_new) <= tl, (c, s)
+            elif c in c2["scale"]:
+                ao = c2["scale"][c][s]
+                assert abs(t.e_old - r.e_old) <= tol_mixed(r.e_old, ao), (tile, c, s)
+                tol = tol_mixed(r.de, 2 * ao)
+                assert abs(t.de - r.de) <= tol, (tile, c, s, t.de, r.de)
+                worst = max(worst, abs(t.de - r.de) / tol)
+        assert st[c].accepted == c2["acc128"][c], (tile, c)
+    allc = bt.download_all()
+    for c, (x, y, z) in enumerate(allc):
+        assert np.array_equal(np.stack([x, y, z], 1), c2["coords128"][c]), (tile, c)
+    # the benchmarked path: graph replay of 32 launches
+    bt.run(GRAPH_STEPS)
+    st = bt.stats()
+    for c in c2["sample"]:
+        x, y, z = bt.download(c)
+        assert np.array_equal(np.stack([x, y, z], 1), c2["coords_end"][c]), (tile, c)
+        assert st[c].accepted == c2["acc_end"][c], (tile, c)
+        assert st[c].steps == TRACE_STEPS + GRAPH_STEPS
+    bt.close()
+    print(f"tile {tuple(tile)}: 512 chains x {TRACE_STEPS} steps equal to the oracle, "
+          f"{len(c2['sample'])} chains x {GRAPH_STEPS} graph steps bit-identical; "
+          f"worst dE error {worst:.3f} of the tolerance, FP64 re-takes {retakes}")
+    return tile
+
+
+TILES = [(96, 1, 64, 0), (96, 1, 64, 1), (160, 1, 64, 0), (160, 1, 64, 1), (160, 1, 64, 2),
+         (192, 1, 64, 0), (192, 1, 64, 1), (224, 1, 64, 0), (224, 1, 64, 1),
+         (256, 1, 64, 0), (256, 1, 64, 1), (256, 2, 64, 0), (512, 1, 64, 0)]
+
+
+@pytest.mark.parametrize("tile", TILES, ids=lambda t: "x".join(map(str, t)))
+def test_batch_512_tile_replay(ctx, c2, tile):
+    check_batch(ctx, c2, tile)
+
+
+def test_batch_512_autotuned_replay(ctx, c2):
+    tile = check_batch(ctx, c2, autotune=True)
+    print("autotuned tile", tile)
+
+
+@pytest.fixture(scope="module")
+def c1():
+    box = W.bicyclic_4000()
+    oc = OracleChain(box, ROT_AXIS)
+    e0 = oc.system_energy()
+    e, acc, tr = oc.run(11, 0, 200, e0)
+    return box, tr, oc.coords(), acc, e
+
+
+@pytest.mark.parametrize("skin", [0.0, 1.5])
+def test_bicyclic_4000_chain_replay(ctx, c1, skin):
+    """4000 x 16-atom molecules, one chain (the 16-warp chain kernel), with
+    and without Verlet lists: 200 steps equal to the oracle."""
+    box, otr, coords, acc, e = c1
+    g = GpuBox(ctx, box, PREC_MIXED)
+    if skin:
+        g.set_verlet(skin)
+    st, tr = g.chain_run(seed=11, n_steps=200, rotation=ROT_AXIS, trace=True)
+    assert st.error == 0 and st.steps == 200
+    for s, (t, r) in enumerate(zip(tr, otr)):
+        assert t.mol == r.mol and t.u == r.u, s
+        assert bool(t.accepted) == bool(r.accepted), (s, t.de, r.de)
+        if t.fp64:
+            tl = 1e-9 * max(1.0, abs(r.e_old) + abs(r.e_new))
+            assert abs(t.de - r.de) <= tl, s
+    x, y, z = g.download()
+    assert np.array_equal(np.stack([x, y, z], 1), coords)
+    assert st.accepted == acc
+    if skin:
+        assert st.nl_builds >= 1
+    g.close()
+    print(f"bicyclic4000 skin {skin}: accepted {acc}/200, FP64 re-takes {st.ties}")
+
+
+def test_water_32768_npt_verlet_replay(ctx):
+    """The 32,768-water system from its relaxed start (512 relaxed waters
+    replicated 4 x 4 x 4), NPT with Verlet lists as measured (one 16-warp
+    group, mixed volume energies), a volume move every 100 steps: 200 steps
+    and 2 volume moves equal to the oracle's (draws, decisions, box edges,
+    coordinates bit for bit)."""
+    from mcgpu_gb300.prepare import relaxed_water_32768
+    box = relaxed_water_32768(ctx)
+    interval, steps, dl, seed = 100, 200, 0.005, 0x5EED
+    bt = ChainBatch(ctx, [box], [seed], rotation=ROT_AXIS)
+    bt.set_tile(512, 1, 64)
+    bt.set_verlet(1.5)
+    bt.set_npt(interval, 1.0, dl, PREC_MIXED)
+    tr, vtr = bt.run_traced(steps, volume=True)
+    st = bt.stats()[0]
+    oc = OracleChain(box, ROT_AXIS)
+    e = oc.system_energy()
+    assert e < 0, e                                  # a liquid, not an overlapping start
+    done, vols, otr = 0, [], []
+    while done < steps:
+        e, _, t = oc.run(seed, 0, interval, e, step0=done)
+        otr += t
+        done += interval
+        vols.append(oc.volume_move(seed, 0, done, 1.0, dl, e))
+        e = vols[-1]["energy"]
+    for s, (t, r) in enumerate(zip(tr[0], otr)):
+        assert t.mol == r.mol and t.u == r.u, s
+        assert bool(t.accepted) == bool(r.accepted), (s, t.de, r.de)
+    assert len(vtr[0]) == len(vols) == steps // interval
+    for t, r in zip(vtr[0], vols):
+        assert t.dlnv == r["dlnv"] and t.u == r["u"]
+        assert bool(t.accepted) == (r["status"] == 1)
+        assert t.edge == r["edge"]
+    assert tuple(st.box) == tuple(oc.ob.s.size)
+    x, y, z = bt.download(0)
+    assert np.array_equal(np.stack([x, y, z], 1), oc.coords())
+    assert st.error == 0
+    bt.close()
+    print(f"water32768 NPT: energy/N {e / box.n_mol:.3f} kcal/mol, accepted "
+          f"{st.accepted}/{steps}, volume moves {st.vol_accepted}/{st.vol_tried}, "
+          f"Verlet builds {st.nl_builds}")

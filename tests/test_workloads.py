@@ -81,3 +81,20 @@ def test_oracle_centre_builder_places_the_same_points():
     b, _ = W.water_chains(6, seed=11, centres=build_centres)
     for x, y in zip(a, b):
         assert np.array_equal(x.x, y.x) and np.array_equal(x.z, y.z)
+
+
+def test_tile_box_images_fit():
+    """A periodic box replicated k x k x k: with the cutoff below half the
+    small edge every molecule sees the same neighbours, so the system
+    energy is k^3 times the small box's (oracle, FP64; the cutoff plus two
+    molecule radii stays below half the small edge, so no atom pair of the
+    small box takes a wrong single image)."""
+    from mcgpu_gb300.prepare import tile_box
+    from oracle.pyoracle import OracleBox
+    small = W.water_box(40, L=13.0, cutoff=4.0, seed=9)
+    big = tile_box(small, 2)
+    assert big.n_mol == 320 and np.allclose(big.size, 26.0)
+    assert np.array_equal(big.pidx[:40], small.pidx) and big.pidx[40] == small.n_atom
+    e_small = OracleBox(small).system_energy()
+    e_big = OracleBox(big).system_energy()
+    assert abs(e_big - 8 * e_small) <= 1e-9 * abs(8 * e_small)

@@ -1,5 +1,7 @@
 """mcgpu_system_energy_static, the system energy that allocates nothing,
-against mcgpu_system_energy (FP64 pairs) through the C ABI.
+through the C ABI, against the oracle: the golden system energies that the
+compiled reference produced, and the oracle's restatement of
+SimulationStep::calcSystemEnergy on the same rows (OracleBox).
 
 The caller owns every device buffer (here torch tensors stand in for an
 offload program's own device rows); the entry point gets device pointers and
@@ -12,8 +14,9 @@ import numpy as np
 import pytest
 
 from helpers import load_golden, tol64
-from mcgpu_gb300 import PREC_FP64, Context, GpuBox, _abi
+from mcgpu_gb300 import Context, _abi
 from mcgpu_gb300.workloads import water_box
+from oracle.pyoracle import OracleBox
 
 pytestmark = pytest.mark.gpu
 
@@ -62,18 +65,30 @@ class DeviceRows:
         return float(self.out.item())
 
 
-def reference_energy(ctx, box) -> float:
-    g = GpuBox(ctx, box, PREC_FP64)
-    e = g.system_energy()
-    g.close()
-    return e
+def reference_energy(box) -> float:
+    """The oracle's FP64 restatement of calcSystemEnergy on the same rows."""
+    return OracleBox(box).system_energy()
+
+
+GOLDEN = ["water256", "t3p64", "bicyclic100", "mixed", "water48_halfbox"]
+
+
+def test_static_energy_matches_golden_and_oracle(ctx):
+    """Every golden box: the compiled reference's system energy (fixture)
+    and the oracle's, to summation order."""
+    for name in GOLDEN:
+        box, z = load_golden(name)
+        gold = float(z["sys_energy"][0])
+        assert reference_energy(box) == gold, name      # the oracle is pinned to the fixture
+        e = DeviceRows(box).energy()
+        assert abs(e - gold) <= tol64(gold), (name, e, gold)
 
 
 def test_static_energy_two_calls_in_a_row(ctx):
     """Two boxes of different sizes back to back, then the first again: the
     scratch left by one call does not leak into the next."""
     boxes = [load_golden("water256")[0], load_golden("t3p64")[0], load_golden("bicyclic100")[0]]
-    refs = [reference_energy(ctx, b) for b in boxes]
+    refs = [reference_energy(b) for b in boxes]
     rows = [DeviceRows(b) for b in boxes]
     for i in (0, 1, 0, 2, 1):
         e = rows[i].energy()
@@ -82,15 +97,50 @@ def test_static_energy_two_calls_in_a_row(ctx):
     assert e1 == e2
 
 
+def test_static_energy_zero_primary_molecule(ctx):
+    """A molecule without primary indexes is never in range
+    (moleculesInRange, SimulationStep.cpp:317-330) and contributes nothing,
+    as in the oracle."""
+    box, _ = load_golden("water256")
+    box = box.copy()
+    box.mol_pidx_count[17] = 0
+    box.mol_pidx_count[200] = 0
+    ref = reference_energy(box)
+    assert ref != reference_energy(load_golden("water256")[0])
+    e = DeviceRows(box).energy()
+    assert abs(e - ref) <= tol64(ref), (e, ref)
+
+
+def test_static_energy_out_of_range_rows_give_nan(ctx):
+    """Rows that index past the arrays are caught by the kernel's own range
+    checks (the bad index is never dereferenced): the result is NaN, and the
+    next valid call is exact again."""
+    box, z = load_golden("t3p64")
+    gold = float(z["sys_energy"][0])
+    bad_start = box.copy()
+    bad_start.mol_start[5] = box.n_atom            # molecule 5 starts past the atoms
+    bad_pidx = box.copy()
+    bad_pidx.pidx[3] = box.n_atom + 7              # a primary index past the atoms
+    bad_count = box.copy()
+    bad_count.mol_pidx_count[box.n_mol - 1] = 2    # runs past the primary table
+    for b in (bad_start, bad_pidx, bad_count):
+        assert np.isnan(DeviceRows(b).energy())
+    e = DeviceRows(box).energy()
+    assert abs(e - gold) <= tol64(gold)
+
+
 def test_static_energy_allocates_nothing_after_setup(ctx):
     import torch
     box = water_box(1000, seed=5)
-    ref = reference_energy(ctx, box)
+    ref = reference_energy(box)
     rows = DeviceRows(box)
     assert abs(rows.energy() - ref) <= tol64(ref)      # first call: address lookup
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
     free0 = torch.cuda.mem_get_info(0)[0]
-    for _ in range(2):
+    for _ in range(3):
         assert abs(rows.energy() - ref) <= tol64(ref)
+    torch.cuda.synchronize()
     assert torch.cuda.mem_get_info(0)[0] == free0
 
 
