@@ -482,6 +482,7 @@ def main():
     # chain's run (relaxed from its random start), not its first.
     pre_steps = max(0, CHAIN_STEPS - (args.warmup + args.steps) * STEPS_PER_BENCH)
     pre_steps -= pre_steps % STEPS_PER_BENCH
+    bt.set_tile(160, 1, STEPS_PER_BENCH, 0)
     bt.run(pre_steps, sync=True)
     if args.tile:
         bt.set_tile(*[int(v) for v in args.tile.split(",")])

@@ -164,6 +164,33 @@ __device__ __forceinline__ int screen_chain(const Pool& P, const ChainHdr& H, co
   return f;
 }
 
+// The single-lane pair batch for the chain's molecule length (inner atom
+// loop unrolled for 3-site molecules).
+__device__ __forceinline__ void batch_u1_any(const Pool& P, const ChainHdr& H, const GroupSmem& s,
+                                             const MovedInfo& mi, const int* rj, int head,
+                                             int count, int w, int lane, AccFF& acc,
+                                             unsigned ljmask) {
+  if (H.ulen == 3)
+    batch_u1<3>(P, H, s, mi, rj, head, count, w, lane, acc, ljmask);
+  else
+    batch_u1<0>(P, H, s, mi, rj, head, count, w, lane, acc, ljmask);
+}
+
+// Bits 4k + i: the LJ term between atoms i and k of a uniform chain's
+// molecules (at most 4 atoms) is not exactly zero (sigma and epsilon
+// products both nonzero in FP32).  The same for every lane.
+__device__ __forceinline__ unsigned uniform_lj_mask(const Pool& P, const ChainHdr& H,
+                                                    const float2* teq) {
+  unsigned m = 0;
+  if (!H.uniform || H.ulen > 4) return ~0u;
+  for (int k = 0; k < H.ulen; k++)
+    for (int i = 0; i < H.ulen; i++) {
+      const float sk = P.aoff[H.atom0 + k].w, si = P.aoff[H.atom0 + i].w;
+      if (si * sk != 0.f && teq[i].x * teq[k].x != 0.f) m |= 1u << (4 * k + i);
+    }
+  return m;
+}
+
 // One warp screens chain candidates [c_begin, c_end) -- or, with a Verlet
 // list, the molecules cand[c_begin .. c_end) -- in warp-strided rounds of 32
 // (screen positions from the shared-memory cache when given) and evaluates
@@ -171,7 +198,7 @@ __device__ __forceinline__ int screen_chain(const Pool& P, const ChainHdr& H, co
 __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const GroupSmem& s,
                                 const MovedInfo& mi, const float4* pcache, int c_begin, int c_end,
                                 int w, int nw, int lane, int T, AccFF& acc,
-                                const int* cand = nullptr) {
+                                const int* cand = nullptr, unsigned ljmask = ~0u) {
   int* rj = s.lj + w * kRing;
   int head = 0, tail = 0;
   const unsigned lt = lanemask_lt();
@@ -208,7 +235,7 @@ __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const G
     if (tail - head >= 32) {
       __syncwarp();
       if (u1)
-        batch_u1(P, H, s, mi, rj, head, 32, w, lane, acc);
+        batch_u1_any(P, H, s, mi, rj, head, 32, w, lane, acc, ljmask);
       else if (H.precise)
         batch_ff<true, false>(P, H, s, mi, rj, head, 32, lane, T, acc);
       else
@@ -220,7 +247,7 @@ __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const G
   __syncwarp();
   if (tail > head) {
     if (u1)
-      batch_u1(P, H, s, mi, rj, head, tail - head, w, lane, acc);
+      batch_u1_any(P, H, s, mi, rj, head, tail - head, w, lane, acc, ljmask);
     else if (H.precise)
       batch_ff<true, false>(P, H, s, mi, rj, head, tail - head, lane, T, acc);
     else

@@ -269,13 +269,19 @@ __device__ __forceinline__ float3 pair_disp(float3 bh, float3 bl, float4 a, floa
 // Sum over the moved molecule's atoms a of the FP32 pair terms with one
 // neighbour atom b, per-pair periodic image (entries whose atom pairs may
 // straddle half a box edge).  abs accumulates |LJ| + |Coulomb|.
-template <bool PRECISE>
+//
+// NLEN > 0 fixes the moved molecule's length at compile time (the loop
+// unrolls and its independent pair terms interleave); bit i of ljmask clear
+// means the LJ term of moved atom i is exactly zero (a sigma or epsilon
+// product of zero) and is not evaluated.  Neither changes a bit of the sum.
+template <bool PRECISE, int NLEN = 0>
 __device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4* lo,
                                                   const float4* eq, int len, float3 bh, float3 bl,
                                                   float sb, float2 qb, const ChainHdr& H,
-                                                  float& abs) {
+                                                  float& abs, unsigned ljmask = ~0u) {
   float acc = 0.f;
-  for (int i = 0; i < len; i++) {
+#pragma unroll
+  for (int i = 0; i < (NLEN > 0 ? NLEN : len); i++) {
     const float4 ea = eq[i];
     const float4 a = o[i];
     const float3 d = pair_disp<PRECISE>(bh, bl, a, PRECISE ? lo[i] : a);
@@ -284,7 +290,7 @@ __device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4*
     const float dz = wrapf(d.z, H.Lf[2]);
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float ir = rsqrt_nr(r2);
-    const float lj = lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x);
+    const float lj = ((ljmask >> i) & 1u) ? lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x) : 0.f;
     const float cl = (ea.y * qb.y) * ir;
     const bool ok = r2 > 0.f;
     acc += ok ? lj + cl : 0.f;
@@ -301,23 +307,24 @@ __device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4*
 // proportionally less FP32 rounding.  A coincident pair (r = 0) is skipped
 // as the reference skips it (BruteForceStep.cpp:68-69).  use_new selects the
 // |o_a|^2 of the placement (eq.z old, eq.w new).
-template <bool PRECISE>
+template <bool PRECISE, int NLEN = 0>
 __device__ __forceinline__ float sum_moved32_cf(const float4* o, const float4* lo,
                                                 const float4* eq, int len, bool use_new,
                                                 float3 bh, float3 bl, float sb, float2 qb,
-                                                float qm, float& abs) {
+                                                float qm, float& abs, unsigned ljmask = ~0u) {
   const float R2 = fmaf(bh.x, bh.x, fmaf(bh.y, bh.y, bh.z * bh.z));
   const float iR = rsqrt_nr(R2);
   const float R = R2 * iR;
   const float tx = bh.x + bh.x, ty = bh.y + bh.y, tz = bh.z + bh.z;
   float lj_acc = 0.f, phi = 0.f, lj_abs = 0.f, c_abs = 0.f;
-  for (int i = 0; i < len; i++) {
+#pragma unroll
+  for (int i = 0; i < (NLEN > 0 ? NLEN : len); i++) {
     const float4 a = o[i];
     const float4 ea = eq[i];
     const float3 d = pair_disp<PRECISE>(bh, bl, a, PRECISE ? lo[i] : a);
     const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
     const float ir = rsqrt_nr(r2);
-    const float lj = lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x);
+    const float lj = ((ljmask >> i) & 1u) ? lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x) : 0.f;
     const float num = fmaf(tx, a.x, fmaf(ty, a.y, fmaf(tz, a.z, -(use_new ? ea.w : ea.z))));
     const float w = ir * rcp_approx(fmaf(r2, ir, R));
     const bool ok = r2 > 0.f;
@@ -445,58 +452,53 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // neighbour index, so each lane requests all of them at once with async
 // copies into its own shared-memory slot (one round trip to L2 instead of
 // one per atom, no registers held), and the pair factors come from the
-// chain's per-slot template.  The atoms are summed in batch_ff's order: the
-// sums are batch_ff's bit for bit.
+// chain's per-slot template.  Each placement's sum is batch_ff's bit for bit.
+//
+// ULEN > 0: molecules of ULEN atoms (the inner atom loop unrolls); ljmask
+// bits 4k..4k+3: the LJ terms of neighbour atom k with moved atoms 0..3 that
+// are not exactly zero (the same in every lane: the chain is uniform).  Both
+// placements run through one copy of the pair code (a rolled loop), which
+// keeps the step loop's code small enough for the instruction cache.
+template <int ULEN>
 __device__ __forceinline__ void batch_u1(const Pool& P, const ChainHdr& H, const GroupSmem& s,
                                          const MovedInfo& mi, const int* rj, int head, int count,
-                                         int w, int lane, AccFF& acc) {
+                                         int w, int lane, AccFF& acc, unsigned ljmask) {
   if (lane >= count) return;  // lanes are independent: no shuffles below
   const int jf = rj[(head + lane) & (kRing - 1)];
   const int j = jf >> 4;
-  int f = jf & 15;
-  const int b0 = H.atom0 + (j - H.mol0) * H.ulen;
-  const int lenj = H.ulen;
+  const int f = jf & 15;
+  const int lenj = ULEN > 0 ? ULEN : H.ulen;
+  const int b0 = H.atom0 + (j - H.mol0) * lenj;
   float4* nb = s.nbuf + (w * 32 + lane) * 5;
   cp_async16(nb + 4, P.mfix + j);
   for (int k = 0; k < lenj; k++) cp_async16(nb + k, P.aoff + b0 + k);
   cp_async_wait_all();
   const uint4 fj = *reinterpret_cast<const uint4*>(nb + 4);
   const float rr = mi.rad + H.umrad;
-  float3 Do = make_float3(0.f, 0.f, 0.f), Dn = Do;
-  const float3 z3 = Do;
-  if (f & kInOld) {
-    Do = fixdiff(fj, mi.fx_old, H);
-    if (needs_wrap(Do, rr, H)) f |= kWrapOld;
-  }
-  if (f & kInNew) {
-    Dn = fixdiff(fj, mi.fx_new, H);
-    if (needs_wrap(Dn, rr, H)) f |= kWrapNew;
-  }
-  float so = 0.f, sn = 0.f, sa = 0.f;
-  for (int k = 0; k < lenj; k++) {
-    const float4 ob = nb[k];
-    const float2 qb = s.teq[k];
-    if (f & kInOld) {
-      const float3 bh = make_float3(Do.x + ob.x, Do.y + ob.y, Do.z + ob.z);
-      so += (f & kWrapOld)
-                ? sum_moved32_wrap<false>(s.o_old, s.l_old, s.eq, mi.len, bh, z3, ob.w, qb, H, sa)
-                : sum_moved32_cf<false>(s.o_old, s.l_old, s.eq, mi.len, false, bh, z3, ob.w, qb,
-                                        mi.qm, sa);
+  const float3 z3 = make_float3(0.f, 0.f, 0.f);
+  float sa = 0.f;
+#pragma unroll 1
+  for (int p = 0; p < 2; p++) {
+    if (!(f & (p ? kInNew : kInOld))) continue;
+    const float3 D = fixdiff(fj, p ? mi.fx_new : mi.fx_old, H);
+    const bool wrap = needs_wrap(D, rr, H);
+    const float4* o = p ? s.o_new : s.o_old;
+    float sp = 0.f;
+#pragma unroll 1
+    for (int k = 0; k < lenj; k++) {
+      const float4 ob = nb[k];
+      const float2 qb = s.teq[k];
+      const unsigned lm = (ljmask >> (4 * k)) & 15u;
+      const float3 bh = make_float3(D.x + ob.x, D.y + ob.y, D.z + ob.z);
+      sp += wrap ? sum_moved32_wrap<false, ULEN>(o, s.l_old, s.eq, mi.len, bh, z3, ob.w, qb, H,
+                                                 sa, lm)
+                 : sum_moved32_cf<false, ULEN>(o, s.l_old, s.eq, mi.len, p != 0, bh, z3, ob.w, qb,
+                                               mi.qm, sa, lm);
     }
-    if (f & kInNew) {
-      const float3 bh = make_float3(Dn.x + ob.x, Dn.y + ob.y, Dn.z + ob.z);
-      sn += (f & kWrapNew)
-                ? sum_moved32_wrap<false>(s.o_new, s.l_new, s.eq, mi.len, bh, z3, ob.w, qb, H, sa)
-                : sum_moved32_cf<false>(s.o_new, s.l_new, s.eq, mi.len, true, bh, z3, ob.w, qb,
-                                        mi.qm, sa);
-    }
-  }
-  if (f & kInOld) {
-    ff_add(acc.oh, acc.ol, so);
-    acc.np += (long long)mi.act * H.uact;
-  }
-  if (f & kInNew) {
-    ff_add(acc.nh, acc.nl, sn);
+    if (p)
+      ff_add(acc.nh, acc.nl, sp);
+    else
+      ff_add(acc.oh, acc.ol, sp);
     acc.np += (long long)mi.act * H.uact;
   }
   acc.ab += sa;
