@@ -120,8 +120,8 @@ __device__ inline void stage_chain(const Pool& P, const ChainHdr& H, const MoveF
     s.misc[kMiscQn + 2] = __float_as_int(qn.y); s.misc[kMiscQn + 3] = __float_as_int(qn.z);
     s.misc[kMiscU] = __float_as_int(mv.u);
     s.misc[kMiscNlTrial] = near ? 1 : 0;
-    s.miscd[0] = (double)(H.uniform ? H.umrad : P.mrad[m]);
-    s.miscd[1] = (double)qsum;
+    s.misc[kMiscRad] = __float_as_int(H.uniform ? H.umrad : P.mrad[m]);
+    s.misc[kMiscQm] = __float_as_int(qsum);
   }
 }
 

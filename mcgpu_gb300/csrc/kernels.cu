@@ -332,7 +332,10 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
     g.sync();
     const unsigned ljmask = uniform_lj_mask(P, H, s.teq);
     int full_scans = 0;
-    double energy = H.energy, err = 0.0;
+    // the accepted dE of this task and their FP32 error bounds, each summed
+    // in double-float (FP64 costs 64 FP32 issue slots on GB300); both join
+    // the FP64 header values once, at the task's end
+    float de_h = 0.f, de_l = 0.f, err_h = 0.f, err_l = 0.f;
     long long acc_n = 0, npairs = 0;
     int ties = 0;
     const unsigned long long step0 = H.step;
@@ -417,20 +420,28 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
       __syncwarp();
       if (ok && !trial_near) nl_ok = false;
       if (w == 0 && lane == 0) {
-        if (!tie) {
-          e_old = (double)acc.oh + (double)acc.ol;
-          e_new = (double)acc.nh + (double)acc.nl;
-        }
-        const double de = e_new - e_old;
         if (ok) {
-          energy += de;
-          err += tie ? 1e-12 * (double)acc.ab : (double)bound;
+          if (tie) {
+            const double d64 = e_new - e_old;
+            const float dh = (float)d64;
+            ff_add2(de_h, de_l, dh, (float)(d64 - (double)dh));
+            ff_add(err_h, err_l, 1e-12f * acc.ab);
+          } else {
+            ff_add2(de_h, de_l, acc.nh, acc.nl);
+            ff_add2(de_h, de_l, -acc.oh, -acc.ol);
+            ff_add(err_h, err_l, bound);
+          }
           acc_n++;
         }
         if (H.nl_on && !use_list) full_scans++;
         npairs += acc.np;
         ties += tie;
         if (trace) {
+          if (!tie) {
+            e_old = (double)acc.oh + (double)acc.ol;
+            e_new = (double)acc.nh + (double)acc.nl;
+          }
+          const double de = e_new - e_old;
           mcgpu_trace t;
           t.mol = mi.mol - H.mol0;
           t.accepted = ok;
@@ -453,8 +464,8 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
       }
     }
     if (g.tid == 0) {
-      Hp->energy = energy;
-      Hp->run_err += err;
+      Hp->energy = H.energy + ((double)de_h + (double)de_l);
+      Hp->run_err += (double)err_h + (double)err_l;
       Hp->step = step0 + my_steps;
       Hp->accepted += acc_n;
       Hp->pairs += npairs;

@@ -84,6 +84,10 @@ __device__ __forceinline__ float r2_screen(float4 a, float4 b, const ChainHdr& H
 
 // ---- staging ------------------------------------------------------------
 
+// misc[] slots of the staged molecule's FP32 radius and net charge factor
+// (float bits: no FP64 on the step's path).
+enum : int { kMiscRad = 21, kMiscQm = 22 };
+
 // Lanes of ONE warp stage molecule m: its current placement ("old") and, if
 // p is non-null, the proposed placement ("new") computed as
 // SimCalcs::intermolecularMove does (SimulationStep.cpp:544-565): every
@@ -120,8 +124,8 @@ __device__ inline void stage(const Pool& P, const ChainHdr& H, int m, const Prop
     s.misc[0] = m; s.misc[1] = a0; s.misc[2] = len; s.misc[3] = pi.y;
     s.misc[4] = lw >> 8; s.misc[5] = p ? 3 : 1; s.misc[6] = p ? p->vertex : -1;
     s.misc[8] = (int)fo.x; s.misc[9] = (int)fo.y; s.misc[10] = (int)fo.z;
-    s.miscd[0] = (double)P.mrad[m];
-    s.miscd[1] = (double)qsum;
+    s.misc[kMiscRad] = __float_as_int(P.mrad[m]);
+    s.misc[kMiscQm] = __float_as_int(qsum);
   }
   if (!p) return;
   Rot R;
@@ -189,8 +193,8 @@ __device__ __forceinline__ MovedInfo load_moved(const GroupSmem& s) {
   mi.act = s.misc[4]; mi.states = s.misc[5]; mi.vertex = s.misc[6]; mi.pad = 0;
   mi.fx_old = make_uint4((unsigned)s.misc[8], (unsigned)s.misc[9], (unsigned)s.misc[10], 0u);
   mi.fx_new = make_uint4((unsigned)s.misc[12], (unsigned)s.misc[13], (unsigned)s.misc[14], 0u);
-  mi.rad = (float)s.miscd[0];
-  mi.qm = (float)s.miscd[1];
+  mi.rad = __int_as_float(s.misc[kMiscRad]);
+  mi.qm = __int_as_float(s.misc[kMiscQm]);
   return mi;
 }
 
