@@ -70,6 +70,12 @@ L2_PEAK_GBS = 36300.0
 ATOMS_PER_WATER = 3
 
 
+def fp32_peak_tflops(sm_count: int = 152, mhz: float = 2070.0) -> float:
+    """Nominal FP32 CUDA-core peak: SMs x 128 lanes x 2 flop x clock
+    (MEASURED_PEAKS.json holds no FP32 figure)."""
+    return sm_count * 128 * 2 * mhz * 1e6 / 1e12
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -319,45 +325,83 @@ def bench_single(ctx, plain_steps: int = 150, chain_steps: int = 4000) -> dict:
     return out
 
 
-def bench_large(ctx, steps: int = 6000) -> dict:
+def bench_large(ctx, steps: int = 200000, interval: int = 500, max_dlnv: float = 0.0015,
+                recompute_every: int = 1000) -> dict:
     """32768 waters (98,304 atoms), L = 99.3 A, rc 12 A, NPT 298 K and
     1 atm, Verlet list (skin 1.5 A) rebuilt on the skin/2 trigger, a volume
-    move every 500 steps (FP32 pair energies, FP64 re-take near the
-    threshold), then a full FP64 recompute for the drift of the running
-    energy.  Beside it the plain FP64 drop-in for a few steps."""
+    move every `interval` steps, `steps` steps from a liquid start (512
+    relaxed waters replicated 4 x 4 x 4): the precision sweep.  Two arms
+    from the same start with the same Philox streams: FP32 pair terms
+    (volume energies FP32 with the threshold re-takes) and FP64 pair terms
+    (every step and volume move).  Their decisions are the FP64 ones in
+    both, so they follow one trajectory and differ only in the rounding of
+    the running energy.  Every `recompute_every` steps a full FP64 system
+    energy gives the drift of the running energy, U/N and the density;
+    block averages (10 blocks) give <U>/N and <rho> with their standard
+    errors.  Beside it the plain FP64 drop-in for a few steps."""
+    import numpy as np
     import torch
     import mcgpu_gb300 as M
     from mcgpu_gb300.prepare import relaxed_water_32768
     t0 = time.perf_counter()
     box = relaxed_water_32768(ctx)
     t_relax = time.perf_counter() - t0
-    out = {"workload": "32768 waters, L=99.3 A, rc 12 A, NPT 298 K / 1 atm, Verlet skin 1.5 A, "
-                       "volume move every 500 steps",
+    n = box.n_mol
+    out = {"workload": f"32768 waters, L=99.3 A, rc 12 A, NPT 298 K / 1 atm, Verlet skin 1.5 A, "
+                       f"volume move every {interval} steps (ln V step +-{max_dlnv}), {steps} steps",
            "start": "512 waters relaxed by the chain kernel (400 sweeps, NVT 298 K, rc 9 A) at "
                     "the same density, replicated 4 x 4 x 4",
-           "relax_s": t_relax}
-    bt = M.ChainBatch(ctx, [box], [0x5EED], rotation=M.ROT_AXIS)
-    bt.set_tile(512, 1, 64)          # one chain: one group of 16 warps
-    bt.set_verlet(1.5)
-    bt.set_npt(500, 1.0, 0.005, M.PREC_MIXED)
-    bt.run(500)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    bt.run(steps)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    st = bt.stats()[0]
-    full = float(bt.system_energies()[0])
-    out.update({"chain_verlet_npt": steps / dt, "unit": "moves/s",
-                "energy_running": st.energy, "energy_fp64_recompute": full,
-                "drift_rel": abs(st.energy - full) / abs(full),
-                "volume_moves": st.vol_tried, "volume_accepted": st.vol_accepted,
-                "edge_A": st.box[0], "density_mol_per_A3": box.n_mol / st.box[0] ** 3,
-                "nl_builds": st.nl_builds, "nl_full_scan_steps": st.nl_full_scans,
-                "acceptance": st.accepted / (steps + 500),
-                "energy_per_molecule": st.energy / box.n_mol,
-                "fp64_retakes": st.ties, "steps": steps + 500})
-    bt.close()
+           "relax_s": t_relax, "unit": "moves/s"}
+
+    def block(x, nb=10):
+        x = np.asarray(x, np.float64)
+        b = x[: len(x) - len(x) % nb].reshape(nb, -1).mean(axis=1)
+        return float(b.mean()), float(b.std(ddof=1) / math.sqrt(nb))
+
+    coords = {}
+    for name, prec in (("fp32_pairs", M.PREC_MIXED), ("fp64_pairs", M.PREC_FP64)):
+        bt = M.ChainBatch(ctx, [box], [0x5EED], rotation=M.ROT_AXIS)
+        bt.set_tile(512, 1, 64)          # one chain: one group of 16 warps
+        bt.set_verlet(1.5)
+        bt.set_npt(interval, 1.0, max_dlnv, prec)
+        bt.set_precision(prec)
+        run_s, drift, u, rho = 0.0, [], [], []
+        for _ in range(steps // recompute_every):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            bt.run(recompute_every)
+            torch.cuda.synchronize()
+            run_s += time.perf_counter() - t1
+            st = bt.stats()[0]
+            full = float(bt.system_energies()[0])
+            vol = st.box[0] * st.box[1] * st.box[2]
+            drift.append((st.energy - full) / abs(full))
+            u.append(full / n)
+            rho.append(n / vol)
+        st = bt.stats()[0]
+        coords[name] = bt.download_all()[0]
+        bt.close()
+        mu, su = block(u)
+        mr, sr = block(rho)
+        out[name] = {"moves_per_s": steps / run_s, "run_s": run_s,
+                     "drift_rel_final": drift[-1], "drift_rel_max": max(abs(d) for d in drift),
+                     "drift_series_every_steps": recompute_every,
+                     "drift_rel_series": [float(f"{d:.3e}") for d in drift[:: max(1, len(drift) // 20)]],
+                     "U_per_molecule": mu, "U_per_molecule_se": su,
+                     "density_mol_per_A3": mr, "density_se": sr,
+                     "acceptance": st.accepted / steps,
+                     "volume_moves": st.vol_tried, "volume_accepted": st.vol_accepted,
+                     "edge_A": st.box[0], "nl_builds": st.nl_builds,
+                     "nl_full_scan_steps": st.nl_full_scans, "fp64_steps": st.ties,
+                     "error": st.error}
+    a, b = out["fp32_pairs"], out["fp64_pairs"]
+    out["same_trajectory"] = all(np.array_equal(p, q) for p, q in
+                                 zip(coords["fp32_pairs"], coords["fp64_pairs"]))
+    out["U_z"] = abs(a["U_per_molecule"] - b["U_per_molecule"]) / max(
+        math.hypot(a["U_per_molecule_se"], b["U_per_molecule_se"]), 1e-300)
+    out["density_z"] = abs(a["density_mol_per_A3"] - b["density_mol_per_A3"]) / max(
+        math.hypot(a["density_se"], b["density_se"]), 1e-300)
+    out["chain_verlet_npt"] = a["moves_per_s"]
     g = M.GpuBox(ctx, box, M.PREC_FP64)
     step = M.GpuSimulationStep(g, M.LibcRand(3))
     M.run_plain(step, 5, fused=True)
@@ -370,9 +414,9 @@ def bench_large(ctx, steps: int = 6000) -> dict:
 
 # ---- served request loop ---------------------------------------------------------------
 
-def bench_served(ctx, rate: float = 200.0, window_s: float = 4.0, steps_per_job: int = 20000,
+def bench_served(ctx, rate: float = 200.0, window_s: float = 60.0, steps_per_job: int = 20000,
                  tile=(256, 1, 0),
-                 pool_each: int = 12, seed: int = 77) -> dict:
+                 pool_each: int = 32, seed: int = 77) -> dict:
     """Jobs arrive as a Poisson stream (rate jobs/s over window_s seconds),
     50/50 water and 16-atom bicyclic, N log-uniform in [128, 8192], NPT at
     1 atm with T uniform in [280, 360] K, a ln V move (+-0.01) every 100
@@ -428,14 +472,36 @@ def bench_served(ctx, rate: float = 200.0, window_s: float = 4.0, steps_per_job:
     moves = sum(r.result.steps for r in done.values())
     errors = sum(1 for r in done.values() if r.result.error)
     ties = sum(r.result.ties for r in done.values())
+    cnt = srv.counters()
     srv.close()
     pct = lambda q: lat[min(len(lat) - 1, int(q * len(lat)))]
+    makespan = t_last - t_first
+    capacity = moves / makespan                       # moves/s the server delivered
+    demand = rate * steps_per_job                     # moves/s the arrivals ask for
+    # achieved pair arithmetic over the GPU time of the rounds (chain kernel +
+    # volume phase; the volume phase's pair terms are not in the count, so
+    # this understates the work)
+    achieved = cnt["pairs"] * FP32_FLOPS_PER_PAIR / max(cnt["gpu_seconds"], 1e-12) / 1e12
+    peak = fp32_peak_tflops()
     return {"workload": f"Poisson {rate:.0f} jobs/s for {window_s:.0f} s ({len(jobs)} jobs), 50/50 "
                         "water / 16-atom bicyclic, N log-uniform [128, 8192], NPT 1 atm, "
                         f"T U[280,360] K, ln V move every 100 steps, {steps_per_job} steps/job",
-            "jobs": len(jobs), "moves_per_s": moves / (t_last - t_first), "unit": "moves/s",
+            "window_s": window_s, "arrival_rate_jobs_per_s": rate,
+            "jobs": len(jobs), "moves_per_s": capacity, "unit": "moves/s",
             "p50_s": pct(0.50), "p99_s": pct(0.99), "max_s": lat[-1],
-            "makespan_s": t_last - t_first, "errors": errors, "fp64_retakes": ties,
+            "makespan_s": makespan, "errors": errors, "fp64_retakes": ties,
+            "demand_moves_per_s": demand,
+            "capacity_jobs_per_s": capacity / steps_per_job,
+            "load": demand / capacity,
+            "load_note": ("demand above capacity: the queue grows through the window, so p50/p99 "
+                          "include the backlog" if demand > capacity else
+                          "demand within capacity: p50/p99 are steady-state times"),
+            "gpu_seconds": cnt["gpu_seconds"], "rounds": cnt["rounds"],
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak,
+                         "work": f"{FP32_FLOPS_PER_PAIR} flop x {cnt['pairs']} device-counted atom "
+                                 "pairs of the chain steps over the GPU time of the rounds "
+                                 "(volume-phase pairs not counted)"},
             "tile": {"threads": tile[0], "chains_per_cta": tile[1], "lanes_per_molecule": tile[2]},
             "note": f"boxes from a pool of {2 * pool_each} pre-built configurations; "
                     "volume-move energies FP32 pairs with FP64 re-take near the threshold"}
@@ -455,7 +521,8 @@ def main():
     ap.add_argument("--no-single", action="store_true", help="skip the 4000 x 16-atom chain")
     ap.add_argument("--no-large", action="store_true", help="skip the 32768-water system")
     ap.add_argument("--no-served", action="store_true", help="skip the served request loop")
-    ap.add_argument("--served-window", type=float, default=4.0)
+    ap.add_argument("--served-window", type=float, default=60.0,
+                    help="Poisson arrival window in seconds (60 in the served workload)")
     ap.add_argument("--served-steps", type=int, default=20000)
     ap.add_argument("--served-tile", default="256,1,0",
                     help="threads,chains_per_cta,lanes of the serving loop's chain kernel")

@@ -264,6 +264,16 @@ int mcgpu_batch_set_verlet(mcgpu_batch* batch, double skin);
  * pair energies; E_LRC at the current box is lrc_v / V. */
 int mcgpu_batch_set_lrc(mcgpu_batch* batch, const double* lrc_v);
 int mcgpu_box_set_verlet(mcgpu_box* box, double skin);
+/* Pair arithmetic of a batch's steps.  MCGPU_PREC_MIXED (the default): FP32
+ * pair terms, double-float sums, the FP64 pairs only for the decisions that
+ * fall within the FP32 rounding bound of the threshold.  MCGPU_PREC_FP64:
+ * every step with the reference's FP64 pair arithmetic (BruteForceStep.cpp:
+ * 48-79, SimulationStep.cpp:317-385) on the chain state's FP64 positions.
+ * The decisions, and so the trajectories, are the same in both; the running
+ * energy of the FP64 form carries FP64 rounding only.  GB300 issues FP64 at
+ * 1/64 of the FP32 rate, so the FP64 form is the slower one.  The stats'
+ * `ties` then count every step. */
+int mcgpu_batch_set_precision(mcgpu_batch* batch, int precision);
 int mcgpu_batch_sync(mcgpu_batch* batch);
 int mcgpu_batch_stats(mcgpu_batch* batch, mcgpu_chain_stats* stats);
 /* Coordinates of chain c (arrays sized like its descriptor). */
@@ -366,6 +376,14 @@ int mcgpu_server_status(mcgpu_server* srv, int* running, int* queued, int64_t* f
 int mcgpu_server_results(mcgpu_server* srv, mcgpu_job_result* out, int max, int* n);
 /* Seconds on the server's clock (the clock of t_submit/t_admit/t_done). */
 double mcgpu_server_clock(const mcgpu_server* srv);
+/* Work counters of the server, for throughput and roofline figures (no
+ * reference counterpart): *pairs the atom pairs (old + new placement) that
+ * the retired jobs evaluated, counted on the device; *gpu_seconds the GPU
+ * time of the rounds completed so far (chain kernel and volume phase,
+ * between CUDA events on the compute stream); *rounds their number.  Any
+ * pointer may be NULL. */
+int mcgpu_server_counters(mcgpu_server* srv, int64_t* pairs, double* gpu_seconds,
+                          int64_t* rounds);
 
 /* ---- no-allocation system energy ---------------------------------------- */
 

@@ -137,6 +137,8 @@ _PROTOS = {
                                       C.POINTER(C.c_uint64)]),
     "mcgpu_server_results": (C.c_int, [_vp, C.POINTER(JobResult), C.c_int, _ip]),
     "mcgpu_server_clock": (C.c_double, [_vp]),
+    "mcgpu_server_counters": (C.c_int, [_vp, C.POINTER(C.c_int64), _dp, C.POINTER(C.c_int64)]),
+    "mcgpu_batch_set_precision": (C.c_int, [_vp, C.c_int]),
     "mcgpu_system_energy_static": (C.c_int, [C.POINTER(BoxDesc), _vp, _vp]),
 }
 

@@ -135,6 +135,11 @@ class ChainBatch:
                                                    d.ctypes.data_as(dp), int(precision)))
         self.vol_interval = int(interval)
 
+    def set_precision(self, precision: int) -> None:
+        """Pair arithmetic of the steps: PREC_MIXED (default) or PREC_FP64
+        (every step with FP64 pairs; same decisions, FP64-rounded energies)."""
+        self._check(_abi.lib().mcgpu_batch_set_precision(self._h, int(precision)))
+
     def set_lrc(self, lrc_v) -> None:
         """Long-range LJ correction in the volume-move criterion: E_LRC * V
         per chain (scalar or one per chain, kcal/mol * A^3; 0 = none)."""

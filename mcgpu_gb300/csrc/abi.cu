@@ -1276,6 +1276,19 @@ extern "C" int mcgpu_batch_set_npt(mcgpu_batch* bt, int interval, const double* 
   return MCGPU_OK;
 }
 
+extern "C" int mcgpu_batch_set_precision(mcgpu_batch* bt, int precision) {
+  if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
+  mcgpu_ctx* ctx = bt->ctx;
+  if (precision != MCGPU_PREC_FP64 && precision != MCGPU_PREC_MIXED)
+    return set_err(ctx, MCGPU_ERR_INVALID, "unknown pair precision %d", precision);
+  const int nc = bt->pool.n_chains;
+  std::vector<int> v(nc, precision == MCGPU_PREC_FP64 ? 1 : 0);
+  CK(ctx, cudaMemcpy2DAsync(&bt->pool.P.hdr->fp64_pairs, sizeof(ChainHdr), v.data(), sizeof(int),
+                            sizeof(int), nc, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MCGPU_OK;
+}
+
 extern "C" int mcgpu_batch_sync(mcgpu_batch* bt) {
   if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
   CK(bt->ctx, cudaStreamSynchronize(bt->ctx->stream));

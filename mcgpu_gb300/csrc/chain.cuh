@@ -345,16 +345,30 @@ __device__ __forceinline__ void batch_chain64(const Pool& P, const ChainHdr& H, 
 
 // The FP64 re-take's screen: the reference's test for every primary pair
 // on the chain state's FP64 positions.
+//
+// With a Verlet list (cand non-null), the molecules cand[c_begin .. c_end),
+// every nw-th entry per warp as in warp_eval_chain.
 __device__ inline void warp_eval_chain64(const Pool& P, const ChainHdr& H, const GroupSmem& s,
                                   const MovedInfo& mi, int c_begin, int c_end, int w, int nw,
-                                  int lane, int T, double& eo, double& en) {
+                                  int lane, int T, double& eo, double& en,
+                                  const int* cand = nullptr) {
   int* rj = s.lj + w * kRing;
   int head = 0, tail = 0;
   const unsigned lt = lanemask_lt();
-  for (int base = c_begin + w * 32; base < c_end; base += nw * 32) {
-    const int j = base + lane;
+  const int rounds = cand ? (c_end - c_begin + 32 * nw - 1) / (32 * nw) : 0;
+  for (int it = 0;; it++) {
+    int idx;
+    if (cand) {
+      if (it >= rounds) break;
+      idx = c_begin + (it * 32 + lane) * nw + w;
+    } else {
+      const int base = c_begin + w * 32 + it * nw * 32;
+      if (base >= c_end) break;
+      idx = base + lane;
+    }
+    const int j = (cand && idx < c_end) ? cand[idx] : idx;
     int f = 0;
-    if (j < c_end && j != mi.mol) {
+    if (idx < c_end && j != mi.mol) {
       const int2 pj = P.mpi[j];
       const uint4 Aj = P.mfix[j];
       for (int k2 = 0; k2 < pj.y; k2++) {

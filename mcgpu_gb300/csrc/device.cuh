@@ -72,7 +72,8 @@ struct __align__(16) ChainHdr {
   double lrc_v;                       // long-range LJ correction x volume (NPT term)
   unsigned long long seed, step;
   long long accepted, pairs;
-  int error, ties, pad3, pad4;        // ties: decisions re-taken with FP64 pairs
+  int error, ties, fp64_pairs, pad4;  // ties: steps evaluated with FP64 pairs;
+                                      // fp64_pairs: every step with FP64 pairs
   // isobaric (NPT) volume moves: every vol_interval steps (0 = NVT), ln V
   // step uniform in +-max_dlnv, pressure in kcal/mol/A^3
   double pressure, max_dlnv;

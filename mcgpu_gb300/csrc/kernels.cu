@@ -377,7 +377,11 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
       const int trial_near = ss.misc[kMiscNlTrial];
       const bool use_list = nl_ok && trial_near;
       AccFF acc = {0.f, 0.f, 0.f, 0.f, 0.f, 0};
-      if (use_list)
+      // FP64-pair chains skip the FP32 evaluation: every step is taken by
+      // the FP64 path below
+      const bool f64all = H.fp64_pairs != 0;
+      if (f64all) {
+      } else if (use_list)
         warp_eval_chain(P, H, ss, mi, pcache, 0, P.nl_cnt[mi.mol], w, nw, lane, T, acc,
                         P.nl + (size_t)mi.mol * P.nl_stride, ljmask);
       else
@@ -397,7 +401,8 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
       const float de_f = __fadd_rn(__fsub_rn(acc.nh, acc.oh), __fsub_rn(acc.nl, acc.ol));
       const float bound = (float)kTieRel * acc.ab + 2.4e-7f * (fabsf(acc.nh) + fabsf(acc.oh)) + 1e-9f;
       const float pf = expf(-fmaxf(de_f, 0.f) * H.kTinvf);
-      const int tie = (de_f >= -bound) && (fabsf(pf - u) <= pf * (1.5f * bound * H.kTinvf) + 1e-6f);
+      const int tie = f64all ||
+                      ((de_f >= -bound) && (fabsf(pf - u) <= pf * (1.5f * bound * H.kTinvf) + 1e-6f));
       double e_old = 0.0, e_new = 0.0;
       int ok;
       if (tie) {
@@ -405,7 +410,11 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
         g.sync();
         double eo = 0.0, en = 0.0, ab2 = 0.0;
         long long np2 = 0;
-        warp_eval_chain64(P, H, ss, mi, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, eo, en);
+        if (use_list)
+          warp_eval_chain64(P, H, ss, mi, 0, P.nl_cnt[mi.mol], w, nw, lane, T, eo, en,
+                            P.nl + (size_t)mi.mol * P.nl_stride);
+        else
+          warp_eval_chain64(P, H, ss, mi, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, eo, en);
         group_reduce(g, ss, eo, en, ab2, np2, st & 1);
         e_old = eo;
         e_new = en;

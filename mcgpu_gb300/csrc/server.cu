@@ -98,6 +98,11 @@ struct mcgpu_server {
   int64_t next_id = 1, finished = 0;
   cudaStream_t copy = nullptr;
   cudaEvent_t ev_round = nullptr, ev_copy = nullptr;
+  // GPU time of the rounds (chain kernel + volume phase), and the atom pairs
+  // the retired jobs evaluated (device-counted)
+  cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
+  double gpu_s = 0.0;
+  long long pairs_done = 0, rounds = 0;
   bool round_in_flight = false, copies_pending = false;
   int gw = 8, grid = 1, smem = 0;
   SmemShape shape{};
@@ -183,6 +188,8 @@ void server_free(mcgpu_server* s) {
   if (s->hlist) cudaFreeHost(s->hlist);
   if (s->stage) cudaFreeHost(s->stage);
   if (s->ev_round) cudaEventDestroy(s->ev_round);
+  if (s->ev_t0) cudaEventDestroy(s->ev_t0);
+  if (s->ev_t1) cudaEventDestroy(s->ev_t1);
   if (s->ev_copy) cudaEventDestroy(s->ev_copy);
   if (s->copy) cudaStreamDestroy(s->copy);
   for (Job* j : s->slot_job) delete j;
@@ -364,6 +371,7 @@ int harvest(mcgpu_server* s) {
     r.footprint_bytes = j->bytes;
     r.error = h.error;
     r.ties = h.ties;
+    s->pairs_done += h.pairs;
     s->done.push_back(r);
     s->finished++;
     s->atoms.release(j->a0, j->n_atom);
@@ -419,6 +427,7 @@ int launch_round(mcgpu_server* s) {
     CK(ctx, cudaStreamWaitEvent(st, s->ev_copy, 0));
     s->copies_pending = false;
   }
+  CK(ctx, cudaEventRecord(s->ev_t0, st));
   CK(ctx, cudaMemsetAsync(s->qctr, 0, sizeof(unsigned), st));
   const int need = ((int)act.size() + s->cfg.chains_per_cta - 1) / s->cfg.chains_per_cta;
   const int grid = std::max(1, std::min(need, s->grid));
@@ -442,6 +451,7 @@ int launch_round(mcgpu_server* s) {
                                 s->vsum, s->vsum_abs, s->vlist, nullptr, 0, 0, st, R, has64,
                                 has32));
   }
+  CK(ctx, cudaEventRecord(s->ev_t1, st));
   CK(ctx, cudaMemcpyAsync(s->hmirror, s->pool.P.hdr, sizeof(ChainHdr) * nc, cudaMemcpyDeviceToHost, st));
   CK(ctx, cudaEventRecord(s->ev_round, st));
   s->round_in_flight = true;
@@ -492,6 +502,8 @@ extern "C" int mcgpu_server_create(mcgpu_ctx* ctx, const mcgpu_server_config* cf
   cudaError_t e = cudaSuccess;
   if (rc == MCGPU_OK) e = cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking);
   if (rc == MCGPU_OK && e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_round, cudaEventDisableTiming);
+  if (rc == MCGPU_OK && e == cudaSuccess) e = cudaEventCreate(&s->ev_t0);
+  if (rc == MCGPU_OK && e == cudaSuccess) e = cudaEventCreate(&s->ev_t1);
   if (rc == MCGPU_OK && e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_copy, cudaEventDisableTiming);
   if (rc == MCGPU_OK && e != cudaSuccess)
     rc = set_err(ctx, MCGPU_ERR_CUDA, "server stream/events: %s", cudaGetErrorString(e));
@@ -587,6 +599,9 @@ extern "C" int mcgpu_server_step(mcgpu_server* s) {
   if (s->round_in_flight) {
     CK(ctx, cudaEventSynchronize(s->ev_round));
     s->round_in_flight = false;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, s->ev_t0, s->ev_t1) == cudaSuccess) s->gpu_s += 1e-3 * ms;
+    s->rounds++;
     rc = harvest(s);
     if (rc) return rc;
     rc = admit(s);
@@ -633,3 +648,12 @@ extern "C" int mcgpu_server_results(mcgpu_server* s, mcgpu_job_result* out, int 
 }
 
 extern "C" double mcgpu_server_clock(const mcgpu_server* s) { return s ? s->now() : 0.0; }
+
+extern "C" int mcgpu_server_counters(mcgpu_server* s, int64_t* pairs, double* gpu_seconds,
+                                     int64_t* rounds) {
+  if (!s) return set_err(nullptr, MCGPU_ERR_INVALID, "null server");
+  if (pairs) *pairs = s->pairs_done;
+  if (gpu_seconds) *gpu_seconds = s->gpu_s;
+  if (rounds) *rounds = s->rounds;
+  return MCGPU_OK;
+}

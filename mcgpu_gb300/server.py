@@ -124,3 +124,11 @@ class JobServer:
 
     def clock(self) -> float:
         return float(_abi.lib().mcgpu_server_clock(self._h))
+
+    def counters(self) -> dict:
+        """Device-counted atom pairs of the retired jobs, GPU seconds and
+        number of the completed rounds (mcgpu_server_counters)."""
+        pairs, rounds, gs = C.c_int64(), C.c_int64(), C.c_double()
+        self._check(_abi.lib().mcgpu_server_counters(self._h, C.byref(pairs), C.byref(gs),
+                                                     C.byref(rounds)))
+        return {"pairs": pairs.value, "gpu_seconds": gs.value, "rounds": rounds.value}

@@ -179,7 +179,7 @@ def test_water_32768_npt_verlet_replay(ctx):
     coordinates bit for bit)."""
     from mcgpu_gb300.prepare import relaxed_water_32768
     box = relaxed_water_32768(ctx)
-    interval, steps, dl, seed = 100, 200, 0.005, 0x5EED
+    interval, steps, dl, seed = 100, 200, 0.0015, 0x5EED
     bt = ChainBatch(ctx, [box], [seed], rotation=ROT_AXIS)
     bt.set_tile(512, 1, 64)
     bt.set_verlet(1.5)
