@@ -260,14 +260,38 @@ def run_reference(args, ws, rank):
 
 # ---- plain single-chain drop-in ---------------------------------------------------
 
+FP64_PEAK_TFLOPS = 1.25    # nominal GB300 FP64 (no measured FP64 figure in MEASURED_PEAKS.json)
+
+
 def bench_plain(ctx, n_steps: int = 2000) -> dict:
     """The SimulationStep contract on the GPU driven from the host, as
     metrosim's loop drives it: one launch (and one D2H scalar) per energy
     call, one launch per move and per rollback; 256 waters (the CPU-runnable
-    reference configuration)."""
+    reference configuration).  Two hosts of the loop: the library's C++
+    (mcgpu_run_plain, the calls a GpuBruteForceStep makes under the
+    reference's own loop) and the Python mirror (step.py), both with the
+    C library's rand() draws.  The C++ entries carry the device-counted pair
+    work and its roofline (FP64 pairs against the nominal FP64 peak, FP32
+    pairs against the nominal FP32 peak)."""
     import mcgpu_gb300 as M
     box = M.water_box(256, L=19.71, seed=12345)
-    out = {}
+    out = {"cpp": {}, "python": {}}
+    for name, prec, fused in (("fp64", M.PREC_FP64, False), ("fp64_fused", M.PREC_FP64, True),
+                              ("mixed", M.PREC_MIXED, False),
+                              ("mixed_fused", M.PREC_MIXED, True)):
+        g = M.GpuBox(ctx, box, prec)
+        g.run_plain_native(41, 50, fused=fused)            # warm-up
+        t0 = time.perf_counter()
+        st = g.run_plain_native(42, n_steps, fused=fused)
+        dt = time.perf_counter() - t0
+        g.close()
+        peak = FP64_PEAK_TFLOPS if prec == M.PREC_FP64 else fp32_peak_tflops()
+        achieved = st.pairs * FP32_FLOPS_PER_PAIR / dt / 1e12
+        out["cpp"][name] = {"moves_per_s": n_steps / dt, "accepted": st.accepted,
+                            "steps": n_steps, "pairs_per_move": st.pairs / n_steps,
+                            "roofline": {"bound": "fp64" if prec == M.PREC_FP64 else "fp32",
+                                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                                         "frac": achieved / peak}}
     for name, prec, fused in (("fp64", M.PREC_FP64, False), ("mixed", M.PREC_MIXED, False),
                               ("mixed_fused", M.PREC_MIXED, True)):
         g = M.GpuBox(ctx, box, prec)
@@ -276,8 +300,12 @@ def bench_plain(ctx, n_steps: int = 2000) -> dict:
         t0 = time.perf_counter()
         res = M.run_plain(step, n_steps, fused=fused)
         dt = time.perf_counter() - t0
-        out[name] = {"moves_per_s": n_steps / dt, "accepted": res.accepted, "steps": n_steps}
+        out["python"][name] = {"moves_per_s": n_steps / dt, "accepted": res.accepted,
+                               "steps": n_steps}
         g.close()
+    out["note"] = ("roofline peaks are nominal (FP64 1.25 TFLOP/s, FP32 152 SMs x 128 x 2 x "
+                   "2.07 GHz); the plain form is launch- and sync-bound by design: one launch "
+                   "and one D2H sync per contract call")
     return out
 
 
@@ -306,10 +334,9 @@ def bench_single(ctx, plain_steps: int = 150, chain_steps: int = 4000) -> dict:
     out = {"workload": "4000 x 16-atom bicyclic, L=86.1 A, rc 12 A, NVT 298 K, single chain"}
     for name, prec in (("plain_fp64", M.PREC_FP64), ("plain_mixed", M.PREC_MIXED)):
         g = M.GpuBox(ctx, box, prec)
-        step = M.GpuSimulationStep(g, M.LibcRand(7))
-        M.run_plain(step, 10, fused=True)
+        g.run_plain_native(6, 10, fused=True)
         t0 = time.perf_counter()
-        M.run_plain(step, plain_steps, fused=True)
+        g.run_plain_native(7, plain_steps, fused=True)
         out[name] = plain_steps / (time.perf_counter() - t0)
         g.close()
     for name, skin in (("chain_full_scan", 0.0), ("chain_verlet", 1.5)):
@@ -403,10 +430,9 @@ def bench_large(ctx, steps: int = 200000, interval: int = 500, max_dlnv: float =
         math.hypot(a["density_se"], b["density_se"]), 1e-300)
     out["chain_verlet_npt"] = a["moves_per_s"]
     g = M.GpuBox(ctx, box, M.PREC_FP64)
-    step = M.GpuSimulationStep(g, M.LibcRand(3))
-    M.run_plain(step, 5, fused=True)
+    g.run_plain_native(2, 5, fused=True)
     t0 = time.perf_counter()
-    M.run_plain(step, 60, fused=True)
+    g.run_plain_native(3, 60, fused=True)
     out["plain_fp64"] = 60 / (time.perf_counter() - t0)
     g.close()
     return out
@@ -694,9 +720,9 @@ def main():
         "clocks": clocks,
         "e2e": e2e,
         "plain_1chain": plain,
-        "batched_over_plain": (value / plain["fp64"]["moves_per_s"]) if plain else None,
+        "batched_over_plain": (value / plain["cpp"]["fp64"]["moves_per_s"]) if plain else None,
         "served": served,
-        "served_over_plain": (served["moves_per_s"] / plain["fp64"]["moves_per_s"])
+        "served_over_plain": (served["moves_per_s"] / plain["cpp"]["fp64"]["moves_per_s"])
                              if (served and plain) else None,
         "single_chain": single,
         "large_system": large,

@@ -176,6 +176,27 @@ int mcgpu_system_energy(mcgpu_box* box, double* out);
 int mcgpu_move_energies(mcgpu_box* box, int mol, const mcgpu_move* mv,
                         double* e_old, double* e_new);
 
+/* Result of mcgpu_run_plain. */
+typedef struct {
+  double energy0;         /* system energy at the start (calcSystemEnergy)   */
+  double energy;          /* running total at the end: energy0 + sum of dE   */
+  int64_t accepted, rejected;
+  int64_t pairs;          /* atom pairs evaluated (old + new), counted on the
+                             device                                          */
+} mcgpu_plain_stats;
+
+/* Simulation::run's NVT loop (Simulation.cpp:219-264) in C++ over the
+ * contract calls above: srand(seed), then per step chooseMolecule, the
+ * seven intermolecularMove draws and acceptMove's uniform from the C
+ * library's rand() in the reference's order (SimulationStep.cpp:25-27,
+ * 527-535, 794-803), calcMolecularEnergyContribution before and after
+ * changeMolecule, rollback on rejection -- the calls a GpuBruteForceStep
+ * makes under the reference's own loop.  fused != 0 takes the old energy,
+ * the move and the new energy in one mcgpu_move_energies launch (the same
+ * draws and decisions). */
+int mcgpu_run_plain(mcgpu_box* box, unsigned int seed, int n_steps, int fused,
+                    mcgpu_plain_stats* out);
+
 /* ---- device-resident chain (Philox RNG, on-device accept) --------------- */
 
 /* Runs n_steps Metropolis steps of this box as chain `chain_id` with the

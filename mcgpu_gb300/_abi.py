@@ -67,6 +67,11 @@ class Trace(C.Structure):
                 ("fp64", C.c_int32), ("pad0", C.c_int32)]
 
 
+class PlainStats(C.Structure):
+    _fields_ = [("energy0", C.c_double), ("energy", C.c_double), ("accepted", C.c_int64),
+                ("rejected", C.c_int64), ("pairs", C.c_int64)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_atoms", C.c_int64),
                 ("max_molecules", C.c_int64), ("max_slots", C.c_int32),
@@ -139,6 +144,7 @@ _PROTOS = {
     "mcgpu_server_clock": (C.c_double, [_vp]),
     "mcgpu_server_counters": (C.c_int, [_vp, C.POINTER(C.c_int64), _dp, C.POINTER(C.c_int64)]),
     "mcgpu_batch_set_precision": (C.c_int, [_vp, C.c_int]),
+    "mcgpu_run_plain": (C.c_int, [_vp, C.c_uint, C.c_int, C.c_int, C.POINTER(PlainStats)]),
     "mcgpu_system_energy_static": (C.c_int, [C.POINTER(BoxDesc), _vp, _vp]),
 }
 

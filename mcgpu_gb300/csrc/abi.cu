@@ -10,6 +10,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -531,6 +532,7 @@ struct mcgpu_box {
   unsigned* counter = nullptr;
   double* dout = nullptr;
   double* hout = nullptr;  // pinned
+  long long* dpairs = nullptr;  // atom pairs the plain energy kernels evaluated
   bool energy_ready = false;
   mcgpu_trace* dtrace = nullptr;
   int trace_cap = 0;
@@ -556,8 +558,12 @@ static void box_plain_moved(mcgpu_box* b) {
   b->energy_ready = false;
 }
 
+// CTAs of a plain energy launch: one per 128 candidates with FP32 pairs, one
+// per 32 with FP64 pairs (GB300 runs FP64 at 1/64 of the FP32 rate, so the
+// pair work is spread over more SMs).
 static int box_grid(const mcgpu_box* b, int n_cand) {
-  int g = (n_cand + 127) / 128;
+  const int per = b->precision == MCGPU_PREC_FP64 ? 32 : 128;
+  int g = (n_cand + per - 1) / per;
   return std::max(1, std::min(g, b->max_grid));
 }
 
@@ -598,6 +604,8 @@ extern "C" int mcgpu_box_upload(mcgpu_ctx* ctx, const mcgpu_box_desc* desc, int 
   b->order = dalloc<int>(1, &e);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&b->hout, 4 * sizeof(double));
   if (e == cudaSuccess) e = cudaMemsetAsync(b->counter, 0, 2 * sizeof(unsigned), ctx->stream);
+  if (e == cudaSuccess) b->dpairs = dalloc<long long>(1, &e);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->dpairs, 0, sizeof(long long), ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->order, 0, sizeof(int), ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
@@ -617,6 +625,7 @@ extern "C" int mcgpu_box_destroy(mcgpu_box* b) {
   if (b->counter) cudaFree(b->counter);
   if (b->dout) cudaFree(b->dout);
   if (b->hout) cudaFreeHost(b->hout);
+  if (b->dpairs) cudaFree(b->dpairs);
   if (b->dtrace) cudaFree(b->dtrace);
   if (b->queue) cudaFree(b->queue);
   if (b->order) cudaFree(b->order);
@@ -655,7 +664,8 @@ extern "C" int mcgpu_mol_energy(mcgpu_box* b, int curr, int start, double* out) 
   SmemShape sh = shape_for(b->pool.max_len, nw);
   const int grid = box_grid(b, n - start);
   CK(ctx, launch_mol_energy(b->precision == MCGPU_PREC_FP64, grid, nw * 32, sh, ctx->stream,
-                            b->pool.P, 0, curr, start, b->partials, b->counter, b->dout));
+                            b->pool.P, 0, curr, start, b->partials, b->counter, b->dout,
+                            b->dpairs));
   CK(ctx, cudaMemcpyAsync(b->hout, b->dout, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   *out = b->hout[0];
@@ -688,7 +698,6 @@ extern "C" int mcgpu_change_molecule(mcgpu_box* b, int mol, const mcgpu_move* mv
   SmemShape sh = shape_for(b->pool.max_len, 1);
   k_change_molecule<<<1, 32, sh.bytes(), ctx->stream>>>(b->pool.P, 0, mol, host_proposal(mv), sh);
   CK(ctx, cudaGetLastError());
-  CK(ctx, cudaStreamSynchronize(ctx->stream));
   return MCGPU_OK;
 }
 
@@ -702,7 +711,6 @@ extern "C" int mcgpu_rollback(mcgpu_box* b, int mol) {
   box_plain_moved(b);
   k_rollback<<<1, 32, 0, ctx->stream>>>(b->pool.P, 0, mol);
   CK(ctx, cudaGetLastError());
-  CK(ctx, cudaStreamSynchronize(ctx->stream));
   return MCGPU_OK;
 }
 
@@ -720,7 +728,7 @@ extern "C" int mcgpu_move_energies(mcgpu_box* b, int mol, const mcgpu_move* mv, 
   const int grid = box_grid(b, b->pool.n_mol);
   CK(ctx, launch_move_energies(b->precision == MCGPU_PREC_FP64, grid, nw * 32, sh, ctx->stream,
                                b->pool.P, 0, mol, host_proposal(mv), b->partials, b->counter,
-                               b->dout));
+                               b->dout, b->dpairs));
   CK(ctx, cudaMemcpyAsync(b->hout, b->dout, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   *e_old = b->hout[0];
@@ -738,6 +746,75 @@ extern "C" int mcgpu_system_energy(mcgpu_box* b, double* out) {
   CK(ctx, cudaMemcpyAsync(b->hout, b->pool.esum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   *out = b->hout[0];
+  return MCGPU_OK;
+}
+
+// ---- the reference's NVT loop over the contract, in C++ -------------------
+
+namespace {
+// randomReal of the reference (MathLibrary.cpp:31-33) over the C library's
+// rand(), seeded with srand().
+double random_real(double start, double end) {
+  return (end - start) * ((double)std::rand() / RAND_MAX) + start;
+}
+}  // namespace
+
+extern "C" int mcgpu_run_plain(mcgpu_box* b, unsigned int seed, int n_steps, int fused,
+                               mcgpu_plain_stats* out) {
+  if (!b || !out) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = b->ctx;
+  if (n_steps < 0) return set_err(ctx, MCGPU_ERR_INVALID, "negative step count");
+  const ChainHdr& h = b->pool.hdr[0];
+  const int n = b->pool.n_mol;
+  const double kT = h.kT, max_t = h.max_t, max_r = h.max_r;
+  std::memset(out, 0, sizeof(*out));
+  CK(ctx, cudaMemsetAsync(b->dpairs, 0, sizeof(long long), ctx->stream));
+  double e = 0.0;
+  int rc = mcgpu_system_energy(b, &e);
+  if (rc) return rc;
+  out->energy0 = e;
+  std::srand(seed);
+  for (int step = 0; step < n_steps; step++) {
+    // chooseMolecule (SimulationStep.cpp:25-27); rand() == RAND_MAX gives n,
+    // clamped to n - 1 (the reference would read past its rows)
+    const int mol = std::min((int)random_real(0, n), n - 1);
+    // the seven draws of intermolecularMove (SimulationStep.cpp:527-535)
+    const int len = b->pool.mlen[mol] & 255;
+    mcgpu_move mv;
+    std::memset(&mv, 0, sizeof(mv));
+    mv.vertex = std::min((int)random_real(0, len), len - 1);
+    mv.dx = random_real(-max_t, max_t);
+    mv.dy = random_real(-max_t, max_t);
+    mv.dz = random_real(-max_t, max_t);
+    mv.rx = random_real(-max_r, max_r);
+    mv.ry = random_real(-max_r, max_r);
+    mv.rz = random_real(-max_r, max_r);
+    double e_old = 0.0, e_new = 0.0;
+    if (fused) {
+      rc = mcgpu_move_energies(b, mol, &mv, &e_old, &e_new);
+    } else {
+      rc = mcgpu_mol_energy(b, mol, 0, &e_old);
+      if (!rc) rc = mcgpu_change_molecule(b, mol, &mv);
+      if (!rc) rc = mcgpu_mol_energy(b, mol, 0, &e_new);
+    }
+    if (rc) return rc;
+    // acceptMove (SimulationStep.cpp:794-803)
+    const double de = e_new - e_old;
+    const bool ok = de < 0 || std::exp(-de / kT) >= random_real(0.0, 1.0);
+    if (ok) {
+      e += de;
+      out->accepted++;
+    } else {
+      out->rejected++;
+      rc = mcgpu_rollback(b, mol);
+      if (rc) return rc;
+    }
+  }
+  long long np = 0;
+  CK(ctx, cudaMemcpyAsync(&np, b->dpairs, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  out->energy = e;
+  out->pairs = np;
   return MCGPU_OK;
 }
 

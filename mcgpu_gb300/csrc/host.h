@@ -37,10 +37,10 @@ __global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol
                                int a_end);
 cudaError_t launch_mol_energy(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
                               Pool P, int chain, int curr, int start, double* partials,
-                              unsigned* counter, double* out);
+                              unsigned* counter, double* out, long long* pairs = nullptr);
 cudaError_t launch_move_energies(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
                                  Pool P, int chain, int mol, Proposal prop, double* partials,
-                                 unsigned* counter, double* out);
+                                 unsigned* counter, double* out, long long* pairs = nullptr);
 cudaError_t launch_mol_pair_sums(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
                                  Pool P, const int* mol_chain, int m_begin, double* emol,
                                  long long* pairs);

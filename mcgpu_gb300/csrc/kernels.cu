@@ -41,7 +41,8 @@ __device__ bool arrive_last(unsigned* counter) {
 template <bool F64>
 __global__ void __launch_bounds__(256) k_mol_energy(Pool P, int chain, int curr, int start,
                                                     SmemShape shape, double* partials,
-                                                    unsigned* counter, double* out) {
+                                                    unsigned* counter, double* out,
+                                                    long long* pairs) {
   extern __shared__ __align__(16) char smem[];
   const ChainHdr& H = P.hdr[chain];
   Group g{(int)threadIdx.x, (int)blockDim.x, 1};
@@ -60,6 +61,7 @@ __global__ void __launch_bounds__(256) k_mol_energy(Pool P, int chain, int curr,
   if (cb < ce) warp_eval<F64>(P, H, s, mi, cb, ce, w, nw, lane, H.tpm, eo, en, ab, np);
   group_reduce(g, s, eo, en, ab, np);
   if (threadIdx.x == 0) {
+    if (pairs) atomicAdd((unsigned long long*)pairs, (unsigned long long)np);
     partials[blockIdx.x] = eo;
     if (arrive_last(counter)) {
       __threadfence();
@@ -77,7 +79,8 @@ __global__ void __launch_bounds__(256) k_mol_energy(Pool P, int chain, int curr,
 template <bool F64>
 __global__ void __launch_bounds__(256) k_move_energies(Pool P, int chain, int mol, Proposal prop,
                                                        SmemShape shape, double* partials,
-                                                       unsigned* counter, double* out) {
+                                                       unsigned* counter, double* out,
+                                                       long long* pairs) {
   extern __shared__ __align__(16) char smem[];
   const ChainHdr& H = P.hdr[chain];
   Group g{(int)threadIdx.x, (int)blockDim.x, 1};
@@ -96,6 +99,7 @@ __global__ void __launch_bounds__(256) k_move_energies(Pool P, int chain, int mo
   group_reduce(g, s, eo, en, ab, np);
   __shared__ int last;
   if (threadIdx.x == 0) {
+    if (pairs) atomicAdd((unsigned long long*)pairs, (unsigned long long)np);
     partials[2 * blockIdx.x] = eo;
     partials[2 * blockIdx.x + 1] = en;
     last = arrive_last(counter) ? 1 : 0;
@@ -515,25 +519,25 @@ __global__ void __launch_bounds__(512, 1) k_chain_steps_wide(Pool P, int n_steps
 
 cudaError_t launch_mol_energy(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
                               Pool P, int chain, int curr, int start, double* partials,
-                              unsigned* counter, double* out) {
+                              unsigned* counter, double* out, long long* pairs) {
   if (f64)
     k_mol_energy<true><<<grid, threads, sh.bytes(), st>>>(P, chain, curr, start, sh, partials,
-                                                          counter, out);
+                                                          counter, out, pairs);
   else
     k_mol_energy<false><<<grid, threads, sh.bytes(), st>>>(P, chain, curr, start, sh, partials,
-                                                           counter, out);
+                                                           counter, out, pairs);
   return cudaGetLastError();
 }
 
 cudaError_t launch_move_energies(bool f64, int grid, int threads, SmemShape sh, cudaStream_t st,
                                  Pool P, int chain, int mol, Proposal prop, double* partials,
-                                 unsigned* counter, double* out) {
+                                 unsigned* counter, double* out, long long* pairs) {
   if (f64)
     k_move_energies<true><<<grid, threads, sh.bytes(), st>>>(P, chain, mol, prop, sh, partials,
-                                                             counter, out);
+                                                             counter, out, pairs);
   else
     k_move_energies<false><<<grid, threads, sh.bytes(), st>>>(P, chain, mol, prop, sh, partials,
-                                                              counter, out);
+                                                              counter, out, pairs);
   return cudaGetLastError();
 }
 

@@ -284,7 +284,7 @@ __device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4*
                                                   float sb, float2 qb, const ChainHdr& H,
                                                   float& abs, unsigned ljmask = ~0u) {
   float acc = 0.f;
-#pragma unroll
+#pragma unroll (NLEN > 0 ? NLEN : 1)
   for (int i = 0; i < (NLEN > 0 ? NLEN : len); i++) {
     const float4 ea = eq[i];
     const float4 a = o[i];
@@ -321,7 +321,7 @@ __device__ __forceinline__ float sum_moved32_cf(const float4* o, const float4* l
   const float R = R2 * iR;
   const float tx = bh.x + bh.x, ty = bh.y + bh.y, tz = bh.z + bh.z;
   float lj_acc = 0.f, phi = 0.f, lj_abs = 0.f, c_abs = 0.f;
-#pragma unroll
+#pragma unroll (NLEN > 0 ? NLEN : 1)
   for (int i = 0; i < (NLEN > 0 ? NLEN : len); i++) {
     const float4 a = o[i];
     const float4 ea = eq[i];

@@ -159,6 +159,15 @@ class GpuBox:
         """Verlet neighbour lists (skin in Angstrom, <= 0 off) for chain_run."""
         self._check(_abi.lib().mcgpu_box_set_verlet(self._h, float(skin)))
 
+    def run_plain_native(self, seed: int, n_steps: int, fused: bool = False) -> "_abi.PlainStats":
+        """Simulation::run's NVT loop in the library's C++ (mcgpu_run_plain):
+        the same calls and the same rand() draws as run_plain over
+        GpuSimulationStep(self, LibcRand(seed))."""
+        st = _abi.PlainStats()
+        self._check(_abi.lib().mcgpu_run_plain(self._h, int(seed) & 0xFFFFFFFF, int(n_steps),
+                                               1 if fused else 0, C.byref(st)))
+        return st
+
     def chain_run(self, seed: int, n_steps: int, chain_id: int = 0,
                   rotation: int = _abi.ROT_AXIS, trace: bool = False):
         st = _abi.ChainStats()

@@ -102,6 +102,26 @@ def test_plain_trajectory_fp64_matches_reference(ctx, fused):
     assert np.allclose(np.stack([x, y, zz], 1), z["traj_final"], rtol=0, atol=1e-8)
 
 
+@pytest.mark.parametrize("fused", [False, True])
+def test_native_plain_loop_matches_reference(ctx, fused):
+    """The C++ loop of the library (mcgpu_run_plain: Simulation::run's NVT
+    loop over the contract calls, the C library's rand() in the reference's
+    draw order): the reference's own run's accepted count, final energy and
+    coordinates, and a device pair count of two evaluations per step."""
+    box, z = load_golden("water256")
+    g = GpuBox(ctx, box, PREC_FP64)
+    n = int(z["traj_steps"][0])
+    st = g.run_plain_native(int(z["traj_seed"][0]), n, fused=fused)
+    assert abs(st.energy0 - z["traj_e0"][0]) <= tol64(z["traj_e0"][0])
+    assert st.accepted == z["traj_accepted"][0] and st.accepted + st.rejected == n
+    assert abs(st.energy - z["traj_energy"][0]) <= 1e-8 * max(1.0, abs(z["traj_energy"][0]))
+    x, y, zz = g.download()
+    assert np.allclose(np.stack([x, y, zz], 1), z["traj_final"], rtol=0, atol=1e-8)
+    # 256 waters, rc 9: about a hundred in-range neighbours of 9 pairs, twice a step
+    assert 500 * n < st.pairs < 3000 * n
+    g.close()
+
+
 def test_plain_trajectory_mixed_lockstep(ctx):
     """FP32 pairs driven in lockstep with the FP64 oracle on the reference's
     rand() proposals: every dE within tolerance, the oracle's decision applied
