@@ -168,12 +168,11 @@ __device__ __forceinline__ int screen_chain(const Pool& P, const ChainHdr& H, co
 // loop unrolled for 3-site molecules).
 __device__ __forceinline__ void batch_u1_any(const Pool& P, const ChainHdr& H, const GroupSmem& s,
                                              const MovedInfo& mi, const int* rj, int head,
-                                             int count, int w, int lane, AccFF& acc,
-                                             unsigned ljmask) {
+                                             int count, int w, int lane, AccFF& acc) {
   if (H.ulen == 3)
-    batch_u1<3>(P, H, s, mi, rj, head, count, w, lane, acc, ljmask);
+    batch_u1<3>(P, H, s, mi, rj, head, count, w, lane, acc, H.ljmask);
   else
-    batch_u1<0>(P, H, s, mi, rj, head, count, w, lane, acc, ljmask);
+    batch_u1<0>(P, H, s, mi, rj, head, count, w, lane, acc, ~0u);
 }
 
 // Bits 4k + i: the LJ term between atoms i and k of a uniform chain's
@@ -198,7 +197,7 @@ __device__ __forceinline__ unsigned uniform_lj_mask(const Pool& P, const ChainHd
 __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const GroupSmem& s,
                                 const MovedInfo& mi, const float4* pcache, int c_begin, int c_end,
                                 int w, int nw, int lane, int T, AccFF& acc,
-                                const int* cand = nullptr, unsigned ljmask = ~0u) {
+                                const int* cand = nullptr) {
   int* rj = s.lj + w * kRing;
   int head = 0, tail = 0;
   const unsigned lt = lanemask_lt();
@@ -235,7 +234,7 @@ __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const G
     if (tail - head >= 32) {
       __syncwarp();
       if (u1)
-        batch_u1_any(P, H, s, mi, rj, head, 32, w, lane, acc, ljmask);
+        batch_u1_any(P, H, s, mi, rj, head, 32, w, lane, acc);
       else if (H.precise)
         batch_ff<true, false>(P, H, s, mi, rj, head, 32, lane, T, acc);
       else
@@ -247,7 +246,7 @@ __device__ inline void warp_eval_chain(const Pool& P, const ChainHdr& H, const G
   __syncwarp();
   if (tail > head) {
     if (u1)
-      batch_u1_any(P, H, s, mi, rj, head, tail - head, w, lane, acc, ljmask);
+      batch_u1_any(P, H, s, mi, rj, head, tail - head, w, lane, acc);
     else if (H.precise)
       batch_ff<true, false>(P, H, s, mi, rj, head, tail - head, lane, T, acc);
     else

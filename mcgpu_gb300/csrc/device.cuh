@@ -98,7 +98,10 @@ struct __align__(16) ChainHdr {
   // primary at slot uprim, radius <= umrad: atom and primary indexes and
   // pair factors follow from the molecule index (no loads)
   int uniform, ulen, uact, uprim;
-  float umrad, pad9, pad10, pad11;
+  float umrad;
+  unsigned ljmask;      // uniform chains of <= 4 atoms: bits 4k + i set where the LJ term
+                        // of atoms i and k is not exactly zero (set by the step kernel)
+  float pad10, pad11;
   // bound on |energy - FP64 system energy of the current state|: the sum of
   // the FP32 step bounds since the energy was last set from a fresh total
   double run_err, pad12;

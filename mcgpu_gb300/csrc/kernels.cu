@@ -284,14 +284,6 @@ __global__ void k_chain_export(Pool P, const int* mol_chain, const int* atom_mol
   P.z[a] = x.z;
 }
 
-// One Philox move draw (the staging warp draws 32 steps' moves at once),
-// out of line to keep the step loop's code compact.
-__device__ __noinline__ void draw_move_out(const ChainHdr& H, const int* mlen_chain,
-                                           unsigned long long step, MoveF* out) {
-  *out = draw_move_f32(H.seed, H.chain_id, step, H.n_mol, mlen_chain, (float)H.max_t,
-                       (float)H.max_r, H.rot_mode);
-}
-
 // Persistent kernel: groups of `gwarps` warps pull chain tasks from `queue`
 // (task k runs chain order[k]) and advance each by n_steps steps on the
 // chain state.  A step: every warp screens its share of the candidates
@@ -334,7 +326,9 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
     if (H.uniform)
       for (int i = g.tid; i < H.ulen; i += gsize) s.teq[i] = P.aeq[H.atom0 + i];
     g.sync();
-    const unsigned ljmask = uniform_lj_mask(P, H, s.teq);
+    // the chain's LJ mask, read by the pair batches after the next barrier
+    // (kept in the header rather than in a register across the step loop)
+    if (g.tid == 0) Hp->ljmask = uniform_lj_mask(P, H, s.teq);
     int full_scans = 0;
     // the accepted dE of this task and their FP32 error bounds, each summed
     // in double-float (FP64 costs 64 FP32 issue slots on GB300); both join
@@ -363,7 +357,9 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
     auto slot = [&](int k) { return shape.ahead_slot(s.ahead + k * sb); };
     // moves are drawn 32 steps at a time (one per lane) by the staging warp
     auto draw32 = [&](int st0) {
-      if (st0 + lane < my_steps) draw_move_out(H, P.mlen + H.mol0, step0 + st0 + lane, props + lane);
+      if (st0 + lane < my_steps)
+        props[lane] = draw_move_f32(H.seed, H.chain_id, step0 + st0 + lane, H.n_mol,
+                                    P.mlen + H.mol0, (float)H.max_t, (float)H.max_r, H.rot_mode);
       __syncwarp();
     };
     if (w == 0 && my_steps > 0) {
@@ -387,10 +383,9 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
       if (f64all) {
       } else if (use_list)
         warp_eval_chain(P, H, ss, mi, pcache, 0, P.nl_cnt[mi.mol], w, nw, lane, T, acc,
-                        P.nl + (size_t)mi.mol * P.nl_stride, ljmask);
+                        P.nl + (size_t)mi.mol * P.nl_stride);
       else
-        warp_eval_chain(P, H, ss, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, acc,
-                        nullptr, ljmask);
+        warp_eval_chain(P, H, ss, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, acc);
       // the last warp (with the fewest screen blocks) stages the next move
       // while the others finish their share
       if (w == nw - 1 && st + 1 < my_steps) {

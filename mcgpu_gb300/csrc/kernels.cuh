@@ -274,18 +274,18 @@ __device__ __forceinline__ float3 pair_disp(float3 bh, float3 bl, float4 a, floa
 // neighbour atom b, per-pair periodic image (entries whose atom pairs may
 // straddle half a box edge).  abs accumulates |LJ| + |Coulomb|.
 //
-// NLEN > 0 fixes the moved molecule's length at compile time (the loop
-// unrolls and its independent pair terms interleave); bit i of ljmask clear
-// means the LJ term of moved atom i is exactly zero (a sigma or epsilon
-// product of zero) and is not evaluated.  Neither changes a bit of the sum.
+// NLEN > 0 fixes the moved molecule's length (at most 4) at compile time:
+// the loop unrolls so its independent pair terms interleave, and bit i of
+// ljmask clear means the LJ term of moved atom i is exactly zero (a sigma or
+// epsilon product of zero) and is not evaluated.  NLEN == 0 (any length up
+// to 64) ignores ljmask.  Neither changes a bit of the sum.
 template <bool PRECISE, int NLEN = 0>
 __device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4* lo,
                                                   const float4* eq, int len, float3 bh, float3 bl,
                                                   float sb, float2 qb, const ChainHdr& H,
                                                   float& abs, unsigned ljmask = ~0u) {
   float acc = 0.f;
-#pragma unroll (NLEN > 0 ? NLEN : 1)
-  for (int i = 0; i < (NLEN > 0 ? NLEN : len); i++) {
+  auto term = [&](int i) {
     const float4 ea = eq[i];
     const float4 a = o[i];
     const float3 d = pair_disp<PRECISE>(bh, bl, a, PRECISE ? lo[i] : a);
@@ -294,11 +294,18 @@ __device__ __forceinline__ float sum_moved32_wrap(const float4* o, const float4*
     const float dz = wrapf(d.z, H.Lf[2]);
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     const float ir = rsqrt_nr(r2);
-    const float lj = ((ljmask >> i) & 1u) ? lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x) : 0.f;
+    const float lj = (NLEN == 0 || ((ljmask >> i) & 1u)) ? lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x)
+                                                         : 0.f;
     const float cl = (ea.y * qb.y) * ir;
     const bool ok = r2 > 0.f;
     acc += ok ? lj + cl : 0.f;
     abs += ok ? fabsf(lj) + fabsf(cl) : 0.f;
+  };
+  if (NLEN > 0) {
+#pragma unroll
+    for (int i = 0; i < (NLEN > 0 ? NLEN : 1); i++) term(i);
+  } else {
+    for (int i = 0; i < len; i++) term(i);
   }
   return acc;
 }
@@ -321,14 +328,14 @@ __device__ __forceinline__ float sum_moved32_cf(const float4* o, const float4* l
   const float R = R2 * iR;
   const float tx = bh.x + bh.x, ty = bh.y + bh.y, tz = bh.z + bh.z;
   float lj_acc = 0.f, phi = 0.f, lj_abs = 0.f, c_abs = 0.f;
-#pragma unroll (NLEN > 0 ? NLEN : 1)
-  for (int i = 0; i < (NLEN > 0 ? NLEN : len); i++) {
+  auto term = [&](int i) {
     const float4 a = o[i];
     const float4 ea = eq[i];
     const float3 d = pair_disp<PRECISE>(bh, bl, a, PRECISE ? lo[i] : a);
     const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
     const float ir = rsqrt_nr(r2);
-    const float lj = ((ljmask >> i) & 1u) ? lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x) : 0.f;
+    const float lj = (NLEN == 0 || ((ljmask >> i) & 1u)) ? lj32(rcp_nr(r2), a.w, sb, ea.x, qb.x)
+                                                         : 0.f;
     const float num = fmaf(tx, a.x, fmaf(ty, a.y, fmaf(tz, a.z, -(use_new ? ea.w : ea.z))));
     const float w = ir * rcp_approx(fmaf(r2, ir, R));
     const bool ok = r2 > 0.f;
@@ -337,6 +344,12 @@ __device__ __forceinline__ float sum_moved32_cf(const float4* o, const float4* l
     lj_abs += ok ? fabsf(lj) : 0.f;
     phi += c;
     c_abs += fabsf(c);
+  };
+  if (NLEN > 0) {
+#pragma unroll
+    for (int i = 0; i < (NLEN > 0 ? NLEN : 1); i++) term(i);
+  } else {
+    for (int i = 0; i < len; i++) term(i);
   }
   const float f = qb.y * iR;
   abs += lj_abs + fabsf(f) * (c_abs + fabsf(qm));
