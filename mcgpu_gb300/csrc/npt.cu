@@ -233,10 +233,20 @@ __global__ void k_vc_scatter(Pool P, const int* mol_chain, const VolMove* vm, Mo
 }
 
 // Sorts each cell's members by index (deterministic candidate order); the
-// work item of molecule mol0 + k sorts cell k.
-__global__ void k_vc_sort(Pool P, const int* mol_chain, const VolMove* vm, MolRanges R,
-                          int n_items) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+// work item of molecule mol0 + k sorts cell k, one warp per work item
+// (blocks of kVcSortWarps warps): the members are read into shared memory
+// and each is written at its rank (the number of smaller members: the
+// indexes are distinct).  A cell of more than kVcSortMax members (a box of
+// fewer than three cells per edge) is sorted by lane 0 in place.
+constexpr int kVcSortWarps = 8;
+constexpr int kVcSortMax = 384;
+
+__global__ void __launch_bounds__(32 * kVcSortWarps) k_vc_sort(Pool P, const int* mol_chain,
+                                                               const VolMove* vm, MolRanges R,
+                                                               int n_items) {
+  __shared__ int buf[kVcSortWarps][kVcSortMax];
+  const int wi = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * kVcSortWarps + wi;
   if (b >= n_items) return;
   const int m = range_mol(R, 0, b);
   const int c = mol_chain[m];
@@ -245,6 +255,19 @@ __global__ void k_vc_sort(Pool P, const int* mol_chain, const VolMove* vm, MolRa
   if (m - H.mol0 >= H.vncell[0] * H.vncell[1] * H.vncell[2]) return;
   int* v = P.vc_mol + P.vc_start[m];
   const int n = P.vc_cnt[m];
+  if (n <= kVcSortMax) {
+    int* sb = buf[wi];
+    for (int i = lane; i < n; i += 32) sb[i] = v[i];
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) {
+      const int key = sb[i];
+      int rank = 0;
+      for (int k = 0; k < n; k++) rank += sb[k] < key;
+      v[rank] = key;
+    }
+    return;
+  }
+  if (lane != 0) return;
   for (int a = 1; a < n; a++) {
     const int key = v[a];
     int k = a - 1;
@@ -844,12 +867,72 @@ __device__ __forceinline__ void vol_atoms32(const float4* so, const float2* sq, 
   }
 }
 
-// E(m, j > m) of a mixed chain's molecule m at V' (.y; a volume move, whose
-// U(V) is the chain's running energy) or, with init, at V (.x; any chain in
-// state 1), with FP32 pair terms (per-pair minimum image, the chain kernel's
-// arithmetic) summed in double-float; eabs2 gets the sums of the terms'
-// magnitudes.  The in-range test is the FP32 screen with the FP64 re-test
-// inside its guard band: the FP64 test's set exactly.
+// E(V') - E(V) of neighbour atom b with every atom of molecule m, for a pair
+// of molecules in range at both volumes that uses the anchors' image at
+// both.  (bx..lz) is b relative to m's anchor at V (double-float), (ex, ey,
+// ez) the change of the anchor difference from V to V', (s' - s) D: every
+// atom pair's displacement changes by it, so r'^2 - r^2 = 2 d.delta +
+// delta^2, a small number with a small relative error, and
+//   1/r' - 1/r      = -(r'^2 - r^2) / (r r' (r + r')),
+//   t' - t          = -sigma^2 (r'^2 - r^2) / (r^2 r'^2),   t = sigma^2/r^2,
+//   t'^3 - t^3      = (t' - t)(t'^2 + t' t + t^2),  t'^6 - t^6 = (t'^3 - t^3)(t'^3 + t^3)
+// give each pair's change without the cancellation of two FP32 energies.
+// a32 gets the magnitude that bounds its rounding: the same expressions with
+// |r'^2 - r^2| replaced by the sum of its terms' magnitudes.  A pair that
+// coincides at either volume is taken as the difference of the two direct
+// terms (the reference skips r = 0).
+__device__ __forceinline__ void vol_atoms_delta(const float4* so, const float2* sq, int len,
+                                                float bx, float by, float bz, float lx, float ly,
+                                                float lz, float ex, float ey, float ez,
+                                                float sig_b, float2 qb, float& e32, float& a32) {
+  for (int i = 0; i < len; i++) {
+    const float4 a4 = so[i];
+    const float2 ea = sq[i];
+    const float dx = (bx - a4.x) + lx, dy = (by - a4.y) + ly, dz = (bz - a4.z) + lz;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float q = fmaf(fmaf(2.f, dx, ex), ex, fmaf(fmaf(2.f, dy, ey), ey, fmaf(2.f, dz, ez) * ez));
+    const float r2p = r2 + q;
+    const float ee = ea.x * qb.x, cq = ea.y * qb.y, s2 = a4.w * sig_b;
+    if (!(r2 > 0.f) || !(r2p > 0.f)) {
+      // degenerate pair: the two direct terms (each only where r > 0)
+      if (r2p > 0.f) {
+        const float lj = lj32(rcp_nr(r2p), a4.w, sig_b, ea.x, qb.x), cl = cq * rsqrt_nr(r2p);
+        e32 += lj + cl;
+        a32 += fabsf(lj) + fabsf(cl);
+      }
+      if (r2 > 0.f) {
+        const float lj = lj32(rcp_nr(r2), a4.w, sig_b, ea.x, qb.x), cl = cq * rsqrt_nr(r2);
+        e32 -= lj + cl;
+        a32 += fabsf(lj) + fabsf(cl);
+      }
+      continue;
+    }
+    const float qa = fabsf(2.f * dx * ex) + fabsf(2.f * dy * ey) + fabsf(2.f * dz * ez) +
+                     fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+    const float ir = rsqrt_nr(r2), irp = rsqrt_nr(r2p);
+    const float ir2 = rcp_nr(r2), ir2p = rcp_nr(r2p);
+    const float w = ir * irp * rcp_approx(fmaf(r2, ir, r2p * irp));  // 1 / (r r' (r + r'))
+    const float dcl = cq * (-q * w);
+    const float t = s2 * ir2;
+    const float g = s2 * ir2 * ir2p;                                  // sigma^2 / (r^2 r'^2)
+    const float tp = fmaf(-q, g, t);
+    const float t3 = t * t * t, tp3 = tp * tp * tp;
+    const float d3 = (-q * g) * fmaf(tp, tp, fmaf(tp, t, t * t));
+    const float dlj = ee * (d3 * (tp3 + t3) - d3);
+    e32 += dlj + dcl;
+    const float tm = fmaxf(t, tp), tm2 = tm * tm;
+    a32 += qa * (fabsf(cq) * w + fabsf(ee) * g * tm2 * (6.f * tm2 * tm + 3.f));
+  }
+}
+
+// E(m, j > m) of a mixed chain's molecule m: with init, at V (.x; any chain
+// in state 1); for a volume move, the change E(V') - E(V) (.y), the pairs in
+// range at both volumes by vol_atoms_delta, the others (crossing the cutoff,
+// or taking their own images) as the difference of the direct terms.  FP32
+// pair terms (the chain kernel's arithmetic) summed in double-float; eabs2
+// gets the sums of the magnitudes that bound their rounding.  The in-range
+// test is the FP32 screen with the FP64 re-test inside its guard band: the
+// FP64 test's set exactly.
 __global__ void __launch_bounds__(kVolThreads, 8) k_vol_pair_sums32(Pool P, const int* mol_chain,
                                                                  const VolMove* vm, int m_begin,
                                                                  MolRanges R, double2* emol2,
@@ -866,9 +949,12 @@ __global__ void __launch_bounds__(kVolThreads, 8) k_vol_pair_sums32(Pool P, cons
   const int c = mol_chain[m];
   const VolMove& v = vm[c];
   const ChainHdr& H = P.hdr[c];
-  // init: a chain's energy at its current box; else U(V') of a mixed move
+  // init: a chain's energy at its current box; else dU of a mixed move
   if (!(v.state == 1 && (H.vol_mixed || init))) return;
-  const int w0 = init ? 0 : 1;
+  const bool delta = !init;
+  __shared__ float sm1[3];   // s - 1 per edge, s = L'/L
+  if (delta && threadIdx.x < 3)
+    sm1[threadIdx.x] = (float)(v.box[1].L[threadIdx.x] / v.box[0].L[threadIdx.x] - 1.0);
   vc_stencil(P, H, m, S);
   const int a0 = P.mstart[m], len = P.mlen[m] & 255;
   const int2 pi = P.mpi[m];
@@ -893,7 +979,8 @@ __global__ void __launch_bounds__(kVolThreads, 8) k_vol_pair_sums32(Pool P, cons
       int f = 0, j = 0;
       if (t < n_cand) {
         j = vc_candidate(P, S, t, kc);
-        if (vc_takes(S, kc, j, m)) f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, w0, 1);
+        if (vc_takes(S, kc, j, m))
+          f = vol_screen(P, H, vb, so, spa, pi.y, Am, j, reach2, sf, 0, delta ? 2 : 1);
       }
       vol_append(ent, wcnt, j, f, r);
     }
@@ -912,6 +999,30 @@ __global__ void __launch_bounds__(kVolThreads, 8) k_vol_pair_sums32(Pool P, cons
       const float2 qb = P.aeq[bb];
       const uint4 Aj = P.mfix[j];
       const float rad_j = P.mrad[j];
+      const float rr = rad_m + rad_j;
+      if (delta && f == 3) {
+        float3 Dh, Dl, Dh1, Dl1;
+        vol_fixdiff(Aj, Am, vb[0], Dh, Dl);
+        vol_fixdiff(Aj, Am, vb[1], Dh1, Dl1);
+        const bool wrap = fabsf(Dh.x) + rr > 0.5f * vb[0].Lf[0] - 1e-3f ||
+                          fabsf(Dh.y) + rr > 0.5f * vb[0].Lf[1] - 1e-3f ||
+                          fabsf(Dh.z) + rr > 0.5f * vb[0].Lf[2] - 1e-3f ||
+                          fabsf(Dh1.x) + rr > 0.5f * vb[1].Lf[0] - 1e-3f ||
+                          fabsf(Dh1.y) + rr > 0.5f * vb[1].Lf[1] - 1e-3f ||
+                          fabsf(Dh1.z) + rr > 0.5f * vb[1].Lf[2] - 1e-3f;
+        if (!wrap) {
+          const float bx = Dh.x + ob.x, by = Dh.y + ob.y, bz = Dh.z + ob.z;
+          const float lx = ((Dh.x - (bx - (bx - Dh.x))) + (ob.x - (bx - Dh.x))) + Dl.x;
+          const float ly = ((Dh.y - (by - (by - Dh.y))) + (ob.y - (by - Dh.y))) + Dl.y;
+          const float lz = ((Dh.z - (bz - (bz - Dh.z))) + (ob.z - (bz - Dh.z))) + Dl.z;
+          float e32 = 0.f, a32 = 0.f;
+          vol_atoms_delta(so, sq, len, bx, by, bz, lx, ly, lz, Dh.x * sm1[0], Dh.y * sm1[1],
+                          Dh.z * sm1[2], ob.w, qb, e32, a32);
+          ff_add(eh[1], el[1], e32);
+          ab[1] += a32;
+          continue;
+        }
+      }
 #pragma unroll
       for (int w = 0; w < 2; w++) {
         if (!(f & (1 << w))) continue;
@@ -924,14 +1035,15 @@ __global__ void __launch_bounds__(kVolThreads, 8) k_vol_pair_sums32(Pool P, cons
         const float ly = ((Dh.y - (by - (by - Dh.y))) + (ob.y - (by - Dh.y))) + Dl.y;
         const float lz = ((Dh.z - (bz - (bz - Dh.z))) + (ob.z - (bz - Dh.z))) + Dl.z;
         float e32 = 0.f, a32 = 0.f;
-        const float rr = rad_m + rad_j;
         if (fabsf(Dh.x) + rr > 0.5f * B.Lf[0] - 1e-3f || fabsf(Dh.y) + rr > 0.5f * B.Lf[1] - 1e-3f ||
             fabsf(Dh.z) + rr > 0.5f * B.Lf[2] - 1e-3f)
           vol_atoms32<true>(so, sq, len, bx, by, bz, lx, ly, lz, ob.w, qb, B, e32, a32);
         else
           vol_atoms32<false>(so, sq, len, bx, by, bz, lx, ly, lz, ob.w, qb, B, e32, a32);
-        ff_add(eh[w], el[w], e32);
-        ab[w] += a32;
+        // the change of a volume move: +E(V') - E(V), both into .y
+        const int wo = delta ? 1 : w;
+        ff_add(eh[wo], el[wo], (delta && w == 0) ? -e32 : e32);
+        ab[wo] += a32;
       }
     }
     __syncthreads();
@@ -966,10 +1078,15 @@ __global__ void __launch_bounds__(kVolThreads, 8) k_vol_pair_sums32(Pool P, cons
 
 // Ordered per-chain sums of emol2 (and, for FP32 energies, of the term
 // magnitudes eabs2) for the chains in state `want`.
-__global__ void k_vol_sums(Pool P, const VolMove* vm, const double2* emol2, const double2* eabs2,
-                           double2* out, double2* out_abs, MolRanges R, int want) {
-  __shared__ double2 red[256];
-  __shared__ double2 rab[256];
+constexpr int kVolSumThreads = 1024;
+
+__global__ void __launch_bounds__(kVolSumThreads) k_vol_sums(Pool P, const VolMove* vm,
+                                                             const double2* emol2,
+                                                             const double2* eabs2, double2* out,
+                                                             double2* out_abs, MolRanges R,
+                                                             int want) {
+  __shared__ double2 red[kVolSumThreads];
+  __shared__ double2 rab[kVolSumThreads];
   const int c = range_chain(R, blockIdx.x);
   if (vm[c].state != want) return;
   const ChainHdr& H = P.hdr[c];
@@ -1020,25 +1137,26 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
   double e_old = H.energy, e_new = 0.0;
   int ok = 0;
   if (v.state != 2) {
-    // a mixed move's U(V) is the running energy (error bound run_err) and
-    // its U(V') the FP32 total; too close to call, U(V') is taken again in
-    // double-float (state 6), then both totals in double-float (state 4),
-    // then both in FP64 (state 5); an FP64 chain has both FP64 totals
+    // a mixed move's dU is summed pair by pair in FP32 (esum.y; its bound
+    // does not involve the running energy U(V)); too close to call, U(V') is
+    // taken in double-float with U(V) the running energy (state 6), then both
+    // totals in double-float (state 4), then both in FP64 (state 5); an FP64
+    // chain has both FP64 totals
     const bool mixed = v.state == 1 && H.vol_mixed;
     const bool vprime = v.state == 6;
     const bool dfl = v.state == 4;
     e_old = (mixed || vprime) ? H.energy : esum[c].x;
-    e_new = esum[c].y;
+    e_new = mixed ? H.energy + esum[c].y : esum[c].y;
     const double vo = H.L[0] * H.L[1] * H.L[2];
     const double vn = v.L[0] * v.L[1] * v.L[2];
     // the tail correction E_LRC = lrc_v / V changes with the volume
     const double d_lrc = H.lrc_v / vn - H.lrc_v / vo;
-    const double arg = -((e_new - e_old) + d_lrc + H.pressure * (vn - vo)) / H.kT +
+    const double du = mixed ? esum[c].y : e_new - e_old;
+    const double arg = -(du + d_lrc + H.pressure * (vn - vo)) / H.kT +
                        (double)(H.n_mol + 1) * v.dlnv;
     double err_old = 0.0, err_new = 0.0;
     if (mixed) {
-      err_old = H.run_err;
-      err_new = kTieRel * eabs[c].y;
+      err_new = kTieRel * eabs[c].y;   // the bound of dU
     } else if (vprime) {
       err_old = H.run_err;
       err_new = kDfRel * eabs[c].y;
@@ -1059,7 +1177,9 @@ __global__ void k_vol_decide(Pool P, VolMove* vm, const double2* esum, const dou
     ok = (arg >= 0.0) || (exp(arg) >= v.u);
     if (ok) {
       H.energy = e_new;
-      H.run_err = err_new;
+      // a mixed move adds dU to the running energy and its bound to run_err;
+      // the other tiers install a fresh total with its own bound
+      H.run_err = mixed ? H.run_err + err_new : err_new;
     } else if (!mixed && !vprime) {
       H.energy = e_old;
       H.run_err = err_old;
@@ -1154,7 +1274,8 @@ cudaError_t launch_chain_energy(Pool P, const int* mol_chain, int n_mol_total, V
   k_vc_count<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
   k_vc_scan<<<nc, 256, 0, st>>>(P, vm, act, nc);
   k_vc_scatter<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
-  k_vc_sort<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
+  k_vc_sort<<<(items + kVcSortWarps - 1) / kVcSortWarps, 32 * kVcSortWarps, 0, st>>>(
+        P, mol_chain, vm, act, items);
   const int chunk = act.act_pref ? items : (1 << 20);
   for (int m0 = 0; m0 < items; m0 += chunk) {
     const int n = items - m0 < chunk ? items - m0 : chunk;
@@ -1163,7 +1284,7 @@ cudaError_t launch_chain_energy(Pool P, const int* mol_chain, int n_mol_total, V
     else
       k_vol_pair_sums32<<<n, kVolThreads, 0, st>>>(P, mol_chain, vm, m0, act, emol2, eabs2, 1);
   }
-  k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 1);
+  k_vol_sums<<<nc, kVolSumThreads, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 1);
   k_vol_self_energy<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, act, nc, f64 ? 1 : 0);
   return cudaGetLastError();
 }
@@ -1187,7 +1308,8 @@ cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, V
     k_vc_count<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
     k_vc_scan<<<nc, 256, 0, st>>>(P, vm, act, nc);
     k_vc_scatter<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
-    k_vc_sort<<<gb, 256, 0, st>>>(P, mol_chain, vm, act, items);
+    k_vc_sort<<<(items + kVcSortWarps - 1) / kVcSortWarps, 32 * kVcSortWarps, 0, st>>>(
+        P, mol_chain, vm, act, items);
   }
   auto pairs = [&](bool f64, int pass) {
     if (items <= 0) return;
@@ -1209,7 +1331,7 @@ cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, V
   };
   if (has64) pairs(true, 0);
   if (has32) pairs(false, 0);
-  k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 1);
+  k_vol_sums<<<nc, kVolSumThreads, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 1);
   k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, trace, trace_slot,
                                                 trace_stride, act, nc, 0);
   if (has32) {
@@ -1219,17 +1341,17 @@ cudaError_t launch_volume_phase(Pool P, const int* mol_chain, int n_mol_total, V
     const int grid = kVolListGrid;
     k_vol_list<<<1, 32, 0, st>>>(P, vm, act, nc, 6, vlist);
     k_vol_pair_sums_df<<<grid, kVolThreads, 0, st>>>(P, mol_chain, vm, vlist, nc, emol2, eabs2);
-    k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 6);
+    k_vol_sums<<<nc, kVolSumThreads, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 6);
     k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, trace, trace_slot,
                                                   trace_stride, act, nc, 3);
     k_vol_list<<<1, 32, 0, st>>>(P, vm, act, nc, 4, vlist);
     k_vol_pair_sums_df<<<grid, kVolThreads, 0, st>>>(P, mol_chain, vm, vlist, nc, emol2, eabs2);
-    k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 4);
+    k_vol_sums<<<nc, kVolSumThreads, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 4);
     k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, trace, trace_slot,
                                                   trace_stride, act, nc, 1);
     k_vol_list<<<1, 32, 0, st>>>(P, vm, act, nc, 5, vlist);
     k_vol_pair_sums_list<<<grid, kVolThreads, 0, st>>>(P, mol_chain, vm, vlist, nc, emol2);
-    k_vol_sums<<<nc, 256, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 5);
+    k_vol_sums<<<nc, kVolSumThreads, 0, st>>>(P, vm, emol2, eabs2, esum, esum_abs, act, 5);
     k_vol_decide<<<(nc + 127) / 128, 128, 0, st>>>(P, vm, esum, esum_abs, trace, trace_slot,
                                                   trace_stride, act, nc, 2);
   }
