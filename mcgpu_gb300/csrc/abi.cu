@@ -567,6 +567,10 @@ static int box_grid(const mcgpu_box* b, int n_cand) {
   return std::max(1, std::min(g, b->max_grid));
 }
 
+// A host-drawn Euler move with its rotation's cosines and sines taken on the
+// host by the C library, from the angle in radians formed as the reference
+// forms it (SimulationStep.cpp:400-422): the reference's values exactly, and
+// no FP64 trigonometry on the device's critical path.
 static Proposal host_proposal(const mcgpu_move* mv) {
   Proposal p;
   std::memset(&p, 0, sizeof(p));
@@ -574,6 +578,13 @@ static Proposal host_proposal(const mcgpu_move* mv) {
   p.mode = MCGPU_ROT_EULER;
   p.dx = mv->dx; p.dy = mv->dy; p.dz = mv->dz;
   p.r0 = mv->rx; p.r1 = mv->ry; p.r2 = mv->rz;
+  const double deg[3] = {mv->rx, mv->ry, mv->rz};
+  for (int k = 0; k < 3; k++) {
+    const double rad = deg[k] * 3.14159265358979 / 180.0;
+    p.cs[k] = std::cos(rad);
+    p.sn[k] = std::sin(rad);
+  }
+  p.trig = 1;
   return p;
 }
 

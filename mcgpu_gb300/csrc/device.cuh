@@ -229,8 +229,9 @@ __device__ __forceinline__ int uidx(unsigned r, int n) {
 
 // A trial move: vertex, translation, rotation (Euler degrees or axis+angle).
 struct Proposal {
-  int mol, vertex, mode, pad;
+  int mol, vertex, mode, trig;   // trig: cos/sin below hold the Euler angles' values
   double dx, dy, dz, r0, r1, r2, r3, u;
+  double cs[3], sn[3];           // host-drawn Euler moves: cos, sin of each angle
 };
 
 // Draws the proposal of (seed, chain, step): the counter layout and the
@@ -247,7 +248,7 @@ __device__ inline Proposal draw_proposal(unsigned long long seed, unsigned chain
   p.mol = uidx(a.x, n_mol);
   p.vertex = uidx(a.y, mlen_chain[p.mol] & 255);
   p.mode = mode;
-  p.pad = 0;
+  p.trig = 0;
   p.dx = __dadd_rn(__dmul_rn(2.0 * max_t, u01(a.z)), -max_t);
   p.dy = __dadd_rn(__dmul_rn(2.0 * max_t, u01(a.w)), -max_t);
   p.dz = __dadd_rn(__dmul_rn(2.0 * max_t, u01(c.x)), -max_t);
@@ -283,7 +284,11 @@ struct Rot {
 __device__ inline Rot make_rot(const Proposal& p) {
   Rot R;
   R.mode = p.mode;
-  if (p.mode == MCGPU_ROT_EULER) {
+  if (p.mode == MCGPU_ROT_EULER && p.trig) {
+    R.cx = p.cs[0]; R.sx = p.sn[0];
+    R.cy = p.cs[1]; R.sy = p.sn[1];
+    R.cz = p.cs[2]; R.sz = p.sn[2];
+  } else if (p.mode == MCGPU_ROT_EULER) {
     sincos(__dmul_rn(p.r0, 3.14159265358979) / 180.0, &R.sx, &R.cx);
     sincos(__dmul_rn(p.r1, 3.14159265358979) / 180.0, &R.sy, &R.cy);
     sincos(__dmul_rn(p.r2, 3.14159265358979) / 180.0, &R.sz, &R.cz);
