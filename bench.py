@@ -44,25 +44,26 @@ WORKLOAD = ("512 independent NVT water chains (3-site TIP3P-like, rigid), N log-
             "+-0.15 A / +-15 deg random-axis moves, Philox proposals, on-device accept")
 FP32_FLOPS_PER_PAIR = 38   # per atom pair, fixed by convention from the reference's arithmetic
 # DRAM bytes (read + write) per launch of k_chain_steps on this workload,
-# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum of the 7th
-# launch, L2 flushed between bench steps), by tile
-# (threads, chains per CTA, steps per launch, lanes per molecule).  A launch
-# reads the chains' rows about once whatever the CTA shape (the captures
-# differ by 0.3 %), so a tile without its own capture reports the one of the
-# nearest captured tile with the same steps per launch, and names it.
-CHAIN_TRAFFIC_BYTES = {(256, 1, 64, 0): 33.60e6, (256, 1, 64, 1): 33.61e6,
-                       (160, 1, 64, 1): 33.72e6}
+# measured with ncu (dram__bytes_read.sum + dram__bytes_write.sum, mean of six
+# launches after the untimed steps, L2 flushed between bench steps), by tile
+# (threads, chains per CTA, steps per launch, lanes per molecule), each with
+# the version of the chain kernel it was captured on.  A capture is reported
+# only for its own tile and kernel version; otherwise the line's traffic is
+# null and says why (a launch reads the chains' rows about once whatever the
+# tile, ~34 MB, but a figure from another tile or kernel is not this run's).
+CHAIN_KERNEL_VERSION = "pair code shared by both placements, LJ mask in the header, FP32-only step"
+CHAIN_TRAFFIC_BYTES = {(160, 1, 64, 1): (34.22e6, CHAIN_KERNEL_VERSION)}
 
 
 def chain_traffic(tile):
-    """(bytes per launch, the tile they were captured on) or (None, None)."""
-    if tile in CHAIN_TRAFFIC_BYTES:
-        return CHAIN_TRAFFIC_BYTES[tile], tile
-    same = [t for t in CHAIN_TRAFFIC_BYTES if t[2] == tile[2]]
-    if not same:
-        return None, None
-    t = min(same, key=lambda t: (abs(t[0] * t[1] - tile[0] * tile[1]), t[3] != tile[3]))
-    return CHAIN_TRAFFIC_BYTES[t], t
+    """(bytes per launch, note): the capture of this tile on the current
+    kernel version, else (None, why not)."""
+    hit = CHAIN_TRAFFIC_BYTES.get(tuple(tile))
+    if hit is None:
+        return None, "no ncu capture of this tile"
+    if hit[1] != CHAIN_KERNEL_VERSION:
+        return None, "the capture of this tile predates the current chain kernel"
+    return hit[0], "ncu capture of this tile and kernel version"
 # L2 sector throughput peak implied by the same captures: lts__t_sectors.sum.per_second
 # (32 B sectors) over lts__t_sectors.sum.pct_of_peak_sustained_elapsed (36.25 and 36.37
 # TB/s on the two tiles); MEASURED_PEAKS.json holds no L2 figure
@@ -630,7 +631,7 @@ def main():
     fp32_peak = sm_count * 128 * 2 * 2.07e9 / 1e12
     achieved = flops_per_launch / kernel_s_per_launch / 1e12
     mean_pairs_per_move = pairs / moves_local
-    traffic, traffic_tile = chain_traffic((threads, cpc, spl, lanes))
+    traffic, traffic_note = chain_traffic((threads, cpc, spl, lanes))
     # 2 n_in a^2 pairs per move (a = 3 on water): 2 n_in a = pairs / a atom rows
     l2_bytes_move = (mean_pairs_per_move / ATOMS_PER_WATER + 2 * ATOMS_PER_WATER) * 16
 
@@ -700,7 +701,7 @@ def main():
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                      "traffic": traffic,
                      "traffic_unit": "bytes per launch (ncu capture)",
-                     "traffic_tile": list(traffic_tile) if traffic_tile else None,
+                     "traffic_note": traffic_note,
                      "kernel": "k_chain_steps",
                      "work": f"{FP32_FLOPS_PER_PAIR} flop x {mean_pairs_per_move:.1f} atom pairs "
                              "per move (device-counted, old+new)",

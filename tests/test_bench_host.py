@@ -32,9 +32,13 @@ def test_clock_summary():
 
 
 def test_chain_traffic_lookup():
+    """A capture is reported only for its own tile and kernel version."""
     b = _bench()
-    for tile, v in b.CHAIN_TRAFFIC_BYTES.items():
-        assert b.chain_traffic(tile) == (v, tile)
-    v, t = b.chain_traffic((192, 1, 64, 0))
-    assert t is not None and t[2] == 64 and v == b.CHAIN_TRAFFIC_BYTES[t]
-    assert b.chain_traffic((128, 2, 5, 0)) == (None, None)
+    for tile, (v, ver) in b.CHAIN_TRAFFIC_BYTES.items():
+        got, note = b.chain_traffic(tile)
+        assert (got == v) == (ver == b.CHAIN_KERNEL_VERSION), (tile, note)
+    got, note = b.chain_traffic((192, 1, 64, 0))
+    assert got is None and "no ncu capture" in note
+    b.CHAIN_TRAFFIC_BYTES[(96, 1, 64, 0)] = (1.0, "an older kernel")
+    got, note = b.chain_traffic((96, 1, 64, 0))
+    assert got is None and "predates" in note
