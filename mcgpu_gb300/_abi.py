@@ -41,6 +41,29 @@ class BoxDesc(C.Structure):
     ]
 
 
+class TopoDesc(C.Structure):
+    _fields_ = [
+        ("n_bond", C.c_int32), ("n_angle", C.c_int32), ("n_type", C.c_int32),
+        ("max_intra_moves", C.c_int32),
+        ("bond_a1", _ip), ("bond_a2", _ip), ("bond_var", _ip),
+        ("bond_k", _dp), ("bond_eq", _dp), ("bond_len", _dp),
+        ("angle_a1", _ip), ("angle_a2", _ip), ("angle_mid", _ip), ("angle_var", _ip),
+        ("angle_k", _dp), ("angle_eq", _dp), ("angle_size", _dp),
+        ("mol_bond_start", _ip), ("mol_bond_count", _ip),
+        ("mol_angle_start", _ip), ("mol_angle_count", _ip), ("mol_type", _ip),
+        ("type_natom", _ip), ("pair_code", C.POINTER(C.c_uint8)),
+        ("max_bond_delta", C.c_double), ("max_angle_delta", C.c_double),
+        ("step_num", C.c_int64),
+    ]
+
+
+class IntraState(C.Structure):
+    _fields_ = [("max_bond_delta", C.c_double), ("max_angle_delta", C.c_double),
+                ("step_num", C.c_int64), ("bond_moves", C.c_int64),
+                ("bond_accepted", C.c_int64), ("angle_moves", C.c_int64),
+                ("angle_accepted", C.c_int64)]
+
+
 class Move(C.Structure):
     _fields_ = [("vertex", C.c_int32), ("pad0", C.c_int32),
                 ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),

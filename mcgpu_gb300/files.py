@@ -7,12 +7,14 @@ SimBox rows and writes files the reference reads:
 * ``.config``   key=value settings             ConfigScanner.cpp:20-227
 * OPLS ``.par`` atom parameter table             OplsScanner.cpp:19-110
 * ``.z``        z-matrix molecule templates      ZmatrixScanner.cpp:21-286, 290-573
+* ``oplsaa.sb`` bond and angle parameter table   SBScanner.cpp:11-148
 * z-matrix -> XYZ of each template               MathLibrary.cpp:751-903
 * box of N molecules on an FCC lattice           FileUtilities.cpp:285-642
 * ``.state``    text checkpoint (read and write) StateScanner.cpp:18-597
 * SimBox rows (coordinates, sigma/epsilon/charge, molecule ranges, primary
   indexes) after Simulation::run's keepMoleculeInBox   SimBoxBuilder.cpp:10-299,
                                                        Box.cpp:84-109, 170-179
+* SimBox bond, angle and exclusion rows          SimBoxBuilder.cpp:44-278
 * ``.pdb`` and ``.results`` outputs              Simulation.cpp:296-417
 * long-range LJ correction                       SerialCalcs.cpp:37-107
 
@@ -37,7 +39,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .workloads import BoxData
+from .workloads import PAIR_EXCLUDED, PAIR_FUDGE, PAIR_FULL, BoxData, Topology
 
 # MathLibrary.h:51 -- the reference's truncated pi (z-matrix angles, LRC)
 REF_PI = 3.14159265
@@ -475,6 +477,95 @@ def read_opls(path: str) -> OplsTable:
                 t.fourier[key] = v
         else:
             t.bad_lines.append(n)
+    return t
+
+
+# ---- bond and angle table (SBScanner.cpp) -----------------------------------------
+
+@dataclass
+class SbTable:
+    """SBScanner's maps: bond (force constant, equilibrium distance) by the
+    two atom names, angle (force constant, equilibrium angle) by end, middle
+    and end name.  Later lines overwrite earlier ones; each entry is stored
+    under both orders of its ends (SBScanner.cpp:11-61)."""
+    bonds: dict = field(default_factory=dict)     # a1 -> a2 -> (k, eq)
+    angles: dict = field(default_factory=dict)    # e1 -> mid -> e2 -> (k, eq)
+
+    def k_bond(self, a1: str, a2: str) -> float:
+        """getKBond (:124-128): -1 when the pair is not in the table."""
+        return self.bonds.get(a1, {}).get(a2, (-1.0, -1.0))[0]
+
+    def eq_bond(self, a1: str, a2: str) -> float:
+        """getEqBondDist (:130-134): -1 when the pair is not in the table."""
+        return self.bonds.get(a1, {}).get(a2, (-1.0, -1.0))[1]
+
+    def k_angle(self, e1: str, mid: str, e2: str) -> float:
+        """getKAngle (:136-141): -1 when the triple is not in the table."""
+        return self.angles.get(e1, {}).get(mid, {}).get(e2, (-1.0, -1.0))[0]
+
+    def eq_angle(self, e1: str, mid: str, e2: str) -> float:
+        """getEqAngle (:143-148): -1 when the first end or the middle is
+        missing, but 0 when only the second end is (the reference's own
+        return value for that branch)."""
+        if e1 not in self.angles or mid not in self.angles[e1]:
+            return -1.0
+        return self.angles[e1][mid].get(e2, (-1.0, 0.0))[1]
+
+
+def _substr(s: str, pos: int, n: int) -> str:
+    """std::string::substr: out_of_range when pos > size."""
+    if pos > len(s):
+        raise IndexError(pos)
+    return s[pos:pos + max(n, 0)]
+
+
+def _sb_values(rest: str) -> tuple[float, float]:
+    """``ss >> a >> b``: a failed first extraction writes 0 and stops the
+    stream; the second value is then left as the reference left it
+    (uninitialised there; 0 here)."""
+    s = _Stream(rest)
+    a = s.float()
+    b = s.float()
+    return (0.0 if a is None else a), (0.0 if b is None else b)
+
+
+def read_sb(path: str) -> SbTable:
+    """SBScanner::readInSB (SBScanner.cpp:76-108): every line not starting
+    with '*', '"' or '#' is an angle when its sixth character is '-'
+    (``E1-MD-E2 k theta``: names in columns 1-2, 4-5, 7-8, one-letter names
+    padded with a blank), else a bond (``A1-A2 k r``, columns 1-2 and 4-5,
+    values from column 7).  A line too short for its fields is skipped, as
+    the reference's out_of_range handler skips it."""
+    if not path:
+        raise FileFormatError("Error: readInOpls(): empty filename given")
+    if not os.path.isfile(path):
+        raise FileFormatError("Error: readInOpls(): could not open file (" + path + ")")
+    t = SbTable()
+    for line in _lines(path):
+        if not line or line[0] in "*\"#":
+            continue
+        try:
+            if len(line) > 5 and line[5] == "-":
+                e1, mid, e2 = _substr(line, 0, 2), _substr(line, 3, 2), _substr(line, 6, 2)
+                if _substr(line, 1, 1) == " ":
+                    e1 = e1[:1]
+                if _substr(line, 4, 1) == " ":
+                    mid = mid[:1]
+                if _substr(line, 7, 1) == " ":
+                    e2 = e2[:1]
+                k, eq = _sb_values(_substr(line, 8, len(line) - 8))
+                t.angles.setdefault(e1, {}).setdefault(mid, {})[e2] = (k, eq)
+                t.angles.setdefault(e2, {}).setdefault(mid, {})[e1] = (k, eq)
+            else:
+                a1 = _substr(line, 0, 1) if _substr(line, 1, 1) == " " else _substr(line, 0, 2)
+                a2 = _substr(line, 3, 1) if _substr(line, 4, 1) == " " else _substr(line, 3, 2)
+                if len(line) < 6:
+                    raise IndexError(6)
+                k, eq = _sb_values(_substr(line, 6, len(line) - 6))
+                t.bonds.setdefault(a1, {})[a2] = (k, eq)
+                t.bonds.setdefault(a2, {})[a1] = (k, eq)
+        except IndexError:
+            continue
     return t
 
 
@@ -978,6 +1069,124 @@ def box_rows(box: Box) -> BoxData:
                    max_rotate=float(env.max_rotation)).normalise()
 
 
+def box_topology(box: Box, sb: SbTable) -> Topology:
+    """SimBoxBuilder::addMolecules' bond, angle and exclusion rows
+    (SimBoxBuilder.cpp:44-278) of the first env.n_molecules molecules.
+
+    Atom ids resolve through the id -> index map the reference fills molecule
+    by molecule, so an id must belong to this or an earlier molecule (the
+    reference would read a null name otherwise; this raises).  An angle's
+    middle atom is its ``common`` id as the loader leaves it: z-matrix angles
+    carry 0 shifted by the copy's first atom (FileUtilities.cpp:508), so
+    their middle row is the first atom of their copy set, not the angle's
+    vertex -- the reference's rows, kept.  Force constants and equilibrium
+    values come from the ``.sb`` table by atom name (-1 when missing).  The
+    pair codes of each type come from its first molecule: excluded for the
+    atoms of a bond and the ends of an angle, 0.5 for atoms exactly three
+    bonds apart (the hop list), full otherwise; an exclusion wins over a
+    fudge, as the reference scans its exclusion list first
+    (SimulationStep.cpp:95-117).  The step counter starts at 0, for a
+    resumed run too (SimBoxBuilder.cpp:37)."""
+    env = box.env
+    n = env.n_molecules
+    if n > len(box.molecules):
+        raise FileFormatError("the environment counts %d molecules, the box holds %d"
+                              % (n, len(box.molecules)))
+    mols = box.molecules[:n]
+    n_types = max(len(env.primary), max((m.type + 1 for m in mols), default=0))
+    id_idx: dict = {}
+    id_name: dict = {}
+    b_rows = {k: [] for k in ("a1", "a2", "k", "eq", "len", "var")}
+    a_rows = {k: [] for k in ("a1", "a2", "mid", "k", "eq", "size", "var")}
+    mb_start, mb_count, ma_start, ma_count, mtype = [], [], [], [], []
+    first_of_type: dict = {}
+    atom_idx = 0
+
+    def idx(aid: int, what: str) -> int:
+        if aid not in id_idx:
+            raise FileFormatError("%s refers to atom id %d, not in this or an earlier molecule"
+                                  % (what, aid))
+        return id_idx[aid]
+
+    for i, m in enumerate(mols):
+        start = atom_idx
+        for a in m.atoms:
+            id_idx[a.id] = atom_idx
+            id_name[a.id] = a.name
+            atom_idx += 1
+        mb_start.append(len(b_rows["a1"]))
+        mb_count.append(len(m.bonds))
+        ma_start.append(len(a_rows["a1"]))
+        ma_count.append(len(m.angles))
+        mtype.append(m.type)
+        for b in m.bonds:
+            i1, i2 = idx(b.atom1, "a bond"), idx(b.atom2, "a bond")
+            n1, n2 = id_name[b.atom1], id_name[b.atom2]
+            b_rows["a1"].append(i1)
+            b_rows["a2"].append(i2)
+            b_rows["k"].append(sb.k_bond(n1, n2))
+            b_rows["eq"].append(sb.eq_bond(n1, n2))
+            b_rows["len"].append(b.distance)
+            b_rows["var"].append(1 if b.variable else 0)
+        for a in m.angles:
+            i1, i2 = idx(a.atom1, "an angle"), idx(a.atom2, "an angle")
+            im = idx(a.common, "an angle's middle")
+            n1, n2, nm = id_name[a.atom1], id_name[a.atom2], id_name[a.common]
+            a_rows["a1"].append(i1)
+            a_rows["a2"].append(i2)
+            a_rows["mid"].append(im)
+            a_rows["k"].append(sb.k_angle(n1, nm, n2))
+            a_rows["eq"].append(sb.eq_angle(n1, nm, n2))
+            a_rows["size"].append(a.value)
+            a_rows["var"].append(1 if a.variable else 0)
+        if m.type not in first_of_type:
+            first_of_type[m.type] = (m, start)
+    natom = np.zeros(n_types, np.int32)
+    codes = []
+    for t in range(n_types):
+        if t not in first_of_type:
+            continue
+        m, start = first_of_type[t]
+        na = len(m.atoms)
+        natom[t] = na
+        excl = [[] for _ in range(na)]
+        fudge = [[] for _ in range(na)]
+
+        def local(aid: int) -> int:
+            return id_idx.get(aid, -1) - start if aid in id_idx else -1
+
+        for e in list(m.bonds) + list(m.angles):
+            l1, l2 = local(e.atom1), local(e.atom2)
+            if 0 <= l1 < na and 0 <= l2 < na:
+                excl[l1].append(l2)
+                excl[l2].append(l1)
+        for h in m.hops:
+            l1, l2 = local(h.atom1), local(h.atom2)
+            if 0 <= l1 < na and 0 <= l2 < na and h.hop == 3:
+                fudge[l1].append(l2)
+                fudge[l2].append(l1)
+        c = np.full((na, na), PAIR_FULL, np.uint8)
+        for r in range(na):
+            for j in fudge[r]:
+                c[r, j] = PAIR_FUDGE
+            for j in excl[r]:
+                c[r, j] = PAIR_EXCLUDED
+        codes.append(c.ravel())
+    i32 = lambda v: np.array(v, np.int32)
+    f64 = lambda v: np.array(v, np.float64)
+    return Topology(
+        bond_a1=i32(b_rows["a1"]), bond_a2=i32(b_rows["a2"]), bond_k=f64(b_rows["k"]),
+        bond_eq=f64(b_rows["eq"]), bond_len=f64(b_rows["len"]), bond_var=i32(b_rows["var"]),
+        angle_a1=i32(a_rows["a1"]), angle_a2=i32(a_rows["a2"]), angle_mid=i32(a_rows["mid"]),
+        angle_k=f64(a_rows["k"]), angle_eq=f64(a_rows["eq"]), angle_size=f64(a_rows["size"]),
+        angle_var=i32(a_rows["var"]), mol_bond_start=i32(mb_start), mol_bond_count=i32(mb_count),
+        mol_angle_start=i32(ma_start), mol_angle_count=i32(ma_count), mol_type=i32(mtype),
+        type_natom=natom,
+        pair_code=np.concatenate(codes).astype(np.uint8) if codes else np.zeros(0, np.uint8),
+        max_bond_delta=float(env.max_bond_delta), max_angle_delta=float(env.max_angle_delta),
+        max_intra_moves=15, step_num=0).normalise()
+
+
 # ---- .state (StateScanner.cpp) ----------------------------------------------------
 
 def _state_env(line: str) -> Environment:
@@ -1270,12 +1479,16 @@ def extension(path: str) -> str:
 
 @dataclass
 class SimInput:
-    """What Simulation's constructor and run() start from."""
+    """What Simulation's constructor and run() start from.  ``topology``:
+    the bond, angle and exclusion rows (flexible-molecule terms); a
+    ``.state`` start has no ``.sb`` table behind it (the reference reads the
+    table for configurations only), so its force constants are -1."""
     box: Box
     rows: BoxData
     steps: int
     start_step: int
     config: Config | None = None
+    topology: Topology | None = None
 
 
 def load(path: str, implied_angles: bool = False, seed_from_file: bool = False) -> SimInput:
@@ -1298,11 +1511,13 @@ def load(path: str, implied_angles: bool = False, seed_from_file: bool = False) 
                 "Error: loadBoxData(): The number of molecules read from the Z Matrix file (%d)"
                 " does not equal the number of primary index definitions in the config file "
                 "(%d)" % (len(templates), cfg.env.primary_defs))
+        sb = read_sb(sb_dir + "/oplsaa.sb")
         box = build_box(cfg.env, templates)
         keep_in_box(box)
-        return SimInput(box, box_rows(box), cfg.steps, 0, cfg)
+        return SimInput(box, box_rows(box), cfg.steps, 0, cfg, box_topology(box, sb))
     if ext == "state":
         box = read_state(path, seed_from_file)
         keep_in_box(box)
-        return SimInput(box, box_rows(box), DEFAULT_STEP_COUNT, box.start_step, None)
+        return SimInput(box, box_rows(box), DEFAULT_STEP_COUNT, box.start_step, None,
+                        box_topology(box, SbTable()))
     raise FileFormatError("Must specify a config or state file")

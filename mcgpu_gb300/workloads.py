@@ -115,6 +115,112 @@ class BoxData:
         return self
 
 
+# Pair codes of the intramolecular non-bonded terms: excluded (bonded or an
+# angle's ends), scaled by 0.5 (three bonds apart), full.
+PAIR_EXCLUDED, PAIR_FUDGE, PAIR_FULL = 0, 1, 2
+
+
+@dataclass
+class Topology:
+    """The SimBox rows of flexible molecules (src/Metropolis/SimBox.h:160-300,
+    filled by SimBoxBuilder.cpp:136-278): per bond its two atoms (box atom
+    indexes), force constant, equilibrium and current length, variable flag;
+    per angle its two ends and middle atom, force constant, equilibrium and
+    current size (degrees), variable flag; per molecule its bond and angle
+    ranges and type; per molecule type the intramolecular pair codes
+    (``pair_code``: each type's natom x natom matrix, row-major,
+    concatenated), built from the exclusion and fudge lists of the first
+    molecule of the type.  ``max_bond_delta`` / ``max_angle_delta`` are the
+    move widths, ``max_intra_moves`` the cap on bonds or angles moved at once
+    (15 in the reference), ``step_num`` the simulation step the tuning
+    counts from."""
+    bond_a1: np.ndarray
+    bond_a2: np.ndarray
+    bond_k: np.ndarray
+    bond_eq: np.ndarray
+    bond_len: np.ndarray
+    bond_var: np.ndarray
+    angle_a1: np.ndarray
+    angle_a2: np.ndarray
+    angle_mid: np.ndarray
+    angle_k: np.ndarray
+    angle_eq: np.ndarray
+    angle_size: np.ndarray
+    angle_var: np.ndarray
+    mol_bond_start: np.ndarray
+    mol_bond_count: np.ndarray
+    mol_angle_start: np.ndarray
+    mol_angle_count: np.ndarray
+    mol_type: np.ndarray
+    type_natom: np.ndarray
+    pair_code: np.ndarray
+    max_bond_delta: float = 0.06
+    max_angle_delta: float = 3.1
+    max_intra_moves: int = 15
+    step_num: int = 0
+
+    @property
+    def n_bond(self) -> int:
+        return int(self.bond_a1.shape[0])
+
+    @property
+    def n_angle(self) -> int:
+        return int(self.angle_a1.shape[0])
+
+    @property
+    def n_type(self) -> int:
+        return int(self.type_natom.shape[0])
+
+    @property
+    def flex_bonds(self) -> bool:
+        """SimBox::hasFlexibleBonds: some bond is variable."""
+        return bool(np.any(self.bond_var != 0))
+
+    @property
+    def flex_angles(self) -> bool:
+        """SimBox::hasFlexibleAngles: some angle is variable."""
+        return bool(np.any(self.angle_var != 0))
+
+    def copy(self) -> "Topology":
+        return Topology(**{k: (v.copy() if isinstance(v, np.ndarray) else v)
+                           for k, v in self.__dict__.items()})
+
+    def normalise(self) -> "Topology":
+        for k in ("bond_k", "bond_eq", "bond_len", "angle_k", "angle_eq", "angle_size"):
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.float64))
+        for k in ("bond_a1", "bond_a2", "bond_var", "angle_a1", "angle_a2", "angle_mid",
+                  "angle_var", "mol_bond_start", "mol_bond_count", "mol_angle_start",
+                  "mol_angle_count", "mol_type", "type_natom"):
+            setattr(self, k, np.ascontiguousarray(getattr(self, k), dtype=np.int32))
+        self.pair_code = np.ascontiguousarray(self.pair_code, dtype=np.uint8)
+        return self
+
+    def type_codes(self, t: int) -> np.ndarray:
+        """Type t's pair-code matrix."""
+        off = int(np.sum(self.type_natom[:t].astype(np.int64) ** 2))
+        n = int(self.type_natom[t])
+        return self.pair_code[off:off + n * n].reshape(n, n)
+
+    def desc(self) -> _abi.TopoDesc:
+        """A C descriptor pointing at these rows (valid while self lives)."""
+        self.normalise()
+        d = _abi.TopoDesc()
+        d.n_bond, d.n_angle, d.n_type = self.n_bond, self.n_angle, self.n_type
+        d.max_intra_moves = int(self.max_intra_moves)
+        dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+        for k in ("bond_k", "bond_eq", "bond_len", "angle_k", "angle_eq", "angle_size"):
+            setattr(d, k, getattr(self, k).ctypes.data_as(dp))
+        for k in ("bond_a1", "bond_a2", "bond_var", "angle_a1", "angle_a2", "angle_mid",
+                  "angle_var", "mol_bond_start", "mol_bond_count", "mol_angle_start",
+                  "mol_angle_count", "mol_type", "type_natom"):
+            setattr(d, k, getattr(self, k).ctypes.data_as(ip))
+        d.pair_code = self.pair_code.ctypes.data_as(C.POINTER(C.c_uint8))
+        d.max_bond_delta = float(self.max_bond_delta)
+        d.max_angle_delta = float(self.max_angle_delta)
+        d.step_num = int(self.step_num)
+        return d
+
+
 # ---- geometry -----------------------------------------------------------------
 
 def water_template() -> tuple[np.ndarray, np.ndarray, np.ndarray, np.ndarray, int]:

@@ -920,3 +920,346 @@ int orc_build_centres(int n, double L, double dmin, uint64_t seed, double* out) 
   free(next);
   return rc;
 }
+
+/* ---- flexible molecules ------------------------------------------------------
+ *
+ * The reference compiles these functions but calls them only with
+ * ENABLE_INTRA true (src/Metropolis/SimulationStep.h:15 sets it false); the
+ * restatement follows them as they run with it true: molecule energies carry
+ * the intramolecular term (SimulationStep.cpp:15-18), a trial move is the
+ * rigid move followed by the intramolecular one (:424-428) and a rollback
+ * also restores the bond lengths and angle sizes (:731-749).  Random draws
+ * come from the C library's rand(), as the reference's randomReal
+ * (MathLibrary.cpp:31-33) takes them. */
+
+static double intra_random_real(double start, double end) {
+  return orc_random_real(start, end, rand());
+}
+
+/* SimCalcs::bondEnergy, src/Metropolis/SimulationStep.cpp:241-255:
+ * sum of k (eq - length)^2 over the molecule's variable bonds. */
+double orc_bond_energy(const orc_topo* t, int mol) {
+  double out = 0;
+  int s = t->mol_bond_start[mol], e = s + t->mol_bond_count[mol];
+  for (int i = s; i < e; i++) {
+    if (t->bond_var[i]) {
+      double diff = t->bond_eq[i] - t->bond_len[i];
+      out += t->bond_k[i] * diff * diff;
+    }
+  }
+  return out;
+}
+
+/* SimCalcs::angleEnergy, :131-146 (sizes in degrees, as tracked). */
+double orc_angle_energy(const orc_topo* t, int mol) {
+  double out = 0;
+  int s = t->mol_angle_start[mol], e = s + t->mol_angle_count[mol];
+  for (int i = s; i < e; i++) {
+    if (t->angle_var[i]) {
+      double diff = t->angle_eq[i] - t->angle_size[i];
+      out += t->angle_k[i] * diff * diff;
+    }
+  }
+  return out;
+}
+
+/* SimCalcs::calcIntraMolecularEnergy, :80-129: angle and bond terms when the
+ * box has variable angles / bonds, then, when it has either, the LJ and
+ * Coulomb terms of every atom pair i < j of the molecule not excluded,
+ * halved for the fudge pairs; no cutoff, minimum image per pair, and the
+ * SimCalcs pair functions (blending by sqrt|a b|, so sites with negative
+ * sigma or epsilon take part here). */
+double orc_intra_energy(const orc_box* b, const orc_topo* t, int mol) {
+  double out = 0.0;
+  if (t->flex_angles) out += orc_angle_energy(t, mol);
+  if (t->flex_bonds) out += orc_bond_energy(t, mol);
+  if (t->flex_bonds || t->flex_angles) {
+    const int s = b->mol_start[mol], e = s + b->mol_len[mol];
+    const int ty = t->mol_type[mol], n = t->type_natom[ty];
+    const unsigned char* code = t->pair_code + t->type_off[ty];
+    for (int i = s; i < e; i++) {
+      for (int j = i + 1; j < e; j++) {
+        const int li = i - s, lj = j - s;
+        /* an atom beyond the type's first molecule's length finds no list
+         * entry: full weight */
+        const int c = (li < n && lj < n) ? code[li * n + lj] : 2;
+        const double fudge = c == 0 ? 0.0 : (c == 1 ? 0.5 : 1.0);
+        if (fudge > 0.0) {
+          double r2 = orc_atom_dist2(b, i, j);
+          double r = sqrt(r2);
+          double energy = orc_lj(b, i, j, r2);
+          energy += orc_charge(b, i, j, r);
+          out += fudge * energy;
+        }
+      }
+    }
+  }
+  return out;
+}
+
+/* SimCalcs::find / unionAtoms, :777-792 (local atom indexes). */
+static int uf_find(int* p, int a) {
+  int r = a;
+  while (p[r] != r) r = p[r];
+  while (p[a] != r) {
+    int nx = p[a];
+    p[a] = r;
+    a = nx;
+  }
+  return r;
+}
+static void uf_union(int* p, int a, int c) {
+  int ra = uf_find(p, a), rc = uf_find(p, c);
+  if (ra != rc) p[ra] = rc;
+}
+
+/* SimCalcs::stretchBond, :257-315: the molecule's atoms split into the two
+ * sides of bond `bond` (the union of every other bond of the molecule); the
+ * side of its second atom moves by +dist/2 along the bond's unit vector and
+ * every other atom by -dist/2; the tracked length grows by dist.  A bond in a
+ * ring (one side) is left alone. */
+void orc_stretch_bond(orc_box* b, orc_topo* t, int mol, int bond, double dist) {
+  const int bs = t->mol_bond_start[mol], be = bs + t->mol_bond_count[mol];
+  const int start = b->mol_start[mol], len = b->mol_len[mol];
+  const int e1 = t->bond_a1[bs + bond], e2 = t->bond_a2[bs + bond];
+  int* p = t->uf;
+  for (int i = 0; i < len; i++) p[i] = i;
+  for (int i = bs; i < be; i++) {
+    if (i == bond + bs) continue;
+    uf_union(p, t->bond_a1[i] - start, t->bond_a2[i] - start);
+  }
+  const int side1 = uf_find(p, e1 - start), side2 = uf_find(p, e2 - start);
+  if (side1 == side2) return;
+  double v[3], denon = 0.0;
+  v[0] = b->x[e2] - b->x[e1];
+  v[1] = b->y[e2] - b->y[e1];
+  v[2] = b->z[e2] - b->z[e1];
+  for (int k = 0; k < 3; k++) denon += v[k] * v[k];
+  denon = sqrt(denon);
+  for (int k = 0; k < 3; k++) v[k] = v[k] / denon / 2.0;
+  double* c[3] = {b->x, b->y, b->z};
+  for (int i = 0; i < len; i++) {
+    if (uf_find(p, i) == side2) {
+      for (int k = 0; k < 3; k++) c[k][i + start] += v[k] * dist;
+    } else {
+      for (int k = 0; k < 3; k++) c[k][i + start] -= v[k] * dist;
+    }
+  }
+  t->bond_len[bs + bond] += dist;
+}
+
+/* SimCalcs::expandAngle, :148-239: with the bonds touching the middle atom
+ * removed, the component of the first end turns by -deg and that of the
+ * second end by +deg about the unit normal of the plane (mid - end1,
+ * mid - end2) through the middle atom (Rodrigues' rotation); the tracked size
+ * grows by deg.  Both ends in one component (a ring) leave the angle alone.
+ * DEG2RAD is the reference's constant, whose digits differ from pi's after
+ * the seventh. */
+void orc_expand_angle(orc_box* b, orc_topo* t, int mol, int angle, double deg) {
+  const int bs = t->mol_bond_start[mol], be = bs + t->mol_bond_count[mol];
+  const int as = t->mol_angle_start[mol];
+  const int start = b->mol_start[mol], len = b->mol_len[mol];
+  const int end1 = t->angle_a1[as + angle], end2 = t->angle_a2[as + angle];
+  const int mid = t->angle_mid[as + angle];
+  int* p = t->uf;
+  for (int i = 0; i < len; i++) p[i] = i;
+  for (int i = bs; i < be; i++) {
+    int a1 = t->bond_a1[i], a2 = t->bond_a2[i];
+    if (a1 == mid || a2 == mid) continue;
+    uf_union(p, a1 - start, a2 - start);
+  }
+  const int group1 = uf_find(p, end1 - start), group2 = uf_find(p, end2 - start);
+  if (group1 == group2) return;
+  const double DEG2RAD = 3.14159256358979323846264 / 180.0;
+  double* c[3] = {b->x, b->y, b->z};
+  double e1m[3], e2m[3], normal[3], mv[3];
+  for (int k = 0; k < 3; k++) {
+    e1m[k] = c[k][mid] - c[k][end1];
+    e2m[k] = c[k][mid] - c[k][end2];
+    mv[k] = c[k][mid];
+  }
+  normal[0] = e1m[1] * e2m[2] - e2m[1] * e1m[2];
+  normal[1] = e2m[0] * e1m[2] - e1m[0] * e2m[2];
+  normal[2] = e1m[0] * e2m[1] - e2m[0] * e1m[1];
+  double nl = 0.0;
+  for (int k = 0; k < 3; k++) nl += normal[k] * normal[k];
+  nl = sqrt(nl);
+  for (int k = 0; k < 3; k++) normal[k] = normal[k] / nl;
+  for (int i = start; i < start + len; i++) {
+    double theta;
+    const int g = uf_find(p, i - start);
+    if (g == group1)
+      theta = deg * -DEG2RAD;
+    else if (g == group2)
+      theta = deg * DEG2RAD;
+    else
+      continue;
+    double pt[3], cr[3], dot = 0.0;
+    for (int k = 0; k < 3; k++) {
+      pt[k] = c[k][i] - mv[k];
+      dot += pt[k] * normal[k];
+    }
+    cr[0] = normal[1] * pt[2] - pt[1] * normal[2];
+    cr[1] = pt[0] * normal[2] - normal[0] * pt[2];
+    cr[2] = normal[0] * pt[1] - pt[0] * normal[1];
+    for (int k = 0; k < 3; k++) {
+      pt[k] = (normal[k] * dot * (1 - cos(theta)) + pt[k] * cos(theta) + cr[k] * sin(theta));
+      c[k][i] = pt[k] + mv[k];
+    }
+  }
+  t->angle_size[as + angle] += deg;
+}
+
+/* SimCalcs::saveBonds / saveAngles, :678-701. */
+void orc_save_intra(orc_topo* t, int mol) {
+  int s = t->mol_bond_start[mol], n = t->mol_bond_count[mol];
+  for (int i = 0; i < n; i++) t->bond_len_rb[i + s] = t->bond_len[i + s];
+  s = t->mol_angle_start[mol];
+  n = t->mol_angle_count[mol];
+  for (int i = 0; i < n; i++) t->angle_size_rb[i + s] = t->angle_size[i + s];
+}
+
+/* SimCalcs::rollbackAngles / rollbackBonds, :751-775. */
+void orc_rollback_intra(orc_topo* t, int mol) {
+  int s = t->mol_angle_start[mol], n = t->mol_angle_count[mol];
+  for (int i = s; i < s + n; i++) t->angle_size[i] = t->angle_size_rb[i];
+  s = t->mol_bond_start[mol];
+  n = t->mol_bond_count[mol];
+  for (int i = s; i < s + n; i++) t->bond_len[i] = t->bond_len_rb[i];
+}
+
+/* Draws the distinct indexes of the bonds or angles to move, as the
+ * reference inserts (int)randomReal(0, count) into a std::set until it holds
+ * `want` of them (:599-601, :631-633), and returns them in ascending order
+ * (the set's iteration order).  A draw equal to count (rand() == RAND_MAX) is
+ * kept as count - 1 here; the reference would index past the molecule. */
+static int draw_set(int want, int count, int* out) {
+  int n = 0;
+  while (n < want) {
+    int v = (int)intra_random_real(0, count);
+    if (v >= count) v = count - 1;
+    int pos = 0;
+    while (pos < n && out[pos] < v) pos++;
+    if (pos < n && out[pos] == v) continue;
+    for (int k = n; k > pos; k--) out[k] = out[k - 1];
+    out[pos] = v;
+    n++;
+  }
+  return n;
+}
+
+/* SimCalcs::intramolecularMove, :568-675 (ENABLE_BOND 1, ENABLE_ANGLE 1,
+ * ENABLE_DIHEDRAL 0, ENABLE_TUNING true, TARGET_RATIO 0.4, RATIO_MARGIN
+ * 1e-4 from SimulationStep.h:16-22): save the rows; stretch a random subset
+ * of the bonds, an MC test on the intramolecular energy that only counts
+ * acceptances (it never rolls back), the same for the angles, and every 1000
+ * steps the widths scaled toward a 40 % acceptance.  The angle width test
+ * reads the width itself where the bond test reads the ratio's distance
+ * (:666), as the reference does. */
+void orc_intramolecular_move(orc_box* b, orc_topo* t, int mol) {
+  orc_save_intra(t, mol);
+  const int n_types = 2;  /* ENABLE_BOND + ENABLE_ANGLE + ENABLE_DIHEDRAL */
+  const double intra_scale = 0.25 + (0.75 / (double)n_types);
+  double scale;
+  int idx[64];
+  double new_e = 0, cur_e = orc_intra_energy(b, t, mol);
+  const int n_bonds = t->mol_bond_count[mol], bond_start = t->mol_bond_start[mol];
+  const int n_angles = t->mol_angle_count[mol], angle_start = t->mol_angle_start[mol];
+  const double bond_delta = t->max_bond_delta, angle_delta = t->max_angle_delta;
+  if (t->flex_bonds) {
+    int n = n_bonds;
+    if (n > 3) {
+      n = (int)intra_random_real(2, n_bonds);
+      if (n > t->max_intra_moves) n = t->max_intra_moves;
+    }
+    scale = 0.25 + (0.75 / (double)n) * intra_scale;
+    t->bond_moves += n;
+    draw_set(n, n_bonds, idx);
+    for (int k = 0; k < n; k++) {
+      double d = scale * intra_random_real(-bond_delta, bond_delta);
+      if (t->bond_var[bond_start + idx[k]]) orc_stretch_bond(b, t, mol, idx[k], d);
+    }
+    new_e = orc_intra_energy(b, t, mol);
+    if (orc_accept(new_e - cur_e, b->kT, new_e - cur_e < 0 ? 0.0
+                                                           : intra_random_real(0.0, 1.0)))
+      t->bond_accepted += n;
+    cur_e = new_e;
+  }
+  if (t->flex_angles) {
+    int n = n_angles;
+    if (n > 3) {
+      n = (int)intra_random_real(2, n_angles);
+      if (n > t->max_intra_moves) n = t->max_intra_moves;
+    }
+    scale = 0.25 + (0.75 / (double)n) * intra_scale;
+    t->angle_moves += n;
+    draw_set(n, n_angles, idx);
+    for (int k = 0; k < n; k++) {
+      double d = scale * intra_random_real(-angle_delta, angle_delta);
+      if (t->angle_var[angle_start + idx[k]]) orc_expand_angle(b, t, mol, idx[k], d);
+    }
+    new_e = orc_intra_energy(b, t, mol);
+    if (orc_accept(new_e - cur_e, b->kT, new_e - cur_e < 0 ? 0.0
+                                                           : intra_random_real(0.0, 1.0)))
+      t->angle_accepted += n;
+    cur_e = new_e;
+  }
+  if (t->step_num != 0 && (t->step_num % 1000) == 0) {
+    double bond_ratio = (double)t->bond_accepted / t->bond_moves;
+    double angle_ratio = (double)t->angle_accepted / t->angle_moves;
+    double diff = bond_ratio - 0.4;
+    if (fabs(diff) > 0.0001) t->max_bond_delta += t->max_bond_delta * diff;
+    diff = angle_ratio - 0.4;
+    if (fabs(angle_delta) > 0.0001) t->max_angle_delta += t->max_angle_delta * diff;
+    t->bond_accepted = t->bond_moves = 0;
+    t->angle_accepted = t->angle_moves = 0;
+  }
+}
+
+/* SimulationStep::calcSystemEnergy with the intramolecular term (:40-71). */
+double orc_system_energy_intra(const orc_box* b, const orc_topo* t) {
+  double total = 0;
+  for (int m = 0; m < b->n_mol; m++)
+    total += orc_mol_energy(b, m, m) + orc_intra_energy(b, t, m);
+  return total;
+}
+
+/* Simulation::run's NVT loop (Simulation.cpp:219-264) with the
+ * intramolecular term and move: choose (rand), E_old, the seven draws of
+ * intermolecularMove and the move, the intramolecular move, E_new, accept or
+ * roll back everything, then the step counter. */
+double orc_run_plain_intra(orc_box* b, orc_topo* t, int steps, double e0, int* accepted) {
+  double e = e0;
+  int acc = 0;
+  for (int s = 0; s < steps; s++) {
+    int mol = (int)intra_random_real(0, b->n_mol);
+    if (mol >= b->n_mol) mol = b->n_mol - 1;
+    double old_e = orc_mol_energy(b, mol, 0) + orc_intra_energy(b, t, mol);
+    orc_move mv;
+    memset(&mv, 0, sizeof(mv));
+    mv.mol = mol;
+    const int len = b->mol_len[mol];
+    mv.vertex = (int)intra_random_real(0, len);
+    if (mv.vertex >= len) mv.vertex = len - 1;
+    mv.dx = intra_random_real(-b->max_translate, b->max_translate);
+    mv.dy = intra_random_real(-b->max_translate, b->max_translate);
+    mv.dz = intra_random_real(-b->max_translate, b->max_translate);
+    mv.r0 = intra_random_real(-b->max_rotate, b->max_rotate);
+    mv.r1 = intra_random_real(-b->max_rotate, b->max_rotate);
+    mv.r2 = intra_random_real(-b->max_rotate, b->max_rotate);
+    orc_apply_move(b, &mv);
+    orc_intramolecular_move(b, t, mol);
+    double new_e = orc_mol_energy(b, mol, 0) + orc_intra_energy(b, t, mol);
+    const double de = new_e - old_e;
+    if (orc_accept(de, b->kT, de < 0 ? 0.0 : intra_random_real(0.0, 1.0))) {
+      acc++;
+      e += de;
+    } else {
+      orc_rollback(b, mol);
+      orc_rollback_intra(t, mol);
+    }
+    t->step_num++;
+  }
+  if (accepted) *accepted = acc;
+  return e;
+}

@@ -125,6 +125,38 @@ int orc_fchain_volume(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step
  * addition (the same points as the product's input builder). */
 int orc_build_centres(int n, double L, double dmin, uint64_t seed, double* out);
 
+/* ---- flexible molecules: the bond / angle rows of the SimBox
+ * (src/Metropolis/SimBox.h:160-305) and the reference's intramolecular
+ * functions as they run with ENABLE_INTRA true. */
+typedef struct {
+  int n_bond, n_angle, n_type, max_intra_moves;
+  int *bond_a1, *bond_a2, *bond_var;          /* bondData[A1/A2/VARIABLE]       */
+  double *bond_k, *bond_eq, *bond_len;        /* bondData[KBOND/EQDIST], bondLengths */
+  double* bond_len_rb;                        /* rollBackBondLengths            */
+  int *angle_a1, *angle_a2, *angle_mid, *angle_var;
+  double *angle_k, *angle_eq, *angle_size;    /* angleData[KANGLE/EQANGLE], angleSizes */
+  double* angle_size_rb;                      /* rollBackAngleSizes             */
+  int *mol_bond_start, *mol_bond_count, *mol_angle_start, *mol_angle_count, *mol_type;
+  int *type_natom, *type_off;                 /* per type: atoms, offset in pair_code */
+  unsigned char* pair_code;                   /* 0 excluded, 1 x0.5, 2 full     */
+  int* uf;                                    /* union-find scratch [largest_mol] */
+  double max_bond_delta, max_angle_delta;
+  long long step_num;
+  long long bond_moves, bond_accepted, angle_moves, angle_accepted;
+  int flex_bonds, flex_angles;
+} orc_topo;
+
+double orc_bond_energy(const orc_topo* t, int mol);
+double orc_angle_energy(const orc_topo* t, int mol);
+double orc_intra_energy(const orc_box* b, const orc_topo* t, int mol);
+void orc_stretch_bond(orc_box* b, orc_topo* t, int mol, int bond, double dist);
+void orc_expand_angle(orc_box* b, orc_topo* t, int mol, int angle, double deg);
+void orc_save_intra(orc_topo* t, int mol);
+void orc_rollback_intra(orc_topo* t, int mol);
+void orc_intramolecular_move(orc_box* b, orc_topo* t, int mol);
+double orc_system_energy_intra(const orc_box* b, const orc_topo* t);
+double orc_run_plain_intra(orc_box* b, orc_topo* t, int steps, double e0, int* accepted);
+
 #ifdef __cplusplus
 }
 #endif

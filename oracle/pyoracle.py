@@ -67,6 +67,26 @@ class OrcTrace(C.Structure):
                 ("e_new", C.c_double), ("de", C.c_double), ("u", C.c_double)]
 
 
+class OrcTopo(C.Structure):
+    _fields_ = [
+        ("n_bond", C.c_int), ("n_angle", C.c_int), ("n_type", C.c_int),
+        ("max_intra_moves", C.c_int),
+        ("bond_a1", _ip), ("bond_a2", _ip), ("bond_var", _ip),
+        ("bond_k", _dp), ("bond_eq", _dp), ("bond_len", _dp), ("bond_len_rb", _dp),
+        ("angle_a1", _ip), ("angle_a2", _ip), ("angle_mid", _ip), ("angle_var", _ip),
+        ("angle_k", _dp), ("angle_eq", _dp), ("angle_size", _dp), ("angle_size_rb", _dp),
+        ("mol_bond_start", _ip), ("mol_bond_count", _ip), ("mol_angle_start", _ip),
+        ("mol_angle_count", _ip), ("mol_type", _ip),
+        ("type_natom", _ip), ("type_off", _ip), ("pair_code", C.POINTER(C.c_uint8)),
+        ("uf", _ip),
+        ("max_bond_delta", C.c_double), ("max_angle_delta", C.c_double),
+        ("step_num", C.c_longlong),
+        ("bond_moves", C.c_longlong), ("bond_accepted", C.c_longlong),
+        ("angle_moves", C.c_longlong), ("angle_accepted", C.c_longlong),
+        ("flex_bonds", C.c_int), ("flex_angles", C.c_int),
+    ]
+
+
 def build(reference: bool = True) -> None:
     """Compiles the restatement and, where the reference sources exist, the
     reference harness."""
@@ -129,6 +149,17 @@ def orc_lib() -> C.CDLL:
                                             C.c_int, C.c_double, C.c_double]),
             "orc_build_centres": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_uint64,
                                             _dp]),
+            "orc_bond_energy": (C.c_double, [C.POINTER(OrcTopo), C.c_int]),
+            "orc_angle_energy": (C.c_double, [C.POINTER(OrcTopo), C.c_int]),
+            "orc_intra_energy": (C.c_double, [P, C.POINTER(OrcTopo), C.c_int]),
+            "orc_stretch_bond": (None, [P, C.POINTER(OrcTopo), C.c_int, C.c_int, C.c_double]),
+            "orc_expand_angle": (None, [P, C.POINTER(OrcTopo), C.c_int, C.c_int, C.c_double]),
+            "orc_save_intra": (None, [C.POINTER(OrcTopo), C.c_int]),
+            "orc_rollback_intra": (None, [C.POINTER(OrcTopo), C.c_int]),
+            "orc_intramolecular_move": (None, [P, C.POINTER(OrcTopo), C.c_int]),
+            "orc_system_energy_intra": (C.c_double, [P, C.POINTER(OrcTopo)]),
+            "orc_run_plain_intra": (C.c_double, [P, C.POINTER(OrcTopo), C.c_int, C.c_double,
+                                                 C.POINTER(C.c_int)]),
         }
         for name, (res, args) in protos.items():
             fn = getattr(L, name)
@@ -210,6 +241,97 @@ class OracleBox:
         e = orc_lib().orc_chain_run(self.ref, int(seed) & (2 ** 64 - 1), int(chain), int(step0),
                                     int(n_steps), int(mode), float(e0), tr, C.byref(acc))
         return e, acc.value, list(tr)[:n_steps]
+
+
+class OracleFlex:
+    """A box of flexible molecules on the restatement: an OracleBox plus the
+    bond / angle rows of a Topology (mcgpu_gb300.workloads), mutated in
+    place, with the intramolecular functions as the reference runs them with
+    ENABLE_INTRA true.  Random draws come from the C library's rand()
+    (seed it with srand, e.g. through LibcRand)."""
+
+    def __init__(self, box, topo):
+        self.ob = OracleBox(box)
+        t = topo.copy().normalise()
+        self.t = t
+        self.bond_len_rb = np.zeros(max(t.n_bond, 1))
+        self.angle_size_rb = np.zeros(max(t.n_angle, 1))
+        self.type_off = np.concatenate([[0], np.cumsum(t.type_natom.astype(np.int64) ** 2)[:-1]]
+                                       ).astype(np.int32) if t.n_type else np.zeros(1, np.int32)
+        self.uf = np.zeros(max(self.ob.largest, 1), np.int32)
+        s = OrcTopo()
+        s.n_bond, s.n_angle, s.n_type = t.n_bond, t.n_angle, t.n_type
+        s.max_intra_moves = int(t.max_intra_moves)
+        I = lambda a: a.ctypes.data_as(_ip)
+        D = lambda a: a.ctypes.data_as(_dp)
+        for k in ("bond_a1", "bond_a2", "bond_var", "angle_a1", "angle_a2", "angle_mid",
+                  "angle_var", "mol_bond_start", "mol_bond_count", "mol_angle_start",
+                  "mol_angle_count", "mol_type", "type_natom"):
+            setattr(s, k, I(getattr(t, k)))
+        for k in ("bond_k", "bond_eq", "bond_len", "angle_k", "angle_eq", "angle_size"):
+            setattr(s, k, D(getattr(t, k)))
+        s.bond_len_rb, s.angle_size_rb = D(self.bond_len_rb), D(self.angle_size_rb)
+        s.type_off, s.uf = I(self.type_off), I(self.uf)
+        s.pair_code = t.pair_code.ctypes.data_as(C.POINTER(C.c_uint8))
+        s.max_bond_delta, s.max_angle_delta = float(t.max_bond_delta), float(t.max_angle_delta)
+        s.step_num = int(t.step_num)
+        s.flex_bonds, s.flex_angles = int(t.flex_bonds), int(t.flex_angles)
+        self.s = s
+
+    @property
+    def ref(self):
+        return C.byref(self.s)
+
+    def intra_energy(self, mol: int) -> float:
+        return orc_lib().orc_intra_energy(self.ob.ref, self.ref, int(mol))
+
+    def bond_energy(self, mol: int) -> float:
+        return orc_lib().orc_bond_energy(self.ref, int(mol))
+
+    def angle_energy(self, mol: int) -> float:
+        return orc_lib().orc_angle_energy(self.ref, int(mol))
+
+    def mol_energy(self, curr: int, start: int = 0) -> float:
+        """SimulationStep::calcMoleculeEnergy with the intramolecular term."""
+        return self.ob.mol_energy(curr, start) + self.intra_energy(curr)
+
+    def system_energy(self) -> float:
+        return orc_lib().orc_system_energy_intra(self.ob.ref, self.ref)
+
+    def stretch_bond(self, mol: int, bond: int, dist: float) -> None:
+        orc_lib().orc_stretch_bond(self.ob.ref, self.ref, int(mol), int(bond), float(dist))
+
+    def expand_angle(self, mol: int, angle: int, deg: float) -> None:
+        orc_lib().orc_expand_angle(self.ob.ref, self.ref, int(mol), int(angle), float(deg))
+
+    def save(self, mol: int) -> None:
+        orc_lib().orc_save_intra(self.ref, int(mol))
+
+    def rollback(self, mol: int) -> None:
+        """Coordinates, angle sizes and bond lengths back (rollback with
+        ENABLE_INTRA)."""
+        self.ob.rollback(mol)
+        orc_lib().orc_rollback_intra(self.ref, int(mol))
+
+    def intramolecular_move(self, mol: int) -> None:
+        orc_lib().orc_intramolecular_move(self.ob.ref, self.ref, int(mol))
+
+    def run_plain(self, steps: int, e0: float) -> tuple[float, int]:
+        acc = C.c_int()
+        e = orc_lib().orc_run_plain_intra(self.ob.ref, self.ref, int(steps), float(e0),
+                                          C.byref(acc))
+        return e, acc.value
+
+    def state(self) -> dict:
+        s = self.s
+        return dict(bond_len=self.t.bond_len.copy(), angle_size=self.t.angle_size.copy(),
+                    max_bond_delta=s.max_bond_delta, max_angle_delta=s.max_angle_delta,
+                    step_num=s.step_num, bond_moves=s.bond_moves,
+                    bond_accepted=s.bond_accepted, angle_moves=s.angle_moves,
+                    angle_accepted=s.angle_accepted)
+
+    def coords(self) -> np.ndarray:
+        return self.ob.coords()
 
 
 class OracleChain:
@@ -348,6 +470,29 @@ class RefHarness:
             "ref_load_seed": (C.c_int, []),
             "ref_load_write_state": (None, [C.c_char_p, C.c_int]),
             "ref_load_set_coords": (None, [_dp, _dp, _dp]),
+            "ref_load_activate": (None, []),
+            "ref_topology_counts": (None, [C.POINTER(C.c_int)] * 3),
+            "ref_topology_rows": (None, [_ip, _ip, _dp, _dp, _dp, _ip, _ip, _ip, _ip, _dp, _dp,
+                                         _dp, _ip, _ip, _ip, _ip, _ip, _ip, _dp]),
+            "ref_type_codes": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_uint8)]),
+            "ref_set_topology": (None, [C.c_int, _ip, _ip, _dp, _dp, _dp, _ip,
+                                        C.c_int, _ip, _ip, _ip, _dp, _dp, _dp, _ip,
+                                        _ip, _ip, _ip, _ip, _ip, C.c_int, _ip,
+                                        C.POINTER(C.c_uint8), C.c_double, C.c_double,
+                                        C.c_int, C.c_int]),
+            "ref_intra_energy": (C.c_double, [C.c_int]),
+            "ref_bond_energy": (C.c_double, [C.c_int]),
+            "ref_angle_energy": (C.c_double, [C.c_int]),
+            "ref_stretch_bond": (None, [C.c_int, C.c_int, C.c_double]),
+            "ref_expand_angle": (None, [C.c_int, C.c_int, C.c_double]),
+            "ref_save_intra": (None, [C.c_int]),
+            "ref_intramolecular_move": (None, [C.c_int]),
+            "ref_intra_rollback": (None, [C.c_int]),
+            "ref_mol_energy_intra": (C.c_double, [C.c_int, C.c_int]),
+            "ref_system_energy_intra": (C.c_double, []),
+            "ref_intra_state": (None, [_dp, _dp, _dp]),
+            "ref_set_step": (None, [C.c_int]),
+            "ref_run_plain_intra": (C.c_double, [C.c_int, C.c_double, C.POINTER(C.c_int)]),
         }
         for name, (res, args) in protos.items():
             fn = getattr(L, name)
@@ -399,6 +544,7 @@ class RefHarness:
                                ("mol_start", "mol_len", "mol_type", "mol_pidx_start",
                                 "mol_pidx_count", "pidx")),
                              out["size"].ctypes.data_as(_dp), out["params"].ctypes.data_as(_dp))
+        self._loaded_atoms = na_
         out["lrc"] = self.L.ref_load_lrc()
         out["seed"] = self.L.ref_load_seed()
         out["start_step"] = st.value
@@ -412,6 +558,73 @@ class RefHarness:
             c = [np.ascontiguousarray(xyz[:, k], dtype=np.float64) for k in range(3)]
             self.L.ref_load_set_coords(*(v.ctypes.data_as(_dp) for v in c))
         self.L.ref_load_write_state(os.path.abspath(path).encode(), int(step))
+
+    def activate_loaded(self) -> None:
+        """Makes the SimBox of the last load_files the one the step functions
+        act on (its rows, bonds, angles and exclusion lists as the
+        reference's loader built them)."""
+        self.L.ref_load_activate()
+        self.n_atom = self._loaded_atoms
+
+    def topology(self, type_natom) -> dict:
+        """The current SimBox's bond/angle rows, per-molecule ranges and
+        types, per-type pair codes (type_natom atoms each, as the
+        reference's exclusion and fudge lists give them) and
+        params = [maxBondDelta, maxAngleDelta, maxIntraMoves,
+        hasFlexibleBonds, hasFlexibleAngles, stepNum]."""
+        nb, na, nm = C.c_int(), C.c_int(), C.c_int()
+        self.L.ref_topology_counts(C.byref(nb), C.byref(na), C.byref(nm))
+        nb, na, nm = nb.value, na.value, nm.value
+        o = {k: np.empty(nb, np.int32) for k in ("bond_a1", "bond_a2", "bond_var")}
+        o.update({k: np.empty(nb) for k in ("bond_k", "bond_eq", "bond_len")})
+        o.update({k: np.empty(na, np.int32) for k in ("angle_a1", "angle_a2", "angle_mid",
+                                                      "angle_var")})
+        o.update({k: np.empty(na) for k in ("angle_k", "angle_eq", "angle_size")})
+        o.update({k: np.empty(nm, np.int32) for k in ("mol_bond_start", "mol_bond_count",
+                                                      "mol_angle_start", "mol_angle_count",
+                                                      "mol_type")})
+        o["params"] = np.empty(6)
+        I = lambda k: o[k].ctypes.data_as(_ip)
+        D = lambda k: o[k].ctypes.data_as(_dp)
+        self.L.ref_topology_rows(I("bond_a1"), I("bond_a2"), D("bond_k"), D("bond_eq"),
+                                 D("bond_len"), I("bond_var"), I("angle_a1"), I("angle_a2"),
+                                 I("angle_mid"), D("angle_k"), D("angle_eq"), D("angle_size"),
+                                 I("angle_var"), I("mol_bond_start"), I("mol_bond_count"),
+                                 I("mol_angle_start"), I("mol_angle_count"), I("mol_type"),
+                                 D("params"))
+        codes = []
+        for t, n in enumerate(type_natom):
+            c = np.zeros(int(n) * int(n), np.uint8)
+            if n and self.L.ref_type_codes(t, int(n), c.ctypes.data_as(C.POINTER(C.c_uint8))):
+                raise RuntimeError("type %d has no exclusion lists" % t)
+            codes.append(c)
+        o["pair_code"] = np.concatenate(codes) if codes else np.zeros(0, np.uint8)
+        return o
+
+    def set_topology(self, t) -> None:
+        """Installs a Topology (mcgpu_gb300.workloads) on the current SimBox."""
+        t = t.copy().normalise()
+        self._topo = t
+        I = lambda k: getattr(t, k).ctypes.data_as(_ip)
+        D = lambda k: getattr(t, k).ctypes.data_as(_dp)
+        self.L.ref_set_topology(t.n_bond, I("bond_a1"), I("bond_a2"), D("bond_k"), D("bond_eq"),
+                                D("bond_len"), I("bond_var"), t.n_angle, I("angle_a1"),
+                                I("angle_a2"), I("angle_mid"), D("angle_k"), D("angle_eq"),
+                                D("angle_size"), I("angle_var"), I("mol_bond_start"),
+                                I("mol_bond_count"), I("mol_angle_start"), I("mol_angle_count"),
+                                I("mol_type"), t.n_type, I("type_natom"),
+                                t.pair_code.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                float(t.max_bond_delta), float(t.max_angle_delta),
+                                int(t.max_intra_moves), int(t.step_num))
+
+    def intra_state(self, n_bond: int, n_angle: int) -> tuple:
+        """(bond lengths, angle sizes, [maxBondDelta, maxAngleDelta, stepNum,
+        numBondMoves, numAcceptedBondMoves, numAngleMoves,
+        numAcceptedAngleMoves])."""
+        bl, asz, out = np.empty(max(n_bond, 1)), np.empty(max(n_angle, 1)), np.empty(7)
+        self.L.ref_intra_state(bl.ctypes.data_as(_dp), asz.ctypes.data_as(_dp),
+                               out.ctypes.data_as(_dp))
+        return bl[:n_bond], asz[:n_angle], out
 
     def coords(self) -> np.ndarray:
         x, y, z = np.empty(self.n_atom), np.empty(self.n_atom), np.empty(self.n_atom)

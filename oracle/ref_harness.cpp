@@ -295,4 +295,272 @@ void ref_load_write_state(const char* path, int step) {
                  step, path, g_lsb->atomCoordinates);
 }
 
+// ---- flexible molecules (the reference's intramolecular code) -----------------------
+//
+// The reference compiles its bond / angle code but gates its three call sites
+// with ENABLE_INTRA (SimulationStep.h:15, false): calcMoleculeEnergy adds
+// calcIntraMolecularEnergy (SimulationStep.cpp:15-18), changeMolecule follows
+// intermolecularMove with intramolecularMove (:424-428), and rollback also
+// restores the angle sizes and bond lengths (:745-748).  The functions below
+// call the reference's own SimCalcs functions and compose them at exactly
+// those three sites, i.e. the reference as it runs with ENABLE_INTRA true.
+
+// Makes the SimBox built by ref_load the one every other harness function
+// acts on (its step object, SimCalcs::sb and the GPUCopy host rows).
+void ref_load_activate(void) {
+  g_sb = g_lsb;
+  GPUCopy::setParallel(false);
+  GPUCopy::copyIn(g_sb);
+  delete g_step;
+  g_step = new BruteForceStep(g_sb);
+}
+
+void ref_topology_counts(int* n_bond, int* n_angle, int* n_mol) {
+  *n_bond = g_sb->numBonds;
+  *n_angle = g_sb->numAngles;
+  *n_mol = g_sb->numMolecules;
+}
+
+// The bond and angle rows, per-molecule ranges and type, and
+// params = [maxBondDelta, maxAngleDelta, maxIntraMoves, hasFlexibleBonds,
+// hasFlexibleAngles, stepNum].
+void ref_topology_rows(int* bond_a1, int* bond_a2, double* bond_k, double* bond_eq,
+                       double* bond_len, int* bond_var, int* angle_a1, int* angle_a2,
+                       int* angle_mid, double* angle_k, double* angle_eq, double* angle_size,
+                       int* angle_var, int* mol_bond_start, int* mol_bond_count,
+                       int* mol_angle_start, int* mol_angle_count, int* mol_type,
+                       double* params) {
+  SimBox* sb = g_sb;
+  for (int i = 0; i < sb->numBonds; i++) {
+    bond_a1[i] = (int)sb->bondData[BOND_A1_IDX][i];
+    bond_a2[i] = (int)sb->bondData[BOND_A2_IDX][i];
+    bond_k[i] = sb->bondData[BOND_KBOND][i];
+    bond_eq[i] = sb->bondData[BOND_EQDIST][i];
+    bond_len[i] = sb->bondLengths[i];
+    bond_var[i] = (int)sb->bondData[BOND_VARIABLE][i];
+  }
+  for (int i = 0; i < sb->numAngles; i++) {
+    angle_a1[i] = (int)sb->angleData[ANGLE_A1_IDX][i];
+    angle_a2[i] = (int)sb->angleData[ANGLE_A2_IDX][i];
+    angle_mid[i] = (int)sb->angleData[ANGLE_MID_IDX][i];
+    angle_k[i] = sb->angleData[ANGLE_KANGLE][i];
+    angle_eq[i] = sb->angleData[ANGLE_EQANGLE][i];
+    angle_size[i] = sb->angleSizes[i];
+    angle_var[i] = (int)sb->angleData[ANGLE_VARIABLE][i];
+  }
+  for (int m = 0; m < sb->numMolecules; m++) {
+    mol_bond_start[m] = sb->moleculeData[MOL_BOND_START][m];
+    mol_bond_count[m] = sb->moleculeData[MOL_BOND_COUNT][m];
+    mol_angle_start[m] = sb->moleculeData[MOL_ANGLE_START][m];
+    mol_angle_count[m] = sb->moleculeData[MOL_ANGLE_COUNT][m];
+    mol_type[m] = sb->moleculeData[MOL_TYPE][m];
+  }
+  params[0] = sb->maxBondDelta;
+  params[1] = sb->maxAngleDelta;
+  params[2] = sb->maxIntraMoves;
+  params[3] = sb->hasFlexibleBonds ? 1 : 0;
+  params[4] = sb->hasFlexibleAngles ? 1 : 0;
+  params[5] = sb->stepNum;
+}
+
+// Type t's intramolecular pair factors as calcIntraMolecularEnergy finds them
+// in the exclusion and fudge lists (SimulationStep.cpp:95-117): out[i*n + j]
+// = 0 (excluded), 1 (fudge 0.5) or 2 (full), for i != j.  Returns 1 when
+// the type has no lists.
+int ref_type_codes(int t, int n, unsigned char* out) {
+  if (!g_sb->excludeAtoms || !g_sb->excludeAtoms[t]) return 1;
+  for (int i = 0; i < n; i++) {
+    for (int j = 0; j < n; j++) {
+      unsigned char c = 2;
+      for (int k = 0;; k++) {
+        int v = g_sb->excludeAtoms[t][i][k];
+        if (v == -1) break;
+        if (v == j) { c = 0; break; }
+      }
+      if (c) {
+        for (int k = 0;; k++) {
+          int v = g_sb->fudgeAtoms[t][i][k];
+          if (v == -1) break;
+          if (v == j) { c = 1; break; }
+        }
+      }
+      out[i * n + j] = c;
+    }
+  }
+  return 0;
+}
+
+// Replaces the current SimBox's bond and angle rows, per-molecule ranges and
+// types, exclusion and fudge lists (from per-type codes as above, natom[t]
+// atoms each, matrices concatenated) and the intramolecular settings, the
+// way SimBoxBuilder.cpp:44-278 leaves them.
+void ref_set_topology(int n_bond, const int* bond_a1, const int* bond_a2, const double* bond_k,
+                      const double* bond_eq, const double* bond_len, const int* bond_var,
+                      int n_angle, const int* angle_a1, const int* angle_a2,
+                      const int* angle_mid, const double* angle_k, const double* angle_eq,
+                      const double* angle_size, const int* angle_var,
+                      const int* mol_bond_start, const int* mol_bond_count,
+                      const int* mol_angle_start, const int* mol_angle_count,
+                      const int* mol_type, int n_type, const int* natom,
+                      const unsigned char* codes, double max_bond_delta,
+                      double max_angle_delta, int max_intra_moves, int step_num) {
+  SimBox* sb = g_sb;
+  sb->numBonds = n_bond;
+  sb->numAngles = n_angle;
+  sb->bondData = new Real*[BOND_DATA_SIZE];
+  for (int r = 0; r < BOND_DATA_SIZE; r++) sb->bondData[r] = new Real[n_bond > 0 ? n_bond : 1];
+  sb->bondLengths = new Real[n_bond > 0 ? n_bond : 1];
+  sb->rollBackBondLengths = new Real[n_bond > 0 ? n_bond : 1];
+  sb->hasFlexibleBonds = false;
+  for (int i = 0; i < n_bond; i++) {
+    sb->bondData[BOND_A1_IDX][i] = bond_a1[i];
+    sb->bondData[BOND_A2_IDX][i] = bond_a2[i];
+    sb->bondData[BOND_KBOND][i] = bond_k[i];
+    sb->bondData[BOND_EQDIST][i] = bond_eq[i];
+    sb->bondData[BOND_VARIABLE][i] = bond_var[i];
+    sb->bondLengths[i] = bond_len[i];
+    sb->rollBackBondLengths[i] = 0;
+    sb->hasFlexibleBonds |= bond_var[i] != 0;
+  }
+  sb->angleData = new Real*[ANGLE_DATA_SIZE];
+  for (int r = 0; r < ANGLE_DATA_SIZE; r++) sb->angleData[r] = new Real[n_angle > 0 ? n_angle : 1];
+  sb->angleSizes = new Real[n_angle > 0 ? n_angle : 1];
+  sb->rollBackAngleSizes = new Real[n_angle > 0 ? n_angle : 1];
+  sb->hasFlexibleAngles = false;
+  for (int i = 0; i < n_angle; i++) {
+    sb->angleData[ANGLE_A1_IDX][i] = angle_a1[i];
+    sb->angleData[ANGLE_A2_IDX][i] = angle_a2[i];
+    sb->angleData[ANGLE_MID_IDX][i] = angle_mid[i];
+    sb->angleData[ANGLE_KANGLE][i] = angle_k[i];
+    sb->angleData[ANGLE_EQANGLE][i] = angle_eq[i];
+    sb->angleData[ANGLE_VARIABLE][i] = angle_var[i];
+    sb->angleSizes[i] = angle_size[i];
+    sb->rollBackAngleSizes[i] = 0;
+    sb->hasFlexibleAngles |= angle_var[i] != 0;
+  }
+  for (int m = 0; m < sb->numMolecules; m++) {
+    sb->moleculeData[MOL_BOND_START][m] = mol_bond_start[m];
+    sb->moleculeData[MOL_BOND_COUNT][m] = mol_bond_count[m];
+    sb->moleculeData[MOL_ANGLE_START][m] = mol_angle_start[m];
+    sb->moleculeData[MOL_ANGLE_COUNT][m] = mol_angle_count[m];
+    sb->moleculeData[MOL_TYPE][m] = mol_type[m];
+  }
+  sb->excludeAtoms = new int**[n_type > 0 ? n_type : 1];
+  sb->fudgeAtoms = new int**[n_type > 0 ? n_type : 1];
+  const unsigned char* c = codes;
+  for (int t = 0; t < n_type; t++) {
+    const int n = natom[t];
+    sb->excludeAtoms[t] = n > 0 ? new int*[n] : NULL;
+    sb->fudgeAtoms[t] = n > 0 ? new int*[n] : NULL;
+    for (int i = 0; i < n; i++) {
+      int ne = 0, nf = 0;
+      for (int j = 0; j < n; j++) {
+        ne += c[i * n + j] == 0;
+        nf += c[i * n + j] == 1;
+      }
+      int* e = new int[ne + 1];
+      int* f = new int[nf + 1];
+      ne = nf = 0;
+      for (int j = 0; j < n; j++) {
+        if (c[i * n + j] == 0) e[ne++] = j;
+        if (c[i * n + j] == 1) f[nf++] = j;
+      }
+      e[ne] = -1;
+      f[nf] = -1;
+      sb->excludeAtoms[t][i] = e;
+      sb->fudgeAtoms[t][i] = f;
+    }
+    c += (size_t)n * n;
+  }
+  sb->maxBondDelta = max_bond_delta;
+  sb->maxAngleDelta = max_angle_delta;
+  sb->maxIntraMoves = max_intra_moves;
+  sb->stepNum = step_num;
+  sb->numBondMoves = sb->numAcceptedBondMoves = 0;
+  sb->numAngleMoves = sb->numAcceptedAngleMoves = 0;
+  GPUCopy::copyIn(sb);
+}
+
+// SimCalcs::calcIntraMolecularEnergy, bondEnergy, angleEnergy
+// (SimulationStep.cpp:80-146, :241-255).
+double ref_intra_energy(int mol) { return SimCalcs::calcIntraMolecularEnergy(mol); }
+double ref_bond_energy(int mol) { return SimCalcs::bondEnergy(mol); }
+double ref_angle_energy(int mol) { return SimCalcs::angleEnergy(mol); }
+
+// SimCalcs::stretchBond (:257-315) and SimCalcs::expandAngle (:148-239).
+void ref_stretch_bond(int mol, int bond, double dist) { SimCalcs::stretchBond(mol, bond, dist); }
+void ref_expand_angle(int mol, int angle, double deg) { SimCalcs::expandAngle(mol, angle, deg); }
+
+// SimCalcs::saveBonds / saveAngles (:677-701).
+void ref_save_intra(int mol) {
+  SimCalcs::saveBonds(mol);
+  SimCalcs::saveAngles(mol);
+}
+
+// SimCalcs::intramolecularMove (:568-675), drawing from rand().
+void ref_intramolecular_move(int mol) { SimCalcs::intramolecularMove(mol); }
+
+// SimCalcs::rollback with its ENABLE_INTRA branch (:731-749).
+void ref_intra_rollback(int mol) {
+  SimCalcs::rollback(mol);
+  SimCalcs::rollbackAngles(mol);
+  SimCalcs::rollbackBonds(mol);
+}
+
+// SimulationStep::calcMoleculeEnergy with ENABLE_INTRA (SimulationStep.cpp:15-18).
+double ref_mol_energy_intra(int curr, int start) {
+  return g_step->calcMolecularEnergyContribution(curr, start) +
+         SimCalcs::calcIntraMolecularEnergy(curr);
+}
+
+// SimulationStep::calcSystemEnergy with ENABLE_INTRA (:40-71, VERBOSE output
+// left out).
+double ref_system_energy_intra(void) {
+  Real total = 0;
+  for (int mol = 0; mol < g_sb->numMolecules; mol++) total += ref_mol_energy_intra(mol, mol);
+  return total;
+}
+
+// The bond lengths, angle sizes and
+// out = [maxBondDelta, maxAngleDelta, stepNum, numBondMoves,
+// numAcceptedBondMoves, numAngleMoves, numAcceptedAngleMoves].
+void ref_intra_state(double* bond_len, double* angle_size, double* out) {
+  std::memcpy(bond_len, g_sb->bondLengths, sizeof(double) * g_sb->numBonds);
+  std::memcpy(angle_size, g_sb->angleSizes, sizeof(double) * g_sb->numAngles);
+  out[0] = g_sb->maxBondDelta;
+  out[1] = g_sb->maxAngleDelta;
+  out[2] = g_sb->stepNum;
+  out[3] = g_sb->numBondMoves;
+  out[4] = g_sb->numAcceptedBondMoves;
+  out[5] = g_sb->numAngleMoves;
+  out[6] = g_sb->numAcceptedAngleMoves;
+}
+
+void ref_set_step(int step) { g_sb->stepNum = step; }
+
+// Simulation::run's NVT loop (Simulation.cpp:219-264) as it runs with
+// ENABLE_INTRA true: molecule energies with the intramolecular term, the
+// intramolecular move after the rigid one, rollbacks restoring angles and
+// bonds, the step counter the tuning reads.
+double ref_run_plain_intra(int steps, double e0, int* accepted) {
+  double e = e0;
+  int acc = 0;
+  for (int move = 0; move < steps; move++) {
+    int idx = g_step->chooseMolecule(g_sb);
+    double old_e = ref_mol_energy_intra(idx, 0);
+    SimCalcs::intermolecularMove(idx);
+    SimCalcs::intramolecularMove(idx);
+    double new_e = ref_mol_energy_intra(idx, 0);
+    if (SimCalcs::acceptMove(new_e - old_e)) {
+      acc++;
+      e += new_e - old_e;
+    } else {
+      ref_intra_rollback(idx);
+    }
+    g_sb->stepNum++;
+  }
+  if (accepted) *accepted = acc;
+  return e;
+}
+
 }  // extern "C"
