@@ -189,13 +189,95 @@ typedef struct {
  * contract calls above: srand(seed), then per step chooseMolecule, the
  * seven intermolecularMove draws and acceptMove's uniform from the C
  * library's rand() in the reference's order (SimulationStep.cpp:25-27,
- * 527-535, 794-803), calcMolecularEnergyContribution before and after
- * changeMolecule, rollback on rejection -- the calls a GpuBruteForceStep
- * makes under the reference's own loop.  fused != 0 takes the old energy,
- * the move and the new energy in one mcgpu_move_energies launch (the same
- * draws and decisions). */
+ * 527-535, 794-803), calcMoleculeEnergy before and after changeMolecule,
+ * rollback on rejection -- the calls a GpuBruteForceStep makes under the
+ * reference's own loop.  fused != 0 takes the old energy, the move and the
+ * new energy in one mcgpu_move_energies launch (the same draws and
+ * decisions; rigid molecules only).  With intramolecular moves on
+ * (mcgpu_box_set_intra) every step also makes the intramolecular move with
+ * its draws, sets the step counter the width tuning reads to the loop's step
+ * (starting from the topology's step_num) and the calls are made one by
+ * one whatever fused says. */
 int mcgpu_run_plain(mcgpu_box* box, unsigned int seed, int n_steps, int fused,
                     mcgpu_plain_stats* out);
+
+/* ---- flexible molecules: bonds, angles, intramolecular moves ------------ *
+ *
+ * The reference compiles bond stretches, angle expansions and the
+ * intramolecular energy but calls them only when ENABLE_INTRA is true
+ * (SimulationStep.h:15; false in its sources).  A box given a topology
+ * carries the bond / angle rows; mcgpu_box_set_intra(box, 1) is ENABLE_INTRA:
+ * mcgpu_mol_energy and mcgpu_system_energy then add the intramolecular
+ * energy (SimulationStep.cpp:15-18), mcgpu_change_molecule follows the rigid
+ * move with the intramolecular move drawing from the C library's rand()
+ * (:424-428, :568-675) and mcgpu_rollback also restores the bond lengths
+ * and angle sizes (:745-748).  Off by default, as in the reference.  The
+ * device-resident chain forms move rigid molecules only: mcgpu_chain_run
+ * refuses a box with intramolecular moves on. */
+
+/* The bond / angle rows of SimBox (SimBox.h:160-305) as SimBoxBuilder fills
+ * them (SimBoxBuilder.cpp:136-278).  Atom indexes are box atom indexes; a
+ * bond's atoms and an angle's ends lie in their molecule, an angle's middle
+ * may be any atom (the reference's loader gives z-matrix angles the first
+ * atom of their copy set).  pair_code holds, per molecule type t (mol_type),
+ * a type_natom[t] x type_natom[t] row-major matrix, the matrices
+ * concatenated: 0 excluded, 1 fudge 0.5, 2 full (the exclusion and fudge
+ * lists, SimBox.h:298-305).  Angle sizes are in degrees. */
+typedef struct {
+  int32_t n_bond, n_angle, n_type, max_intra_moves;
+  const int32_t *bond_a1, *bond_a2, *bond_var;      /* bondData A1/A2/VARIABLE */
+  const double *bond_k, *bond_eq, *bond_len;        /* KBOND, EQDIST, bondLengths */
+  const int32_t *angle_a1, *angle_a2, *angle_mid, *angle_var;
+  const double *angle_k, *angle_eq, *angle_size;    /* KANGLE, EQANGLE, angleSizes */
+  const int32_t *mol_bond_start, *mol_bond_count;   /* moleculeData MOL_BOND_* */
+  const int32_t *mol_angle_start, *mol_angle_count; /* moleculeData MOL_ANGLE_* */
+  const int32_t *mol_type;                          /* moleculeData MOL_TYPE */
+  const int32_t *type_natom;
+  const uint8_t *pair_code;
+  double max_bond_delta, max_angle_delta;           /* maxBondDelta, maxAngleDelta */
+  int64_t step_num;                                 /* stepNum */
+} mcgpu_topology_desc;
+
+/* Tuned widths, step counter and the tuning counters of a box
+ * (maxBondDelta, maxAngleDelta, stepNum, numBondMoves, numAcceptedBondMoves,
+ * numAngleMoves, numAcceptedAngleMoves; SimBox.h:23-72). */
+typedef struct {
+  double max_bond_delta, max_angle_delta;
+  int64_t step_num;
+  int64_t bond_moves, bond_accepted, angle_moves, angle_accepted;
+} mcgpu_intra_state;
+
+/* Uploads the topology (replaces any earlier one; the counters start at 0).
+ * Checks every index against the box; a bond or angle end outside its
+ * molecule is MCGPU_ERR_INVALID (the reference would index its union-find
+ * scratch out of range). */
+int mcgpu_box_set_topology(mcgpu_box* box, const mcgpu_topology_desc* topo);
+/* ENABLE_INTRA for this box (needs a topology). */
+int mcgpu_box_set_intra(mcgpu_box* box, int enable);
+/* SimCalcs::calcIntraMolecularEnergy (SimulationStep.cpp:80-129): angle and
+ * bond terms of the variable entries when the box has variable angles /
+ * bonds, and when it has either the LJ and Coulomb terms of every
+ * non-excluded atom pair of the molecule (fudge pairs halved, no cutoff). */
+int mcgpu_intra_energy(mcgpu_box* box, int mol, double* out);
+/* SimCalcs::stretchBond (:257-315): bond index within the molecule. */
+int mcgpu_stretch_bond(mcgpu_box* box, int mol, int bond, double dist);
+/* SimCalcs::expandAngle (:148-239): angle index within the molecule,
+ * degrees. */
+int mcgpu_expand_angle(mcgpu_box* box, int mol, int angle, double deg);
+/* SimCalcs::saveBonds / saveAngles (:678-701). */
+int mcgpu_save_intra(mcgpu_box* box, int mol);
+/* SimCalcs::intramolecularMove (:568-675), its draws from the C library's
+ * rand(): save, stretch a random set of bonds, count the MC test, the same
+ * for the angles, tune the widths when the step counter is a nonzero
+ * multiple of 1000. */
+int mcgpu_intramolecular_move(mcgpu_box* box, int mol);
+/* Sets stepNum, the counter the width tuning reads (Simulation::run
+ * increments the reference's after every step, Simulation.cpp:263). */
+int mcgpu_intra_set_step(mcgpu_box* box, int64_t step);
+/* Current bond lengths [n_bond], angle sizes [n_angle] (either may be NULL)
+ * and state. */
+int mcgpu_intra_get(mcgpu_box* box, double* bond_len, double* angle_size,
+                    mcgpu_intra_state* state);
 
 /* ---- device-resident chain (Philox RNG, on-device accept) --------------- */
 

@@ -168,6 +168,16 @@ _PROTOS = {
     "mcgpu_server_counters": (C.c_int, [_vp, C.POINTER(C.c_int64), _dp, C.POINTER(C.c_int64)]),
     "mcgpu_batch_set_precision": (C.c_int, [_vp, C.c_int]),
     "mcgpu_run_plain": (C.c_int, [_vp, C.c_uint, C.c_int, C.c_int, C.POINTER(PlainStats)]),
+    "mcgpu_box_set_topology": (C.c_int, [_vp, C.POINTER(TopoDesc)]),
+    "mcgpu_box_set_intra": (C.c_int, [_vp, C.c_int]),
+    "mcgpu_intra_energy": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_double)]),
+    "mcgpu_stretch_bond": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double]),
+    "mcgpu_expand_angle": (C.c_int, [_vp, C.c_int, C.c_int, C.c_double]),
+    "mcgpu_save_intra": (C.c_int, [_vp, C.c_int]),
+    "mcgpu_intramolecular_move": (C.c_int, [_vp, C.c_int]),
+    "mcgpu_intra_set_step": (C.c_int, [_vp, C.c_int64]),
+    "mcgpu_intra_get": (C.c_int, [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                  C.POINTER(IntraState)]),
     "mcgpu_system_energy_static": (C.c_int, [C.POINTER(BoxDesc), _vp, _vp]),
 }
 

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "host.h"
+#include "intra.h"
 
 
 using namespace mcgpu;
@@ -540,6 +541,8 @@ struct mcgpu_box {
   int* order = nullptr;
   bool chain_state = false;  // pool holds a valid device-resident chain state
   bool rows_stale = false;   // FP64 rows lag the chain state (export before use)
+  std::unique_ptr<IntraHost> intra;  // bond / angle rows (flexible molecules)
+  bool intra_on = false;             // ENABLE_INTRA for this box
 };
 
 // FP64 rows current before a plain entry point reads them.
@@ -667,7 +670,7 @@ extern "C" int mcgpu_mol_energy(mcgpu_box* b, int curr, int start, double* out) 
   if (start < 0 || start > n) return set_err(ctx, MCGPU_ERR_INVALID, "start %d out of [0,%d]", start, n);
   if (start == n) {
     *out = 0.0;
-    return MCGPU_OK;
+    return b->intra_on ? mcgpu_intra_energy(b, curr, out) : MCGPU_OK;
   }
   int rc = box_rows(b);
   if (rc) return rc;
@@ -677,6 +680,15 @@ extern "C" int mcgpu_mol_energy(mcgpu_box* b, int curr, int start, double* out) 
   CK(ctx, launch_mol_energy(b->precision == MCGPU_PREC_FP64, grid, nw * 32, sh, ctx->stream,
                             b->pool.P, 0, curr, start, b->partials, b->counter, b->dout,
                             b->dpairs));
+  if (b->intra_on) {
+    // SimulationStep::calcMoleculeEnergy with ENABLE_INTRA (SimulationStep.cpp:15-18)
+    CK(ctx, launch_intra_energy(b->pool.P, b->intra->R, 0, curr, b->dout + 1, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(b->hout, b->dout, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    *out = b->hout[0] + b->hout[1];
+    return MCGPU_OK;
+  }
   CK(ctx, cudaMemcpyAsync(b->hout, b->dout, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   *out = b->hout[0];
@@ -709,6 +721,8 @@ extern "C" int mcgpu_change_molecule(mcgpu_box* b, int mol, const mcgpu_move* mv
   SmemShape sh = shape_for(b->pool.max_len, 1);
   k_change_molecule<<<1, 32, sh.bytes(), ctx->stream>>>(b->pool.P, 0, mol, host_proposal(mv), sh);
   CK(ctx, cudaGetLastError());
+  // SimCalcs::changeMolecule with ENABLE_INTRA (SimulationStep.cpp:424-428)
+  if (b->intra_on) return mcgpu_intramolecular_move(b, mol);
   return MCGPU_OK;
 }
 
@@ -720,6 +734,11 @@ extern "C" int mcgpu_rollback(mcgpu_box* b, int mol) {
   int rc = box_rows(b);
   if (rc) return rc;
   box_plain_moved(b);
+  if (b->intra_on) {
+    // SimCalcs::rollback's ENABLE_INTRA branch (SimulationStep.cpp:745-748)
+    CK(ctx, launch_intra_rollback(b->pool.P, b->intra->R, 0, mol, ctx->stream));
+    return MCGPU_OK;
+  }
   k_rollback<<<1, 32, 0, ctx->stream>>>(b->pool.P, 0, mol);
   CK(ctx, cudaGetLastError());
   return MCGPU_OK;
@@ -728,6 +747,10 @@ extern "C" int mcgpu_rollback(mcgpu_box* b, int mol) {
 extern "C" int mcgpu_move_energies(mcgpu_box* b, int mol, const mcgpu_move* mv, double* e_old,
                                    double* e_new) {
   if (!b || !e_old || !e_new) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  if (b->intra_on)
+    return set_err(b->ctx, MCGPU_ERR_UNSUPPORTED,
+                   "mcgpu_move_energies moves rigid molecules; with intramolecular moves on use "
+                   "mcgpu_mol_energy and mcgpu_change_molecule");
   int rc = check_move(b, mol, mv);
   if (rc) return rc;
   rc = box_rows(b);
@@ -752,8 +775,24 @@ extern "C" int mcgpu_system_energy(mcgpu_box* b, double* out) {
   mcgpu_ctx* ctx = b->ctx;
   int rc = box_rows(b);
   if (rc) return rc;
-  rc = pool_system_energy(ctx, b->pool, b->precision == MCGPU_PREC_FP64, ctx->stream);
-  if (rc) return rc;
+  if (b->intra_on) {
+    // calcSystemEnergy with ENABLE_INTRA: molecule m adds E(m, j > m) and its
+    // intramolecular energy (SimulationStep.cpp:40-71 over :15-18)
+    DevPool& dp = b->pool;
+    const int nw = 4;
+    SmemShape sh = shape_for(dp.max_len, nw);
+    const int chunk = 1 << 20;
+    for (int m0 = 0; m0 < dp.n_mol; m0 += chunk)
+      CK(ctx, launch_mol_pair_sums(b->precision == MCGPU_PREC_FP64,
+                                   std::min(chunk, dp.n_mol - m0), nw * 32, sh, ctx->stream,
+                                   dp.P, dp.mol_chain, m0, dp.emol, dp.pairs));
+    CK(ctx, launch_intra_add(dp.P, b->intra->R, dp.n_mol, dp.emol, ctx->stream));
+    k_chain_sums<<<dp.n_chains, 256, 0, ctx->stream>>>(dp.P, dp.emol, dp.esum);
+    CK(ctx, cudaGetLastError());
+  } else {
+    rc = pool_system_energy(ctx, b->pool, b->precision == MCGPU_PREC_FP64, ctx->stream);
+    if (rc) return rc;
+  }
   CK(ctx, cudaMemcpyAsync(b->hout, b->pool.esum, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   *out = b->hout[0];
@@ -784,8 +823,12 @@ extern "C" int mcgpu_run_plain(mcgpu_box* b, unsigned int seed, int n_steps, int
   int rc = mcgpu_system_energy(b, &e);
   if (rc) return rc;
   out->energy0 = e;
+  if (b->intra_on) fused = 0;
+  const long long step0 = b->intra ? b->intra->step : 0;
   std::srand(seed);
   for (int step = 0; step < n_steps; step++) {
+    // the counter Simulation::run increments after every step (Simulation.cpp:263)
+    if (b->intra_on) b->intra->step = step0 + step;
     // chooseMolecule (SimulationStep.cpp:25-27); rand() == RAND_MAX gives n,
     // clamped to n - 1 (the reference would read past its rows)
     const int mol = std::min((int)random_real(0, n), n - 1);
@@ -821,11 +864,254 @@ extern "C" int mcgpu_run_plain(mcgpu_box* b, unsigned int seed, int n_steps, int
       if (rc) return rc;
     }
   }
+  if (b->intra_on) b->intra->step = step0 + n_steps;
   long long np = 0;
   CK(ctx, cudaMemcpyAsync(&np, b->dpairs, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   out->energy = e;
   out->pairs = np;
+  return MCGPU_OK;
+}
+
+// ---- flexible molecules ----------------------------------------------------------
+
+extern "C" int mcgpu_box_set_topology(mcgpu_box* b, const mcgpu_topology_desc* t) {
+  if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  mcgpu_ctx* ctx = b->ctx;
+  int rc = box_rows(b);
+  if (rc) return rc;
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  const DevPool& dp = b->pool;
+  std::vector<int> len(dp.n_mol);
+  for (int m = 0; m < dp.n_mol; m++) len[m] = dp.mlen[m] & 255;  // atoms | active << 8
+  std::unique_ptr<IntraHost> I;
+  rc = intra_upload(ctx, dp.n_mol, dp.n_atom, dp.mstart.data(), len.data(), t, &I);
+  if (rc) return rc;
+  b->intra = std::move(I);
+  box_plain_moved(b);
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_box_set_intra(mcgpu_box* b, int enable) {
+  if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  if (enable && !b->intra)
+    return set_err(b->ctx, MCGPU_ERR_INVALID, "intramolecular moves need a topology");
+  b->intra_on = enable != 0;
+  box_plain_moved(b);
+  return MCGPU_OK;
+}
+
+static int intra_checks(mcgpu_box* b, int mol) {
+  if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  if (!b->intra) return set_err(b->ctx, MCGPU_ERR_INVALID, "the box has no topology");
+  if (mol < 0 || mol >= b->pool.n_mol)
+    return set_err(b->ctx, MCGPU_ERR_INVALID, "molecule %d out of [0,%d)", mol, b->pool.n_mol);
+  return box_rows(b);
+}
+
+extern "C" int mcgpu_intra_energy(mcgpu_box* b, int mol, double* out) {
+  int rc = intra_checks(b, mol);
+  if (rc) return rc;
+  if (!out) return set_err(b->ctx, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = b->ctx;
+  IntraHost& I = *b->intra;
+  CK(ctx, launch_intra_energy(b->pool.P, I.R, 0, mol, I.dout, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(I.hout, I.dout, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = I.hout[0];
+  return MCGPU_OK;
+}
+
+// SimCalcs::expandAngle's constant (SimulationStep.cpp:181): its digits
+// differ from pi's after the seventh; kept, since the moved coordinates
+// depend on it.
+static const double kIntraDeg2Rad = 3.14159256358979323846264 / 180.0;
+
+// The cosines and sines of an expansion's two group angles, by the C
+// library, from the angles formed as the reference forms them.
+static void angle_trig(IntraOps& ops, int k, double deg) {
+  const double t1 = deg * -kIntraDeg2Rad, t2 = deg * kIntraDeg2Rad;
+  ops.c1[k] = std::cos(t1);
+  ops.s1[k] = std::sin(t1);
+  ops.c2[k] = std::cos(t2);
+  ops.s2[k] = std::sin(t2);
+}
+
+// Runs ops (kind 0 bonds, 1 angles) of molecule mol in launches of
+// kIntraOps, the first with `first_flags`, the last with the energy after;
+// waits for the energies when `flags` ask for them.
+static int intra_run_ops(mcgpu_box* b, int mol, int kind, const std::vector<int>& idx,
+                         const std::vector<double>& amt, int first_flags, bool energy_after) {
+  mcgpu_ctx* ctx = b->ctx;
+  IntraHost& I = *b->intra;
+  const int n = (int)idx.size();
+  int done = 0;
+  do {
+    IntraOps ops;
+    std::memset(&ops, 0, sizeof(ops));
+    ops.mol = mol;
+    ops.kind = kind;
+    ops.n = std::min(kIntraOps, n - done);
+    for (int k = 0; k < ops.n; k++) {
+      ops.idx[k] = idx[done + k];
+      ops.amt[k] = amt[done + k];
+      if (kind == 1) angle_trig(ops, k, amt[done + k]);
+    }
+    ops.flags = done == 0 ? first_flags : 0;
+    if (done + ops.n >= n && energy_after) ops.flags |= kIntraEnergyAfter;
+    CK(ctx, launch_intra_ops(b->pool.P, I.R, 0, ops, I.dout, ctx->stream));
+    done += ops.n;
+  } while (done < n);
+  box_plain_moved(b);
+  if (first_flags & kIntraEnergyBefore || energy_after) {
+    CK(ctx, cudaMemcpyAsync(I.hout, I.dout, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_stretch_bond(mcgpu_box* b, int mol, int bond, double dist) {
+  int rc = intra_checks(b, mol);
+  if (rc) return rc;
+  if (bond < 0 || bond >= b->intra->bcount[mol])
+    return set_err(b->ctx, MCGPU_ERR_INVALID, "bond %d out of [0,%d) for molecule %d", bond,
+                   b->intra->bcount[mol], mol);
+  return intra_run_ops(b, mol, 0, {bond}, {dist}, 0, false);
+}
+
+extern "C" int mcgpu_expand_angle(mcgpu_box* b, int mol, int angle, double deg) {
+  int rc = intra_checks(b, mol);
+  if (rc) return rc;
+  if (angle < 0 || angle >= b->intra->acount[mol])
+    return set_err(b->ctx, MCGPU_ERR_INVALID, "angle %d out of [0,%d) for molecule %d", angle,
+                   b->intra->acount[mol], mol);
+  return intra_run_ops(b, mol, 1, {angle}, {deg}, 0, false);
+}
+
+extern "C" int mcgpu_save_intra(mcgpu_box* b, int mol) {
+  int rc = intra_checks(b, mol);
+  if (rc) return rc;
+  return intra_run_ops(b, mol, 0, {}, {}, kIntraSave, false);
+}
+
+// The distinct indexes std::set collects from (int)randomReal(0, count)
+// draws until it holds `want` (SimulationStep.cpp:599-601, 631-633), in the
+// set's ascending order; a draw of count (rand() == RAND_MAX) is taken as
+// count - 1 (the reference would index past the molecule's rows).
+static void intra_draw_set(int want, int count, std::vector<int>& out) {
+  out.clear();
+  while ((int)out.size() < want) {
+    int v = std::min((int)random_real(0, count), count - 1);
+    auto it = std::lower_bound(out.begin(), out.end(), v);
+    if (it != out.end() && *it == v) continue;
+    out.insert(it, v);
+  }
+}
+
+extern "C" int mcgpu_intramolecular_move(mcgpu_box* b, int mol) {
+  int rc = intra_checks(b, mol);
+  if (rc) return rc;
+  IntraHost& I = *b->intra;
+  const double kT = b->pool.hdr[0].kT;
+  // ENABLE_BOND + ENABLE_ANGLE + ENABLE_DIHEDRAL = 2 move types
+  const double intra_scale = 0.25 + (0.75 / (double)2);
+  const double bond_delta = I.max_bond_delta, angle_delta = I.max_angle_delta;
+  // acceptMove (SimulationStep.cpp:794-803): a decrease is accepted without a draw
+  auto accept = [&](double de) { return de < 0 || std::exp(-(de) / kT) >= random_real(0.0, 1.0); };
+  std::vector<int> set, idx;
+  std::vector<double> amt;
+  bool saved = false;
+  double cur_e = 0.0;
+  if (I.flex_bonds) {
+    const int nb = I.bcount[mol], bs = I.bstart[mol];
+    int n = nb;
+    if (n > 3) n = std::min((int)random_real(2, nb), I.max_intra_moves);
+    const double scale = 0.25 + (0.75 / (double)n) * intra_scale;
+    I.bond_moves += n;
+    intra_draw_set(n, nb, set);
+    idx.clear();
+    amt.clear();
+    for (int k : set) {
+      const double d = scale * random_real(-bond_delta, bond_delta);
+      if (I.bvar[bs + k]) {
+        idx.push_back(k);
+        amt.push_back(d);
+      }
+    }
+    rc = intra_run_ops(b, mol, 0, idx, amt, kIntraSave | kIntraEnergyBefore, true);
+    if (rc) return rc;
+    saved = true;
+    const double e0 = I.hout[0], e1 = I.hout[1];
+    if (accept(e1 - e0)) I.bond_accepted += n;
+    cur_e = e1;
+  }
+  if (I.flex_angles) {
+    const int na = I.acount[mol], as = I.astart[mol];
+    int n = na;
+    if (n > 3) n = std::min((int)random_real(2, na), I.max_intra_moves);
+    const double scale = 0.25 + (0.75 / (double)n) * intra_scale;
+    I.angle_moves += n;
+    intra_draw_set(n, na, set);
+    idx.clear();
+    amt.clear();
+    for (int k : set) {
+      const double d = scale * random_real(-angle_delta, angle_delta);
+      if (I.avar[as + k]) {
+        idx.push_back(k);
+        amt.push_back(d);
+      }
+    }
+    rc = intra_run_ops(b, mol, 1, idx, amt, saved ? 0 : (kIntraSave | kIntraEnergyBefore), true);
+    if (rc) return rc;
+    if (!saved) cur_e = I.hout[0];
+    const double e1 = I.hout[1];
+    if (accept(e1 - cur_e)) I.angle_accepted += n;
+  }
+  // width tuning (SimulationStep.cpp:656-674): TARGET_RATIO 0.4, RATIO_MARGIN
+  // 1e-4; the angle test reads the entry width, as the reference's does
+  if (I.step != 0 && (I.step % 1000) == 0) {
+    const double bond_ratio = (double)I.bond_accepted / I.bond_moves;
+    const double angle_ratio = (double)I.angle_accepted / I.angle_moves;
+    double diff = bond_ratio - 0.4;
+    if (std::fabs(diff) > 0.0001) I.max_bond_delta += I.max_bond_delta * diff;
+    diff = angle_ratio - 0.4;
+    if (std::fabs(angle_delta) > 0.0001) I.max_angle_delta += I.max_angle_delta * diff;
+    I.bond_accepted = I.bond_moves = 0;
+    I.angle_accepted = I.angle_moves = 0;
+  }
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_intra_set_step(mcgpu_box* b, int64_t step) {
+  if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  if (!b->intra) return set_err(b->ctx, MCGPU_ERR_INVALID, "the box has no topology");
+  b->intra->step = step;
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_intra_get(mcgpu_box* b, double* bond_len, double* angle_size,
+                               mcgpu_intra_state* state) {
+  if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  if (!b->intra) return set_err(b->ctx, MCGPU_ERR_INVALID, "the box has no topology");
+  mcgpu_ctx* ctx = b->ctx;
+  IntraHost& I = *b->intra;
+  if (bond_len && I.n_bond)
+    CK(ctx, cudaMemcpyAsync(bond_len, I.R.b_len, sizeof(double) * I.n_bond,
+                            cudaMemcpyDeviceToHost, ctx->stream));
+  if (angle_size && I.n_angle)
+    CK(ctx, cudaMemcpyAsync(angle_size, I.R.a_size, sizeof(double) * I.n_angle,
+                            cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (state) {
+    state->max_bond_delta = I.max_bond_delta;
+    state->max_angle_delta = I.max_angle_delta;
+    state->step_num = I.step;
+    state->bond_moves = I.bond_moves;
+    state->bond_accepted = I.bond_accepted;
+    state->angle_moves = I.angle_moves;
+    state->angle_accepted = I.angle_accepted;
+  }
   return MCGPU_OK;
 }
 
@@ -836,6 +1122,10 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
   if (n_steps < 0) return set_err(ctx, MCGPU_ERR_INVALID, "negative step count");
   if (rotation != MCGPU_ROT_EULER && rotation != MCGPU_ROT_AXIS)
     return set_err(ctx, MCGPU_ERR_INVALID, "unknown rotation form %d", rotation);
+  if (b->intra_on)
+    return set_err(ctx, MCGPU_ERR_UNSUPPORTED,
+                   "the device-resident chain moves rigid molecules; intramolecular moves run "
+                   "on the plain path");
   cudaStream_t st = ctx->stream;
   DevPool& dp = b->pool;
   ChainHdr* dh = dp.P.hdr;

@@ -100,6 +100,8 @@ class GpuBox:
         _abi.check(_abi.lib().mcgpu_box_upload(ctx.handle, C.byref(self._desc), int(precision),
                                                C.byref(self._h)), ctx.handle)
         self.precision = precision
+        self.topology = None
+        self.intra = False
         ctx.adopt(self)
 
     def _check(self, st: int) -> None:
@@ -168,6 +170,58 @@ class GpuBox:
                                                1 if fused else 0, C.byref(st)))
         return st
 
+    # ---- flexible molecules (the reference's code behind ENABLE_INTRA) ----
+
+    def set_topology(self, topo) -> None:
+        """Bond / angle / exclusion rows (workloads.Topology) for this box
+        (mcgpu_box_set_topology); intramolecular moves stay off."""
+        t = topo.copy().normalise()
+        self._topo = t
+        d = t.desc()
+        self._check(_abi.lib().mcgpu_box_set_topology(self._h, C.byref(d)))
+        self.topology = t
+
+    def set_intra(self, on: bool = True) -> None:
+        """ENABLE_INTRA for this box (mcgpu_box_set_intra): molecule and
+        system energies carry the intramolecular term, change_molecule makes
+        the intramolecular move with its rand() draws, rollback restores the
+        bond lengths and angle sizes."""
+        self._check(_abi.lib().mcgpu_box_set_intra(self._h, 1 if on else 0))
+        self.intra = bool(on)
+
+    def intra_energy(self, mol: int) -> float:
+        out = C.c_double()
+        self._check(_abi.lib().mcgpu_intra_energy(self._h, int(mol), C.byref(out)))
+        return out.value
+
+    def stretch_bond(self, mol: int, bond: int, dist: float) -> None:
+        self._check(_abi.lib().mcgpu_stretch_bond(self._h, int(mol), int(bond), float(dist)))
+
+    def expand_angle(self, mol: int, angle: int, deg: float) -> None:
+        self._check(_abi.lib().mcgpu_expand_angle(self._h, int(mol), int(angle), float(deg)))
+
+    def save_intra(self, mol: int) -> None:
+        self._check(_abi.lib().mcgpu_save_intra(self._h, int(mol)))
+
+    def intramolecular_move(self, mol: int) -> None:
+        self._check(_abi.lib().mcgpu_intramolecular_move(self._h, int(mol)))
+
+    def set_step(self, step: int) -> None:
+        self._check(_abi.lib().mcgpu_intra_set_step(self._h, int(step)))
+
+    def intra_state(self) -> dict:
+        t = self.topology
+        bl, asz = np.empty(max(t.n_bond, 1)), np.empty(max(t.n_angle, 1))
+        st = _abi.IntraState()
+        dp = C.POINTER(C.c_double)
+        self._check(_abi.lib().mcgpu_intra_get(self._h, bl.ctypes.data_as(dp),
+                                               asz.ctypes.data_as(dp), C.byref(st)))
+        return dict(bond_len=bl[:t.n_bond], angle_size=asz[:t.n_angle],
+                    max_bond_delta=st.max_bond_delta, max_angle_delta=st.max_angle_delta,
+                    step_num=st.step_num, bond_moves=st.bond_moves,
+                    bond_accepted=st.bond_accepted, angle_moves=st.angle_moves,
+                    angle_accepted=st.angle_accepted)
+
     def chain_run(self, seed: int, n_steps: int, chain_id: int = 0,
                   rotation: int = _abi.ROT_AXIS, trace: bool = False):
         st = _abi.ChainStats()
@@ -198,7 +252,9 @@ class GpuSimulationStep:
     def calc_molecular_energy_contribution(self, curr: int, start: int) -> float:
         return self.box.mol_energy(curr, start)
 
-    # SimulationStep::calcMoleculeEnergy (SimulationStep.cpp:15-18), intra off.
+    # SimulationStep::calcMoleculeEnergy (SimulationStep.cpp:15-18): with
+    # intramolecular moves on (GpuBox.set_intra) the library adds the
+    # intramolecular energy to the molecule's.
     def calc_molecule_energy(self, curr: int, start: int) -> float:
         return self.calc_molecular_energy_contribution(curr, start)
 
@@ -216,7 +272,9 @@ class GpuSimulationStep:
         rz = self.rng.random_real(-r, r)
         return vertex, dx, dy, dz, rx, ry, rz
 
-    # SimulationStep::changeMolecule -> SimCalcs::intermolecularMove.
+    # SimulationStep::changeMolecule -> SimCalcs::intermolecularMove (and,
+    # with intramolecular moves on, SimCalcs::intramolecularMove, whose draws
+    # the library takes from the same C-library rand()).
     def change_molecule(self, mol: int) -> tuple:
         mv = self.draw_move(mol)
         self.box.change_molecule(mol, *mv)
@@ -249,13 +307,21 @@ def run_plain(step: GpuSimulationStep, n_steps: int, fused: bool = False) -> Pla
     """Simulation::run's NVT loop (Simulation.cpp:219-264) driving the GPU
     step object: choose, old energy, change, new energy, accept or roll back.
     With fused=True the old energy, move and new energy go in one launch
-    (mcgpu_move_energies); the draws and decisions are the same."""
+    (mcgpu_move_energies); the draws and decisions are the same.  With
+    intramolecular moves on the calls are made one by one (fused moves are
+    rigid)."""
     e = step.calc_system_energy()
     e0 = e
     acc = rej = 0
-    for _ in range(n_steps):
+    intra = getattr(step.box, "intra", False)
+    step0 = step.box.topology.step_num if intra else 0
+    for s in range(n_steps):
+        if intra:
+            # the counter Simulation::run increments after every step
+            # (Simulation.cpp:263), read by the intramolecular width tuning
+            step.box.set_step(step0 + s)
         idx = step.choose_molecule()
-        if fused:
+        if fused and not intra:
             mv = step.draw_move(idx)
             old, new = step.box.move_energies(idx, *mv)
         else:

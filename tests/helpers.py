@@ -160,3 +160,40 @@ def random_flex_box(seed: int, n_mol: int = 12):
                     type_natom=natom, pair_code=np.concatenate(codes), max_bond_delta=0.08,
                     max_angle_delta=5.0).normalise()
     return box, topo
+
+
+def intra_abs(box, topo, xyz, mol, bond_len=None, angle_size=None) -> float:
+    """Sum of the magnitudes of the intramolecular terms of molecule mol at
+    coordinates xyz (n_atom x 3): the rounding scale of an FP64 sum of them
+    taken in a different order."""
+    s, n = int(box.mol_start[mol]), int(box.mol_len[mol])
+    t = int(topo.mol_type[mol])
+    code = topo.type_codes(t)
+    L = box.size
+    tot = 0.0
+    bl = topo.bond_len if bond_len is None else bond_len
+    asz = topo.angle_size if angle_size is None else angle_size
+    for k in range(topo.mol_bond_start[mol], topo.mol_bond_start[mol] + topo.mol_bond_count[mol]):
+        if topo.bond_var[k]:
+            tot += abs(topo.bond_k[k]) * (topo.bond_eq[k] - bl[k]) ** 2
+    for k in range(topo.mol_angle_start[mol],
+                   topo.mol_angle_start[mol] + topo.mol_angle_count[mol]):
+        if topo.angle_var[k]:
+            tot += abs(topo.angle_k[k]) * (topo.angle_eq[k] - asz[k]) ** 2
+    for i in range(n):
+        for j in range(i + 1, n):
+            c = code[i, j] if i < code.shape[0] and j < code.shape[0] else 2
+            if c == 0:
+                continue
+            d = xyz[s + j] - xyz[s + i]
+            d -= L * (d < -0.5 * L) - L * (d > 0.5 * L)
+            r2 = float(d @ d)
+            if r2 == 0:
+                continue
+            sg = np.sqrt(abs(box.sigma[s + i] * box.sigma[s + j]))
+            ep = np.sqrt(abs(box.epsilon[s + i] * box.epsilon[s + j]))
+            s6 = (sg * sg / r2) ** 3
+            term = 4 * ep * (s6 * s6 + s6) + abs(box.charge[s + i] * box.charge[s + j]
+                                                  * 332.06) / np.sqrt(r2)
+            tot += (0.5 if c == 1 else 1.0) * term
+    return tot
