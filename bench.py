@@ -8,7 +8,9 @@ FP64 per-move dE and running totals).  One bench step = ``STEPS_PER_BENCH``
 Metropolis steps of every chain (one CUDA-graph replay).  Beside it, the
 plain single-chain GPU drop-in (the SimulationStep contract driven from the
 host with the C library's rand(), one launch per contract call) on the
-256-water box, so the batched/plain ratio of the metric is on the line.
+256-water box, so the batched/plain ratio of the metric is on the line, and
+the same plain path with intramolecular moves on a flexible-molecule box
+(``flexible``).
 
 ``--impl reference`` times the reference's CPU implementation of the path
 (the FP64 restatement in oracle/, bit-identical to the compiled reference)
@@ -293,6 +295,17 @@ def bench_plain(ctx, n_steps: int = 2000) -> dict:
                             "roofline": {"bound": "fp64" if prec == M.PREC_FP64 else "fp32",
                                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                                          "frac": achieved / peak}}
+    out["device"] = {}
+    for name, prec in (("fp64", M.PREC_FP64), ("mixed", M.PREC_MIXED)):
+        g = M.GpuBox(ctx, box, prec)
+        g.run_plain_device(41, 200)                          # warm-up
+        n_dev = 10 * n_steps
+        t0 = time.perf_counter()
+        st = g.run_plain_device(42, n_dev)
+        dt = time.perf_counter() - t0
+        g.close()
+        out["device"][name] = {"moves_per_s": n_dev / dt, "accepted": st.accepted,
+                               "steps": n_dev, "pairs_per_move": st.pairs / n_dev}
     for name, prec, fused in (("fp64", M.PREC_FP64, False), ("mixed", M.PREC_MIXED, False),
                               ("mixed_fused", M.PREC_MIXED, True)):
         g = M.GpuBox(ctx, box, prec)
@@ -306,7 +319,85 @@ def bench_plain(ctx, n_steps: int = 2000) -> dict:
         g.close()
     out["note"] = ("roofline peaks are nominal (FP64 1.25 TFLOP/s, FP32 152 SMs x 128 x 2 x "
                    "2.07 GHz); the plain form is launch- and sync-bound by design: one launch "
-                   "and one D2H sync per contract call")
+                   "and one D2H sync per contract call; 'device' runs the same loop (same "
+                   "rand() stream, restated on the device) on one CTA with no host round trip")
+    return out
+
+
+def bench_flex(ctx, n_steps: int = 3000, cpu_target_s: float = 3.0) -> dict:
+    """Flexible molecules: the plain path with intramolecular moves on (the
+    reference's code behind ENABLE_INTRA), 512 molecules (256 amine chains
+    with every bond and angle variable, 256 rigid waters; the synthetic
+    stand-in for the reference's flexible example, 500 methanols).  Every
+    step: molecule energies with the intramolecular term, the rigid move,
+    a random set of bond stretches and of angle expansions with their MC
+    tests, the width tuning every 1000 steps, accept or roll back (lengths
+    and sizes too); rand() draws in the reference's order.  GPU: the
+    library's C++ loop (two waits a step), FP64 and FP32 intermolecular
+    pairs (intramolecular terms FP64), and the Python mirror making the
+    contract calls one by one.  CPU baseline: the oracle's loop (the
+    reference's arithmetic, one core) on the same box, a bounded sample."""
+    import mcgpu_gb300 as M
+    box, topo = M.workloads.flex_amine_water(512)
+    out = {"workload": f"{box.n_mol} molecules (256 flexible 9-atom amine chains, 256 rigid "
+                       f"waters), {topo.n_bond} bonds, {topo.n_angle} angles, L = "
+                       f"{box.size[0]:.2f} A, rc {box.cutoff} A, {box.temperature} K",
+           "unit": "moves/s"}
+    for name, prec in (("cpp_fp64", M.PREC_FP64), ("cpp_mixed", M.PREC_MIXED)):
+        g = M.GpuBox(ctx, box, prec)
+        g.set_topology(topo)
+        g.set_intra(True)
+        g.run_plain_native(41, 100)                          # warm-up
+        t0 = time.perf_counter()
+        st = g.run_plain_native(42, n_steps)
+        dt = time.perf_counter() - t0
+        s = g.intra_state()
+        out[name] = {"moves_per_s": n_steps / dt, "accepted": st.accepted, "steps": n_steps,
+                     "pairs_per_move": st.pairs / n_steps,
+                     "bond_width": s["max_bond_delta"], "angle_width": s["max_angle_delta"]}
+        g.close()
+    for name, prec in (("device_fp64", M.PREC_FP64), ("device_mixed", M.PREC_MIXED)):
+        g = M.GpuBox(ctx, box, prec)
+        g.set_topology(topo)
+        g.set_intra(True)
+        g.run_plain_device(41, 100)                          # warm-up
+        n_dev = 5 * n_steps
+        t0 = time.perf_counter()
+        st = g.run_plain_device(42, n_dev)
+        dt = time.perf_counter() - t0
+        s = g.intra_state()
+        out[name] = {"moves_per_s": n_dev / dt, "accepted": st.accepted, "steps": n_dev,
+                     "pairs_per_move": st.pairs / n_dev,
+                     "bond_width": s["max_bond_delta"], "angle_width": s["max_angle_delta"]}
+        g.close()
+    g = M.GpuBox(ctx, box, M.PREC_FP64)
+    g.set_topology(topo)
+    g.set_intra(True)
+    step = M.GpuSimulationStep(g, M.LibcRand(42))
+    M.run_plain(step, 50)
+    n_py = max(200, n_steps // 3)
+    t0 = time.perf_counter()
+    res = M.run_plain(step, n_py)
+    out["python_fp64"] = {"moves_per_s": n_py / (time.perf_counter() - t0),
+                          "accepted": res.accepted, "steps": n_py}
+    g.close()
+    from oracle.pyoracle import OracleFlex
+    o = OracleFlex(box, topo)
+    e0 = o.system_energy()
+    M.LibcRand(42)
+    done, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < cpu_target_s:
+        o.run_plain(200, e0)
+        done += 200
+    out["cpu_baseline"] = {"moves_per_s": done / (time.perf_counter() - t0), "kind": "port",
+                           "cores": 1, "sample": f"{done} steps of the oracle's loop"}
+    cpu_v = out["cpu_baseline"]["moves_per_s"]
+    out["gpu_over_cpu"] = {k: out[k]["moves_per_s"] / cpu_v
+                           for k in ("cpp_fp64", "cpp_mixed", "device_fp64", "device_mixed")}
+    out["note"] = ("cpp_*: the host loop over the contract calls, two device waits per step "
+                   "(the bond and angle MC tests decide whether rand() is drawn again before "
+                   "the next draws); device_*: the same loop on one CTA with the C library's "
+                   "generator restated on the device, no host round trip")
     return out
 
 
@@ -548,6 +639,8 @@ def main():
     ap.add_argument("--no-single", action="store_true", help="skip the 4000 x 16-atom chain")
     ap.add_argument("--no-large", action="store_true", help="skip the 32768-water system")
     ap.add_argument("--no-served", action="store_true", help="skip the served request loop")
+    ap.add_argument("--no-flex", action="store_true",
+                    help="skip the flexible-molecule plain path (intramolecular moves)")
     ap.add_argument("--served-window", type=float, default=60.0,
                     help="Poisson arrival window in seconds (60 in the served workload)")
     ap.add_argument("--served-steps", type=int, default=20000)
@@ -663,7 +756,9 @@ def main():
     plain = None
     if rank == 0 and not args.no_plain:
         plain = bench_plain(ctx)
-    single = large = served = None
+    single = large = served = flex = None
+    if rank == 0 and not args.no_flex:
+        flex = bench_flex(ctx)
     if rank == 0 and not args.no_single:
         single = bench_single(ctx)
     if rank == 0 and not args.no_large:
@@ -727,6 +822,7 @@ def main():
                              if (served and plain) else None,
         "single_chain": single,
         "large_system": large,
+        "flexible": flex,
         "cpu_baseline": cpu,
         "wall_s_timed": wall,
     }

@@ -201,6 +201,24 @@ typedef struct {
 int mcgpu_run_plain(mcgpu_box* box, unsigned int seed, int n_steps, int fused,
                     mcgpu_plain_stats* out);
 
+/* The same loop run on the device: one CTA of the GPU takes every step
+ * (chooseMolecule, the rigid move and, with intramolecular moves on, the
+ * stages, their MC tests and the width tuning; energies; acceptMove;
+ * rollback) with no host round trip.  Its draws come from the C library's
+ * generator restated on the device and seeded as srand(seed) seeds it
+ * (glibc's random(): the degree-31 additive feedback generator), so it draws
+ * the numbers the reference's randomReal draws and takes the same decisions
+ * (up to near-ties of FP64 energies summed in another order); rotations use
+ * the device's sin/cos, so coordinates equal the reference's to a few ulps
+ * rather than bit for bit.  The host C library's own rand() state is not
+ * advanced. */
+int mcgpu_run_plain_device(mcgpu_box* box, unsigned int seed, int n_steps,
+                           mcgpu_plain_stats* out);
+
+/* The first n values the restated generator gives after srand(seed)
+ * (host only; for checking it against the C library). */
+int mcgpu_rand_stream(unsigned int seed, int n, int32_t* out);
+
 /* ---- flexible molecules: bonds, angles, intramolecular moves ------------ *
  *
  * The reference compiles bond stretches, angle expansions and the

@@ -543,6 +543,7 @@ struct mcgpu_box {
   bool rows_stale = false;   // FP64 rows lag the chain state (export before use)
   std::unique_ptr<IntraHost> intra;  // bond / angle rows (flexible molecules)
   bool intra_on = false;             // ENABLE_INTRA for this box
+  PlainLoop* dloop = nullptr;        // state of mcgpu_run_plain_device
 };
 
 // FP64 rows current before a plain entry point reads them.
@@ -640,6 +641,7 @@ extern "C" int mcgpu_box_destroy(mcgpu_box* b) {
   if (b->dout) cudaFree(b->dout);
   if (b->hout) cudaFreeHost(b->hout);
   if (b->dpairs) cudaFree(b->dpairs);
+  if (b->dloop) cudaFree(b->dloop);
   if (b->dtrace) cudaFree(b->dtrace);
   if (b->queue) cudaFree(b->queue);
   if (b->order) cudaFree(b->order);
@@ -809,26 +811,16 @@ double random_real(double start, double end) {
 }
 }  // namespace
 
-extern "C" int mcgpu_run_plain(mcgpu_box* b, unsigned int seed, int n_steps, int fused,
-                               mcgpu_plain_stats* out) {
-  if (!b || !out) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
-  mcgpu_ctx* ctx = b->ctx;
-  if (n_steps < 0) return set_err(ctx, MCGPU_ERR_INVALID, "negative step count");
+static int run_plain_intra(mcgpu_box* b, int n_steps, mcgpu_plain_stats* out, double& e);
+
+// The rigid loop: the contract calls one after another (or the fused
+// energy-move-energy call), as a GpuBruteForceStep sees them.
+static int run_plain_rigid(mcgpu_box* b, int n_steps, int fused, mcgpu_plain_stats* out,
+                           double& e) {
   const ChainHdr& h = b->pool.hdr[0];
   const int n = b->pool.n_mol;
   const double kT = h.kT, max_t = h.max_t, max_r = h.max_r;
-  std::memset(out, 0, sizeof(*out));
-  CK(ctx, cudaMemsetAsync(b->dpairs, 0, sizeof(long long), ctx->stream));
-  double e = 0.0;
-  int rc = mcgpu_system_energy(b, &e);
-  if (rc) return rc;
-  out->energy0 = e;
-  if (b->intra_on) fused = 0;
-  const long long step0 = b->intra ? b->intra->step : 0;
-  std::srand(seed);
   for (int step = 0; step < n_steps; step++) {
-    // the counter Simulation::run increments after every step (Simulation.cpp:263)
-    if (b->intra_on) b->intra->step = step0 + step;
     // chooseMolecule (SimulationStep.cpp:25-27); rand() == RAND_MAX gives n,
     // clamped to n - 1 (the reference would read past its rows)
     const int mol = std::min((int)random_real(0, n), n - 1);
@@ -844,6 +836,7 @@ extern "C" int mcgpu_run_plain(mcgpu_box* b, unsigned int seed, int n_steps, int
     mv.ry = random_real(-max_r, max_r);
     mv.rz = random_real(-max_r, max_r);
     double e_old = 0.0, e_new = 0.0;
+    int rc;
     if (fused) {
       rc = mcgpu_move_energies(b, mol, &mv, &e_old, &e_new);
     } else {
@@ -864,12 +857,102 @@ extern "C" int mcgpu_run_plain(mcgpu_box* b, unsigned int seed, int n_steps, int
       if (rc) return rc;
     }
   }
-  if (b->intra_on) b->intra->step = step0 + n_steps;
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_run_plain(mcgpu_box* b, unsigned int seed, int n_steps, int fused,
+                               mcgpu_plain_stats* out) {
+  if (!b || !out) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = b->ctx;
+  if (n_steps < 0) return set_err(ctx, MCGPU_ERR_INVALID, "negative step count");
+  std::memset(out, 0, sizeof(*out));
+  CK(ctx, cudaMemsetAsync(b->dpairs, 0, sizeof(long long), ctx->stream));
+  double e = 0.0;
+  int rc = mcgpu_system_energy(b, &e);
+  if (rc) return rc;
+  out->energy0 = e;
+  std::srand(seed);
+  rc = b->intra_on ? run_plain_intra(b, n_steps, out, e)
+                   : run_plain_rigid(b, n_steps, fused, out, e);
+  if (rc) return rc;
   long long np = 0;
   CK(ctx, cudaMemcpyAsync(&np, b->dpairs, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   out->energy = e;
   out->pairs = np;
+  return MCGPU_OK;
+}
+
+// The same loop on the device: one CTA runs the steps with the restated
+// C-library generator, launches of kDeviceLoopSteps steps.
+static constexpr int kDeviceLoopSteps = 4096;
+
+extern "C" int mcgpu_run_plain_device(mcgpu_box* b, unsigned int seed, int n_steps,
+                                      mcgpu_plain_stats* out) {
+  if (!b || !out) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
+  mcgpu_ctx* ctx = b->ctx;
+  if (n_steps < 0) return set_err(ctx, MCGPU_ERR_INVALID, "negative step count");
+  if (b->intra_on && b->intra->max_intra_moves > kLoopSel)
+    return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "max_intra_moves %d above %d",
+                   b->intra->max_intra_moves, kLoopSel);
+  std::memset(out, 0, sizeof(*out));
+  double e = 0.0;
+  int rc = mcgpu_system_energy(b, &e);
+  if (rc) return rc;
+  out->energy0 = e;
+  if (!b->dloop) CK(ctx, cudaMalloc((void**)&b->dloop, sizeof(PlainLoop)));
+  PlainLoop L;
+  std::memset(&L, 0, sizeof(L));
+  crand_seed(L.rng, seed);
+  L.energy = e;
+  IntraRows R{};
+  if (b->intra_on) {
+    IntraHost& I = *b->intra;
+    R = I.R;
+    L.step = I.step;
+    L.max_bond_delta = I.max_bond_delta;
+    L.max_angle_delta = I.max_angle_delta;
+    L.bond_moves = I.bond_moves;
+    L.bond_accepted = I.bond_accepted;
+    L.angle_moves = I.angle_moves;
+    L.angle_accepted = I.angle_accepted;
+    L.max_intra_moves = I.max_intra_moves;
+  }
+  CK(ctx, cudaMemcpyAsync(b->dloop, &L, sizeof(L), cudaMemcpyHostToDevice, ctx->stream));
+  SmemShape sh = shape_for(b->pool.max_len, 8);
+  for (int done = 0; done < n_steps; done += kDeviceLoopSteps) {
+    const int k = std::min(kDeviceLoopSteps, n_steps - done);
+    CK(ctx, launch_plain_steps(b->precision == MCGPU_PREC_FP64, b->pool.P, R, b->intra_on ? 1 : 0,
+                               b->dloop, k, sh, ctx->stream));
+  }
+  box_plain_moved(b);
+  CK(ctx, cudaMemcpyAsync(&L, b->dloop, sizeof(L), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (L.error)
+    return set_err(ctx, MCGPU_ERR_DEVICE, "an intramolecular stage's index draws did not fill "
+                   "its set (device loop stopped after %lld steps)", L.accepted + L.rejected);
+  if (b->intra_on) {
+    IntraHost& I = *b->intra;
+    I.step = L.step;
+    I.max_bond_delta = L.max_bond_delta;
+    I.max_angle_delta = L.max_angle_delta;
+    I.bond_moves = L.bond_moves;
+    I.bond_accepted = L.bond_accepted;
+    I.angle_moves = L.angle_moves;
+    I.angle_accepted = L.angle_accepted;
+  }
+  out->energy = L.energy;
+  out->accepted = L.accepted;
+  out->rejected = L.rejected;
+  out->pairs = L.pairs;
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_rand_stream(unsigned int seed, int n, int32_t* out) {
+  if (n < 0 || (n && !out)) return set_err(nullptr, MCGPU_ERR_INVALID, "bad argument");
+  CRand g;
+  crand_seed(g, seed);
+  for (int k = 0; k < n; k++) out[k] = crand_next(g);
   return MCGPU_OK;
 }
 
@@ -937,11 +1020,11 @@ static void angle_trig(IntraOps& ops, int k, double deg) {
   ops.s2[k] = std::sin(t2);
 }
 
-// Runs ops (kind 0 bonds, 1 angles) of molecule mol in launches of
-// kIntraOps, the first with `first_flags`, the last with the energy after;
-// waits for the energies when `flags` ask for them.
-static int intra_run_ops(mcgpu_box* b, int mol, int kind, const std::vector<int>& idx,
-                         const std::vector<double>& amt, int first_flags, bool energy_after) {
+// Launches ops (kind 0 bonds, 1 angles) of molecule mol in launches of
+// kIntraOps, the first with `first_flags`, the last with the energy after
+// (into the topology's device out[0..1]); no wait.
+static int intra_launch_ops(mcgpu_box* b, int mol, int kind, const std::vector<int>& idx,
+                            const std::vector<double>& amt, int first_flags, bool energy_after) {
   mcgpu_ctx* ctx = b->ctx;
   IntraHost& I = *b->intra;
   const int n = (int)idx.size();
@@ -963,7 +1046,17 @@ static int intra_run_ops(mcgpu_box* b, int mol, int kind, const std::vector<int>
     done += ops.n;
   } while (done < n);
   box_plain_moved(b);
+  return MCGPU_OK;
+}
+
+// intra_launch_ops, then the stage's energies in the topology's host out[0..1].
+static int intra_run_ops(mcgpu_box* b, int mol, int kind, const std::vector<int>& idx,
+                         const std::vector<double>& amt, int first_flags, bool energy_after) {
+  int rc = intra_launch_ops(b, mol, kind, idx, amt, first_flags, energy_after);
+  if (rc) return rc;
   if (first_flags & kIntraEnergyBefore || energy_after) {
+    mcgpu_ctx* ctx = b->ctx;
+    IntraHost& I = *b->intra;
     CK(ctx, cudaMemcpyAsync(I.hout, I.dout, 2 * sizeof(double), cudaMemcpyDeviceToHost,
                             ctx->stream));
     CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1009,77 +1102,185 @@ static void intra_draw_set(int want, int count, std::vector<int>& out) {
   }
 }
 
+// The draws of one stage of SimCalcs::intramolecularMove (kind 0: bonds,
+// :589-609; kind 1: angles, :621-640) with the entry width `delta`: how many
+// (2 move types, ENABLE_BOND + ENABLE_ANGLE), which, and an amount for each
+// drawn whether or not the entry is variable; idx / amt keep the variable
+// ones.  Returns the count the move counters take.
+static int intra_draw_stage(IntraHost& I, int mol, int kind, double delta,
+                            std::vector<int>& idx, std::vector<double>& amt) {
+  const double intra_scale = 0.25 + (0.75 / (double)2);
+  const int count = kind == 0 ? I.bcount[mol] : I.acount[mol];
+  const int start = kind == 0 ? I.bstart[mol] : I.astart[mol];
+  const std::vector<int>& var = kind == 0 ? I.bvar : I.avar;
+  int n = count;
+  if (n > 3) n = std::min((int)random_real(2, count), I.max_intra_moves);
+  const double scale = 0.25 + (0.75 / (double)n) * intra_scale;
+  std::vector<int> set;
+  intra_draw_set(n, count, set);
+  idx.clear();
+  amt.clear();
+  for (int k : set) {
+    const double d = scale * random_real(-delta, delta);
+    if (var[start + k]) {
+      idx.push_back(k);
+      amt.push_back(d);
+    }
+  }
+  return n;
+}
+
+// acceptMove (SimulationStep.cpp:794-803): a decrease is accepted without a
+// draw, otherwise exp(-dE/kT) against a uniform from rand().
+static bool host_accept(double de, double kT) {
+  return de < 0 || std::exp(-(de) / kT) >= random_real(0.0, 1.0);
+}
+
+// The width tuning at the end of SimCalcs::intramolecularMove (:656-674):
+// TARGET_RATIO 0.4, RATIO_MARGIN 1e-4; the angle test reads the entry width,
+// as the reference's does.
+static void intra_tune(IntraHost& I, double angle_delta) {
+  if (I.step == 0 || (I.step % 1000) != 0) return;
+  const double bond_ratio = (double)I.bond_accepted / I.bond_moves;
+  const double angle_ratio = (double)I.angle_accepted / I.angle_moves;
+  double diff = bond_ratio - 0.4;
+  if (std::fabs(diff) > 0.0001) I.max_bond_delta += I.max_bond_delta * diff;
+  diff = angle_ratio - 0.4;
+  if (std::fabs(angle_delta) > 0.0001) I.max_angle_delta += I.max_angle_delta * diff;
+  I.bond_accepted = I.bond_moves = 0;
+  I.angle_accepted = I.angle_moves = 0;
+}
+
 extern "C" int mcgpu_intramolecular_move(mcgpu_box* b, int mol) {
   int rc = intra_checks(b, mol);
   if (rc) return rc;
   IntraHost& I = *b->intra;
   const double kT = b->pool.hdr[0].kT;
-  // ENABLE_BOND + ENABLE_ANGLE + ENABLE_DIHEDRAL = 2 move types
-  const double intra_scale = 0.25 + (0.75 / (double)2);
   const double bond_delta = I.max_bond_delta, angle_delta = I.max_angle_delta;
-  // acceptMove (SimulationStep.cpp:794-803): a decrease is accepted without a draw
-  auto accept = [&](double de) { return de < 0 || std::exp(-(de) / kT) >= random_real(0.0, 1.0); };
-  std::vector<int> set, idx;
+  std::vector<int> idx;
   std::vector<double> amt;
   bool saved = false;
   double cur_e = 0.0;
   if (I.flex_bonds) {
-    const int nb = I.bcount[mol], bs = I.bstart[mol];
-    int n = nb;
-    if (n > 3) n = std::min((int)random_real(2, nb), I.max_intra_moves);
-    const double scale = 0.25 + (0.75 / (double)n) * intra_scale;
+    const int n = intra_draw_stage(I, mol, 0, bond_delta, idx, amt);
     I.bond_moves += n;
-    intra_draw_set(n, nb, set);
-    idx.clear();
-    amt.clear();
-    for (int k : set) {
-      const double d = scale * random_real(-bond_delta, bond_delta);
-      if (I.bvar[bs + k]) {
-        idx.push_back(k);
-        amt.push_back(d);
-      }
-    }
     rc = intra_run_ops(b, mol, 0, idx, amt, kIntraSave | kIntraEnergyBefore, true);
     if (rc) return rc;
     saved = true;
-    const double e0 = I.hout[0], e1 = I.hout[1];
-    if (accept(e1 - e0)) I.bond_accepted += n;
-    cur_e = e1;
+    if (host_accept(I.hout[1] - I.hout[0], kT)) I.bond_accepted += n;
+    cur_e = I.hout[1];
   }
   if (I.flex_angles) {
-    const int na = I.acount[mol], as = I.astart[mol];
-    int n = na;
-    if (n > 3) n = std::min((int)random_real(2, na), I.max_intra_moves);
-    const double scale = 0.25 + (0.75 / (double)n) * intra_scale;
+    const int n = intra_draw_stage(I, mol, 1, angle_delta, idx, amt);
     I.angle_moves += n;
-    intra_draw_set(n, na, set);
-    idx.clear();
-    amt.clear();
-    for (int k : set) {
-      const double d = scale * random_real(-angle_delta, angle_delta);
-      if (I.avar[as + k]) {
-        idx.push_back(k);
-        amt.push_back(d);
-      }
-    }
     rc = intra_run_ops(b, mol, 1, idx, amt, saved ? 0 : (kIntraSave | kIntraEnergyBefore), true);
     if (rc) return rc;
     if (!saved) cur_e = I.hout[0];
-    const double e1 = I.hout[1];
-    if (accept(e1 - cur_e)) I.angle_accepted += n;
+    if (host_accept(I.hout[1] - cur_e, kT)) I.angle_accepted += n;
   }
-  // width tuning (SimulationStep.cpp:656-674): TARGET_RATIO 0.4, RATIO_MARGIN
-  // 1e-4; the angle test reads the entry width, as the reference's does
-  if (I.step != 0 && (I.step % 1000) == 0) {
-    const double bond_ratio = (double)I.bond_accepted / I.bond_moves;
-    const double angle_ratio = (double)I.angle_accepted / I.angle_moves;
-    double diff = bond_ratio - 0.4;
-    if (std::fabs(diff) > 0.0001) I.max_bond_delta += I.max_bond_delta * diff;
-    diff = angle_ratio - 0.4;
-    if (std::fabs(angle_delta) > 0.0001) I.max_angle_delta += I.max_angle_delta * diff;
-    I.bond_accepted = I.bond_moves = 0;
-    I.angle_accepted = I.angle_moves = 0;
+  intra_tune(I, angle_delta);
+  return MCGPU_OK;
+}
+
+// mcgpu_run_plain's loop with intramolecular moves: the calls and draws of
+// the reference's loop with ENABLE_INTRA, launched so that each step waits
+// on the device twice.  Draws that do not depend on an energy are taken
+// ahead: molecule, the rigid move and the bond stage's draws go before the
+// first wait, with the old energy, the rigid move and the bond stage
+// launched behind them; the bond test's uniform (when drawn) and the angle
+// stage's draws go before the second wait, behind which run the angle stage
+// and the new energy.  The draw order and every value are those of the
+// one-call-at-a-time sequence.
+static int run_plain_intra(mcgpu_box* b, int n_steps, mcgpu_plain_stats* out, double& e) {
+  mcgpu_ctx* ctx = b->ctx;
+  IntraHost& I = *b->intra;
+  const ChainHdr& h = b->pool.hdr[0];
+  const int n = b->pool.n_mol;
+  const double kT = h.kT, max_t = h.max_t, max_r = h.max_r;
+  const bool f64 = b->precision == MCGPU_PREC_FP64;
+  const int nw = 4;
+  SmemShape sh = shape_for(b->pool.max_len, nw);
+  SmemShape sh1 = shape_for(b->pool.max_len, 1);
+  const int grid = box_grid(b, n);
+  const long long step0 = I.step;
+  std::vector<int> idx;
+  std::vector<double> amt;
+  double* hv = b->hout;   // [0] inter, [1] intra (host copies), [2..3] stage energies
+  for (int step = 0; step < n_steps; step++) {
+    I.step = step0 + step;
+    const int mol = std::min((int)random_real(0, n), n - 1);
+    const int len = b->pool.mlen[mol] & 255;
+    mcgpu_move mv;
+    std::memset(&mv, 0, sizeof(mv));
+    mv.vertex = std::min((int)random_real(0, len), len - 1);
+    mv.dx = random_real(-max_t, max_t);
+    mv.dy = random_real(-max_t, max_t);
+    mv.dz = random_real(-max_t, max_t);
+    mv.rx = random_real(-max_r, max_r);
+    mv.ry = random_real(-max_r, max_r);
+    mv.rz = random_real(-max_r, max_r);
+    const double bond_delta = I.max_bond_delta, angle_delta = I.max_angle_delta;
+    // old energy (inter + intra), the rigid move, the bond stage
+    CK(ctx, launch_mol_energy(f64, grid, nw * 32, sh, ctx->stream, b->pool.P, 0, mol, 0,
+                              b->partials, b->counter, b->dout, b->dpairs));
+    CK(ctx, launch_intra_energy(b->pool.P, I.R, 0, mol, b->dout + 1, ctx->stream));
+    k_change_molecule<<<1, 32, sh1.bytes(), ctx->stream>>>(b->pool.P, 0, mol,
+                                                           host_proposal(&mv), sh1);
+    CK(ctx, cudaGetLastError());
+    box_plain_moved(b);
+    int nb = 0;
+    if (I.flex_bonds) {
+      nb = intra_draw_stage(I, mol, 0, bond_delta, idx, amt);
+      I.bond_moves += nb;
+      int rc = intra_launch_ops(b, mol, 0, idx, amt, kIntraSave | kIntraEnergyBefore, true);
+      if (rc) return rc;
+    }
+    CK(ctx, cudaMemcpyAsync(hv, b->dout, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    if (I.flex_bonds)
+      CK(ctx, cudaMemcpyAsync(I.hout, I.dout, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    const double e_old = hv[0] + hv[1];
+    double cur_e = 0.0;
+    if (I.flex_bonds) {
+      if (host_accept(I.hout[1] - I.hout[0], kT)) I.bond_accepted += nb;
+      cur_e = I.hout[1];
+    }
+    // the angle stage and the new energy
+    int na = 0;
+    if (I.flex_angles) {
+      na = intra_draw_stage(I, mol, 1, angle_delta, idx, amt);
+      I.angle_moves += na;
+      int rc = intra_launch_ops(b, mol, 1, idx, amt,
+                                I.flex_bonds ? 0 : (kIntraSave | kIntraEnergyBefore), true);
+      if (rc) return rc;
+    }
+    CK(ctx, launch_mol_energy(f64, grid, nw * 32, sh, ctx->stream, b->pool.P, 0, mol, 0,
+                              b->partials, b->counter, b->dout, b->dpairs));
+    CK(ctx, launch_intra_energy(b->pool.P, I.R, 0, mol, b->dout + 1, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(hv, b->dout, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    if (I.flex_angles)
+      CK(ctx, cudaMemcpyAsync(I.hout, I.dout, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                              ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    if (I.flex_angles) {
+      if (!I.flex_bonds) cur_e = I.hout[0];
+      if (host_accept(I.hout[1] - cur_e, kT)) I.angle_accepted += na;
+    }
+    intra_tune(I, angle_delta);
+    const double e_new = hv[0] + hv[1];
+    const double de = e_new - e_old;
+    if (host_accept(de, kT)) {
+      e += de;
+      out->accepted++;
+    } else {
+      out->rejected++;
+      CK(ctx, launch_intra_rollback(b->pool.P, I.R, 0, mol, ctx->stream));
+    }
   }
+  I.step = step0 + n_steps;
   return MCGPU_OK;
 }
 

@@ -29,24 +29,22 @@ constexpr int kIntraThreads = 128;
 
 // The SimCalcs pair terms of the intramolecular energy (SimulationStep.cpp:
 // 344-375): blending by sqrt|a b| (sites with negative sigma or epsilon take
-// part), no cutoff, zero at r = 0.
+// part), no cutoff, zero at r = 0.  1/r from one FP64 rsqrt (a few ulps from
+// the reference's sqrt and divisions, which cost many FP64 passes on this
+// part); sigma^2 = |s_i s_j| and 4 eps = 4 sqrt|e_i e_j|.
 __device__ __forceinline__ double intra_pair(const Pool& P, int i, int j, const ChainHdr& H) {
   const double dx = make_periodic(__dsub_rn(P.x[j], P.x[i]), H.L[0]);
   const double dy = make_periodic(__dsub_rn(P.y[j], P.y[i]), H.L[1]);
   const double dz = make_periodic(__dsub_rn(P.z[j], P.z[i]), H.L[2]);
   const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-  const double r = sqrt(r2);
-  double lj = 0.0, c = 0.0;
-  if (r2 != 0.0) {
-    const double ss = P.sig[i] * P.sig[j], ee = P.eps[i] * P.eps[j];
-    const double sigma = sqrt(ss >= 0 ? ss : -ss);
-    const double eps = sqrt(ee >= 0 ? ee : -ee);
-    const double s2 = sigma * sigma / r2;
-    const double s6 = s2 * s2 * s2;
-    lj = 4.0 * eps * (s6 * s6 - s6);
-  }
-  if (r != 0.0) c = (P.q[i] * P.q[j] * 332.06) / r;
-  return lj + c;
+  if (r2 == 0.0) return 0.0;
+  const double ri = rsqrt(r2);
+  const double ss = fabs(P.sig[i] * P.sig[j]);
+  const double ee = P.eps[i] * P.eps[j];
+  const double s2 = ss * (ri * ri);
+  const double s6 = s2 * s2 * s2;
+  const double lj = 4.0 * sqrt(fabs(ee)) * (s6 * s6 - s6);
+  return lj + P.q[i] * P.q[j] * 332.06 * ri;
 }
 
 // Block-wide deterministic sum of three values (every thread gets them).
@@ -155,125 +153,159 @@ __global__ void __launch_bounds__(kIntraThreads) k_intra_add(Pool P, IntraRows R
   if (threadIdx.x == 0) emol[H.mol0 + mol] += e;
 }
 
+// One SimCalcs::stretchBond (kind 0, SimulationStep.cpp:257-315) or
+// SimCalcs::expandAngle (kind 1, :148-239) of entry i of box molecule mol,
+// every thread of the block; c1, s1 / c2, s2: the cosine and sine of the
+// first / second group's angle.  Returns false when the call changes nothing
+// (a bond in a ring, an angle whose ends share a component).
+__device__ bool apply_op(const Pool& P, const IntraRows& R, const ChainHdr& H, int mol, int kind,
+                         int i, double amt, double c1, double s1, double c2, double s2,
+                         double* sv) {
+  const int m = H.mol0 + mol;
+  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
+  const int tid = threadIdx.x;
+  if (kind == 0) {
+    const int b = R.m_bstart[mol] + i;
+    const int off = R.b_part[b];
+    if (off < 0) return false;  // a ring: the reference returns before moving
+    if (tid < 3) {
+      // lanes 0-2 each form the whole vector and its length (same values)
+      // and divide their own component: one division's latency, not three.
+      // (v / d) / 2 == (v / d) * 0.5 exactly.
+      const int e1 = H.atom0 + R.b_a1[b], e2 = H.atom0 + R.b_a2[b];
+      const double vx = __dsub_rn(P.x[e2], P.x[e1]);
+      const double vy = __dsub_rn(P.y[e2], P.y[e1]);
+      const double vz = __dsub_rn(P.z[e2], P.z[e1]);
+      double d = __dadd_rn(0.0, __dmul_rn(vx, vx));
+      d = __dadd_rn(d, __dmul_rn(vy, vy));
+      d = __dadd_rn(d, __dmul_rn(vz, vz));
+      d = __dsqrt_rn(d);
+      const double vc = tid == 0 ? vx : (tid == 1 ? vy : vz);
+      sv[tid] = __dmul_rn(__ddiv_rn(vc, d), 0.5);
+      if (tid == 0) R.b_len[b] = __dadd_rn(R.b_len[b], amt);
+    }
+    __syncthreads();
+    if (tid < len) {
+      const int a = a0 + tid;
+      const double sx = __dmul_rn(sv[0], amt), sy = __dmul_rn(sv[1], amt),
+                   sz = __dmul_rn(sv[2], amt);
+      if (R.part[off + tid] == 1) {
+        P.x[a] = __dadd_rn(P.x[a], sx);
+        P.y[a] = __dadd_rn(P.y[a], sy);
+        P.z[a] = __dadd_rn(P.z[a], sz);
+      } else {
+        P.x[a] = __dsub_rn(P.x[a], sx);
+        P.y[a] = __dsub_rn(P.y[a], sy);
+        P.z[a] = __dsub_rn(P.z[a], sz);
+      }
+    }
+    __syncthreads();
+    return true;
+  }
+  const int g = R.m_astart[mol] + i;
+  const int off = R.a_part[g];
+  if (off < 0) return false;  // both ends in one component
+  if (tid < 3) {
+    // lanes 0-2: the same normal and length, one component's division each
+    const int e1 = H.atom0 + R.a_a1[g], e2 = H.atom0 + R.a_a2[g], md = H.atom0 + R.a_mid[g];
+    const double m0 = P.x[md], m1 = P.y[md], m2 = P.z[md];
+    const double p0 = __dsub_rn(m0, P.x[e1]), p1 = __dsub_rn(m1, P.y[e1]),
+                 p2 = __dsub_rn(m2, P.z[e1]);
+    const double q0 = __dsub_rn(m0, P.x[e2]), q1 = __dsub_rn(m1, P.y[e2]),
+                 q2 = __dsub_rn(m2, P.z[e2]);
+    const double n0 = __dsub_rn(__dmul_rn(p1, q2), __dmul_rn(q1, p2));
+    const double n1 = __dsub_rn(__dmul_rn(q0, p2), __dmul_rn(p0, q2));
+    const double n2 = __dsub_rn(__dmul_rn(p0, q1), __dmul_rn(q0, p1));
+    double nl = __dadd_rn(0.0, __dmul_rn(n0, n0));
+    nl = __dadd_rn(nl, __dmul_rn(n1, n1));
+    nl = __dadd_rn(nl, __dmul_rn(n2, n2));
+    nl = __dsqrt_rn(nl);
+    const double nc = tid == 0 ? n0 : (tid == 1 ? n1 : n2);
+    sv[tid] = __ddiv_rn(nc, nl);
+    sv[3 + tid] = tid == 0 ? m0 : (tid == 1 ? m1 : m2);
+    if (tid == 0) R.a_size[g] = __dadd_rn(R.a_size[g], amt);
+  }
+  __syncthreads();
+  if (tid < len) {
+    const int lab = R.part[off + tid];
+    if (lab) {
+      const double cs = lab == 1 ? c1 : c2;
+      const double sn = lab == 1 ? s1 : s2;
+      const double omc = __dsub_rn(1.0, cs);
+      const int a = a0 + tid;
+      const double t0 = __dsub_rn(P.x[a], sv[3]), t1 = __dsub_rn(P.y[a], sv[4]),
+                   t2 = __dsub_rn(P.z[a], sv[5]);
+      double dot = __dadd_rn(0.0, __dmul_rn(t0, sv[0]));
+      dot = __dadd_rn(dot, __dmul_rn(t1, sv[1]));
+      dot = __dadd_rn(dot, __dmul_rn(t2, sv[2]));
+      const double k0 = __dsub_rn(__dmul_rn(sv[1], t2), __dmul_rn(t1, sv[2]));
+      const double k1 = __dsub_rn(__dmul_rn(t0, sv[2]), __dmul_rn(sv[0], t2));
+      const double k2 = __dsub_rn(__dmul_rn(sv[0], t1), __dmul_rn(t0, sv[1]));
+      const double u0 = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(sv[0], dot), omc),
+                                            __dmul_rn(t0, cs)), __dmul_rn(k0, sn));
+      const double u1 = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(sv[1], dot), omc),
+                                            __dmul_rn(t1, cs)), __dmul_rn(k1, sn));
+      const double u2 = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(sv[2], dot), omc),
+                                            __dmul_rn(t2, cs)), __dmul_rn(k2, sn));
+      P.x[a] = __dadd_rn(u0, sv[3]);
+      P.y[a] = __dadd_rn(u1, sv[4]);
+      P.z[a] = __dadd_rn(u2, sv[5]);
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+// SimCalcs::saveBonds / saveAngles (SimulationStep.cpp:678-701), all threads.
+__device__ void save_rows(const IntraRows& R, int mol) {
+  for (int k = R.m_bstart[mol] + threadIdx.x; k < R.m_bstart[mol] + R.m_bcount[mol];
+       k += blockDim.x)
+    R.b_len_rb[k] = R.b_len[k];
+  for (int k = R.m_astart[mol] + threadIdx.x; k < R.m_astart[mol] + R.m_acount[mol];
+       k += blockDim.x)
+    R.a_size_rb[k] = R.a_size[k];
+}
+
+// Rollback with the ENABLE_INTRA branch (SimulationStep.cpp:731-775):
+// coordinates from the rollback copy, angle sizes and bond lengths from
+// theirs, then the mirrors; all threads.
+__device__ void rollback_rows(const Pool& P, const IntraRows& R, const ChainHdr& H, int chain,
+                              int mol, double* red) {
+  const int m = H.mol0 + mol;
+  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
+  const double* rb = P.rb + (size_t)chain * 3 * H.max_len;
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    P.x[a0 + i] = rb[i];
+    P.y[a0 + i] = rb[H.max_len + i];
+    P.z[a0 + i] = rb[2 * H.max_len + i];
+  }
+  for (int k = R.m_astart[mol] + threadIdx.x; k < R.m_astart[mol] + R.m_acount[mol];
+       k += blockDim.x)
+    R.a_size[k] = R.a_size_rb[k];
+  for (int k = R.m_bstart[mol] + threadIdx.x; k < R.m_bstart[mol] + R.m_bcount[mol];
+       k += blockDim.x)
+    R.b_len[k] = R.b_len_rb[k];
+  __syncthreads();
+  refresh_flexible(P, H, m, red);
+}
+
 __global__ void __launch_bounds__(kIntraThreads) k_intra_ops(Pool P, IntraRows R, int chain,
                                                              IntraOps ops, double* out) {
   __shared__ double red[3 * (kIntraThreads / 32)];
   __shared__ double sv[9];
   const ChainHdr& H = P.hdr[chain];
   const int mol = ops.mol, m = H.mol0 + mol;
-  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
   const int tid = threadIdx.x;
-  if (ops.flags & kIntraSave) {
-    // SimCalcs::saveBonds / saveAngles (SimulationStep.cpp:678-701)
-    for (int k = R.m_bstart[mol] + tid; k < R.m_bstart[mol] + R.m_bcount[mol]; k += blockDim.x)
-      R.b_len_rb[k] = R.b_len[k];
-    for (int k = R.m_astart[mol] + tid; k < R.m_astart[mol] + R.m_acount[mol]; k += blockDim.x)
-      R.a_size_rb[k] = R.a_size[k];
-  }
+  if (ops.flags & kIntraSave) save_rows(R, mol);
   __syncthreads();
   if (ops.flags & kIntraEnergyBefore) {
     const double e = intra_energy(P, R, H, mol, red);
     if (tid == 0) out[0] = e;
   }
   bool moved = false;
-  for (int k = 0; k < ops.n; k++) {
-    const int i = ops.idx[k];
-    if (ops.kind == 0) {
-      // SimCalcs::stretchBond (SimulationStep.cpp:257-315)
-      const int b = R.m_bstart[mol] + i;
-      const int off = R.b_part[b];
-      if (off < 0) continue;  // a ring: the reference returns before moving
-      const double dist = ops.amt[k];
-      if (tid == 0) {
-        const int e1 = H.atom0 + R.b_a1[b], e2 = H.atom0 + R.b_a2[b];
-        const double vx = __dsub_rn(P.x[e2], P.x[e1]);
-        const double vy = __dsub_rn(P.y[e2], P.y[e1]);
-        const double vz = __dsub_rn(P.z[e2], P.z[e1]);
-        double d = __dadd_rn(0.0, __dmul_rn(vx, vx));
-        d = __dadd_rn(d, __dmul_rn(vy, vy));
-        d = __dadd_rn(d, __dmul_rn(vz, vz));
-        d = __dsqrt_rn(d);
-        sv[0] = __ddiv_rn(__ddiv_rn(vx, d), 2.0);
-        sv[1] = __ddiv_rn(__ddiv_rn(vy, d), 2.0);
-        sv[2] = __ddiv_rn(__ddiv_rn(vz, d), 2.0);
-        R.b_len[b] = __dadd_rn(R.b_len[b], dist);
-      }
-      __syncthreads();
-      if (tid < len) {
-        const int a = a0 + tid;
-        const double sx = __dmul_rn(sv[0], dist), sy = __dmul_rn(sv[1], dist),
-                     sz = __dmul_rn(sv[2], dist);
-        if (R.part[off + tid] == 1) {
-          P.x[a] = __dadd_rn(P.x[a], sx);
-          P.y[a] = __dadd_rn(P.y[a], sy);
-          P.z[a] = __dadd_rn(P.z[a], sz);
-        } else {
-          P.x[a] = __dsub_rn(P.x[a], sx);
-          P.y[a] = __dsub_rn(P.y[a], sy);
-          P.z[a] = __dsub_rn(P.z[a], sz);
-        }
-      }
-      moved = true;
-      __syncthreads();
-    } else {
-      // SimCalcs::expandAngle (SimulationStep.cpp:148-239)
-      const int g = R.m_astart[mol] + i;
-      const int off = R.a_part[g];
-      if (off < 0) continue;  // both ends in one component
-      if (tid == 0) {
-        const int e1 = H.atom0 + R.a_a1[g], e2 = H.atom0 + R.a_a2[g],
-                  md = H.atom0 + R.a_mid[g];
-        const double m0 = P.x[md], m1 = P.y[md], m2 = P.z[md];
-        const double p0 = __dsub_rn(m0, P.x[e1]), p1 = __dsub_rn(m1, P.y[e1]),
-                     p2 = __dsub_rn(m2, P.z[e1]);
-        const double q0 = __dsub_rn(m0, P.x[e2]), q1 = __dsub_rn(m1, P.y[e2]),
-                     q2 = __dsub_rn(m2, P.z[e2]);
-        double n0 = __dsub_rn(__dmul_rn(p1, q2), __dmul_rn(q1, p2));
-        double n1 = __dsub_rn(__dmul_rn(q0, p2), __dmul_rn(p0, q2));
-        double n2 = __dsub_rn(__dmul_rn(p0, q1), __dmul_rn(q0, p1));
-        double nl = __dadd_rn(0.0, __dmul_rn(n0, n0));
-        nl = __dadd_rn(nl, __dmul_rn(n1, n1));
-        nl = __dadd_rn(nl, __dmul_rn(n2, n2));
-        nl = __dsqrt_rn(nl);
-        sv[0] = __ddiv_rn(n0, nl);
-        sv[1] = __ddiv_rn(n1, nl);
-        sv[2] = __ddiv_rn(n2, nl);
-        sv[3] = m0;
-        sv[4] = m1;
-        sv[5] = m2;
-        R.a_size[g] = __dadd_rn(R.a_size[g], ops.amt[k]);
-      }
-      __syncthreads();
-      if (tid < len) {
-        const int lab = R.part[off + tid];
-        if (lab) {
-          const double cs = lab == 1 ? ops.c1[k] : ops.c2[k];
-          const double sn = lab == 1 ? ops.s1[k] : ops.s2[k];
-          const double omc = __dsub_rn(1.0, cs);
-          const int a = a0 + tid;
-          const double t0 = __dsub_rn(P.x[a], sv[3]), t1 = __dsub_rn(P.y[a], sv[4]),
-                       t2 = __dsub_rn(P.z[a], sv[5]);
-          double dot = __dadd_rn(0.0, __dmul_rn(t0, sv[0]));
-          dot = __dadd_rn(dot, __dmul_rn(t1, sv[1]));
-          dot = __dadd_rn(dot, __dmul_rn(t2, sv[2]));
-          const double c0 = __dsub_rn(__dmul_rn(sv[1], t2), __dmul_rn(t1, sv[2]));
-          const double c1 = __dsub_rn(__dmul_rn(t0, sv[2]), __dmul_rn(sv[0], t2));
-          const double c2 = __dsub_rn(__dmul_rn(sv[0], t1), __dmul_rn(t0, sv[1]));
-          const double u0 = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(sv[0], dot), omc),
-                                                __dmul_rn(t0, cs)), __dmul_rn(c0, sn));
-          const double u1 = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(sv[1], dot), omc),
-                                                __dmul_rn(t1, cs)), __dmul_rn(c1, sn));
-          const double u2 = __dadd_rn(__dadd_rn(__dmul_rn(__dmul_rn(sv[2], dot), omc),
-                                                __dmul_rn(t2, cs)), __dmul_rn(c2, sn));
-          P.x[a] = __dadd_rn(u0, sv[3]);
-          P.y[a] = __dadd_rn(u1, sv[4]);
-          P.z[a] = __dadd_rn(u2, sv[5]);
-        }
-      }
-      moved = true;
-      __syncthreads();
-    }
-  }
+  for (int k = 0; k < ops.n; k++)
+    moved |= apply_op(P, R, H, mol, ops.kind, ops.idx[k], ops.amt[k], ops.c1[k], ops.s1[k],
+                      ops.c2[k], ops.s2[k], sv);
   if (moved) {
     refresh_flexible(P, H, m, red);
     __syncthreads();
@@ -287,24 +319,251 @@ __global__ void __launch_bounds__(kIntraThreads) k_intra_ops(Pool P, IntraRows R
 __global__ void __launch_bounds__(kIntraThreads) k_intra_rollback(Pool P, IntraRows R, int chain,
                                                                   int mol) {
   __shared__ double red[3 * (kIntraThreads / 32)];
-  const ChainHdr& H = P.hdr[chain];
-  const int m = H.mol0 + mol;
-  const int a0 = P.mstart[m], len = P.mlen[m] & 255;
-  const double* rb = P.rb + (size_t)chain * 3 * H.max_len;
-  for (int i = threadIdx.x; i < len; i += blockDim.x) {
-    P.x[a0 + i] = rb[i];
-    P.y[a0 + i] = rb[H.max_len + i];
-    P.z[a0 + i] = rb[2 * H.max_len + i];
+  rollback_rows(P, R, P.hdr[chain], chain, mol, red);
+}
+
+// ---- the reference's loop on the device ----------------------------------------
+
+constexpr int kLoopThreads = 256;
+constexpr int kLoopDrawCap = 1 << 20;
+
+// randomReal (MathLibrary.cpp:31-33) on the restated C-library stream,
+// operation by operation.
+__device__ __forceinline__ double loop_real(CRand& g, double start, double end) {
+  const double r = __ddiv_rn((double)crand_next(g), 2147483647.0);
+  return __dadd_rn(__dmul_rn(__dsub_rn(end, start), r), start);
+}
+
+// acceptMove (SimulationStep.cpp:794-803): no draw for a decrease.
+__device__ __forceinline__ bool loop_accept(CRand& g, double de, double kT) {
+  if (de < 0) return true;
+  return exp(-(de) / kT) >= loop_real(g, 0.0, 1.0);
+}
+
+// Thread 0: the draws of one stage of intramolecularMove (kind 0 bonds,
+// :589-609; kind 1 angles, :621-640): how many, which (a std::set's distinct
+// draws in ascending order), an amount each; the variable entries go to
+// sel / amt.  Returns the count the counters take, or -1 when the set did
+// not fill within the draw cap.
+__device__ int loop_draw_stage(CRand& g, const IntraRows& R, int mol, int kind, double delta,
+                               int max_moves, int* sel, double* amt, int* n_sel) {
+  const int count = kind == 0 ? R.m_bcount[mol] : R.m_acount[mol];
+  const int start = kind == 0 ? R.m_bstart[mol] : R.m_astart[mol];
+  const int* var = kind == 0 ? R.b_var : R.a_var;
+  int n = count;
+  if (n > 3) n = min((int)loop_real(g, 2, count), max_moves);
+  // 0.25 + (0.75 / n) * intraScaleFactor, rounded step by step as the host does
+  const double scale = __dadd_rn(0.25, __dmul_rn(__ddiv_rn(0.75, (double)n), 0.625));
+  int have = 0, draws = 0;
+  while (have < n) {
+    if (++draws > kLoopDrawCap) return -1;
+    const int v = min((int)loop_real(g, 0, count), count - 1);
+    int pos = 0;
+    while (pos < have && sel[pos] < v) pos++;
+    if (pos < have && sel[pos] == v) continue;
+    for (int k = have; k > pos; k--) sel[k] = sel[k - 1];
+    sel[pos] = v;
+    have++;
   }
-  // SimCalcs::rollbackAngles / rollbackBonds (SimulationStep.cpp:751-775)
-  for (int k = R.m_astart[mol] + threadIdx.x; k < R.m_astart[mol] + R.m_acount[mol];
-       k += blockDim.x)
-    R.a_size[k] = R.a_size_rb[k];
-  for (int k = R.m_bstart[mol] + threadIdx.x; k < R.m_bstart[mol] + R.m_bcount[mol];
-       k += blockDim.x)
-    R.b_len[k] = R.b_len_rb[k];
+  int ns = 0;
+  for (int k = 0; k < have; k++) {
+    const double d = __dmul_rn(scale, loop_real(g, -delta, delta));
+    if (var[start + sel[k]]) {
+      sel[ns] = sel[k];
+      amt[ns] = d;
+      ns++;
+    }
+  }
+  *n_sel = ns;
+  return n;
+}
+
+template <bool F64>
+__global__ void __launch_bounds__(kLoopThreads) k_plain_steps(Pool P, IntraRows R, int intra,
+                                                              PlainLoop* L, int n_steps,
+                                                              SmemShape shape) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ PlainLoop st;
+  __shared__ Proposal prop;
+  __shared__ double red[3 * (kLoopThreads / 32)];
+  __shared__ double sv[9];
+  __shared__ int sel[kLoopSel];
+  __shared__ double amt[kLoopSel], trig[4 * kLoopSel];
+  __shared__ int n_sel, flag, stop;
+  const ChainHdr& H = P.hdr[0];
+  Group grp{(int)threadIdx.x, (int)blockDim.x, 1};
+  GroupSmem s = shape.carve(smem);
+  const int tid = threadIdx.x, lane = tid & 31, w = grp.warp(), nw = grp.nwarps();
+  const int n = H.n_mol;
+  const double kT = H.kT, max_t = H.max_t, max_r = H.max_r;
+  const double deg2rad = 3.14159256358979323846264 / 180.0;   // expandAngle's constant
+  if (tid == 0) {
+    st = *L;
+    stop = 0;
+  }
   __syncthreads();
-  refresh_flexible(P, H, m, red);
+  for (int k = 0; k < n_steps; k++) {
+    if (tid == 0) {
+      // chooseMolecule and the seven intermolecularMove draws
+      // (SimulationStep.cpp:25-27, 527-535), clamped as the host loop clamps
+      CRand& g = st.rng;
+      const int mol = min((int)loop_real(g, 0, n), n - 1);
+      const int len = P.mlen[H.mol0 + mol] & 255;
+      memset(&prop, 0, sizeof(prop));
+      prop.mol = mol;
+      prop.mode = MCGPU_ROT_EULER;
+      prop.vertex = min((int)loop_real(g, 0, len), len - 1);
+      prop.dx = loop_real(g, -max_t, max_t);
+      prop.dy = loop_real(g, -max_t, max_t);
+      prop.dz = loop_real(g, -max_t, max_t);
+      prop.r0 = loop_real(g, -max_r, max_r);
+      prop.r1 = loop_real(g, -max_r, max_r);
+      prop.r2 = loop_real(g, -max_r, max_r);
+    }
+    __syncthreads();
+    const int mol = prop.mol, m = H.mol0 + mol;
+    double eo = 0.0, en = 0.0, ab = 0.0;
+    long long np = 0;
+    if (!intra) {
+      // old and new placement in one pass (k_move_energies on one CTA)
+      if (w == 0) stage(P, H, m, &prop, s, lane);
+      grp.sync();
+      const MovedInfo mi = load_moved(s);
+      warp_eval<F64>(P, H, s, mi, H.mol0, H.mol0 + n, w, nw, lane, H.tpm, eo, en, ab, np);
+      group_reduce(grp, s, eo, en, ab, np);
+      if (tid == 0) {
+        const double de = en - eo;
+        flag = loop_accept(st.rng, de, kT);
+        st.pairs += np;
+        if (flag) {
+          st.energy += de;
+          st.accepted++;
+        } else {
+          st.rejected++;
+        }
+      }
+      __syncthreads();
+      if (flag && w == 0) commit(P, s, mi, lane);
+      __syncthreads();
+      continue;
+    }
+    // ---- with the intramolecular term and move ----
+    const double ei_old = intra_energy(P, R, H, mol, red);
+    if (w == 0) stage(P, H, m, nullptr, s, lane);
+    grp.sync();
+    {
+      const MovedInfo mi = load_moved(s);
+      warp_eval<F64>(P, H, s, mi, H.mol0, H.mol0 + n, w, nw, lane, H.tpm, eo, en, ab, np);
+      group_reduce(grp, s, eo, en, ab, np);
+    }
+    const double e_old = eo + ei_old;
+    long long pairs = np;
+    __syncthreads();
+    // the rigid move: rollback copy, move, wrap, commit
+    if (w == 0) {
+      stage(P, H, m, &prop, s, lane);
+      __syncwarp();
+      const MovedInfo mi = load_moved(s);
+      double* rb = P.rb;
+      for (int i = lane; i < mi.len; i += 32) {
+        rb[i] = s.ox[i];
+        rb[H.max_len + i] = s.oy[i];
+        rb[2 * H.max_len + i] = s.oz[i];
+      }
+      commit(P, s, mi, lane);
+    }
+    __syncthreads();
+    // SimCalcs::intramolecularMove (SimulationStep.cpp:568-675)
+    save_rows(R, mol);
+    const double bond_delta = st.max_bond_delta, angle_delta = st.max_angle_delta;
+    __syncthreads();
+    double cur = 0.0;
+    bool have_cur = false;
+    for (int kind = 0; kind < 2; kind++) {
+      if (kind == 0 ? !R.flex_bonds : !R.flex_angles) continue;
+      if (tid == 0) {
+        const int cnt = loop_draw_stage(st.rng, R, mol, kind, kind == 0 ? bond_delta : angle_delta,
+                                        st.max_intra_moves, sel, amt, &n_sel);
+        if (cnt < 0) {
+          st.error = 1;
+          stop = 1;
+        } else if (kind == 0) {
+          st.bond_moves += cnt;
+        } else {
+          st.angle_moves += cnt;
+        }
+        flag = cnt;
+        for (int q = 0; kind == 1 && q < n_sel; q++) {
+          sincos(__dmul_rn(amt[q], -deg2rad), &trig[4 * q + 1], &trig[4 * q]);
+          sincos(__dmul_rn(amt[q], deg2rad), &trig[4 * q + 3], &trig[4 * q + 2]);
+        }
+      }
+      __syncthreads();
+      if (stop) break;
+      const int cnt = flag;
+      const double e0 = have_cur ? cur : intra_energy(P, R, H, mol, red);
+      bool moved = false;
+      for (int q = 0; q < n_sel; q++)
+        moved |= apply_op(P, R, H, mol, kind, sel[q], amt[q], trig[4 * q], trig[4 * q + 1],
+                          trig[4 * q + 2], trig[4 * q + 3], sv);
+      if (moved) {
+        refresh_flexible(P, H, m, red);
+        __syncthreads();
+      }
+      const double e1 = intra_energy(P, R, H, mol, red);
+      if (tid == 0 && loop_accept(st.rng, e1 - e0, kT)) {
+        if (kind == 0)
+          st.bond_accepted += cnt;
+        else
+          st.angle_accepted += cnt;
+      }
+      cur = e1;
+      have_cur = true;
+      __syncthreads();
+    }
+    if (stop) break;
+    if (tid == 0 && st.step != 0 && (st.step % 1000) == 0) {
+      // width tuning (:656-674); the angle test reads the entry width
+      const double bond_ratio = (double)st.bond_accepted / st.bond_moves;
+      const double angle_ratio = (double)st.angle_accepted / st.angle_moves;
+      double diff = bond_ratio - 0.4;
+      if (fabs(diff) > 0.0001)
+        st.max_bond_delta = __dadd_rn(st.max_bond_delta, __dmul_rn(st.max_bond_delta, diff));
+      diff = angle_ratio - 0.4;
+      if (fabs(angle_delta) > 0.0001)
+        st.max_angle_delta = __dadd_rn(st.max_angle_delta, __dmul_rn(st.max_angle_delta, diff));
+      st.bond_accepted = st.bond_moves = 0;
+      st.angle_accepted = st.angle_moves = 0;
+    }
+    // the new energy: the intramolecular part is the last stage's (the same
+    // coordinates and rows), else computed here
+    const double ei_new = have_cur ? cur : intra_energy(P, R, H, mol, red);
+    if (w == 0) stage(P, H, m, nullptr, s, lane);
+    grp.sync();
+    eo = en = ab = 0.0;
+    np = 0;
+    {
+      const MovedInfo mi = load_moved(s);
+      warp_eval<F64>(P, H, s, mi, H.mol0, H.mol0 + n, w, nw, lane, H.tpm, eo, en, ab, np);
+      group_reduce(grp, s, eo, en, ab, np);
+    }
+    if (tid == 0) {
+      const double de = (eo + ei_new) - e_old;
+      flag = loop_accept(st.rng, de, kT);
+      st.pairs += pairs + np;
+      if (flag) {
+        st.energy += de;
+        st.accepted++;
+      } else {
+        st.rejected++;
+      }
+      st.step++;
+    }
+    __syncthreads();
+    if (!flag) rollback_rows(P, R, H, 0, mol, red);
+    __syncthreads();
+  }
+  if (tid == 0) *L = st;
 }
 
 // Union-find over local atom indexes (the partition is all that is used).
@@ -483,6 +742,19 @@ cudaError_t launch_intra_ops(const Pool& P, const IntraRows& R, int chain, const
 cudaError_t launch_intra_rollback(const Pool& P, const IntraRows& R, int chain, int mol,
                                   cudaStream_t st) {
   k_intra_rollback<<<1, kIntraThreads, 0, st>>>(P, R, chain, mol);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plain_steps(bool f64, const Pool& P, const IntraRows& R, int intra,
+                               PlainLoop* L, int n_steps, SmemShape sh, cudaStream_t st) {
+  const int bytes = sh.bytes();
+  if (f64) {
+    cudaFuncSetAttribute(k_plain_steps<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    k_plain_steps<true><<<1, kLoopThreads, bytes, st>>>(P, R, intra, L, n_steps, sh);
+  } else {
+    cudaFuncSetAttribute(k_plain_steps<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    k_plain_steps<false><<<1, kLoopThreads, bytes, st>>>(P, R, intra, L, n_steps, sh);
+  }
   return cudaGetLastError();
 }
 

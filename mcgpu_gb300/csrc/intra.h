@@ -7,6 +7,7 @@
 #include <memory>
 #include <vector>
 
+#include "crand.h"
 #include "host.h"
 #include "mcgpu_gb300.h"
 
@@ -86,5 +87,29 @@ cudaError_t launch_intra_rollback(const Pool& P, const IntraRows& R, int chain, 
 // (the intramolecular terms of calcSystemEnergy).
 cudaError_t launch_intra_add(const Pool& P, const IntraRows& R, int n_mol, double* emol,
                              cudaStream_t st);
+
+// Most bonds or angles one stage of the device loop moves (max_intra_moves).
+constexpr int kLoopSel = 64;
+
+// State of the device-resident run of the reference's loop (kept in device
+// memory between launches): the C library's generator, the running energy,
+// the counters, and the intramolecular widths, step counter and tuning
+// counters.  error: 1 when a stage's index draws did not fill its set within
+// kLoopDrawCap draws (the loop stops).
+struct PlainLoop {
+  CRand rng;
+  double energy;
+  long long accepted, rejected, pairs;
+  long long step;
+  double max_bond_delta, max_angle_delta;
+  long long bond_moves, bond_accepted, angle_moves, angle_accepted;
+  int max_intra_moves, error;
+};
+
+// n_steps of Simulation::run's loop for chain 0 of the pool on one CTA, the
+// draws from L->rng; intra != 0: with the intramolecular term and move
+// (R valid).  f64: FP64 intermolecular pair terms, else FP32.
+cudaError_t launch_plain_steps(bool f64, const Pool& P, const IntraRows& R, int intra,
+                               PlainLoop* L, int n_steps, SmemShape sh, cudaStream_t st);
 
 }  // namespace mcgpu

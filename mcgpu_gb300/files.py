@@ -1491,13 +1491,20 @@ class SimInput:
     topology: Topology | None = None
 
 
-def load(path: str, implied_angles: bool = False, seed_from_file: bool = False) -> SimInput:
+def load(path: str, implied_angles: bool = False, seed_from_file: bool = False,
+         env: dict | None = None) -> SimInput:
     """loadBoxData: a ``.config`` builds the box from its z-matrix and OPLS
     table on the FCC lattice; a ``.state`` restores the box it holds.  Then
-    Simulation::run's keepMoleculeInBox and the SimBox rows."""
+    Simulation::run's keepMoleculeInBox and the SimBox rows.  ``env``
+    overrides settings of a ``.config`` (Environment field names, e.g.
+    ``{"n_molecules": 512, "x": 41.8}``) before the box is built."""
     ext = extension(path)
     if ext == "config":
         cfg = read_config(path)
+        for k, v in (env or {}).items():
+            if not hasattr(cfg.env, k):
+                raise FileFormatError("no environment setting " + k)
+            setattr(cfg.env, k, v)
         par = cfg.opls_path
         cut = par.rfind("/")
         sb_dir = par[:cut] if cut >= 0 else par

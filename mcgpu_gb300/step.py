@@ -170,6 +170,15 @@ class GpuBox:
                                                1 if fused else 0, C.byref(st)))
         return st
 
+    def run_plain_device(self, seed: int, n_steps: int) -> "_abi.PlainStats":
+        """The same loop as run_plain_native entirely on the device
+        (mcgpu_run_plain_device): one CTA, the C library's generator
+        restated on the device and seeded as srand(seed) seeds it."""
+        st = _abi.PlainStats()
+        self._check(_abi.lib().mcgpu_run_plain_device(self._h, int(seed) & 0xFFFFFFFF,
+                                                      int(n_steps), C.byref(st)))
+        return st
+
     # ---- flexible molecules (the reference's code behind ENABLE_INTRA) ----
 
     def set_topology(self, topo) -> None:

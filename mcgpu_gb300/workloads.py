@@ -510,6 +510,30 @@ def bicyclic_4000() -> BoxData:
     return bicyclic_box(4000, L=86.1, seed=4000, lattice=True)
 
 
+def flex_amine_water(n_mol: int = 512, files_dir=None):
+    """The flexible-molecule workload: alternating flexible amine chains (9
+    atoms: N, three C, five H; every bond and angle variable, so each move
+    also stretches a random set of bonds and opens a random set of angles)
+    and rigid 3-site waters, from the synthetic inputs flex.config / flex.z /
+    synth.par / oplsaa.sb (tests/golden/files), with N molecules and the
+    edge scaled to keep the configuration's density; built by the package's
+    loader (FCC lattice, implied angles on).  Returns (BoxData, Topology)."""
+    import os
+    from pathlib import Path
+    from . import files as F
+    d = Path(files_dir) if files_dir else Path(__file__).resolve().parents[1] / "tests" / \
+        "golden" / "files"
+    edge = 19.0 * (n_mol / 48) ** (1 / 3)
+    cwd = os.getcwd()
+    os.chdir(d)
+    try:
+        si = F.load("flex.config", implied_angles=True,
+                    env={"n_molecules": int(n_mol), "x": edge, "y": edge, "z": edge})
+    finally:
+        os.chdir(cwd)
+    return si.rows, si.topology
+
+
 def water_32768() -> BoxData:
     """32,768 waters (98,304 atoms), L = 99.3 A, rc 12 A, 298 K: the large
     single system (NPT at 1 atm with Verlet lists in its measurement)."""

@@ -101,3 +101,15 @@ def test_batch_descriptor_rows():
     ints64 = np.arange(4, dtype=np.int64)
     B._row_address(ints64, i32, keep)
     assert keep[2].dtype == i32 and np.array_equal(keep[2], ints64)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 42, 4321, 2147483647, 2147483648, 4294967295])
+def test_restated_rand_stream_equals_c_library(seed):
+    """The device loop's generator (the C library's rand() restated, seeded
+    as srand seeds it) gives the C library's own numbers, here on the host."""
+    from mcgpu_gb300.step import LibcRand
+    n = 20000
+    out = np.empty(n, np.int32)
+    assert _abi.lib().mcgpu_rand_stream(seed, n, out.ctypes.data_as(C.POINTER(C.c_int32))) == 0
+    r = LibcRand(seed)
+    assert all(int(out[k]) == r.rand() for k in range(n))

@@ -232,3 +232,76 @@ def test_intra_off_by_default_and_refusals(ctx):
     with pytest.raises(MCGPUError, match="outside molecule"):
         g.set_topology(bad)
     g.close()
+
+
+# ---- the loop on the device (mcgpu_run_plain_device) ----------------------------
+
+
+def test_device_loop_flexible_golden(ctx):
+    """The reference's 2500-step flexible trajectory run entirely on the
+    device (one CTA, the C library's generator restated there): the same
+    accepted count, tuned widths and counters; bond lengths and angle sizes
+    bit for bit (their updates are exact functions of the draws); energy
+    within the FP64-sum tolerance; coordinates within 1e-9 A (device sin /
+    cos in the rotations)."""
+    g, box, topo, z = flex_box(ctx)
+    n, seed = int(z["traj_steps"][0]), int(z["traj_seed"][0])
+    st = g.run_plain_device(seed, n)
+    assert st.accepted == z["traj_accepted"][0] and st.accepted + st.rejected == n
+    assert abs(st.energy - z["traj_energy"][0]) <= 1e-8 * max(1.0, abs(z["traj_e0"][0]))
+    s = g.intra_state()
+    ref = z["traj_state"]
+    assert [s["max_bond_delta"], s["max_angle_delta"], s["step_num"], s["bond_moves"],
+            s["bond_accepted"], s["angle_moves"], s["angle_accepted"]] == list(ref)
+    assert np.array_equal(s["bond_len"], z["traj_bond_len"])
+    assert np.array_equal(s["angle_size"], z["traj_angle_size"])
+    d = np.abs(coords(g) - z["traj_coords"]).max()
+    assert d <= 1e-9, d
+    print(f"device loop, flexible: max |coordinate - reference| {d:.2e} A")
+    g.close()
+
+
+@pytest.mark.parametrize("prec", [PREC_FP64, PREC_MIXED])
+def test_device_loop_rigid_golden(ctx, prec):
+    """The reference's 3000-step rigid trajectory of 256 waters on the device:
+    the same accepted count and final energy; coordinates within 1e-9 A
+    (FP64 pairs).  With FP32 pairs the decisions are taken on FP32-pair
+    energies, so only the counts' closeness and a fresh FP64 recompute of
+    the running energy are checked."""
+    from helpers import load_golden
+    box, z = load_golden("water256")
+    g = GpuBox(ctx, box, prec)
+    n, seed = int(z["traj_steps"][0]), int(z["traj_seed"][0])
+    st = g.run_plain_device(seed, n)
+    assert st.accepted + st.rejected == n
+    if prec == PREC_FP64:
+        assert st.accepted == z["traj_accepted"][0]
+        assert abs(st.energy - z["traj_energy"][0]) <= 1e-8 * max(1.0, abs(z["traj_energy"][0]))
+        d = np.abs(coords(g) - z["traj_final"]).max()
+        assert d <= 1e-9, d
+        print(f"device loop, rigid FP64: max |coordinate - reference| {d:.2e} A")
+    else:
+        assert abs(st.accepted - z["traj_accepted"][0]) <= 0.05 * n
+        e = g.system_energy()
+        assert abs(st.energy - e) <= 1e-5 * max(1.0, abs(e))
+    g.close()
+
+
+def test_device_loop_random_topologies(ctx):
+    """Random flexible molecules (rings, degenerate angles giving NaN
+    placements, which are rejected): the device loop takes the oracle's
+    decisions over 400 steps (accepted count equal, rows bit for bit)."""
+    box, topo = random_flex_box(2)
+    g = GpuBox(ctx, box, PREC_FP64)
+    g.set_topology(topo)
+    g.set_intra(True)
+    o = OracleFlex(box, topo)
+    LibcRand(7)
+    e, acc = o.run_plain(400, o.system_energy())
+    st = g.run_plain_device(7, 400)
+    assert st.accepted == acc
+    assert abs(st.energy - e) <= 1e-8 * max(1.0, abs(e))
+    s = g.intra_state()
+    assert np.array_equal(s["bond_len"], o.t.bond_len, equal_nan=True)
+    assert np.array_equal(s["angle_size"], o.t.angle_size, equal_nan=True)
+    g.close()
