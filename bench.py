@@ -306,6 +306,20 @@ def bench_plain(ctx, n_steps: int = 2000) -> dict:
         g.close()
         out["device"][name] = {"moves_per_s": n_dev / dt, "accepted": st.accepted,
                                "steps": n_dev, "pairs_per_move": st.pairs / n_dev}
+    # an ensemble of the same box, one per CTA, two CTAs per SM, own seeds
+    n_boxes = 2 * ctx_sm_count()
+    for name, prec, n_ens in (("ensemble_mixed", M.PREC_MIXED, 2000),
+                              ("ensemble_fp64", M.PREC_FP64, 500)):
+        gs = [M.GpuBox(ctx, box, prec) for _ in range(n_boxes)]
+        M.run_plain_device_many(gs, range(1, n_boxes + 1), 20)      # warm-up
+        t0 = time.perf_counter()
+        res = M.run_plain_device_many(gs, range(101, n_boxes + 101), n_ens)
+        dt = time.perf_counter() - t0
+        out["device"][name] = {"moves_per_s": n_boxes * n_ens / dt, "boxes": n_boxes,
+                               "steps": n_ens,
+                               "pairs_per_move": sum(r.pairs for r in res) / (n_boxes * n_ens)}
+        for g in gs:
+            g.close()
     for name, prec, fused in (("fp64", M.PREC_FP64, False), ("mixed", M.PREC_MIXED, False),
                               ("mixed_fused", M.PREC_MIXED, True)):
         g = M.GpuBox(ctx, box, prec)
@@ -322,6 +336,11 @@ def bench_plain(ctx, n_steps: int = 2000) -> dict:
                    "and one D2H sync per contract call; 'device' runs the same loop (same "
                    "rand() stream, restated on the device) on one CTA with no host round trip")
     return out
+
+
+def ctx_sm_count() -> int:
+    import torch
+    return torch.cuda.get_device_properties(0).multi_processor_count
 
 
 def bench_flex(ctx, n_steps: int = 3000, cpu_target_s: float = 3.0) -> dict:
@@ -370,6 +389,25 @@ def bench_flex(ctx, n_steps: int = 3000, cpu_target_s: float = 3.0) -> dict:
                      "pairs_per_move": st.pairs / n_dev,
                      "bond_width": s["max_bond_delta"], "angle_width": s["max_angle_delta"]}
         g.close()
+    # an ensemble: one box per CTA, two CTAs per SM, each its own seed
+    n_boxes = 2 * ctx_sm_count()
+    for name, prec in (("device_ensemble_mixed", M.PREC_MIXED),
+                       ("device_ensemble_fp64", M.PREC_FP64)):
+        gs = []
+        for _ in range(n_boxes):
+            g = M.GpuBox(ctx, box, prec)
+            g.set_topology(topo)
+            g.set_intra(True)
+            gs.append(g)
+        n_ens = 1000 if prec == M.PREC_MIXED else 300
+        M.run_plain_device_many(gs, range(1, n_boxes + 1), 20)      # warm-up
+        t0 = time.perf_counter()
+        res = M.run_plain_device_many(gs, range(101, n_boxes + 101), n_ens)
+        dt = time.perf_counter() - t0
+        out[name] = {"moves_per_s": n_boxes * n_ens / dt, "boxes": n_boxes, "steps": n_ens,
+                     "accepted": int(sum(r.accepted for r in res))}
+        for g in gs:
+            g.close()
     g = M.GpuBox(ctx, box, M.PREC_FP64)
     g.set_topology(topo)
     g.set_intra(True)
@@ -392,8 +430,15 @@ def bench_flex(ctx, n_steps: int = 3000, cpu_target_s: float = 3.0) -> dict:
     out["cpu_baseline"] = {"moves_per_s": done / (time.perf_counter() - t0), "kind": "port",
                            "cores": 1, "sample": f"{done} steps of the oracle's loop"}
     cpu_v = out["cpu_baseline"]["moves_per_s"]
+    cores = os.cpu_count() or 1
+    out["cpu_ensemble_bound"] = {"moves_per_s": cpu_v * cores, "cores": cores,
+                                 "note": "the one-core rate times the host's cores (ideal "
+                                         "scaling of independent boxes)"}
     out["gpu_over_cpu"] = {k: out[k]["moves_per_s"] / cpu_v
                            for k in ("cpp_fp64", "cpp_mixed", "device_fp64", "device_mixed")}
+    out["ensemble_over_cpu_cores"] = {
+        k: out[k]["moves_per_s"] / (cpu_v * cores)
+        for k in ("device_ensemble_mixed", "device_ensemble_fp64")}
     out["note"] = ("cpp_*: the host loop over the contract calls, two device waits per step "
                    "(the bond and angle MC tests decide whether rand() is drawn again before "
                    "the next draws); device_*: the same loop on one CTA with the C library's "

@@ -214,6 +214,12 @@ int mcgpu_run_plain(mcgpu_box* box, unsigned int seed, int n_steps, int fused,
  * advanced. */
 int mcgpu_run_plain_device(mcgpu_box* box, unsigned int seed, int n_steps,
                            mcgpu_plain_stats* out);
+/* The device loop of n_boxes boxes of one context and one pair precision at
+ * once, one CTA each, box i seeded with seeds[i]; out[i] its result (the
+ * same as running it alone). */
+int mcgpu_boxes_run_plain_device(mcgpu_box* const* boxes, int n_boxes,
+                                 const unsigned int* seeds, int n_steps,
+                                 mcgpu_plain_stats* out);
 
 /* The first n values the restated generator gives after srand(seed)
  * (host only; for checking it against the C library). */

@@ -9,13 +9,13 @@ does the work; this package is the host side above its C ABI:
 """
 from . import _abi
 from ._abi import (PREC_FP64, PREC_MIXED, ROT_AXIS, ROT_EULER, MCGPUError)
-from .workloads import BoxData, bicyclic_box, water_box, water_chains
-from .step import Context, GpuBox, GpuSimulationStep, LibcRand, run_plain
+from .workloads import BoxData, Topology, bicyclic_box, water_box, water_chains
+from .step import Context, GpuBox, GpuSimulationStep, LibcRand, run_plain, run_plain_device_many
 from .batch import ChainBatch
 from .server import JobServer
 
 __all__ = [
     "PREC_FP64", "PREC_MIXED", "ROT_AXIS", "ROT_EULER", "MCGPUError", "BoxData",
     "bicyclic_box", "water_box", "water_chains", "Context", "GpuBox", "GpuSimulationStep",
-    "LibcRand", "run_plain", "ChainBatch", "JobServer",
+    "LibcRand", "run_plain", "run_plain_device_many", "Topology", "ChainBatch", "JobServer",
 ]

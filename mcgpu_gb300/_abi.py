@@ -169,6 +169,8 @@ _PROTOS = {
     "mcgpu_batch_set_precision": (C.c_int, [_vp, C.c_int]),
     "mcgpu_run_plain": (C.c_int, [_vp, C.c_uint, C.c_int, C.c_int, C.POINTER(PlainStats)]),
     "mcgpu_run_plain_device": (C.c_int, [_vp, C.c_uint, C.c_int, C.POINTER(PlainStats)]),
+    "mcgpu_boxes_run_plain_device": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(C.c_uint),
+                                               C.c_int, C.POINTER(PlainStats)]),
     "mcgpu_rand_stream": (C.c_int, [C.c_uint, C.c_int, C.POINTER(C.c_int32)]),
     "mcgpu_box_set_topology": (C.c_int, [_vp, C.POINTER(TopoDesc)]),
     "mcgpu_box_set_intra": (C.c_int, [_vp, C.c_int]),

@@ -883,69 +883,112 @@ extern "C" int mcgpu_run_plain(mcgpu_box* b, unsigned int seed, int n_steps, int
   return MCGPU_OK;
 }
 
-// The same loop on the device: one CTA runs the steps with the restated
-// C-library generator, launches of kDeviceLoopSteps steps.
+// The same loop on the device: one CTA per box runs the steps with the
+// restated C-library generator, launches of kDeviceLoopSteps steps.
 static constexpr int kDeviceLoopSteps = 4096;
+
+extern "C" int mcgpu_boxes_run_plain_device(mcgpu_box* const* boxes, int n_boxes,
+                                            const unsigned int* seeds, int n_steps,
+                                            mcgpu_plain_stats* out) {
+  if (!boxes || !seeds || !out || n_boxes < 1)
+    return set_err(nullptr, MCGPU_ERR_INVALID, "null argument or no boxes");
+  mcgpu_box* b0 = boxes[0];
+  if (!b0) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  mcgpu_ctx* ctx = b0->ctx;
+  if (n_steps < 0) return set_err(ctx, MCGPU_ERR_INVALID, "negative step count");
+  int max_len = 0;
+  for (int i = 0; i < n_boxes; i++) {
+    mcgpu_box* b = boxes[i];
+    if (!b) return set_err(ctx, MCGPU_ERR_INVALID, "null box %d", i);
+    if (b->ctx != ctx) return set_err(ctx, MCGPU_ERR_INVALID, "box %d: another context", i);
+    if (b->precision != b0->precision)
+      return set_err(ctx, MCGPU_ERR_INVALID, "box %d: another pair precision", i);
+    for (int j = 0; j < i; j++)
+      if (boxes[j] == b) return set_err(ctx, MCGPU_ERR_INVALID, "box %d given twice", i);
+    if (b->intra_on && b->intra->max_intra_moves > kLoopSel)
+      return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "box %d: max_intra_moves %d above %d", i,
+                     b->intra->max_intra_moves, kLoopSel);
+    max_len = std::max(max_len, b->pool.max_len);
+  }
+  std::vector<LoopTask> tasks(n_boxes);
+  std::vector<PlainLoop> loops(n_boxes);
+  for (int i = 0; i < n_boxes; i++) {
+    mcgpu_box* b = boxes[i];
+    mcgpu_plain_stats& o = out[i];
+    std::memset(&o, 0, sizeof(o));
+    double e = 0.0;
+    int rc = mcgpu_system_energy(b, &e);
+    if (rc) return rc;
+    o.energy0 = e;
+    if (!b->dloop) CK(ctx, cudaMalloc((void**)&b->dloop, sizeof(PlainLoop)));
+    PlainLoop& L = loops[i];
+    std::memset(&L, 0, sizeof(L));
+    crand_seed(L.rng, seeds[i]);
+    L.energy = e;
+    LoopTask& T = tasks[i];
+    std::memset(&T, 0, sizeof(T));
+    T.P = b->pool.P;
+    T.L = b->dloop;
+    T.intra = b->intra_on ? 1 : 0;
+    if (b->intra_on) {
+      IntraHost& I = *b->intra;
+      T.R = I.R;
+      L.step = I.step;
+      L.max_bond_delta = I.max_bond_delta;
+      L.max_angle_delta = I.max_angle_delta;
+      L.bond_moves = I.bond_moves;
+      L.bond_accepted = I.bond_accepted;
+      L.angle_moves = I.angle_moves;
+      L.angle_accepted = I.angle_accepted;
+      L.max_intra_moves = I.max_intra_moves;
+    }
+    CK(ctx, cudaMemcpyAsync(b->dloop, &L, sizeof(L), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  LoopTask* dt = nullptr;
+  CK(ctx, cudaMalloc((void**)&dt, sizeof(LoopTask) * n_boxes));
+  cudaError_t e = cudaMemcpyAsync(dt, tasks.data(), sizeof(LoopTask) * n_boxes,
+                                  cudaMemcpyHostToDevice, ctx->stream);
+  SmemShape sh = shape_for(max_len, 8);
+  for (int done = 0; e == cudaSuccess && done < n_steps; done += kDeviceLoopSteps)
+    e = launch_plain_steps(b0->precision == MCGPU_PREC_FP64, dt, n_boxes,
+                           std::min(kDeviceLoopSteps, n_steps - done), sh, ctx->stream);
+  for (int i = 0; e == cudaSuccess && i < n_boxes; i++)
+    e = cudaMemcpyAsync(&loops[i], boxes[i]->dloop, sizeof(PlainLoop), cudaMemcpyDeviceToHost,
+                        ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(dt);
+  if (e != cudaSuccess)
+    return set_err(ctx, MCGPU_ERR_CUDA, "device loop failed: %s", cudaGetErrorString(e));
+  for (int i = 0; i < n_boxes; i++) {
+    mcgpu_box* b = boxes[i];
+    const PlainLoop& L = loops[i];
+    box_plain_moved(b);
+    if (L.error)
+      return set_err(ctx, MCGPU_ERR_DEVICE, "box %d: an intramolecular stage's index draws did "
+                     "not fill its set (device loop stopped after %lld steps)", i,
+                     L.accepted + L.rejected);
+    if (b->intra_on) {
+      IntraHost& I = *b->intra;
+      I.step = L.step;
+      I.max_bond_delta = L.max_bond_delta;
+      I.max_angle_delta = L.max_angle_delta;
+      I.bond_moves = L.bond_moves;
+      I.bond_accepted = L.bond_accepted;
+      I.angle_moves = L.angle_moves;
+      I.angle_accepted = L.angle_accepted;
+    }
+    out[i].energy = L.energy;
+    out[i].accepted = L.accepted;
+    out[i].rejected = L.rejected;
+    out[i].pairs = L.pairs;
+  }
+  return MCGPU_OK;
+}
 
 extern "C" int mcgpu_run_plain_device(mcgpu_box* b, unsigned int seed, int n_steps,
                                       mcgpu_plain_stats* out) {
   if (!b || !out) return set_err(b ? b->ctx : nullptr, MCGPU_ERR_INVALID, "null argument");
-  mcgpu_ctx* ctx = b->ctx;
-  if (n_steps < 0) return set_err(ctx, MCGPU_ERR_INVALID, "negative step count");
-  if (b->intra_on && b->intra->max_intra_moves > kLoopSel)
-    return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "max_intra_moves %d above %d",
-                   b->intra->max_intra_moves, kLoopSel);
-  std::memset(out, 0, sizeof(*out));
-  double e = 0.0;
-  int rc = mcgpu_system_energy(b, &e);
-  if (rc) return rc;
-  out->energy0 = e;
-  if (!b->dloop) CK(ctx, cudaMalloc((void**)&b->dloop, sizeof(PlainLoop)));
-  PlainLoop L;
-  std::memset(&L, 0, sizeof(L));
-  crand_seed(L.rng, seed);
-  L.energy = e;
-  IntraRows R{};
-  if (b->intra_on) {
-    IntraHost& I = *b->intra;
-    R = I.R;
-    L.step = I.step;
-    L.max_bond_delta = I.max_bond_delta;
-    L.max_angle_delta = I.max_angle_delta;
-    L.bond_moves = I.bond_moves;
-    L.bond_accepted = I.bond_accepted;
-    L.angle_moves = I.angle_moves;
-    L.angle_accepted = I.angle_accepted;
-    L.max_intra_moves = I.max_intra_moves;
-  }
-  CK(ctx, cudaMemcpyAsync(b->dloop, &L, sizeof(L), cudaMemcpyHostToDevice, ctx->stream));
-  SmemShape sh = shape_for(b->pool.max_len, 8);
-  for (int done = 0; done < n_steps; done += kDeviceLoopSteps) {
-    const int k = std::min(kDeviceLoopSteps, n_steps - done);
-    CK(ctx, launch_plain_steps(b->precision == MCGPU_PREC_FP64, b->pool.P, R, b->intra_on ? 1 : 0,
-                               b->dloop, k, sh, ctx->stream));
-  }
-  box_plain_moved(b);
-  CK(ctx, cudaMemcpyAsync(&L, b->dloop, sizeof(L), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(ctx, cudaStreamSynchronize(ctx->stream));
-  if (L.error)
-    return set_err(ctx, MCGPU_ERR_DEVICE, "an intramolecular stage's index draws did not fill "
-                   "its set (device loop stopped after %lld steps)", L.accepted + L.rejected);
-  if (b->intra_on) {
-    IntraHost& I = *b->intra;
-    I.step = L.step;
-    I.max_bond_delta = L.max_bond_delta;
-    I.max_angle_delta = L.max_angle_delta;
-    I.bond_moves = L.bond_moves;
-    I.bond_accepted = L.bond_accepted;
-    I.angle_moves = L.angle_moves;
-    I.angle_accepted = L.angle_accepted;
-  }
-  out->energy = L.energy;
-  out->accepted = L.accepted;
-  out->rejected = L.rejected;
-  out->pairs = L.pairs;
-  return MCGPU_OK;
+  return mcgpu_boxes_run_plain_device(&b, 1, &seed, n_steps, out);
 }
 
 extern "C" int mcgpu_rand_stream(unsigned int seed, int n, int32_t* out) {

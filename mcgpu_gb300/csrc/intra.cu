@@ -379,10 +379,16 @@ __device__ int loop_draw_stage(CRand& g, const IntraRows& R, int mol, int kind, 
 }
 
 template <bool F64>
-__global__ void __launch_bounds__(kLoopThreads) k_plain_steps(Pool P, IntraRows R, int intra,
-                                                              PlainLoop* L, int n_steps,
+__global__ void __launch_bounds__(kLoopThreads) k_plain_steps(const LoopTask* tasks, int n_steps,
                                                               SmemShape shape) {
   extern __shared__ __align__(16) char smem[];
+  __shared__ LoopTask task;
+  if (threadIdx.x == 0) task = tasks[blockIdx.x];
+  __syncthreads();
+  const Pool& P = task.P;
+  const IntraRows& R = task.R;
+  const int intra = task.intra;
+  PlainLoop* L = task.L;
   __shared__ PlainLoop st;
   __shared__ Proposal prop;
   __shared__ double red[3 * (kLoopThreads / 32)];
@@ -745,15 +751,16 @@ cudaError_t launch_intra_rollback(const Pool& P, const IntraRows& R, int chain, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_plain_steps(bool f64, const Pool& P, const IntraRows& R, int intra,
-                               PlainLoop* L, int n_steps, SmemShape sh, cudaStream_t st) {
+cudaError_t launch_plain_steps(bool f64, const LoopTask* tasks, int n_tasks, int n_steps,
+                               SmemShape sh, cudaStream_t st) {
+  if (n_tasks <= 0) return cudaSuccess;
   const int bytes = sh.bytes();
   if (f64) {
     cudaFuncSetAttribute(k_plain_steps<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    k_plain_steps<true><<<1, kLoopThreads, bytes, st>>>(P, R, intra, L, n_steps, sh);
+    k_plain_steps<true><<<n_tasks, kLoopThreads, bytes, st>>>(tasks, n_steps, sh);
   } else {
     cudaFuncSetAttribute(k_plain_steps<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-    k_plain_steps<false><<<1, kLoopThreads, bytes, st>>>(P, R, intra, L, n_steps, sh);
+    k_plain_steps<false><<<n_tasks, kLoopThreads, bytes, st>>>(tasks, n_steps, sh);
   }
   return cudaGetLastError();
 }

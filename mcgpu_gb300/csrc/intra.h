@@ -106,10 +106,20 @@ struct PlainLoop {
   int max_intra_moves, error;
 };
 
-// n_steps of Simulation::run's loop for chain 0 of the pool on one CTA, the
-// draws from L->rng; intra != 0: with the intramolecular term and move
-// (R valid).  f64: FP64 intermolecular pair terms, else FP32.
-cudaError_t launch_plain_steps(bool f64, const Pool& P, const IntraRows& R, int intra,
-                               PlainLoop* L, int n_steps, SmemShape sh, cudaStream_t st);
+// One box of a device loop launch: its pool (chain 0), bond / angle rows
+// (when intra != 0) and loop state.
+struct LoopTask {
+  Pool P;
+  IntraRows R;
+  PlainLoop* L;
+  int intra, pad;
+};
+
+// n_steps of Simulation::run's loop for each of n_tasks boxes, one CTA per
+// box, the draws from each L->rng; intra != 0: with the intramolecular term
+// and move.  f64: FP64 intermolecular pair terms, else FP32.  tasks is a
+// device array.
+cudaError_t launch_plain_steps(bool f64, const LoopTask* tasks, int n_tasks, int n_steps,
+                               SmemShape sh, cudaStream_t st);
 
 }  // namespace mcgpu

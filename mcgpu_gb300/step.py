@@ -304,6 +304,19 @@ class GpuSimulationStep:
         return math.exp(-delta_e / self.kT) >= self.rng.random_real(0.0, 1.0)
 
 
+def run_plain_device_many(boxes: list, seeds, n_steps: int) -> list:
+    """The device loop of several boxes (one context, one pair precision) in
+    one launch, one CTA per box (mcgpu_boxes_run_plain_device); box i seeded
+    with seeds[i].  Returns each box's PlainStats."""
+    n = len(boxes)
+    hs = (C.c_void_p * n)(*[b._h.value for b in boxes])
+    sd = (C.c_uint * n)(*[int(s) & 0xFFFFFFFF for s in seeds])
+    out = (_abi.PlainStats * n)()
+    _abi.check(_abi.lib().mcgpu_boxes_run_plain_device(hs, n, sd, int(n_steps), out),
+               boxes[0].ctx.handle)
+    return list(out)
+
+
 @dataclass
 class PlainResult:
     energy: float

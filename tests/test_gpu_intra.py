@@ -305,3 +305,33 @@ def test_device_loop_random_topologies(ctx):
     assert np.array_equal(s["bond_len"], o.t.bond_len, equal_nan=True)
     assert np.array_equal(s["angle_size"], o.t.angle_size, equal_nan=True)
     g.close()
+
+
+def test_device_loop_many_boxes_equal_alone(ctx):
+    """Several boxes in one launch (flexible and rigid, different seeds):
+    each ends where it ends when run alone, the flexible golden box where the
+    reference ends."""
+    from helpers import load_golden
+    from mcgpu_gb300 import run_plain_device_many
+    def make():
+        g1, box, topo, z = flex_box(ctx, PREC_FP64)
+        wb, _ = load_golden("water256")
+        g2 = GpuBox(ctx, wb, PREC_FP64)
+        rb, rt = random_flex_box(3)
+        g3 = GpuBox(ctx, rb, PREC_FP64)
+        g3.set_topology(rt)
+        g3.set_intra(True)
+        return [g1, g2, g3], z
+    seeds = [4321, 99, 5]
+    boxes, z = make()
+    many = run_plain_device_many(boxes, seeds, 2500)
+    got = [coords(g) for g in boxes]
+    for g in boxes:
+        g.close()
+    assert many[0].accepted == z["traj_accepted"][0]
+    alone_boxes, _ = make()
+    for k, (g, sd) in enumerate(zip(alone_boxes, seeds)):
+        st = g.run_plain_device(sd, 2500)
+        assert st.accepted == many[k].accepted and st.energy == many[k].energy, k
+        assert np.array_equal(coords(g), got[k], equal_nan=True), k
+        g.close()
