@@ -8,6 +8,7 @@ does the work; this package is the host side above its C ABI:
 * ``workloads``  seeded synthetic boxes in the SimBox row layout
 """
 from . import _abi
+from . import files
 from ._abi import (PREC_FP64, PREC_MIXED, ROT_AXIS, ROT_EULER, MCGPUError)
 from .workloads import BoxData, Topology, bicyclic_box, water_box, water_chains
 from .step import Context, GpuBox, GpuSimulationStep, LibcRand, run_plain, run_plain_device_many

@@ -1,6 +1,7 @@
 // GpuBruteForceStep.cpp -- see GpuBruteForceStep.h.
 #include "GpuBruteForceStep.h"
 
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -15,8 +16,8 @@ void GpuBruteForceStep::check(int status, const char* what) {
   std::exit(EXIT_FAILURE);  // the reference's own error behaviour (Simulation.cpp:48)
 }
 
-GpuBruteForceStep::GpuBruteForceStep(SimBox* sb, int precision, int device)
-    : SimulationStep(sb) {
+GpuBruteForceStep::GpuBruteForceStep(SimBox* sb, int precision, int device, bool intra)
+    : SimulationStep(sb), intra_(intra) {
   check(mcgpu_ctx_create(&ctx_, device), "mcgpu_ctx_create");
   mcgpu_box_desc d = {};
   d.n_mol = sb->numMolecules;
@@ -39,6 +40,83 @@ GpuBruteForceStep::GpuBruteForceStep(SimBox* sb, int precision, int device)
   d.max_translate = sb->maxTranslate;
   d.max_rotate = sb->maxRotate;
   check(mcgpu_box_upload(ctx_, &d, precision, &gbox_), "mcgpu_box_upload");
+  if (intra_) {
+    uploadTopology(sb);
+    check(mcgpu_box_set_intra(gbox_, 1), "mcgpu_box_set_intra");
+  }
+}
+
+// The SimBox's bond / angle rows (SimBox.h:160-221, Real rows holding
+// indexes and flags) and exclusion / fudge lists (SimBox.h:298-305, one list
+// set per molecule type, sized by the type's first molecule) as the C ABI's
+// integer rows and per-type pair codes.
+void GpuBruteForceStep::uploadTopology(SimBox* sb) {
+  const int nb = sb->numBonds, na = sb->numAngles, nm = sb->numMolecules;
+  std::vector<int> ba1(nb), ba2(nb), bvar(nb), aa1(na), aa2(na), amid(na), avar(na);
+  for (int i = 0; i < nb; i++) {
+    ba1[i] = (int)sb->bondData[BOND_A1_IDX][i];
+    ba2[i] = (int)sb->bondData[BOND_A2_IDX][i];
+    bvar[i] = sb->bondData[BOND_VARIABLE][i] != 0;
+  }
+  for (int i = 0; i < na; i++) {
+    aa1[i] = (int)sb->angleData[ANGLE_A1_IDX][i];
+    aa2[i] = (int)sb->angleData[ANGLE_A2_IDX][i];
+    amid[i] = (int)sb->angleData[ANGLE_MID_IDX][i];
+    avar[i] = sb->angleData[ANGLE_VARIABLE][i] != 0;
+  }
+  int n_type = 0;
+  for (int m = 0; m < nm; m++) n_type = std::max(n_type, sb->moleculeData[MOL_TYPE][m] + 1);
+  std::vector<int> natom(n_type, 0);
+  for (int m = nm - 1; m >= 0; m--) natom[sb->moleculeData[MOL_TYPE][m]] = sb->moleculeData[MOL_LEN][m];
+  std::vector<unsigned char> codes;
+  for (int t = 0; t < n_type; t++) {
+    const int n = natom[t];
+    for (int i = 0; i < n; i++) {
+      for (int j = 0; j < n; j++) {
+        unsigned char c = 2;
+        for (int k = 0; sb->excludeAtoms && sb->excludeAtoms[t]; k++) {
+          const int v = sb->excludeAtoms[t][i][k];
+          if (v == -1) break;
+          if (v == j) { c = 0; break; }
+        }
+        for (int k = 0; c && sb->fudgeAtoms && sb->fudgeAtoms[t]; k++) {
+          const int v = sb->fudgeAtoms[t][i][k];
+          if (v == -1) break;
+          if (v == j) { c = 1; break; }
+        }
+        codes.push_back(c);
+      }
+    }
+  }
+  mcgpu_topology_desc t = {};
+  t.n_bond = nb;
+  t.n_angle = na;
+  t.n_type = n_type;
+  t.max_intra_moves = sb->maxIntraMoves;
+  t.bond_a1 = ba1.data();
+  t.bond_a2 = ba2.data();
+  t.bond_var = bvar.data();
+  t.bond_k = sb->bondData[BOND_KBOND];
+  t.bond_eq = sb->bondData[BOND_EQDIST];
+  t.bond_len = sb->bondLengths;
+  t.angle_a1 = aa1.data();
+  t.angle_a2 = aa2.data();
+  t.angle_mid = amid.data();
+  t.angle_var = avar.data();
+  t.angle_k = sb->angleData[ANGLE_KANGLE];
+  t.angle_eq = sb->angleData[ANGLE_EQANGLE];
+  t.angle_size = sb->angleSizes;
+  t.mol_bond_start = sb->moleculeData[MOL_BOND_START];
+  t.mol_bond_count = sb->moleculeData[MOL_BOND_COUNT];
+  t.mol_angle_start = sb->moleculeData[MOL_ANGLE_START];
+  t.mol_angle_count = sb->moleculeData[MOL_ANGLE_COUNT];
+  t.mol_type = sb->moleculeData[MOL_TYPE];
+  t.type_natom = natom.data();
+  t.pair_code = codes.data();
+  t.max_bond_delta = sb->maxBondDelta;
+  t.max_angle_delta = sb->maxAngleDelta;
+  t.step_num = sb->stepNum;
+  check(mcgpu_box_set_topology(gbox_, &t), "mcgpu_box_set_topology");
 }
 
 GpuBruteForceStep::~GpuBruteForceStep() {
@@ -64,6 +142,7 @@ void GpuBruteForceStep::changeMolecule(int molIdx, SimBox* sb) {
   mv.rx = randomReal(-maxR, maxR);
   mv.ry = randomReal(-maxR, maxR);
   mv.rz = randomReal(-maxR, maxR);
+  if (intra_) check(mcgpu_intra_set_step(gbox_, sb->stepNum), "mcgpu_intra_set_step");
   check(mcgpu_change_molecule(gbox_, molIdx, &mv), "mcgpu_change_molecule");
 }
 

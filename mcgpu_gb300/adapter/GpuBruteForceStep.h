@@ -14,13 +14,23 @@ class GpuBruteForceStep : public SimulationStep {
   // Uploads the SimBox rows to the GPU (replaces GPUCopy::copyIn).
   // precision: MCGPU_PREC_FP64 (the reference's Real=double arithmetic) or
   // MCGPU_PREC_MIXED (FP32 pair terms, FP64 sums).
-  explicit GpuBruteForceStep(SimBox* box, int precision = MCGPU_PREC_FP64, int device = 0);
+  // intra: the reference's intramolecular moves on the GPU (what its
+  // ENABLE_INTRA, SimulationStep.h:15, turns on in its own code): the SimBox's
+  // bond / angle rows and exclusion lists are uploaded, molecule energies
+  // carry the intramolecular term and changeMolecule makes the
+  // intramolecular move.  Build the reference with ENABLE_INTRA false when
+  // using it, so that SimulationStep::calcMoleculeEnergy does not add the
+  // host's own intramolecular term on top.
+  explicit GpuBruteForceStep(SimBox* box, int precision = MCGPU_PREC_FP64, int device = 0,
+                             bool intra = false);
   ~GpuBruteForceStep();
 
   // BruteForceCalcs::calcMolecularEnergyContribution (BruteForceStep.cpp:15-46).
   Real calcMolecularEnergyContribution(int currMol, int startMol) override;
   // SimCalcs::intermolecularMove (SimulationStep.cpp:520-566): the seven draws
-  // come from the reference's randomReal in its order; the move runs on the GPU.
+  // come from the reference's randomReal in its order; the move runs on the
+  // GPU.  With intra, then SimCalcs::intramolecularMove (:568-675) on the GPU,
+  // its draws from the same rand(), the tuning reading box->stepNum.
   void changeMolecule(int molIdx, SimBox* box) override;
   // SimCalcs::rollback (SimulationStep.cpp:731-749).
   void rollback(int molIdx, SimBox* box) override;
@@ -33,8 +43,10 @@ class GpuBruteForceStep : public SimulationStep {
 
  private:
   void check(int status, const char* what);
+  void uploadTopology(SimBox* box);
   mcgpu_ctx* ctx_ = nullptr;
   mcgpu_box* gbox_ = nullptr;
+  bool intra_ = false;
 };
 
 #endif

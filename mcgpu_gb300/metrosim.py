@@ -16,13 +16,16 @@ Options follow CommandParsing.cpp:40-190: ``-n/--steps``,
 ``-p/--parallel``, ``-V/--version``.  ``-s`` is accepted for compatibility;
 every form runs on the GPU.
 
-Two forms of the loop:
+Three forms of the loop:
 
 * ``--form plain`` (default): the reference's loop step for step -- the C
   library's ``rand()`` seeded with the environment's seed, moves drawn in the
   reference's order, the decision on the host -- with the energies on the
   GPU (FP64 pairs, or FP32 pairs with ``--precision mixed``).  With FP64 it
   reproduces the reference's trajectory.
+* ``--form device``: the same loop entirely on the GPU (one CTA, the C
+  library's generator restated on the device and seeded with the
+  environment's seed): the same draws and decisions, no intermediate states.
 * ``--form chain``: one device-resident chain (Philox draws, the decision on
   the GPU, rotations as X->Y->Z Euler angles like the reference's) advanced in
   launches of many steps; ``ensemble=npt`` gives isobaric ln V moves every
@@ -30,6 +33,13 @@ Two forms of the loop:
   ``-l`` Verlet lists.  ``--checkpoint-interval`` also writes
   ``<name>_<step>.ckpt`` (the exact device state) and ``--resume`` continues
   one bit for bit.
+
+``--intra`` turns on the reference's intramolecular moves (its compile-time
+ENABLE_INTRA, SimulationStep.h:15, false in its sources): bond stretches and
+angle expansions of the molecules' variable bonds and angles, with their
+energies, in the plain and device forms.  ``--implied-angles`` starts the
+z-matrix scanner's implied-angle flag set (the reference leaves it
+uninitialised; its program was seen to run with it clear).
 
 Every strategy gives the exact in-range molecule set here, so ``-S`` only
 chooses Verlet lists for the chain form; the reference's NLC and Verlet
@@ -85,7 +95,9 @@ def parse_args(argv):
     p.add_argument("-s", "--serial", action="store_true")
     p.add_argument("-p", "--parallel", action="store_true")
     p.add_argument("-V", "--version", action="store_true")
-    p.add_argument("--form", choices=("plain", "chain"), default="plain")
+    p.add_argument("--form", choices=("plain", "device", "chain"), default="plain")
+    p.add_argument("--intra", action="store_true")
+    p.add_argument("--implied-angles", action="store_true")
     p.add_argument("--precision", choices=("fp64", "mixed"), default="fp64")
     p.add_argument("--device", type=int, default=0)
     p.add_argument("--skin", type=float, default=1.5)
@@ -126,7 +138,10 @@ def run(argv=None, out=sys.stdout) -> RunResult | None:
     if a.version:
         _log(VERSION + "\n", out)
         return None
-    inp = F.load(a.input)
+    inp = F.load(a.input, implied_angles=a.implied_angles)
+    if a.intra and a.form == "chain":
+        raise F.FileFormatError("--intra runs in the plain or device form (the chain form moves "
+                                "rigid molecules)")
     cfg = inp.config
     name = a.name or (cfg.sim_name if cfg else "")
     pdb_dir = cfg.pdb_output if cfg else ""
@@ -168,6 +183,10 @@ def run(argv=None, out=sys.stdout) -> RunResult | None:
             if ensemble == "npt":
                 raise F.FileFormatError("ensemble=npt runs in the chain form (--form chain)")
             res = _run_plain(a, ctx, inp, steps, lrc0, save_state, out)
+        elif a.form == "device":
+            if ensemble == "npt":
+                raise F.FileFormatError("ensemble=npt runs in the chain form (--form chain)")
+            res = _run_device(a, ctx, inp, steps, lrc0)
         else:
             res = _run_chain(a, ctx, inp, steps, lrc0, ensemble, vol_interval, strategy, base,
                              state_dir, save_state, written, out)
@@ -203,12 +222,37 @@ def run(argv=None, out=sys.stdout) -> RunResult | None:
                      written)
 
 
-def _run_plain(a, ctx, inp, steps, lrc0, save_state, out):
-    """Simulation::run's loop (Simulation.cpp:219-264) on GpuSimulationStep."""
+def _box(a, ctx, inp):
     prec = _abi.PREC_FP64 if a.precision == "fp64" else _abi.PREC_MIXED
+    g = GpuBox(ctx, inp.rows, prec)
+    if a.intra:
+        g.set_topology(inp.topology)
+        g.set_intra(True)
+    return g
+
+
+def _run_device(a, ctx, inp, steps, lrc0):
+    """The same loop entirely on the GPU (mcgpu_run_plain_device): the C
+    library's generator restated on the device, seeded with the
+    environment's seed; no intermediate states."""
+    env = inp.box.env
+    g = _box(a, ctx, inp)
+    st = g.run_plain_device(env.random_seed, steps)
+    coords = g.download()
+    g.close()
+    return st.energy + lrc0, st.accepted, st.rejected, coords, (env.x, env.y, env.z), \
+        inp.start_step
+
+
+def _run_plain(a, ctx, inp, steps, lrc0, save_state, out):
+    """Simulation::run's loop (Simulation.cpp:219-264) on GpuSimulationStep.
+    With --intra (the reference's ENABLE_INTRA): molecule energies with the
+    intramolecular term, the intramolecular move after the rigid one (its
+    draws taken by the library from the same rand()), the step counter the
+    width tuning reads starting at 0 (SimBoxBuilder.cpp:37)."""
     env = inp.box.env
     edges = (env.x, env.y, env.z)
-    g = GpuBox(ctx, inp.rows, prec)
+    g = _box(a, ctx, inp)
     rng = LibcRand(env.random_seed)
     step = GpuSimulationStep(g, rng)
     energy = step.calc_system_energy() + lrc0
@@ -220,8 +264,14 @@ def _run_plain(a, ctx, inp, steps, lrc0, save_state, out):
         if a.state_interval > 0 and move > start and (move - start) % a.state_interval == 0:
             save_state(move, g.download(), edges)
         idx = step.choose_molecule()
-        mv = step.draw_move(idx)
-        old, new = g.move_energies(idx, *mv)
+        if a.intra:
+            g.set_step(move - start)
+            old = step.calc_molecule_energy(idx, 0)
+            step.change_molecule(idx)
+            new = step.calc_molecule_energy(idx, 0)
+        else:
+            mv = step.draw_move(idx)
+            old, new = g.move_energies(idx, *mv)
         if step.accept_move(new - old):
             acc += 1
             energy += new - old

@@ -29,7 +29,7 @@ pytestmark = pytest.mark.gpu
 FILES = Path(__file__).resolve().parent / "golden" / "files"
 REF = FILES / "ref"
 INPUTS = ["synth.par", "oplsaa.sb", "wat4.z", "mix.z", "wat.config", "mix.config",
-          "mixp.config"]
+          "mixp.config", "flex.z", "flex.config"]
 
 
 @contextlib.contextmanager
@@ -106,6 +106,21 @@ def test_plain_mixture_reproduces_reference(tmp_path, name):
         ours = atoms_of(Path("%s_200.state" % name).read_text())
         ref = atoms_of((REF / ("%s_200.state" % name)).read_text())
         assert ours.shape == ref.shape and np.array_equal(ours, ref)
+
+
+@pytest.mark.parametrize("form", ["plain", "device"])
+def test_intra_run_reproduces_reference(tmp_path, form):
+    """flex.config with the reference's intramolecular moves on (--intra,
+    implied angles as the golden vectors were made): the reference's
+    accepted count and final energy after the config's 2500 steps (its
+    random-seed 4321), through the host loop and the device loop."""
+    from helpers import load_intra_golden
+    _, _, z = load_intra_golden()
+    with workdir(tmp_path):
+        res = M.run(["flex.config", "--intra", "--implied-angles", "--form", form], out=None)
+    assert res.steps == int(z["traj_steps"][0]) and res.lrc == 0.0
+    assert res.accepted == int(z["traj_accepted"][0])
+    assert abs(res.energy - z["traj_energy"][0]) <= 1e-8 * max(1.0, abs(z["traj_e0"][0]))
 
 
 def test_plain_state_interval(tmp_path):
