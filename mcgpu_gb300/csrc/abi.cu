@@ -302,7 +302,7 @@ int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
   P.x = dalloc<double>(na, &e); P.y = dalloc<double>(na, &e); P.z = dalloc<double>(na, &e);
   P.sig = dalloc<double>(na, &e); P.eps = dalloc<double>(na, &e); P.q = dalloc<double>(na, &e);
   P.aoff = dalloc<float4>(na, &e); P.aeq = dalloc<float2>(na, &e);
-  P.aofl = dalloc<float4>(na, &e);
+  P.aofl = dalloc<float4>(na, &e); P.blend = dalloc<double2>(na, &e);
   P.mstart = dalloc<int>(nm, &e); P.mlen = dalloc<int>(nm, &e); P.mpi = dalloc<int2>(nm, &e);
   P.mfix = dalloc<uint4>(nm, &e); P.mrad = dalloc<float>(nm, &e);
   P.mq = dalloc<float4>(nm, &e); P.atpl = dalloc<float4>(na, &e);
@@ -331,6 +331,8 @@ int upload_pool(mcgpu_ctx* ctx, HostPool& hp, DevPool& dp) {
 #undef UP
   const int wpb = 8;
   k_refresh_mirrors<<<(int)((nm + wpb - 1) / wpb), wpb * 32, 0, st>>>(P, dp.mol_chain, 0, (int)nm);
+  CK(ctx, cudaGetLastError());
+  if (na > 0) k_blend_rows<<<(int)((na + 255) / 256), 256, 0, st>>>(P, (int)na);
   CK(ctx, cudaGetLastError());
   CK(ctx, cudaStreamSynchronize(st));
   dp.hdr.assign(hp.hdr.begin(), hp.hdr.end());

@@ -290,16 +290,17 @@ __device__ __forceinline__ void group_reduce_ff(const Group& g, const GroupSmem&
   }
 }
 
-// FP64 re-take of a step near the decision threshold: the reference's pair
-// arithmetic (BruteForceStep.cpp:48-79) on the FP64 positions of the chain
+// FP64 re-take of a step near the decision threshold: FP64 pair terms
+// (pair64, BruteForceStep.cpp:48-79) on the FP64 positions of the chain
 // state (anchor + offset).  Warp 0 first writes the moved molecule's old
 // and new FP64 coordinates and its FP64 parameters to shared memory; the
 // caller synchronises.
 __device__ inline void stage_chain_f64(const Pool& P, const ChainHdr& H, const GroupSmem& s,
                                        const MovedInfo& mi, int lane) {
   for (int i = lane; i < mi.len; i += 32) {
-    s.sd[i] = P.sig[mi.atom0 + i];
-    s.ed[i] = P.eps[mi.atom0 + i];
+    const double2 bl = blend64(P.sig[mi.atom0 + i], P.eps[mi.atom0 + i]);
+    s.sd[i] = bl.x;
+    s.ed[i] = bl.y;
     s.qd[i] = P.q[mi.atom0 + i];
     const double3 a = chain_pos3(mi.fx_old, s.o_old[i], H);
     const double3 b = chain_pos3(mi.fx_new, s.o_new[i], H);
@@ -327,7 +328,8 @@ __device__ __forceinline__ void batch_chain64(const Pool& P, const ChainHdr& H, 
     double so = 0.0, sn = 0.0;
     for (int b = b0 + tl; b < b0 + lenj; b += T) {
       const double3 xb = chain_pos3(Aj, P.aoff[b], H);
-      const double sb = P.sig[b], eb = P.eps[b], qb = P.q[b];
+      const double2 bl = P.blend ? P.blend[b] : blend64(P.sig[b], P.eps[b]);
+      const double sb = bl.x, eb = bl.y, qb = P.q[b];
       if (f & kInOld) so += sum_moved64(s, false, mi.len, xb.x, xb.y, xb.z, sb, eb, qb, H);
       if (f & kInNew) sn += sum_moved64(s, true, mi.len, xb.x, xb.y, xb.z, sb, eb, qb, H);
     }

@@ -177,6 +177,8 @@ struct Pool {
   double *x, *y, *z, *sig, *eps, *q;
   float4* aoff;
   float4* aofl;        // plain path: low part of the offsets (FP64 offset - aoff)
+  double2* blend;      // FP64 blending factors (sqrt sigma, sqrt eps; -1 for a skipped
+                       // site), or null (pools of the served form)
   float2* aeq;
   int *mstart, *mlen;
   int2* mpi;
@@ -597,18 +599,31 @@ __device__ __forceinline__ float lj32(float ir2, float sa, float sb, float ea, f
 
 // FP64 pair term restating SimulationStep.cpp:344-375 and
 // BruteForceStep.cpp:64-73 for a non-dummy pair at squared distance r2.
-__device__ __forceinline__ double pair64(double r2, double sa, double sb, double ea,
-                                         double eb, double qa, double qb) {
+// FP64 pair term of the reference (SimCalcs::calcLJEnergy / calcChargeEnergy
+// with BruteForceStep's blending, SimulationStep.cpp:344-375) from the
+// blending factors sa = sqrt(sigma_a), sb = sqrt(sigma_b), ea = sqrt(eps_a),
+// eb = sqrt(eps_b) and 1/r from one FP64 rsqrt: sigma_ab^2 = (sa sb)^2,
+// eps_ab = ea eb.  Each term is within a few ulps of the reference's (two
+// square roots, a square root and two divisions per pair cost many passes
+// of GB300's FP64 pipe); sums differ from the reference's at the FP64
+// rounding of their order.
+__device__ __forceinline__ double pair64(double r2, double sa, double sb, double ea, double eb,
+                                         double qa, double qb) {
   if (r2 == 0.0) return 0.0;
-  double ss = sa * sb, ee = ea * eb;
-  double sigma = sqrt(ss >= 0 ? ss : -ss);
-  double eps = sqrt(ee >= 0 ? ee : -ee);
-  double s2r2 = (sigma * sigma) / r2;
-  double s6r6 = s2r2 * s2r2 * s2r2;
-  double s12r12 = s6r6 * s6r6;
-  double lj = 4.0 * eps * (s12r12 - s6r6);
-  double r = sqrt(r2);
-  return lj + (qa * qb * kCoulomb) / r;
+  const double ri = rsqrt(r2);
+  const double sig = sa * sb;
+  const double s2r2 = (sig * sig) * (ri * ri);
+  const double s6r6 = s2r2 * s2r2 * s2r2;
+  const double lj = 4.0 * (ea * eb) * (s6r6 * s6r6 - s6r6);
+  return lj + (qa * qb * kCoulomb) * ri;
+}
+
+// The blending factor rows of an atom for pair64: sqrt(sigma) and
+// sqrt(eps); sigma = -1 marks a site the reference skips (a negative sigma
+// or epsilon, BruteForceStep.cpp:64-65).
+__device__ __forceinline__ double2 blend64(double sig, double eps) {
+  if (!(sig >= 0 && eps >= 0)) return make_double2(-1.0, 0.0);
+  return make_double2(sqrt(sig), sqrt(eps));
 }
 
 }  // namespace mcgpu

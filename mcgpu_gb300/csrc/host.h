@@ -18,6 +18,7 @@ namespace mcgpu {
 
 // ---- kernels (kernels.cu, npt.cu) ----
 __global__ void k_refresh_mirrors(Pool P, const int* mol_chain, int m_begin, int m_end);
+__global__ void k_blend_rows(Pool P, int n_atom);
 __global__ void k_change_molecule(Pool P, int chain, int mol, Proposal prop, SmemShape shape);
 __global__ void k_rollback(Pool P, int chain, int mol);
 __global__ void k_chain_sums(Pool P, const double* emol, double* out);
@@ -167,7 +168,8 @@ struct DevPool {
   int nl_max_cells = 0;           // largest per-chain cell allocation
 
   void release() {
-    void* ptrs[] = {P.x, P.y, P.z, P.sig, P.eps, P.q, P.aoff, P.aofl, P.aeq, P.mstart, P.mlen, P.mpi,
+    void* ptrs[] = {P.x, P.y, P.z, P.sig, P.eps, P.q, P.aoff, P.aofl, P.blend, P.aeq, P.mstart,
+                    P.mlen, P.mpi,
                     P.mfix, P.mrad, P.mq, P.atpl, P.pidx, P.ppos, P.hdr, P.rb, P.trace,
                     P.nl, P.nl_cnt, P.pbuild, P.mcell, P.cell_cnt, P.cell_start, P.cell_mol,
                     P.vc_cnt, P.vc_start, P.vc_mol, P.vc_of,

@@ -23,6 +23,12 @@ __global__ void k_refresh_mirrors(Pool P, const int* mol_chain, int m_begin, int
   refresh_molecule(P, P.hdr[mol_chain[m]], m, threadIdx.x & 31, 32);
 }
 
+// The FP64 pair terms' per-atom blending factors (blend64).
+__global__ void k_blend_rows(Pool P, int n_atom) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a < n_atom) P.blend[a] = blend64(P.sig[a], P.eps[a]);
+}
+
 // ---- deterministic last-CTA sum ------------------------------------------
 
 // Thread 0 of a CTA: publishes its writes and reports whether this CTA is

@@ -104,7 +104,8 @@ __device__ inline void stage(const Pool& P, const ChainHdr& H, int m, const Prop
   for (int i = lane; i < len; i += 32) {
     int a = a0 + i;
     s.ox[i] = P.x[a]; s.oy[i] = P.y[a]; s.oz[i] = P.z[a];
-    s.sd[i] = P.sig[a]; s.ed[i] = P.eps[a]; s.qd[i] = P.q[a];
+    const double2 bl = blend64(P.sig[a], P.eps[a]);
+    s.sd[i] = bl.x; s.ed[i] = bl.y; s.qd[i] = P.q[a];
     const float4 o = P.aoff[a];
     const float2 q = P.aeq[a];
     s.o_old[i] = o;
@@ -522,7 +523,9 @@ __device__ __forceinline__ void batch_u1(const Pool& P, const ChainHdr& H, const
 }
 
 // FP64 pair terms from the master rows, the reference's per-pair minimum
-// image and dummy-site rule (BruteForceStep.cpp:61-76).
+// image and dummy-site rule (BruteForceStep.cpp:61-76); sb, eb: the
+// neighbour atom's blending factors (blend64), the moved atoms' staged in
+// s.sd / s.ed.
 __device__ __forceinline__ double sum_moved64(const GroupSmem& s, bool use_new, int len, double xb,
                                               double yb, double zb, double sb, double eb, double qb,
                                               const ChainHdr& H) {
@@ -530,9 +533,10 @@ __device__ __forceinline__ double sum_moved64(const GroupSmem& s, bool use_new, 
   const double* ys = use_new ? s.ny : s.oy;
   const double* zs = use_new ? s.nz : s.oz;
   double acc = 0.0;
+  if (sb < 0) return acc;
   for (int i = 0; i < len; i++) {
     const double sa = s.sd[i], ea = s.ed[i];
-    if (!(sa >= 0 && sb >= 0 && ea >= 0 && eb >= 0)) continue;
+    if (sa < 0) continue;
     const double dx = make_periodic(xb - xs[i], H.L[0]);
     const double dy = make_periodic(yb - ys[i], H.L[1]);
     const double dz = make_periodic(zb - zs[i], H.L[2]);
@@ -562,9 +566,10 @@ __device__ __forceinline__ void batch_f64(const Pool& P, const ChainHdr& H, cons
     double so = 0.0, sn = 0.0;
     for (int b = b0 + tl; b < b0 + lenj; b += T) {
       const double xb = P.x[b], yb = P.y[b], zb = P.z[b];
-      const double sb = P.sig[b], eb = P.eps[b], qb = P.q[b];
-      if (f & kInOld) so += sum_moved64(s, false, mi.len, xb, yb, zb, sb, eb, qb, H);
-      if (f & kInNew) sn += sum_moved64(s, true, mi.len, xb, yb, zb, sb, eb, qb, H);
+      const double2 bl = P.blend[b];
+      const double qb = P.q[b];
+      if (f & kInOld) so += sum_moved64(s, false, mi.len, xb, yb, zb, bl.x, bl.y, qb, H);
+      if (f & kInNew) sn += sum_moved64(s, true, mi.len, xb, yb, zb, bl.x, bl.y, qb, H);
     }
     for (int off = T >> 1; off > 0; off >>= 1) {
       so += __shfl_xor_sync(~0u, so, off);
