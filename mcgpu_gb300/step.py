@@ -336,7 +336,7 @@ def run_plain(step: GpuSimulationStep, n_steps: int, fused: bool = False) -> Pla
     e0 = e
     acc = rej = 0
     intra = getattr(step.box, "intra", False)
-    step0 = step.box.topology.step_num if intra else 0
+    step0 = step.box.intra_state()["step_num"] if intra else 0
     for s in range(n_steps):
         if intra:
             # the counter Simulation::run increments after every step
@@ -356,4 +356,6 @@ def run_plain(step: GpuSimulationStep, n_steps: int, fused: bool = False) -> Pla
         else:
             rej += 1
             step.rollback(idx)
+    if intra:
+        step.box.set_step(step0 + n_steps)
     return PlainResult(e, acc, rej, e0)

@@ -154,7 +154,6 @@ def test_plain_trajectory_intra_golden(ctx, native):
     else:
         res = run_plain(GpuSimulationStep(g, LibcRand(seed)), n)
         e0, e, acc = res.initial_energy, res.energy, res.accepted
-        g.set_step(n)
     assert abs(e0 - z["traj_e0"][0]) <= 1e-11 * max(1.0, abs(z["traj_e0"][0]))
     assert acc == z["traj_accepted"][0]
     assert abs(e - z["traj_energy"][0]) <= 1e-8 * max(1.0, abs(z["traj_e0"][0]))
