@@ -254,3 +254,61 @@ def test_random_topologies_vs_reference(ref, seed):
     s = o.state()
     assert same(bl, s["bond_len"]) and same(asz, s["angle_size"])
     assert [s["max_bond_delta"], s["max_angle_delta"], s["step_num"]] == list(st[:3])
+
+
+@live
+@pytest.mark.parametrize("name", ["meoh500", "indole267"])
+def test_reference_flexible_examples_live(tmp_path, ref, name):
+    """The reference's own flexible examples (methanol: variable bonds 2-6,
+    angles 3-6; indole: variable ranges too), where its sources are present:
+    the package loader's bond / angle / exclusion rows equal the reference
+    loader's (for the implied-angle setting its flag took), and the oracle's
+    loop with the intramolecular term and move on the reference's rows equals
+    the reference's own code run with ENABLE_INTRA's composition, 300 steps,
+    bit for bit."""
+    import shutil
+    from mcgpu_gb300.workloads import BoxData, Topology
+    from oracle.pyoracle import REFERENCE_SRC
+    res = REFERENCE_SRC / "resources"
+    if not res.is_dir():
+        pytest.skip("reference resources not present")
+    shutil.copytree(res, tmp_path / "resources")
+    shutil.copy(res / "exampleFiles" / (name + ".config"), tmp_path / (name + ".config"))
+    rows = ref.load_files(str(tmp_path / (name + ".config")))
+    ref.activate_loaded()
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        cands = [F.load(name + ".config", implied_angles=v).topology for v in (False, True)]
+    finally:
+        os.chdir(cwd)
+    r = ref.topology(cands[0].type_natom)
+    keys = [k for k in TOPO_KEYS if k != "type_natom"]
+    match = [t for t in cands if all(np.array_equal(getattr(t, k), r[k]) for k in keys)]
+    assert match, name
+    topo = match[0]
+    assert topo.flex_bonds and topo.flex_angles
+    p = r["params"]
+    assert (topo.max_bond_delta, topo.max_angle_delta) == (p[0], p[1])
+    box = BoxData(x=rows["x"], y=rows["y"], z=rows["z"], sigma=rows["sigma"],
+                  epsilon=rows["epsilon"], charge=rows["charge"], mol_start=rows["mol_start"],
+                  mol_len=rows["mol_len"], mol_pidx_start=rows["mol_pidx_start"],
+                  mol_pidx_count=rows["mol_pidx_count"], pidx=rows["pidx"], size=rows["size"],
+                  cutoff=rows["params"][0], temperature=rows["params"][1],
+                  max_translate=rows["params"][3], max_rotate=rows["params"][4]).normalise()
+    o = OracleFlex(box, topo)
+    e0 = o.system_energy()
+    same = lambda a, b: np.array_equal(np.asarray(a), np.asarray(b), equal_nan=True)
+    assert same(e0, ref.L.ref_system_energy_intra())
+    LibcRand(12345)
+    e, acc = o.run_plain(300, e0)
+    ref.L.ref_seed(12345)
+    a = C.c_int()
+    er = ref.L.ref_run_plain_intra(300, e0, C.byref(a))
+    assert same(e, er) and acc == a.value
+    assert same(o.coords(), ref.coords())
+    bl, asz, st = ref.intra_state(topo.n_bond, topo.n_angle)
+    s = o.state()
+    assert same(bl, s["bond_len"]) and same(asz, s["angle_size"])
+    print(f"{name}: {box.n_mol} molecules, {topo.n_bond} bonds, {topo.n_angle} angles, "
+          f"accepted {acc}/300, E {e0:.4f} -> {e:.4f}")
