@@ -53,8 +53,9 @@ FP32_FLOPS_PER_PAIR = 38   # per atom pair, fixed by convention from the referen
 # only for its own tile and kernel version; otherwise the line's traffic is
 # null and says why (a launch reads the chains' rows about once whatever the
 # tile, ~34 MB, but a figure from another tile or kernel is not this run's).
-CHAIN_KERNEL_VERSION = "pair code shared by both placements, LJ mask in the header, FP32-only step"
-CHAIN_TRAFFIC_BYTES = {(160, 1, 64, 1): (34.22e6, CHAIN_KERNEL_VERSION)}
+CHAIN_KERNEL_VERSION = ("pair code shared by both placements, LJ mask in the header, FP32-only "
+                        "step, FP64 re-takes from per-atom blending rows and one rsqrt")
+CHAIN_TRAFFIC_BYTES = {(160, 1, 64, 1): (33.97e6, CHAIN_KERNEL_VERSION)}
 
 
 def chain_traffic(tile):
