@@ -55,6 +55,8 @@ FP32_FLOPS_PER_PAIR = 38   # per atom pair, fixed by convention from the referen
 # tile, ~34 MB, but a figure from another tile or kernel is not this run's).
 CHAIN_KERNEL_VERSION = ("pair code shared by both placements, LJ mask in the header, FP32-only "
                         "step, FP64 re-takes from per-atom blending rows and one rsqrt")
+# (the re-take's screen reusing the step's FP32 screen changed no row a launch
+# reads outside the rare re-takes; the capture above stands for it)
 CHAIN_TRAFFIC_BYTES = {(160, 1, 64, 1): (33.97e6, CHAIN_KERNEL_VERSION)}
 
 

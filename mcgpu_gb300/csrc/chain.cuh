@@ -350,9 +350,9 @@ __device__ __forceinline__ void batch_chain64(const Pool& P, const ChainHdr& H, 
 // With a Verlet list (cand non-null), the molecules cand[c_begin .. c_end),
 // every nw-th entry per warp as in warp_eval_chain.
 __device__ inline void warp_eval_chain64(const Pool& P, const ChainHdr& H, const GroupSmem& s,
-                                  const MovedInfo& mi, int c_begin, int c_end, int w, int nw,
-                                  int lane, int T, double& eo, double& en,
-                                  const int* cand = nullptr) {
+                                  const MovedInfo& mi, const float4* pcache, int c_begin,
+                                  int c_end, int w, int nw, int lane, int T, double& eo,
+                                  double& en, const int* cand = nullptr) {
   int* rj = s.lj + w * kRing;
   int head = 0, tail = 0;
   const unsigned lt = lanemask_lt();
@@ -369,21 +369,20 @@ __device__ inline void warp_eval_chain64(const Pool& P, const ChainHdr& H, const
     }
     const int j = (cand && idx < c_end) ? cand[idx] : idx;
     int f = 0;
+    // the step's own screen: FP32 outside the guard band, the FP64 test on
+    // these same FP64 positions inside it -- the FP64 in-range set exactly,
+    // without an FP64 distance for every candidate
     if (idx < c_end && j != mi.mol) {
-      const int2 pj = P.mpi[j];
-      const uint4 Aj = P.mfix[j];
-      for (int k2 = 0; k2 < pj.y; k2++) {
-        const double3 b = chain_pos3(Aj, P.aoff[P.pidx[pj.x + k2]], H);
-        for (int k1 = 0; k1 < mi.npidx; k1++) {
-          const int pa = s.pa[k1];
-          const double3 ao = make_double3(s.ox[pa], s.oy[pa], s.oz[pa]);
-          const double3 an = make_double3(s.nx[pa], s.ny[pa], s.nz[pa]);
-          if (!(f & kInOld) && in_range_pos64(ao, b, H)) f |= kInOld;
-          if (!(f & kInNew) && in_range_pos64(an, b, H)) f |= kInNew;
-        }
-      }
+      float4 q0;
+      if (pcache)
+        q0 = pcache[j - H.mol0];
+      else if (H.simple_prim)
+        q0 = P.ppos[H.pidx0 + (j - H.mol0)];
+      else
+        q0 = P.ppos[P.mpi[j].x];
+      f = screen_chain(P, H, s, mi, j, q0);
     }
-    const unsigned bal = __ballot_sync(~0u, f != 0);
+  const unsigned bal = __ballot_sync(~0u, f != 0);
     if (f) rj[(tail + __popc(bal & lt)) & (kRing - 1)] = (j << 4) | f;
     tail += __popc(bal);
     if (tail - head >= 32) {

@@ -416,10 +416,11 @@ __device__ __forceinline__ void chain_steps(Pool P, int n_steps, unsigned* queue
         double eo = 0.0, en = 0.0, ab2 = 0.0;
         long long np2 = 0;
         if (use_list)
-          warp_eval_chain64(P, H, ss, mi, 0, P.nl_cnt[mi.mol], w, nw, lane, T, eo, en,
+          warp_eval_chain64(P, H, ss, mi, pcache, 0, P.nl_cnt[mi.mol], w, nw, lane, T, eo, en,
                             P.nl + (size_t)mi.mol * P.nl_stride);
         else
-          warp_eval_chain64(P, H, ss, mi, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, eo, en);
+          warp_eval_chain64(P, H, ss, mi, pcache, H.mol0, H.mol0 + H.n_mol, w, nw, lane, T, eo,
+                            en);
         group_reduce(g, ss, eo, en, ab2, np2, st & 1);
         e_old = eo;
         e_new = en;
