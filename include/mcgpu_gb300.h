@@ -92,6 +92,11 @@ typedef struct {
   int32_t nl_builds;      /* Verlet-list builds                            */
   int32_t nl_full_scans;  /* steps screened over all molecules while a list
                              was on (trial beyond skin/2, or list stale)   */
+  int32_t window_redo;    /* steps of a window (mcgpu_chain_set_window,
+                             mcgpu_batch_set_window) evaluated again after
+                             an earlier accepted step of the window moved
+                             their molecule or one within range of it      */
+  int32_t pad0;
 } mcgpu_chain_stats;
 
 /* One volume move of an NPT chain (for replay checks). */
@@ -312,6 +317,17 @@ int mcgpu_intra_get(mcgpu_box* box, double* bond_len, double* angle_size,
 int mcgpu_chain_run(mcgpu_box* box, uint64_t seed, uint32_t chain_id,
                     int n_steps, int rotation, mcgpu_chain_stats* stats,
                     mcgpu_trace* trace);
+/* Steps per window of this box's device-resident runs: k = 1 (one step at a
+ * time, the default), 2, 4 or 8.  With k > 1 a chain is advanced by a
+ * thread-block cluster of k CTAs: each window's k moves (known in advance:
+ * counter-based draws) are evaluated at once, one per CTA, against the state
+ * at the window's start; then every CTA takes the k decisions in step order
+ * and evaluates a step again on the current state when an earlier accepted
+ * step of the window moved its molecule or a molecule within range of it.
+ * Decisions, coordinates and counters equal those of k = 1; only the FP32
+ * summation order of re-evaluated steps can differ.  Needs k CTAs on k SMs
+ * of one GPC. */
+int mcgpu_chain_set_window(mcgpu_box* box, int k);
 
 /* ---- batched chains: one persistent kernel advances many chains --------- */
 
@@ -346,6 +362,12 @@ int mcgpu_batch_set_tile(mcgpu_batch* batch, int threads, int chains_per_cta,
                          int steps_per_launch, int lanes_per_molecule);
 int mcgpu_batch_get_tile(mcgpu_batch* batch, int* threads, int* chains_per_cta,
                          int* steps_per_launch, int* lanes_per_molecule);
+/* Windows of k steps (1, 2, 4, 8) for the batch's chains, as
+ * mcgpu_chain_set_window: one cluster of k CTAs per chain, each CTA one
+ * group of the tile's threads (the tile must have one chain per CTA and at
+ * least k warps).  For a few large chains; a batch of many chains already
+ * fills the device one chain per group. */
+int mcgpu_batch_set_window(mcgpu_batch* batch, int k);
 /* Like mcgpu_batch_run (synchronous, no graph) and records every step:
  * out[c * n_steps + s] is step s of chain c.  If vol_out is non-NULL it
  * receives the volume moves of an NPT batch: vol_out[c * (n_steps /

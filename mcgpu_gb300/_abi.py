@@ -74,7 +74,8 @@ class ChainStats(C.Structure):
     _fields_ = [("energy", C.c_double), ("steps", C.c_int64), ("accepted", C.c_int64),
                 ("pairs", C.c_int64), ("error", C.c_int32), ("ties", C.c_int32),
                 ("box", C.c_double * 3), ("vol_tried", C.c_int32), ("vol_accepted", C.c_int32),
-                ("nl_builds", C.c_int32), ("nl_full_scans", C.c_int32)]
+                ("nl_builds", C.c_int32), ("nl_full_scans", C.c_int32),
+                ("window_redo", C.c_int32), ("pad0", C.c_int32)]
 
 
 class VolTrace(C.Structure):
@@ -142,6 +143,8 @@ _PROTOS = {
     "mcgpu_batch_run": (C.c_int, [_vp, C.c_int, C.c_int]),
     "mcgpu_batch_autotune": (C.c_int, [_vp, C.c_int]),
     "mcgpu_batch_set_tile": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "mcgpu_batch_set_window": (C.c_int, [_vp, C.c_int]),
+    "mcgpu_chain_set_window": (C.c_int, [_vp, C.c_int]),
     "mcgpu_batch_get_tile": (C.c_int, [_vp, _ip, _ip, _ip, _ip]),
     "mcgpu_batch_sync": (C.c_int, [_vp]),
     "mcgpu_batch_run_traced": (C.c_int, [_vp, C.c_int, C.POINTER(Trace), C.POINTER(VolTrace)]),

@@ -159,6 +159,12 @@ class ChainBatch:
         self._check(_abi.lib().mcgpu_batch_set_tile(self._h, threads, chains_per_cta,
                                                     steps_per_launch, lanes_per_molecule))
 
+    def set_window(self, k: int) -> None:
+        """Windows of k steps (1, 2, 4, 8): one cluster of k CTAs per chain,
+        the window's moves evaluated at once and decided in step order
+        (mcgpu_batch_set_window); results equal k = 1."""
+        self._check(_abi.lib().mcgpu_batch_set_window(self._h, int(k)))
+
     @property
     def tile(self) -> tuple[int, int, int, int]:
         """(threads per CTA, chains per CTA, steps per launch, lanes cap)."""

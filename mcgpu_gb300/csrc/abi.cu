@@ -492,7 +492,8 @@ extern "C" int mcgpu_ctx_create(mcgpu_ctx** out, int device) {
   if (cudaFuncSetAttribute(k_chain_steps, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            200 * 1024) != cudaSuccess ||
       cudaFuncSetAttribute(k_chain_steps_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           200 * 1024) != cudaSuccess) {
+                           200 * 1024) != cudaSuccess ||
+      window_init() != cudaSuccess) {
     cudaStreamDestroy(c->own);
     delete c;
     return set_err(nullptr, MCGPU_ERR_CUDA, "cannot enable large shared memory for the chain kernel");
@@ -546,6 +547,7 @@ struct mcgpu_box {
   std::unique_ptr<IntraHost> intra;  // bond / angle rows (flexible molecules)
   bool intra_on = false;             // ENABLE_INTRA for this box
   PlainLoop* dloop = nullptr;        // state of mcgpu_run_plain_device
+  int window = 1;                    // steps per window of mcgpu_chain_run (cluster CTAs)
 };
 
 // FP64 rows current before a plain entry point reads them.
@@ -1403,9 +1405,15 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
     CK(ctx, cudaMalloc((void**)&b->dtrace, sizeof(mcgpu_trace) * (size_t)n_steps));
     b->trace_cap = n_steps;
   }
-  // one group for the chain: up to 16 warps (the wide kernel above 8)
-  const int nw = std::max(1, std::min(16, dp.n_mol / 256));
+  // one group for the chain: up to 16 warps (the wide kernel above 8); a
+  // window of K steps: one such group per CTA of a K-CTA cluster, at least
+  // K warps (one stages each step of the window)
+  const int K = b->window;
+  const int nw = std::max(K > 1 ? K : 1, std::min(16, dp.n_mol / 256));
   SmemShape sh = shape_for(dp.max_len, nw, pool_cache_n(dp));
+  const int wsmem = K > 1 ? window_smem_bytes(sh, K) : 0;
+  if (K > 1 && wsmem > kWindowSmemMax)
+    return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "a %d-step window needs %d B shared memory", K, wsmem);
   // with a Verlet list, short launches let stale lists be rebuilt promptly
   const int seg = dp.nl_on ? 64 : 1024;
   for (int done = 0; done < n_steps; done += seg) {
@@ -1415,7 +1423,10 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
     CK(ctx, cudaMemsetAsync(b->queue, 0, sizeof(unsigned), st));
     Pool P = dp.P;
     P.trace = nullptr;
-    if (nw > 8)
+    if (K > 1)
+      CK(ctx, launch_chain_window(K, 1, nw * 32, wsmem, st, P, k, b->order, 1, sh,
+                                  trace ? b->dtrace : nullptr, done, 0, 0));
+    else if (nw > 8)
       k_chain_steps_wide<<<1, nw * 32, sh.bytes(), st>>>(P, k, b->queue, b->order, 1, nw, sh,
                                                          trace ? b->dtrace : nullptr, done, 0, 0);
     else
@@ -1442,6 +1453,7 @@ extern "C" int mcgpu_chain_run(mcgpu_box* b, uint64_t seed, uint32_t chain_id, i
     stats->vol_accepted = h.vol_accepted;
     stats->nl_builds = h.nl_builds;
     stats->nl_full_scans = h.nl_full;
+    stats->window_redo = h.win_redo;
   }
   CK(ctx, cudaStreamSynchronize(st));
   return MCGPU_OK;
@@ -1462,6 +1474,8 @@ struct mcgpu_batch {
   cudaGraphExec_t graph = nullptr;
   int graph_launches = 0, graph_spl = 0, graph_threads = 0, graph_cpc = 0, graph_lanes = 0;
   int graph_interval = 0;                 // NPT interval the graph covers (0 = NVT graph)
+  int window = 1;                         // steps per window (clusters of `window` CTAs)
+  int graph_window = 0;
   // NPT: steps every chain has taken (all chains advance together), the
   // volume interval, and the volume phase's device buffers
   long long steps_done = 0;
@@ -1503,6 +1517,14 @@ static int batch_launch(mcgpu_batch* bt, int steps, unsigned* q, cudaStream_t st
   int rc = pool_nl_rebuild(ctx, bt->pool, st);
   if (rc) return rc;
   CK(ctx, cudaMemsetAsync(q, 0, sizeof(unsigned), st));
+  if (bt->window > 1) {
+    const int K = bt->window, wsmem = window_smem_bytes(sh, K);
+    const int n_cl = std::max(1, std::min(bt->pool.n_chains,
+                                          window_max_clusters(K, bt->threads, wsmem)));
+    CK(ctx, launch_chain_window(K, n_cl, bt->threads, wsmem, st, bt->pool.P, steps, bt->order,
+                                bt->pool.n_chains, sh, trace, trace_off, trace_stride, bt->lanes));
+    return MCGPU_OK;
+  }
   if (bt->threads > 256)
     k_chain_steps_wide<<<grid, bt->threads, smem, st>>>(bt->pool.P, steps, q, bt->order,
                                                         bt->pool.n_chains, gw, sh, trace,
@@ -1631,11 +1653,63 @@ extern "C" int mcgpu_batch_set_tile(mcgpu_batch* bt, int threads, int cpc, int s
                    lanes);
   int smem = shape_for(bt->pool.max_len, (threads / 32) / cpc, bt->cache_n).bytes() * cpc;
   if (smem > 200 * 1024) return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "tile needs %d B shared memory", smem);
+  if (bt->window > 1 && (cpc != 1 || threads / 32 < bt->window))
+    return set_err(ctx, MCGPU_ERR_INVALID,
+                   "the batch runs %d-step windows (one chain per CTA, at least %d warps): set the "
+                   "window to 1 first", bt->window, bt->window);
+  if (bt->window > 1 &&
+      window_smem_bytes(shape_for(bt->pool.max_len, threads / 32, bt->cache_n), bt->window) >
+          kWindowSmemMax)
+    return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "tile too large for a %d-step window", bt->window);
   bt->threads = threads;
   bt->cpc = cpc;
   bt->spl = spl;
   bt->lanes = lanes;
   batch_drop_graph(bt);
+  return MCGPU_OK;
+}
+
+// Window sizes the windowed chain kernel takes (they divide the 32 moves
+// drawn at a time).
+static bool window_size_ok(int k) { return k == 1 || k == 2 || k == 4 || k == 8; }
+
+extern "C" int mcgpu_batch_set_window(mcgpu_batch* bt, int k) {
+  if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
+  mcgpu_ctx* ctx = bt->ctx;
+  if (!window_size_ok(k)) return set_err(ctx, MCGPU_ERR_INVALID, "window %d must be 1, 2, 4 or 8", k);
+  if (k > 1) {
+    if (bt->cpc != 1)
+      return set_err(ctx, MCGPU_ERR_INVALID, "a window needs one chain per CTA (tile has %d)", bt->cpc);
+    if (bt->threads / 32 < k)
+      return set_err(ctx, MCGPU_ERR_INVALID, "a %d-step window needs at least %d warps per CTA", k, k);
+    const SmemShape sh = shape_for(bt->pool.max_len, bt->threads / 32, bt->cache_n);
+    const int wsmem = window_smem_bytes(sh, k);
+    if (wsmem > kWindowSmemMax)
+      return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "a %d-step window needs %d B shared memory", k, wsmem);
+    if (window_max_clusters(k, bt->threads, wsmem) < 1)
+      return set_err(ctx, MCGPU_ERR_UNSUPPORTED, "no cluster of %d CTAs of %d threads fits the device",
+                     k, bt->threads);
+  }
+  bt->window = k;
+  batch_drop_graph(bt);
+  return MCGPU_OK;
+}
+
+extern "C" int mcgpu_chain_set_window(mcgpu_box* b, int k) {
+  if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
+  if (!window_size_ok(k)) return set_err(b->ctx, MCGPU_ERR_INVALID, "window %d must be 1, 2, 4 or 8", k);
+  if (k > 1) {
+    const int nw = std::max(k, std::min(16, b->pool.n_mol / 256));
+    const SmemShape sh = shape_for(b->pool.max_len, nw, pool_cache_n(b->pool));
+    const int wsmem = window_smem_bytes(sh, k);
+    if (wsmem > kWindowSmemMax)
+      return set_err(b->ctx, MCGPU_ERR_UNSUPPORTED, "a %d-step window needs %d B shared memory", k,
+                     wsmem);
+    if (window_max_clusters(k, nw * 32, wsmem) < 1)
+      return set_err(b->ctx, MCGPU_ERR_UNSUPPORTED, "no cluster of %d CTAs of %d threads fits the device",
+                     k, nw * 32);
+  }
+  b->window = k;
   return MCGPU_OK;
 }
 
@@ -1691,13 +1765,15 @@ static int batch_build_graph(mcgpu_batch* bt, int launches, int interval) {
   bt->graph_cpc = bt->cpc;
   bt->graph_lanes = bt->lanes;
   bt->graph_interval = interval;
+  bt->graph_window = bt->window;
   return MCGPU_OK;
 }
 
 static bool batch_graph_matches(const mcgpu_batch* bt, int launches, int interval) {
   return bt->graph && bt->graph_spl == bt->spl && bt->graph_launches == launches &&
          bt->graph_threads == bt->threads && bt->graph_cpc == bt->cpc &&
-         bt->graph_lanes == bt->lanes && bt->graph_interval == interval;
+         bt->graph_lanes == bt->lanes && bt->graph_interval == interval &&
+         bt->graph_window == bt->window;
 }
 
 // Steps n_steps with direct launches of at most spl steps (recording steps
@@ -1939,6 +2015,7 @@ extern "C" int mcgpu_batch_stats(mcgpu_batch* bt, mcgpu_chain_stats* stats) {
     stats[c].vol_accepted = h[c].vol_accepted;
     stats[c].nl_builds = h[c].nl_builds;
     stats[c].nl_full_scans = h[c].nl_full;
+    stats[c].window_redo = h[c].win_redo;
     err |= h[c].error;
   }
   if (err) return set_err(ctx, MCGPU_ERR_DEVICE, "a chain reported device error status %d", err);
@@ -2156,6 +2233,8 @@ extern "C" int mcgpu_batch_autotune(mcgpu_batch* bt, int trial_steps) {
   if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
   mcgpu_ctx* ctx = bt->ctx;
   if (trial_steps < 1) trial_steps = 64;
+  if (bt->window > 1)
+    return set_err(ctx, MCGPU_ERR_INVALID, "the tile search times one-step kernels: set the window to 1 first");
   int rc = batch_snapshot(bt, false);
   if (rc) return rc;
   const long long steps0 = bt->steps_done;

@@ -53,6 +53,7 @@ enum : int {
   kErrListOverflow = 1,
   kErrBadIndex = 2,
   kErrNonFinite = 3,
+  kErrWindowSync = 4,   // a cluster-wide wait of the windowed chain kernel ran out
 };
 
 // Per-chain header, one per chain (a single box is chain 0).
@@ -72,8 +73,10 @@ struct __align__(16) ChainHdr {
   double lrc_v;                       // long-range LJ correction x volume (NPT term)
   unsigned long long seed, step;
   long long accepted, pairs;
-  int error, ties, fp64_pairs, pad4;  // ties: steps evaluated with FP64 pairs;
-                                      // fp64_pairs: every step with FP64 pairs
+  int error, ties, fp64_pairs, win_redo;  // ties: steps evaluated with FP64 pairs;
+                                          // fp64_pairs: every step with FP64 pairs;
+                                          // win_redo: steps of a window (windowed chain
+                                          // kernel) re-evaluated after earlier steps
   // isobaric (NPT) volume moves: every vol_interval steps (0 = NVT), ln V
   // step uniform in +-max_dlnv, pressure in kcal/mol/A^3
   double pressure, max_dlnv;

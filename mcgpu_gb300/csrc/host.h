@@ -201,4 +201,21 @@ int pool_set_verlet(mcgpu_ctx* ctx, DevPool& dp, double skin, cudaStream_t st);
 // Rebuilds the stale lists (no-op launches when none is stale).
 int pool_nl_rebuild(mcgpu_ctx* ctx, DevPool& dp, cudaStream_t st);
 
+// ---- windowed chain kernel (window.cu) ----------------------------------------
+// Shared memory the windowed kernel may use per CTA.
+constexpr int kWindowSmemMax = 220 * 1024;
+// Dynamic shared memory of one CTA of a K-step window for group shape sh.
+int window_smem_bytes(const SmemShape& sh, int K);
+// Enables the kernel's shared memory (once per context).
+cudaError_t window_init();
+// Clusters of K CTAs (threads, smem bytes each) that fit on the device at
+// once (0 if none).
+int window_max_clusters(int K, int threads, int smem);
+// n_clusters clusters of K CTAs of `threads` threads, chain tasks order[0
+// .. n_tasks) advanced n_steps steps each in windows of K steps.
+cudaError_t launch_chain_window(int K, int n_clusters, int threads, int smem, cudaStream_t st,
+                                const Pool& P, int n_steps, const int* order, int n_tasks,
+                                SmemShape sh, mcgpu_trace* trace, int trace_off, int trace_stride,
+                                int lanes_cap);
+
 }  // namespace mcgpu

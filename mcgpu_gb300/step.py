@@ -161,6 +161,12 @@ class GpuBox:
         """Verlet neighbour lists (skin in Angstrom, <= 0 off) for chain_run."""
         self._check(_abi.lib().mcgpu_box_set_verlet(self._h, float(skin)))
 
+    def set_window(self, k: int) -> None:
+        """Windows of k steps (1, 2, 4, 8) for chain_run: a cluster of k CTAs
+        evaluates each window's moves at once and takes the decisions in step
+        order (mcgpu_chain_set_window); results equal k = 1."""
+        self._check(_abi.lib().mcgpu_chain_set_window(self._h, int(k)))
+
     def run_plain_native(self, seed: int, n_steps: int, fused: bool = False) -> "_abi.PlainStats":
         """Simulation::run's NVT loop in the library's C++ (mcgpu_run_plain):
         the same calls and the same rand() draws as run_plain over

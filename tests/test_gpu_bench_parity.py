@@ -11,8 +11,10 @@
   largest among them): coordinates bit for bit and accepted counts equal.
   The worst per-step dE error as a fraction of the FP32-pair tolerance
   (|dE_gpu - dE_ref| <= 1e-5 max(|dE_ref|, 1e-3 sum k|terms|)) is printed.
-* The 4000 x 16-atom chain (bicyclic_4000), full scan and Verlet lists.
-* The 32,768-water NPT chain with Verlet lists and volume moves.
+* The 4000 x 16-atom chain (bicyclic_4000), full scan and Verlet lists,
+  one step at a time and in windows of 4 and 8 steps (thread-block clusters).
+* The 32,768-water NPT chain with Verlet lists and volume moves, one step
+  at a time and in windows of 8 steps.
 
 The oracle's decisions are the reference's FP64 decisions
 (SimulationStep.cpp:794-803) on the reference's FP64 energies
@@ -146,14 +148,16 @@ def c1():
     return box, tr, oc.coords(), acc, e
 
 
-@pytest.mark.parametrize("skin", [0.0, 1.5])
-def test_bicyclic_4000_chain_replay(ctx, c1, skin):
-    """4000 x 16-atom molecules, one chain (the 16-warp chain kernel), with
-    and without Verlet lists: 200 steps equal to the oracle."""
+@pytest.mark.parametrize("skin,window", [(0.0, 1), (1.5, 1), (1.5, 8), (0.0, 4)])
+def test_bicyclic_4000_chain_replay(ctx, c1, skin, window):
+    """4000 x 16-atom molecules, one chain (the 16-warp chain kernel, or
+    windows of 4 / 8 steps over a cluster of as many CTAs), with and without
+    Verlet lists: 200 steps equal to the oracle."""
     box, otr, coords, acc, e = c1
     g = GpuBox(ctx, box, PREC_MIXED)
     if skin:
         g.set_verlet(skin)
+    g.set_window(window)
     st, tr = g.chain_run(seed=11, n_steps=200, rotation=ROT_AXIS, trace=True)
     assert st.error == 0 and st.steps == 200
     for s, (t, r) in enumerate(zip(tr, otr)):
@@ -168,20 +172,24 @@ def test_bicyclic_4000_chain_replay(ctx, c1, skin):
     if skin:
         assert st.nl_builds >= 1
     g.close()
-    print(f"bicyclic4000 skin {skin}: accepted {acc}/200, FP64 re-takes {st.ties}")
+    print(f"bicyclic4000 skin {skin} window {window}: accepted {acc}/200, FP64 re-takes "
+          f"{st.ties}, re-evaluated in a window {st.window_redo}")
 
 
-def test_water_32768_npt_verlet_replay(ctx):
+@pytest.mark.parametrize("window", [1, 8])
+def test_water_32768_npt_verlet_replay(ctx, window):
     """The 32,768-water system from its relaxed start (512 relaxed waters
     replicated 4 x 4 x 4), NPT with Verlet lists as measured (one 16-warp
-    group, mixed volume energies), a volume move every 100 steps: 200 steps
-    and 2 volume moves equal to the oracle's (draws, decisions, box edges,
-    coordinates bit for bit)."""
+    group, or windows of 8 steps over a cluster of 8 such CTAs; mixed volume
+    energies), a volume move every 100 steps: 200 steps and 2 volume moves
+    equal to the oracle's (draws, decisions, box edges, coordinates bit for
+    bit)."""
     from mcgpu_gb300.prepare import relaxed_water_32768
     box = relaxed_water_32768(ctx)
     interval, steps, dl, seed = 100, 200, 0.0015, 0x5EED
     bt = ChainBatch(ctx, [box], [seed], rotation=ROT_AXIS)
     bt.set_tile(512, 1, 64)
+    bt.set_window(window)
     bt.set_verlet(1.5)
     bt.set_npt(interval, 1.0, dl, PREC_MIXED)
     tr, vtr = bt.run_traced(steps, volume=True)
@@ -209,6 +217,6 @@ def test_water_32768_npt_verlet_replay(ctx):
     assert np.array_equal(np.stack([x, y, z], 1), oc.coords())
     assert st.error == 0
     bt.close()
-    print(f"water32768 NPT: energy/N {e / box.n_mol:.3f} kcal/mol, accepted "
+    print(f"water32768 NPT window {window}: energy/N {e / box.n_mol:.3f} kcal/mol, accepted "
           f"{st.accepted}/{steps}, volume moves {st.vol_accepted}/{st.vol_tried}, "
           f"Verlet builds {st.nl_builds}")
