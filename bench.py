@@ -465,7 +465,8 @@ def bench_single(ctx, plain_steps: int = 150, chain_steps: int = 4000) -> dict:
     +-0.2 A / +-10 deg: the plain GPU drop-in (host loop over the
     SimulationStep contract, FP64 and FP32 pairs) against the device-resident
     chain (FP32 pairs, FP64 sums, on-device RNG and accept), with and without
-    the Verlet list (skin 1.5 A).  Start: FCC lattice (10^3 cells hold the
+    the Verlet list (skin 1.5 A), one step at a time and in windows of 8 and
+    16 steps (a thread-block cluster per chain).  Start: FCC lattice (10^3 cells hold the
     4000 centres exactly), one common orientation, as the reference builds
     its boxes; random centres at this density put atoms of neighbours on top
     of each other (energies ~1e19 kcal/mol)."""
@@ -479,15 +480,34 @@ def bench_single(ctx, plain_steps: int = 150, chain_steps: int = 4000) -> dict:
         g.run_plain_native(7, plain_steps, fused=True)
         out[name] = plain_steps / (time.perf_counter() - t0)
         g.close()
-    for name, skin in (("chain_full_scan", 0.0), ("chain_verlet", 1.5)):
+    for name, skin, window in (("chain_full_scan", 0.0, 1), ("chain_verlet", 1.5, 1),
+                               ("chain_verlet_w8", 1.5, 8), ("chain_verlet_w16", 1.5, 16)):
         g = M.GpuBox(ctx, box, M.PREC_MIXED)
         if skin > 0:
             g.set_verlet(skin)
+        try:
+            g.set_window(window)
+        except M.MCGPUError as e:
+            out[name] = None
+            out[name + "_refused"] = str(e)
+            g.close()
+            continue
         g.chain_run(seed=11, n_steps=64)
         out[name], st = timed_chain(g, 11, chain_steps)
         out[name + "_fp64_retakes"] = st.ties
+        if window > 1:
+            out[name + "_redo"] = st.window_redo
         g.close()
-    out["chain_over_plain_fp64"] = out["chain_verlet"] / out["plain_fp64"]
+    win = {k: out.get(f"chain_verlet_w{k}") for k in (8, 16)}
+    best = max((k for k in win if win[k]), key=lambda k: win[k], default=None)
+    out["chain_verlet_window"] = win[best] if best else None
+    out["chain_verlet_window_steps"] = best
+    out["window_note"] = ("windows of K steps: one thread-block cluster of K CTAs per chain, "
+                          "the K moves evaluated at once against the window's start state and "
+                          "decided in step order (a step re-evaluated when an earlier accepted "
+                          "step of its window moved its molecule or one within range of it); "
+                          "the same decisions and coordinates as one step at a time")
+    out["chain_over_plain_fp64"] = (out["chain_verlet_window"] or out["chain_verlet"]) / out["plain_fp64"]
     out["unit"] = "moves/s"
     return out
 
@@ -502,7 +522,10 @@ def bench_large(ctx, steps: int = 200000, interval: int = 500, max_dlnv: float =
     (volume energies FP32 with the threshold re-takes) and FP64 pair terms
     (every step and volume move).  Their decisions are the FP64 ones in
     both, so they follow one trajectory and differ only in the rounding of
-    the running energy.  Every `recompute_every` steps a full FP64 system
+    the running energy.  The FP32 arm runs in windows of 8 steps and the
+    FP64 arm in windows of 16 (a thread-block cluster of as many CTAs, the
+    same decisions as one step at a time); beside them the FP32 arm one step
+    at a time for 20,000 steps.  Every `recompute_every` steps a full FP64 system
     energy gives the drift of the running energy, U/N and the density;
     block averages (10 blocks) give <U>/N and <rho> with their standard
     errors.  Beside it the plain FP64 drop-in for a few steps."""
@@ -525,10 +548,37 @@ def bench_large(ctx, steps: int = 200000, interval: int = 500, max_dlnv: float =
         b = x[: len(x) - len(x) % nb].reshape(nb, -1).mean(axis=1)
         return float(b.mean()), float(b.std(ddof=1) / math.sqrt(nb))
 
+    # one step at a time (one group of 16 warps), FP32 pairs, for comparison
+    bt = M.ChainBatch(ctx, [box], [0x5EED], rotation=M.ROT_AXIS)
+    bt.set_tile(512, 1, 64)
+    bt.set_verlet(1.5)
+    bt.set_npt(interval, 1.0, max_dlnv, M.PREC_MIXED)
+    n1 = min(steps, 20000)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    bt.run(n1)
+    torch.cuda.synchronize()
+    out["fp32_pairs_one_step_moves_per_s"] = n1 / (time.perf_counter() - t1)
+    out["fp32_pairs_one_step_steps"] = n1
+    bt.close()
+
+    def windowed(bt, k):
+        """Windows of k steps (a cluster of k CTAs), else the largest that fits."""
+        for w in (k, 8, 4, 2, 1):
+            if w > k:
+                continue
+            try:
+                bt.set_window(w)
+                return w
+            except M.MCGPUError:
+                pass
+        return 1
+
     coords = {}
-    for name, prec in (("fp32_pairs", M.PREC_MIXED), ("fp64_pairs", M.PREC_FP64)):
+    for name, prec, want in (("fp32_pairs", M.PREC_MIXED, 8), ("fp64_pairs", M.PREC_FP64, 16)):
         bt = M.ChainBatch(ctx, [box], [0x5EED], rotation=M.ROT_AXIS)
-        bt.set_tile(512, 1, 64)          # one chain: one group of 16 warps
+        bt.set_tile(512, 1, 64)          # one chain: groups of 16 warps
+        window = windowed(bt, want)
         bt.set_verlet(1.5)
         bt.set_npt(interval, 1.0, max_dlnv, prec)
         bt.set_precision(prec)
@@ -550,7 +600,8 @@ def bench_large(ctx, steps: int = 200000, interval: int = 500, max_dlnv: float =
         bt.close()
         mu, su = block(u)
         mr, sr = block(rho)
-        out[name] = {"moves_per_s": steps / run_s, "run_s": run_s,
+        out[name] = {"moves_per_s": steps / run_s, "run_s": run_s, "window_steps": window,
+                     "window_redo": st.window_redo,
                      "drift_rel_final": drift[-1], "drift_rel_max": max(abs(d) for d in drift),
                      "drift_series_every_steps": recompute_every,
                      "drift_rel_series": [float(f"{d:.3e}") for d in drift[:: max(1, len(drift) // 20)]],

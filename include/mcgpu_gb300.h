@@ -318,7 +318,7 @@ int mcgpu_chain_run(mcgpu_box* box, uint64_t seed, uint32_t chain_id,
                     int n_steps, int rotation, mcgpu_chain_stats* stats,
                     mcgpu_trace* trace);
 /* Steps per window of this box's device-resident runs: k = 1 (one step at a
- * time, the default), 2, 4 or 8.  With k > 1 a chain is advanced by a
+ * time, the default), 2, 4, 8 or 16 (16: a non-portable cluster size).  With k > 1 a chain is advanced by a
  * thread-block cluster of k CTAs: each window's k moves (known in advance:
  * counter-based draws) are evaluated at once, one per CTA, against the state
  * at the window's start; then every CTA takes the k decisions in step order
@@ -326,7 +326,7 @@ int mcgpu_chain_run(mcgpu_box* box, uint64_t seed, uint32_t chain_id,
  * step of the window moved its molecule or a molecule within range of it.
  * Decisions, coordinates and counters equal those of k = 1; only the FP32
  * summation order of re-evaluated steps can differ.  Needs k CTAs on k SMs
- * of one GPC. */
+ * of one GPC (refused with MCGPU_ERR_UNSUPPORTED where none fits). */
 int mcgpu_chain_set_window(mcgpu_box* box, int k);
 
 /* ---- batched chains: one persistent kernel advances many chains --------- */
@@ -362,7 +362,7 @@ int mcgpu_batch_set_tile(mcgpu_batch* batch, int threads, int chains_per_cta,
                          int steps_per_launch, int lanes_per_molecule);
 int mcgpu_batch_get_tile(mcgpu_batch* batch, int* threads, int* chains_per_cta,
                          int* steps_per_launch, int* lanes_per_molecule);
-/* Windows of k steps (1, 2, 4, 8) for the batch's chains, as
+/* Windows of k steps (1, 2, 4, 8, 16) for the batch's chains, as
  * mcgpu_chain_set_window: one cluster of k CTAs per chain, each CTA one
  * group of the tile's threads (the tile must have one chain per CTA and at
  * least k warps).  For a few large chains; a batch of many chains already

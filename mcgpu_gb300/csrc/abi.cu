@@ -1670,13 +1670,13 @@ extern "C" int mcgpu_batch_set_tile(mcgpu_batch* bt, int threads, int cpc, int s
 }
 
 // Window sizes the windowed chain kernel takes (they divide the 32 moves
-// drawn at a time).
-static bool window_size_ok(int k) { return k == 1 || k == 2 || k == 4 || k == 8; }
+// drawn at a time; 16 is a non-portable cluster size).
+static bool window_size_ok(int k) { return k == 1 || k == 2 || k == 4 || k == 8 || k == 16; }
 
 extern "C" int mcgpu_batch_set_window(mcgpu_batch* bt, int k) {
   if (!bt) return set_err(nullptr, MCGPU_ERR_INVALID, "null batch");
   mcgpu_ctx* ctx = bt->ctx;
-  if (!window_size_ok(k)) return set_err(ctx, MCGPU_ERR_INVALID, "window %d must be 1, 2, 4 or 8", k);
+  if (!window_size_ok(k)) return set_err(ctx, MCGPU_ERR_INVALID, "window %d must be 1, 2, 4, 8 or 16", k);
   if (k > 1) {
     if (bt->cpc != 1)
       return set_err(ctx, MCGPU_ERR_INVALID, "a window needs one chain per CTA (tile has %d)", bt->cpc);
@@ -1697,7 +1697,7 @@ extern "C" int mcgpu_batch_set_window(mcgpu_batch* bt, int k) {
 
 extern "C" int mcgpu_chain_set_window(mcgpu_box* b, int k) {
   if (!b) return set_err(nullptr, MCGPU_ERR_INVALID, "null box");
-  if (!window_size_ok(k)) return set_err(b->ctx, MCGPU_ERR_INVALID, "window %d must be 1, 2, 4 or 8", k);
+  if (!window_size_ok(k)) return set_err(b->ctx, MCGPU_ERR_INVALID, "window %d must be 1, 2, 4, 8 or 16", k);
   if (k > 1) {
     const int nw = std::max(k, std::min(16, b->pool.n_mol / 256));
     const SmemShape sh = shape_for(b->pool.max_len, nw, pool_cache_n(b->pool));

@@ -1,6 +1,6 @@
 // window.cu -- one chain advanced in windows of K consecutive steps by a
-// thread-block cluster of K CTAs (K = 2, 4 or 8), one step of each window
-// per CTA.
+// thread-block cluster of K CTAs (K = 2, 4, 8 or 16), one step of each
+// window per CTA.
 //
 // The reference's loop (Simulation.cpp:219-264) is sequential: step s + 1
 // sees the state step s left.  Its moves here come from counter-based draws
@@ -26,8 +26,9 @@
 // step while the slower one still reads the state for an earlier step;
 // that happens only during a re-evaluation, and a re-evaluated step ends
 // with a cluster-wide wait before anyone commits it.  The waits are counts
-// stored into every CTA's shared memory (release) and polled in the CTA's
-// own (acquire) with a time limit: on expiry the chain's error word is set
+// stored into every CTA's shared memory (after a release fence) and polled
+// in the CTA's own (then an acquire fence), one lane per CTA of the cluster,
+// with a time limit: on expiry the chain's error word is set
 // and the CTA leaves its loop, so a fault in this protocol ends the launch
 // with an error status instead of a stalled GPU.  The only hardware cluster
 // barriers are at entry (before any remote store) and at exit (no CTA
@@ -91,14 +92,18 @@ __device__ __forceinline__ void st_remote_u64(unsigned a, unsigned long long v) 
   asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(a), "l"(v) : "memory");
 }
 
-__device__ __forceinline__ void st_remote_release(unsigned a, unsigned v) {
-  asm volatile("st.release.cluster.shared::cluster.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+__device__ __forceinline__ void st_remote_relaxed(unsigned a, unsigned v) {
+  asm volatile("st.relaxed.cluster.shared::cluster.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ unsigned ld_acquire_cluster(unsigned a) {
+__device__ __forceinline__ unsigned ld_relaxed_cluster(unsigned a) {
   unsigned v;
-  asm volatile("ld.acquire.cluster.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+  asm volatile("ld.relaxed.cluster.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
   return v;
+}
+
+__device__ __forceinline__ void fence_cluster() {
+  asm volatile("fence.acq_rel.cluster;" ::: "memory");
 }
 
 // Shared memory of the window protocol, after the group's own.
@@ -114,35 +119,38 @@ __host__ __device__ inline int win_extra_bytes(const SmemShape& sh, int K) {
          2 * K * sh.ahead_bytes();
 }
 
-// Cluster-wide wait number n: thread 0 stores rec (if any) into slot
-// rec_at of every CTA's records, then the count n into its own flag slot in
-// every CTA (release: the record first), then polls its own flag row until
-// every CTA has reached n (acquire) or the limit passes.  The outcome is the
-// same in every thread of the CTA.
+// Cluster-wide wait number n, lane q of warp 0 serving CTA q: it stores
+// rec (if any) into slot rec_at of CTA q's records, fences (release), stores
+// the count n into this CTA's flag slot in CTA q, then polls CTA q's slot of
+// this CTA's flag row until it reaches n or the limit passes, and fences
+// (acquire).  The CTA barrier after it carries what the lanes acquired to
+// every thread.  The outcome is the same in every thread of the CTA.
 __device__ bool win_wait(const Group& g, const WinSmem& ws, unsigned K, unsigned rank, unsigned n,
                          const WinRec* rec, int rec_at) {
-  if (g.tid == 0) {
-    for (unsigned q = 0; q < K; q++) {
+  if (g.tid < 32) {
+    const unsigned q = g.tid;
+    bool ok = true;
+    if (q < K) {
       if (rec) {
         const unsigned a = remote_addr(ws.rec + rec_at, q);
         const unsigned long long* w = (const unsigned long long*)rec;
         for (int k = 0; k < (int)(sizeof(WinRec) / 8); k++) st_remote_u64(a + 8 * k, w[k]);
       }
-    }
-    for (unsigned q = 0; q < K; q++) st_remote_release(remote_addr(ws.flag + rank, q), n);
-    bool ok = true;
-    const unsigned long long t0 = global_ns();
-    for (unsigned q = 0; q < K && ok; q++) {
+      fence_cluster();
+      st_remote_relaxed(remote_addr(ws.flag + rank, q), n);
       const unsigned a = remote_addr(ws.flag + q, rank);
+      const unsigned long long t0 = global_ns();
       unsigned it = 0;
-      while (ld_acquire_cluster(a) < n) {
+      while (ld_relaxed_cluster(a) < n) {
         if ((++it & 63) == 0 && global_ns() - t0 > kWinWaitNs) {
           ok = false;
           break;
         }
       }
+      fence_cluster();
     }
-    ws.ok[n & 1] = ok ? 1u : 0u;
+    ok = __all_sync(~0u, ok);
+    if (g.tid == 0) ws.ok[n & 1] = ok ? 1u : 0u;
   }
   g.sync();
   return ws.ok[n & 1] != 0;
@@ -418,8 +426,16 @@ __global__ void __launch_bounds__(512, 1)
 int window_smem_bytes(const SmemShape& sh, int K) { return sh.bytes() + win_extra_bytes(sh, K); }
 
 cudaError_t window_init() {
-  return cudaFuncSetAttribute(k_chain_window, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              kWindowSmemMax);
+  const cudaError_t e = cudaFuncSetAttribute(
+      k_chain_window, cudaFuncAttributeMaxDynamicSharedMemorySize, kWindowSmemMax);
+  if (e != cudaSuccess) return e;
+  // clusters of 16 CTAs are beyond the portable size of 8; where the device
+  // refuses them, window_max_clusters reports none and the setters refuse
+  // the window
+  if (cudaFuncSetAttribute(k_chain_window, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+      cudaSuccess)
+    cudaGetLastError();
+  return cudaSuccess;
 }
 
 int window_max_clusters(int K, int threads, int smem) {

@@ -29,6 +29,17 @@ def ctx():
     c.close()
 
 
+def set_window(obj, k):
+    """obj.set_window(k); a 16-CTA cluster (a non-portable size) is skipped
+    where the device places none."""
+    try:
+        obj.set_window(k)
+    except MCGPUError as e:
+        if k == 16 and e.status == 4:
+            pytest.skip(f"no 16-CTA cluster fits: {e}")
+        raise
+
+
 def oracle_check(box, seed, chain, trace, mode, coords, accepted):
     """The oracle's run of the same chain: every step's molecule, uniform and
     decision; FP64 energies of the steps taken with FP64 pairs; the final
@@ -58,7 +69,7 @@ def same_run(tr_a, tr_b, tol_rel=1e-5):
         assert abs(a.e_old - b.e_old) <= tl and abs(a.e_new - b.e_new) <= tl, s
 
 
-@pytest.mark.parametrize("window", [2, 4, 8])
+@pytest.mark.parametrize("window", [2, 4, 8, 16])
 @pytest.mark.parametrize("name,mode", [("water256", ROT_AXIS), ("water48_halfbox", ROT_EULER),
                                        ("mixed", ROT_AXIS), ("bicyclic100", ROT_AXIS)])
 def test_window_small_boxes_replay(ctx, name, mode, window):
@@ -67,7 +78,7 @@ def test_window_small_boxes_replay(ctx, name, mode, window):
     of them re-evaluated in their window."""
     box, _ = load_golden(name)
     g = GpuBox(ctx, box, PREC_MIXED)
-    g.set_window(window)
+    set_window(g, window)
     seed, steps = 987654321, 600
     st, tr = g.chain_run(seed=seed, n_steps=steps, chain_id=0, rotation=mode, trace=True)
     assert st.steps == steps and st.error == 0
@@ -79,7 +90,7 @@ def test_window_small_boxes_replay(ctx, name, mode, window):
           f"{st.window_redo}, FP64 re-takes {st.ties}")
 
 
-@pytest.mark.parametrize("window", [2, 4, 8])
+@pytest.mark.parametrize("window", [2, 4, 8, 16])
 @pytest.mark.parametrize("skin", [0.0, 1.5])
 def test_window_equals_one_step_kernel(ctx, window, skin):
     """3000 waters (L = 44.8 A, rc 9 A), 1024 steps with and without Verlet
@@ -92,7 +103,7 @@ def test_window_equals_one_step_kernel(ctx, window, skin):
         g = GpuBox(ctx, box, PREC_MIXED)
         if skin:
             g.set_verlet(skin)
-        g.set_window(k)
+        set_window(g, k)
         st, tr = g.chain_run(seed=2468, n_steps=1024, rotation=ROT_AXIS, trace=True)
         assert st.error == 0 and st.steps == 1024
         x, y, z = g.download()
@@ -119,16 +130,17 @@ def test_window_equals_one_step_kernel(ctx, window, skin):
           f"re-evaluated {sk.window_redo}")
 
 
-def test_window_fp64_pairs_batch(ctx):
+@pytest.mark.parametrize("window", [8, 16])
+def test_window_fp64_pairs_batch(ctx, window):
     """A 2000-water chain with FP64 pair terms at every step (the FP64 arm of
-    the precision sweep), windows of 8 against one step at a time: the same
-    decisions and coordinates, FP64 energies equal to 1e-12."""
+    the precision sweep), windows of 8 and 16 against one step at a time: the
+    same decisions and coordinates, FP64 energies equal to 1e-12."""
     box = W.water_box(2000, seed=19)
     runs = {}
-    for k in (1, 8):
+    for k in (1, window):
         bt = ChainBatch(ctx, [box], [0xC0FFEE], rotation=ROT_AXIS)
         bt.set_tile(512, 1, 64)
-        bt.set_window(k)
+        set_window(bt, k)
         bt.set_verlet(1.5)
         bt.set_precision(PREC_FP64)
         tr = bt.run_traced(512)[0]
@@ -136,7 +148,7 @@ def test_window_fp64_pairs_batch(ctx):
         assert st.error == 0 and st.ties == 512
         runs[k] = (st, tr, np.stack(bt.download(0), 1))
         bt.close()
-    (s1, t1, c1), (s8, t8, c8) = runs[1], runs[8]
+    (s1, t1, c1), (s8, t8, c8) = runs[1], runs[window]
     same_run(t8, t1, tol_rel=1e-12)
     assert np.array_equal(c8, c1)
     assert s8.accepted == s1.accepted
@@ -172,7 +184,7 @@ def test_window_refusals(ctx):
     tile search (it times one-step kernels)."""
     box = W.water_box(300, seed=3)
     g = GpuBox(ctx, box, PREC_MIXED)
-    for k in (0, 3, 16, -1):
+    for k in (0, 3, 12, 32, -1):
         with pytest.raises(MCGPUError):
             g.set_window(k)
     g.close()
