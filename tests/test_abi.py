@@ -59,6 +59,8 @@ def test_null_arguments_rejected():
     assert lib.mcgpu_box_upload(None, None, 0, None) == 1
     assert lib.mcgpu_mol_energy(None, 0, 0, None) == 1
     assert lib.mcgpu_batch_run(None, 1, 1) == 1
+    assert lib.mcgpu_chain_set_window(None, 8) == 1
+    assert lib.mcgpu_batch_set_window(None, 8) == 1
 
 
 def test_build_centres_min_distance():
