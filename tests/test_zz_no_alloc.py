@@ -144,6 +144,35 @@ def test_static_energy_allocates_nothing_after_setup(ctx):
     assert torch.cuda.mem_get_info(0)[0] == free0
 
 
+def test_static_energy_captures_into_a_graph(ctx):
+    """After the first call, a call captures into a CUDA graph (stream
+    capture refuses allocations and host synchronisation, so the capture
+    itself shows the call does neither) and the graph's replays give the
+    oracle's energy without changing the device's free memory."""
+    import torch
+    box = water_box(1000, seed=5)
+    ref = reference_energy(box)
+    rows = DeviceRows(box)
+    assert abs(rows.energy() - ref) <= tol64(ref)      # first call: address lookup
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=side):
+        st = _abi.lib().mcgpu_system_energy_static(
+            C.byref(rows.desc), C.c_void_p(rows.out.data_ptr()),
+            C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    free0 = torch.cuda.mem_get_info(0)[0]
+    for _ in range(3):
+        rows.out.fill_(float("nan"))
+        graph.replay()
+        torch.cuda.synchronize()
+        assert abs(float(rows.out.item()) - ref) <= tol64(ref)
+    assert torch.cuda.mem_get_info(0)[0] == free0
+
+
 def test_static_energy_rejects_oversized_box():
     import torch
     d = _abi.BoxDesc()
