@@ -694,6 +694,66 @@ void orc_fchain_draw(const orc_chain* c, uint64_t seed, uint32_t chain, uint64_t
   mv->u = u01f(d[0]);
 }
 
+/* A move of chain molecule m proposed on the current state: its new
+ * anchor, quaternion and offsets. */
+typedef struct {
+  int mol;
+  uint32_t A[3];
+  qf qn;
+  float* off; /* [3 * mol_len] */
+} fprop;
+
+static void fchain_propose(const orc_chain* c, const orc_movef* mv, fprop* p) {
+  const orc_box* b = c->b;
+  const int m = mv->mol, a0 = b->mol_start[m], len = b->mol_len[m];
+  qf q = {c->q[4 * m], c->q[4 * m + 1], c->q[4 * m + 2], c->q[4 * m + 3]};
+  qf qd = {mv->qw, mv->qx, mv->qy, mv->qz};
+  const qf qn = q_norm(q_mul(qd, q));
+  float R[9];
+  q_matrix(qn, R);
+  const int v = a0 + mv->vertex;
+  float onv[3];
+  m_vec(R, &c->tpl[3 * v], onv);
+  const float dl[3] = {(c->off[3 * v] - onv[0]) + mv->dx, (c->off[3 * v + 1] - onv[1]) + mv->dy,
+                       (c->off[3 * v + 2] - onv[2]) + mv->dz};
+  const float inv[3] = {(float)(4294967296.0 / b->size[0]), (float)(4294967296.0 / b->size[1]),
+                        (float)(4294967296.0 / b->size[2])};
+  p->mol = m;
+  for (int k = 0; k < 3; k++) p->A[k] = c->A[3 * m + k] + (uint32_t)fix_step(dl[k], inv[k]);
+  for (int i = 0; i < len; i++) m_vec(R, &c->tpl[3 * (a0 + i)], &p->off[3 * i]);
+  p->qn = qn;
+}
+
+/* Molecule m of the state at anchor A and offsets off, its FP64 rows
+ * refreshed. */
+static void fchain_place(orc_chain* c, int m, const uint32_t* A, const float* off) {
+  const orc_box* b = c->b;
+  const int a0 = b->mol_start[m], len = b->mol_len[m];
+  for (int k = 0; k < 3; k++) c->A[3 * m + k] = A[k];
+  memcpy(&c->off[3 * a0], off, sizeof(float) * 3 * (size_t)len);
+  chain_rows(c, m);
+}
+
+/* E_old and E_new of proposal p on the current state (the state is left
+ * as it was); save holds 3 * mol_len floats. */
+static void fchain_eval(orc_chain* c, const fprop* p, float* save, double* e_old, double* e_new) {
+  orc_box* b = c->b;
+  const int m = p->mol, a0 = b->mol_start[m], len = b->mol_len[m];
+  uint32_t A0[3] = {c->A[3 * m], c->A[3 * m + 1], c->A[3 * m + 2]};
+  memcpy(save, &c->off[3 * a0], sizeof(float) * 3 * (size_t)len);
+  *e_old = orc_mol_energy(b, m, 0);
+  fchain_place(c, m, p->A, p->off);
+  *e_new = orc_mol_energy(b, m, 0);
+  fchain_place(c, m, A0, save);
+}
+
+static int fchain_largest(const orc_box* b) {
+  int big = 0;
+  for (int m = 0; m < b->n_mol; m++)
+    if (b->mol_len[m] > big) big = b->mol_len[m];
+  return big;
+}
+
 /* The chain's Metropolis loop: draw, FP64 old energy, FP32 move of the
  * state, FP64 new energy, the reference's decision on the FP64 dE
  * (SimulationStep.cpp:794-803), commit or restore. */
@@ -702,51 +762,25 @@ double orc_fchain_run(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step
   orc_box* b = c->b;
   double e = e0;
   long long acc = 0;
-  int big = 0;
-  for (int m = 0; m < b->n_mol; m++)
-    if (b->mol_len[m] > big) big = b->mol_len[m];
+  const int big = fchain_largest(b);
   float* save_off = (float*)malloc(sizeof(float) * 3 * (size_t)big);
+  fprop p;
+  p.off = (float*)malloc(sizeof(float) * 3 * (size_t)big);
   for (int st = 0; st < n_steps; st++) {
     orc_movef mv;
     orc_fchain_draw(c, seed, chain, step0 + (uint64_t)st, &mv);
-    const int m = mv.mol, a0 = b->mol_start[m], len = b->mol_len[m];
-    const double e_old = orc_mol_energy(b, m, 0);
-    /* move */
-    qf q = {c->q[4 * m], c->q[4 * m + 1], c->q[4 * m + 2], c->q[4 * m + 3]};
-    qf qd = {mv.qw, mv.qx, mv.qy, mv.qz};
-    const qf qn = q_norm(q_mul(qd, q));
-    float R[9];
-    q_matrix(qn, R);
-    const int v = a0 + mv.vertex;
-    float onv[3];
-    m_vec(R, &c->tpl[3 * v], onv);
-    const float dl[3] = {(c->off[3 * v] - onv[0]) + mv.dx, (c->off[3 * v + 1] - onv[1]) + mv.dy,
-                         (c->off[3 * v + 2] - onv[2]) + mv.dz};
-    const float inv[3] = {(float)(4294967296.0 / b->size[0]), (float)(4294967296.0 / b->size[1]),
-                          (float)(4294967296.0 / b->size[2])};
-    uint32_t Aold[3], qsave[4];
-    (void)qsave;
-    for (int k = 0; k < 3; k++) {
-      Aold[k] = c->A[3 * m + k];
-      c->A[3 * m + k] = Aold[k] + (uint32_t)fix_step(dl[k], inv[k]);
-    }
-    for (int i = 0; i < len; i++) {
-      for (int k = 0; k < 3; k++) save_off[3 * i + k] = c->off[3 * (a0 + i) + k];
-      m_vec(R, &c->tpl[3 * (a0 + i)], &c->off[3 * (a0 + i)]);
-    }
-    chain_rows(c, m);
-    const double e_new = orc_mol_energy(b, m, 0);
+    const int m = mv.mol;
+    double e_old, e_new;
+    fchain_propose(c, &mv, &p);
+    fchain_eval(c, &p, save_off, &e_old, &e_new);
     const double de = e_new - e_old;
     const int ok = (de < 0) || (exp(-de / b->kT) >= (double)mv.u);
     if (ok) {
       e += de;
       acc++;
-      c->q[4 * m] = qn.w; c->q[4 * m + 1] = qn.x; c->q[4 * m + 2] = qn.y; c->q[4 * m + 3] = qn.z;
-    } else {
-      for (int k = 0; k < 3; k++) c->A[3 * m + k] = Aold[k];
-      for (int i = 0; i < len; i++)
-        for (int k = 0; k < 3; k++) c->off[3 * (a0 + i) + k] = save_off[3 * i + k];
-      chain_rows(c, m);
+      fchain_place(c, m, p.A, p.off);
+      c->q[4 * m] = p.qn.w; c->q[4 * m + 1] = p.qn.x; c->q[4 * m + 2] = p.qn.y;
+      c->q[4 * m + 3] = p.qn.z;
     }
     if (trace) {
       trace[st].mol = m;
@@ -757,8 +791,126 @@ double orc_fchain_run(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step
       trace[st].u = (double)mv.u;
     }
   }
+  free(p.off);
   free(save_off);
   if (n_accepted) *n_accepted = acc;
+  return e;
+}
+
+/* Molecule m's primary positions (FP64, as its rows would hold them) at
+ * anchor A and offsets off: out[3 * k + d] for primary k. */
+static void fchain_prims(const orc_chain* c, int m, const uint32_t* A, const float* off,
+                         double* out) {
+  const orc_box* b = c->b;
+  const int a0 = b->mol_start[m], ps = b->mol_pidx_start[m], pc = b->mol_pidx_count[m];
+  for (int k = 0; k < pc; k++) {
+    const int i = b->pidx[ps + k] - a0;
+    for (int d = 0; d < 3; d++) out[3 * k + d] = chain_coord(A[d], off[3 * i + d], b->size[d]);
+  }
+}
+
+/* The reference's in-range test (SimulationStep.cpp:317-342, the other
+ * molecule's primary minus the moved one's) between primary sets pj (the
+ * moved molecule, nj primaries) and pi (ni). */
+static int prims_in_range(const orc_box* b, const double* pj, int nj, const double* pi, int ni) {
+  for (int k1 = 0; k1 < nj; k1++)
+    for (int k2 = 0; k2 < ni; k2++) {
+      const double dx = orc_make_periodic(pi[3 * k2] - pj[3 * k1], b->size[0]);
+      const double dy = orc_make_periodic(pi[3 * k2 + 1] - pj[3 * k1 + 1], b->size[1]);
+      const double dz = orc_make_periodic(pi[3 * k2 + 2] - pj[3 * k1 + 2], b->size[2]);
+      if (dx * dx + dy * dy + dz * dz <= b->cutoff * b->cutoff) return 1;
+    }
+  return 0;
+}
+
+/* The window form of the chain loop (the device's windowed kernel,
+ * restated to check its rule exactly): windows of K steps; every step of a
+ * window is proposed and evaluated on the state at the window's start; then,
+ * in step order, a step's energies stand unless an earlier accepted step of
+ * the window moved the same molecule (the move is then proposed again on the
+ * current state) or moved a molecule that is in range of it (the reference's
+ * test, either placement of either molecule); such a step is evaluated
+ * again on the current state.  Otherwise orc_fchain_run: the same trace,
+ * state and return value; *n_redo counts the steps evaluated again.
+ * in_range_rule = 0 drops the in-range half of the rule (a planted mistake,
+ * for the tests that show the rule is needed). */
+double orc_fchain_run_window(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step0,
+                             int n_steps, int K, double e0, orc_trace* trace,
+                             long long* n_accepted, long long* n_redo, int in_range_rule) {
+  orc_box* b = c->b;
+  double e = e0;
+  long long acc = 0, redo = 0;
+  const int big = fchain_largest(b);
+  int maxp = 0;
+  for (int m = 0; m < b->n_mol; m++)
+    if (b->mol_pidx_count[m] > maxp) maxp = b->mol_pidx_count[m];
+  float* save = (float*)malloc(sizeof(float) * 3 * (size_t)big);
+  fprop* p = (fprop*)malloc(sizeof(fprop) * (size_t)K);
+  orc_movef* mv = (orc_movef*)malloc(sizeof(orc_movef) * (size_t)K);
+  double* eo = (double*)malloc(sizeof(double) * (size_t)K);
+  double* en = (double*)malloc(sizeof(double) * (size_t)K);
+  int* ok = (int*)malloc(sizeof(int) * (size_t)K);
+  /* primaries before and after each step: [K][2][3 * maxp] */
+  double* pr = (double*)malloc(sizeof(double) * (size_t)K * 2 * 3 * (size_t)(maxp > 0 ? maxp : 1));
+  for (int j = 0; j < K; j++) p[j].off = (float*)malloc(sizeof(float) * 3 * (size_t)big);
+#define PR(j, t) (pr + ((size_t)(j) * 2 + (t)) * 3 * (size_t)maxp)
+  for (int s0 = 0; s0 < n_steps; s0 += K) {
+    const int nst = (n_steps - s0 < K) ? n_steps - s0 : K;
+    for (int j = 0; j < nst; j++) {
+      orc_fchain_draw(c, seed, chain, step0 + (uint64_t)(s0 + j), &mv[j]);
+      fchain_propose(c, &mv[j], &p[j]);
+      fchain_eval(c, &p[j], save, &eo[j], &en[j]);
+    }
+    for (int j = 0; j < nst; j++) {
+      const int m = mv[j].mol, a0 = b->mol_start[m], nj = b->mol_pidx_count[m];
+      int same = 0, near = 0;
+      for (int i = 0; i < j; i++)
+        if (ok[i] && mv[i].mol == m) same = 1;
+      if (same) fchain_propose(c, &mv[j], &p[j]);
+      fchain_prims(c, m, &c->A[3 * m], &c->off[3 * a0], PR(j, 0));
+      fchain_prims(c, m, p[j].A, p[j].off, PR(j, 1));
+      for (int i = 0; i < j && !same && !near && in_range_rule; i++) {
+        if (!ok[i]) continue;
+        const int ni = b->mol_pidx_count[mv[i].mol];
+        for (int ti = 0; ti < 2 && !near; ti++)
+          for (int tj = 0; tj < 2 && !near; tj++)
+            near = prims_in_range(b, PR(j, tj), nj, PR(i, ti), ni);
+      }
+      if (same || near) {
+        fchain_eval(c, &p[j], save, &eo[j], &en[j]);
+        redo++;
+      }
+      const double de = en[j] - eo[j];
+      ok[j] = (de < 0) || (exp(-de / b->kT) >= (double)mv[j].u);
+      if (ok[j]) {
+        e += de;
+        acc++;
+        fchain_place(c, m, p[j].A, p[j].off);
+        c->q[4 * m] = p[j].qn.w; c->q[4 * m + 1] = p[j].qn.x; c->q[4 * m + 2] = p[j].qn.y;
+        c->q[4 * m + 3] = p[j].qn.z;
+      }
+      if (trace) {
+        orc_trace* t = &trace[s0 + j];
+        t->mol = m;
+        t->accepted = ok[j];
+        t->e_old = eo[j];
+        t->e_new = en[j];
+        t->de = de;
+        t->u = (double)mv[j].u;
+      }
+    }
+  }
+#undef PR
+  for (int j = 0; j < K; j++) free(p[j].off);
+  free(pr);
+  free(ok);
+  free(en);
+  free(eo);
+  free(mv);
+  free(p);
+  free(save);
+  if (n_accepted) *n_accepted = acc;
+  if (n_redo) *n_redo = redo;
   return e;
 }
 

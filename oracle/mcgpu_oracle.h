@@ -116,6 +116,15 @@ void orc_fchain_draw(const orc_chain* c, uint64_t seed, uint32_t chain, uint64_t
                     orc_movef* mv);
 double orc_fchain_run(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step0,
                      int n_steps, double e0, orc_trace* trace, long long* n_accepted);
+/* The same loop in windows of K steps, each step evaluated first on the
+ * state at its window's start and again only when an earlier accepted step
+ * of the window moved its molecule or one in range of it; *n_redo counts
+ * those.  Returns what orc_fchain_run returns, with the same trace.
+ * in_range_rule = 0 plants a mistake (only same-molecule steps are evaluated
+ * again), for tests. */
+double orc_fchain_run_window(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step0,
+                             int n_steps, int K, double e0, orc_trace* trace,
+                             long long* n_accepted, long long* n_redo, int in_range_rule);
 void orc_sincos_f32(float x, float* s, float* c);
 int orc_fchain_volume(orc_chain* c, uint64_t seed, uint32_t chain, uint64_t step,
                       double p_kcal, double max_dlnv, float rad_max, double lrc_v, double* energy,

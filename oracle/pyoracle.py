@@ -138,6 +138,10 @@ def orc_lib() -> C.CDLL:
             "orc_fchain_run": (C.c_double, [C.POINTER(OrcChainS), C.c_uint64, C.c_uint32,
                                             C.c_uint64, C.c_int, C.c_double, C.POINTER(OrcTrace),
                                             C.POINTER(C.c_longlong)]),
+            "orc_fchain_run_window": (C.c_double, [C.POINTER(OrcChainS), C.c_uint64, C.c_uint32,
+                                                   C.c_uint64, C.c_int, C.c_int, C.c_double,
+                                                   C.POINTER(OrcTrace), C.POINTER(C.c_longlong),
+                                                   C.POINTER(C.c_longlong), C.c_int]),
             "orc_sincos_f32": (None, [C.c_float, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
             "orc_fchain_volume": (C.c_int, [C.POINTER(OrcChainS), C.c_uint64, C.c_uint32,
                                             C.c_uint64, C.c_double, C.c_double, C.c_float,
@@ -373,6 +377,21 @@ class OracleChain:
         e = orc_lib().orc_fchain_run(C.byref(self.s), int(seed) & (2 ** 64 - 1), int(chain),
                                      int(step0), int(n_steps), float(e0), tr, C.byref(acc))
         return e, acc.value, list(tr)[:n_steps]
+
+    def run_window(self, seed: int, chain: int, n_steps: int, e0: float, window: int,
+                   step0: int = 0, in_range_rule: bool = True):
+        """run() in windows of `window` steps (orc_fchain_run_window): each
+        step evaluated on its window's start state and again only when an
+        earlier accepted step of the window moved its molecule or one in
+        range of it (in_range_rule=False drops the latter: a planted
+        mistake).  Returns (energy, accepted, trace, re-evaluated steps)."""
+        tr = (OrcTrace * max(1, n_steps))()
+        acc, redo = C.c_longlong(), C.c_longlong()
+        e = orc_lib().orc_fchain_run_window(C.byref(self.s), int(seed) & (2 ** 64 - 1),
+                                            int(chain), int(step0), int(n_steps), int(window),
+                                            float(e0), tr, C.byref(acc), C.byref(redo),
+                                            1 if in_range_rule else 0)
+        return e, acc.value, list(tr)[:n_steps], redo.value
 
     def system_energy(self) -> float:
         return self.ob.system_energy()
