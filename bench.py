@@ -10,7 +10,10 @@ plain single-chain GPU drop-in (the SimulationStep contract driven from the
 host with the C library's rand(), one launch per contract call) on the
 256-water box, so the batched/plain ratio of the metric is on the line, and
 the same plain path with intramolecular moves on a flexible-molecule box
-(``flexible``).
+(``flexible``), the single large chains (``single_chain``: 4000 x 16-atom
+molecules; ``large_system``: 32,768 waters, NPT, the precision sweep) one
+step at a time and in windows of 8 and 16 steps over a thread-block
+cluster, and the served request loop (``served``).
 
 ``--impl reference`` times the reference's CPU implementation of the path
 (the FP64 restatement in oracle/, bit-identical to the compiled reference)
