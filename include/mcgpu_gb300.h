@@ -82,7 +82,10 @@ typedef struct {
   int64_t steps;          /* steps taken so far                            */
   int64_t accepted;       /* accepted moves so far                         */
   int64_t pairs;          /* atom pairs evaluated (old + new), if counted  */
-  int32_t error;          /* device error status word (0 = none)           */
+  int32_t error;          /* device error status word: 0 none; 4 a
+                             cluster-wide wait of a windowed run ran out
+                             (the launch ended early); other values are
+                             reserved                                       */
   int32_t ties;           /* decisions re-taken with FP64 pairs because the
                              FP32 dE fell within its rounding bound of the
                              acceptance threshold                           */
